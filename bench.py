@@ -1,0 +1,352 @@
+#!/usr/bin/env python3
+"""Benchmark of the ray-traced visibility + deferred-lighting frame.
+
+Workload: the large two-level scene at 1920x1080 — 64 icospheres (subdivision 6,
+81,920 triangles each, radially displaced by 8 seeded spherical sinusoids), 1024
+instances in a 200^3 box (83.9 M instanced triangles), 1 directional + 32 point + 8
+spot lights, 1 shadow ray per light and 16 cosine-weighted AO rays (radius 2.0) per
+lit pixel, FP32. Synthetic, seeded scene (seed 1002).
+
+A step is one frame: TLAS rebuild from the host instance array, primary-ray
+G-buffer, shadow + AO visibility, deferred light pass. Rays per frame = primary
+rays (one per pixel) + lit pixels x (41 shadow + 16 AO). The BLAS are built once
+before timing, as the reference builds them at import.
+
+value: Grays/s with every input resident in device memory (CUDA events around each
+frame on the launching stream; a 256 MB buffer is written between frames to flush
+L2). e2e: the same frame through the C ABI from pinned host buffers — scene,
+light and model blocks and the instance array copied host->device, the RGBA32F
+light image read back — timed on the host around the synchronised call.
+
+--impl reference runs the reference path's CPU restatement (the oracle) on all
+host cores over a bounded row sample of the same frame.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms/frame @1080p: denoised 1spp vs plain at equal AO RMSE vs 1024spp; Grays/s"
+UNIT = "Grays/s"
+CONFIG = {"workload": "two-level scene 1920x1080: 64 displaced icospheres (81,920 tris) x 1024 instances, "
+                      "41 lights (1 dir + 32 point + 8 spot), 1 shadow ray/light + 16 AO rays/px, FP32",
+          "width": 1920, "height": 1080, "instances": 1024, "blas": 64, "triangles_per_blas": 81920,
+          "shadow_rays_per_px": 41, "ao_rays_per_px": 16, "seed": 1002, "l2": "flushed between frames (256 MB write)"}
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-rows", type=int, default=24, help="rows of the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", FALLBACK_HBM_GBS), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the visibility kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "visibility_kernel_config2.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (200 ms period)."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.file.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(scene, rows: int, repeats: int = 1):
+    """Oracle frame over a bounded band of rows at the image centre, all host cores."""
+    import numpy as np
+
+    import luz_gb300 as L
+    import oracle as O
+
+    meshes = scene.meshes()
+    ob = [O.OracleBlas(v, i) for v, i in meshes]          # BLAS: built once, not timed
+    im = scene.instance_mesh()
+    tr = scene.transforms()
+    b, lights, models = scene.block(), scene.lights(), scene.models()
+    W, H = scene.width, scene.height
+    y0 = max(0, H // 2 - rows // 2)
+    y1 = min(H, y0 + rows)
+    bn = L.blue_noise()
+    nthreads = O.threads()
+    S = sum(lights[i].num_shadow_samples for i in range(scene.light_count)) + b.ao_num_samples
+    times, rays_list = [], []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        tl = O.OracleTlas([ob[m] for m in im], tr)
+        f = O.OracleFrame(tl, b, lights, scene.light_count, models, scene.instance_count, W, H)
+        f.gbuffer(nthreads, y0, y1)
+        f.visibility(0, bn, y0, y1, nthreads=nthreads)
+        f.light_pass(nthreads=nthreads, y0=y0, y1=y1)
+        dt = time.perf_counter() - t0
+        lit = int((np.linalg.norm(f.normal[y0 * W:y1 * W, :3], axis=1) > 0).sum())
+        rays_list.append((y1 - y0) * W + lit * S)
+        times.append(dt)
+    value = sum(rays_list) / sum(times) / 1e9
+    return {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"rows {y0}-{y1} of 1920x1080 ({(y1 - y0) * W} px, {rays_list[0]} rays per sample): "
+                      f"TLAS build + G-buffer + shadow/AO any-hit + light pass; BLAS build untimed"}, times
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    import luz_gb300 as L
+    scene = L.HostScene(2)
+    K = args.steps
+    res, times = cpu_baseline(scene, args.cpu_rows, repeats=max(1, args.warmup) + K)
+    times = times[max(1, args.warmup):]
+    value = res["value"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": K, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator)", "config": CONFIG,
+            "cpu_baseline": res, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------- GPU arm
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import luz_gb300 as L
+    from luz_gb300 import _abi
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    scene = L.HostScene(2)
+    ctx = L.Context(local)
+    stream = torch.cuda.current_stream(dev)
+    L.lib.luz_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream))
+    g = L.GPUScene(ctx, scene)
+    g.update_resources_gpu()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    fr, tl = g.frame, g.tlas
+
+    def frame(fi: int, ev=None):
+        if ev:
+            ev[0].record(stream)
+        tl.build(g.instances, g.n_instances)
+        if ev:
+            ev[1].record(stream)
+        fr.gbuffer(tl)
+        if ev:
+            ev[2].record(stream)
+        fr.trace(tl, fi)
+        if ev:
+            ev[3].record(stream)
+        fr.light_pass(False)
+        if ev:
+            ev[4].record(stream)
+
+    for w in range(args.warmup):
+        frame(w)
+    torch.cuda.synchronize()
+    lit = fr.lit_count()
+    S = fr_shadow = sum(g.lights[i].num_shadow_samples for i in range(scene.light_count))
+    S = fr_shadow + g.block.ao_num_samples
+    rays_per_frame = scene.width * scene.height + lit * S
+    stats = fr.trace_stats(tl, 0)
+    torch.cuda.synchronize()
+    assert stats["rays"] == lit * S, (stats, lit, S)
+    if ctx.device_status() != 0:
+        raise RuntimeError("device status word raised during warm-up")
+
+    K = args.steps
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(K)]
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    launches0 = ctx.launch_count()
+    for k in range(K):
+        flush.zero_()
+        frame(args.warmup + k, evs[k])
+    torch.cuda.synchronize()
+    launches = ctx.launch_count() - launches0
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    frame_ms = [e[0].elapsed_time(e[4]) for e in evs]
+    stage_ms = {name: statistics.mean(e[i].elapsed_time(e[i + 1]) for e in evs)
+                for i, name in enumerate(["tlas_build", "gbuffer", "visibility", "light_pass"])}
+    ms = statistics.mean(frame_ms)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * rays_per_frame / (ms * 1e-3) / 1e9
+    if ctx.device_status() != 0:
+        raise RuntimeError("device status word raised during timing")
+
+    # roofline of the dominant kernel (visibility): algorithmic bytes per launch
+    vis_bytes = (stats["rays"] * (32 + 0.125) + (stats["tlas_nodes"] + stats["blas_nodes"]) * 64 +
+                 stats["tris"] * 48 + stats["instances"] * 80)
+    vis_s = stage_ms["visibility"] * 1e-3
+    peak, peak_kind = measured_peaks()
+    achieved = vis_bytes / vis_s / 1e9
+    roofline = {"bound": "hbm", "kernel": "visibility_kernel", "achieved": achieved, "peak": peak,
+                "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profiled_traffic(), "algorithmic_bytes": vis_bytes,
+                "per_ray": {k: stats[k] / max(stats["rays"], 1) for k in
+                            ("tlas_nodes", "blas_nodes", "tris", "instances")}}
+
+    # e2e through the C ABI from pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        nbytes = fr.plane_bytes(L.PLANE_LIGHT)
+        out = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        models_p = torch.empty(C.sizeof(g.models), dtype=torch.uint8, pin_memory=True)
+        lights_p = torch.empty(C.sizeof(g.lights), dtype=torch.uint8, pin_memory=True)
+        scene_p = torch.empty(C.sizeof(g.block), dtype=torch.uint8, pin_memory=True)
+        inst_p = torch.empty(C.sizeof(g.instances), dtype=torch.uint8, pin_memory=True)
+        C.memmove(models_p.data_ptr(), g.models, C.sizeof(g.models))
+        C.memmove(lights_p.data_ptr(), g.lights, C.sizeof(g.lights))
+        C.memmove(scene_p.data_ptr(), C.byref(g.block), C.sizeof(g.block))
+        C.memmove(inst_p.data_ptr(), g.instances, C.sizeof(g.instances))
+        lib = L.lib
+        sp = C.cast(C.c_void_p(scene_p.data_ptr()), C.POINTER(_abi.Scene))
+        lp = C.cast(C.c_void_p(lights_p.data_ptr()), C.POINTER(_abi.Light))
+        mp = C.cast(C.c_void_p(models_p.data_ptr()), C.POINTER(_abi.Model))
+        ip = C.cast(C.c_void_p(inst_p.data_ptr()), C.POINTER(_abi.Instance))
+
+        def e2e_step(fi):
+            st = lib.luz_frame_upload(ctx.handle, fr.handle, sp, lp, scene.light_count, mp, scene.instance_count)
+            st |= lib.luz_render_frame(ctx.handle, fr.handle, tl.handle, ip, g.n_instances, fi)
+            st |= lib.luz_frame_read(ctx.handle, fr.handle, L.PLANE_LIGHT, C.c_void_p(out.data_ptr()), nbytes)
+            if st != 0:
+                raise RuntimeError(lib.luz_last_error(ctx.handle).decode())
+
+        for w in range(args.warmup):
+            e2e_step(w)
+        torch.cuda.synchronize()
+        ts = []
+        for k in range(K):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_step(k)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        e2e_s = statistics.mean(ts)
+        h2d = C.sizeof(g.block) + C.sizeof(_abi.Light) * scene.light_count + \
+            C.sizeof(_abi.Model) * scene.instance_count + C.sizeof(_abi.Instance) * g.n_instances
+        e2e = {"value": world * rays_per_frame / e2e_s / 1e9, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nbytes)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu, _ = cpu_baseline(scene, args.cpu_rows)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
+                "config": dict(CONFIG, parallelism=f"replicas{world}" if world > 1 else "single"),
+                "rays_per_frame": rays_per_frame, "lit_pixels": lit, "stage_ms": stage_ms,
+                "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,272 @@
+/*
+ * luz.h — C ABI of the GB300-native ray-traced visibility and deferred-lighting path.
+ *
+ * Every entry point replaces one call of the reference renderer's RHI / renderer
+ * surface (hadryansalles/Luz); the replaced interface is cited beside each one as
+ * file:line within that project. Plain C types only: pointers, sizes, PODs and
+ * opaque handles. No exception crosses this boundary; every call returns a
+ * luz_status and the context keeps a human-readable message (luz_last_error).
+ *
+ * Threading: a luz_ctx is thread-compatible (one host thread at a time), like the
+ * reference's single global Vulkan context `_ctx` (source/Graphics/VulkanWrapper.cpp).
+ * All GPU work of a context is ordered on the context's CUDA stream.
+ */
+#ifndef LUZ_GB300_H
+#define LUZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+typedef int32_t luz_status;
+enum {
+    LUZ_OK = 0,
+    LUZ_ERR_INVALID = 1,        /* bad argument / handle / size                 */
+    LUZ_ERR_CUDA = 2,           /* a CUDA runtime call failed                   */
+    LUZ_ERR_OOM = 3,            /* device allocation failed                     */
+    LUZ_ERR_DEVICE = 4,         /* a kernel raised its status word (see below)  */
+    LUZ_ERR_LIMIT = 5,          /* a documented size limit was exceeded         */
+    LUZ_ERR_NO_DEVICE = 6       /* no CUDA device / driver                      */
+};
+
+/* Device status-word bits (luz_ctx_device_status). Kernels never trap; every
+ * spin or traversal loop has an iteration cap and sets one of these instead. */
+enum {
+    LUZ_DEV_SORT_LOOKBACK_TIMEOUT = 1u << 0,
+    LUZ_DEV_STACK_OVERFLOW = 1u << 1,
+    LUZ_DEV_TRAVERSAL_CAP = 1u << 2,
+    LUZ_DEV_KARRAS_RANGE = 1u << 3,
+    LUZ_DEV_BATCH_QUEUE = 1u << 4
+};
+
+/* ------------------------------------------------------------------ limits */
+#define LUZ_MAX_SHADOW_SLOTS 1024   /* Σ_lights numShadowSamples per pixel      */
+#define LUZ_MAX_AO_SAMPLES 4096     /* aoNumSamples per pixel                   */
+#define LUZ_BLUE_NOISE_SIZE 128     /* substitute blue-noise texture, RGBA8     */
+
+/* Light types and shadow types: source/Shaders/LuzCommon.h:24-29. */
+#define LUZ_LIGHT_POINT 0
+#define LUZ_LIGHT_SPOT 1
+#define LUZ_LIGHT_DIRECTIONAL 2
+#define LUZ_SHADOW_DISABLED 0
+#define LUZ_SHADOW_RAYTRACING 1
+#define LUZ_SHADOW_MAP 2
+
+/* Sample sequences. PARITY reproduces BlueNoiseSample (source/Shaders/light.frag:71-75)
+ * over the seeded substitute texture; STRATIFIED is a per-pixel rotated R2 sequence
+ * evaluated in 32-bit fixed point, which stays unbiased at 1024+ samples. */
+#define LUZ_SAMPLER_PARITY 0
+#define LUZ_SAMPLER_STRATIFIED 1
+
+/* ------------------------------------------------------------------ data contract */
+
+/* MeshAsset::MeshVertex, 48 B (source/Resources/AssetManager.hpp:83-91). */
+typedef struct luz_vertex {
+    float position[3];
+    float normal[3];
+    float tangent[4];
+    float texcoord[2];
+} luz_vertex;
+
+/* The fields of LightBlock (source/Shaders/LuzCommon.h:37-50) that the ray-traced
+ * light pass reads; 64 B. Angles are radians (GPUScene.cpp:244,246 converts). The
+ * shadow-map matrices and volumetric fields (LuzCommon.h:52-60) are not on the path. */
+typedef struct luz_light {
+    float color[3];
+    float intensity;
+    float position[3];
+    float inner_angle;
+    float direction[3];
+    float outer_angle;
+    int32_t type;
+    int32_t num_shadow_samples;
+    float radius;
+    int32_t shadow_map;
+} luz_light;
+
+/* ModelBlock, 128 B (source/Shaders/LuzCommon.h:76-92). model_mat is column-major
+ * (glm layout). Texture and buffer RIDs are kept for layout parity; texture maps
+ * index luz_frame textures (-1 = none). */
+typedef struct luz_model {
+    float model_mat[16];
+    float color[4];
+    float emission[3];
+    float metallic;
+    float roughness;
+    int32_t ao_map;
+    int32_t color_map;
+    int32_t normal_map;
+    int32_t emission_map;
+    int32_t metallic_roughness_map;
+    int32_t vertex_buffer;
+    int32_t index_buffer;
+} luz_model;
+
+/* SceneBlock (source/Shaders/LuzCommon.h:94-125) without its fixed
+ * `LightBlock lights[LUZ_MAX_LIGHTS]` array: lights travel as a separate array of
+ * any length (the reference caps them at 64, LuzCommon.h:20). Matrices column-major. */
+typedef struct luz_scene {
+    float ambient_light_color[3];
+    float ambient_light_intensity;
+    float proj[16];
+    float view[16];
+    float view_proj[16];
+    float prev_view_proj[16];
+    float inverse_proj[16];
+    float inverse_view[16];
+    float jitter[2];
+    float prev_jitter[2];
+    float cam_pos[3];
+    int32_t num_lights;
+    float ao_min;
+    float ao_max;
+    float exposure;
+    int32_t ao_num_samples;
+    int32_t white_texture;
+    int32_t black_texture;
+    int32_t blue_noise_texture;
+    int32_t tlas_rid;
+    int32_t shadow_type;
+    int32_t sampler;          /* LUZ_SAMPLER_*; occupies SceneBlock.pad[0]        */
+    int32_t pad[2];
+} luz_scene;
+
+typedef struct luz_blas luz_blas;
+typedef struct luz_tlas luz_tlas;
+typedef struct luz_ctx luz_ctx;
+typedef struct luz_frame luz_frame;
+
+/* VkAccelerationStructureInstanceKHR as filled by vkw::CmdBuildTLAS
+ * (source/Graphics/VulkanWrapper.cpp:1111-1126): 3x4 row-major object-to-world
+ * transform (rows = the first three rows of modelMat), custom index = modelRID,
+ * mask 0xFF, triangle facing cull disabled (every traversal here is two-sided). */
+typedef struct luz_instance {
+    const luz_blas* blas;
+    float transform[3][4];
+    uint32_t custom_index;
+    uint32_t mask;
+} luz_instance;
+
+/* BLASDesc (source/Graphics/VulkanWrapper.h:206-213) with host-side buffers. */
+typedef struct luz_blas_desc {
+    const void* vertices;       /* positions as float[3] at offset 0 of each vertex */
+    uint32_t vertex_count;
+    uint32_t vertex_stride;     /* bytes; 48 for luz_vertex                          */
+    const uint32_t* indices;
+    uint32_t index_count;       /* multiple of 3                                     */
+} luz_blas_desc;
+
+/* G-buffer / frame planes (formats of DeferredRenderer::CreateImages,
+ * source/Graphics/DeferredRenderer.cpp:175-248). */
+enum {
+    LUZ_PLANE_ALBEDO = 0,       /* RGBA8 UNORM, 4 B/px                               */
+    LUZ_PLANE_NORMAL = 1,       /* RGBA32F, 16 B/px                                  */
+    LUZ_PLANE_MATERIAL = 2,     /* RGBA8 UNORM (rough, metal, occl, 1)               */
+    LUZ_PLANE_EMISSION = 3,     /* RGBA8 UNORM                                       */
+    LUZ_PLANE_DEPTH = 4,        /* F32, NDC z in [0,1]                               */
+    LUZ_PLANE_LIGHT = 5,        /* RGBA32F light-pass output                         */
+    LUZ_PLANE_SHADOW_BITS = 6,  /* u32 bit planes: [slot][ceil(W*H/32)], hit = 1     */
+    LUZ_PLANE_AO_BITS = 7,      /* u32 bit planes: [sample][ceil(W*H/32)], miss = 1  */
+    LUZ_PLANE_AO = 8,           /* F32 per-pixel AO value (mean of misses)            */
+    LUZ_PLANE_AO_DENOISED = 9,  /* F32 per-pixel denoised AO                          */
+    LUZ_PLANE_PRIMARY_HIT = 10, /* u32x2 per pixel: (instance custom index, prim id), ~0 = miss */
+    LUZ_PLANE_COUNT = 11
+};
+
+/* ------------------------------------------------------------------ context */
+luz_status luz_ctx_create(int device, luz_ctx** out);
+void luz_ctx_destroy(luz_ctx* ctx);
+const char* luz_last_error(const luz_ctx* ctx);
+luz_status luz_ctx_synchronize(luz_ctx* ctx);
+/* Reads and clears the device status word (LUZ_DEV_* bits). */
+luz_status luz_ctx_device_status(luz_ctx* ctx, uint32_t* bits);
+/* Number of kernels this context has launched so far. */
+uint64_t luz_ctx_launch_count(const luz_ctx* ctx);
+/* Uses `stream` (a cudaStream_t) for all later work; NULL = the context's own. */
+luz_status luz_ctx_set_stream(luz_ctx* ctx, void* stream);
+/* Uploads the substitute blue-noise texture (RGBA8, size*size texels). */
+luz_status luz_ctx_set_blue_noise(luz_ctx* ctx, const uint8_t* rgba8, uint32_t size);
+
+/* ------------------------------------------------------------------ BLAS
+ * Replaces vkw::CreateBLAS + vkw::CmdBuildBLAS (source/Graphics/VulkanWrapper.h:236,
+ * :229; VulkanWrapper.cpp:743-836, 1089-1104) as called by GPUScene::AddMesh
+ * (source/Graphics/GPUScene.cpp:108-138). The reference builds one BLAS per
+ * synchronous submit; the batched form builds all of them in one device pipeline. */
+luz_status luz_blas_build(luz_ctx* ctx, const luz_blas_desc* desc, luz_blas** out);
+luz_status luz_blas_build_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* descs,
+                                luz_blas** out);
+void luz_blas_destroy(luz_blas* blas);
+uint32_t luz_blas_primitive_count(const luz_blas* blas);
+/* Copies the built BLAS to host memory: nodes (64 B each, count = max(n-1,1)),
+ * triangles (48 B each, sorted leaf order), the sorted Morton keys (u32) and the
+ * sorted primitive order (u32). Any pointer may be NULL. For parity tests. */
+luz_status luz_blas_download(luz_ctx* ctx, const luz_blas* blas, void* nodes, void* tris,
+                             uint32_t* morton_sorted, uint32_t* order);
+
+/* ------------------------------------------------------------------ TLAS
+ * Replaces vkw::CreateTLAS(maxInstances) and vkw::CmdBuildTLAS(tlas, instances)
+ * (source/Graphics/VulkanWrapper.h:235,:243; VulkanWrapper.cpp:657-741, 1106-1139),
+ * rebuilt every frame by GPUScene::UpdateResourcesGPU (GPUScene.cpp:348-366). */
+luz_status luz_tlas_create(luz_ctx* ctx, uint32_t max_instances, luz_tlas** out);
+luz_status luz_tlas_build(luz_ctx* ctx, luz_tlas* tlas, const luz_instance* instances,
+                          uint32_t count);
+void luz_tlas_destroy(luz_tlas* tlas);
+/* Copies the TLAS nodes (64 B each, breadth-first order) and the sorted instance
+ * order (u32) to host memory. For parity tests. */
+luz_status luz_tlas_download(luz_ctx* ctx, const luz_tlas* tlas, void* nodes,
+                             uint32_t* morton_sorted, uint32_t* order, uint32_t* node_count);
+
+/* ------------------------------------------------------------------ frame
+ * A luz_frame owns the per-resolution images of DeferredRenderer::CreateImages
+ * (source/Graphics/DeferredRenderer.cpp:175-248) plus the visibility planes and the
+ * device copies of SceneBlock/ModelBlock/lights (GPUScene.cpp:348-353). */
+luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_frame** out);
+void luz_frame_destroy(luz_frame* frame);
+/* Host→device copy of the scene constants, lights and model blocks; mirrors the two
+ * CmdCopy calls of GPUScene::UpdateResourcesGPU (GPUScene.cpp:352-353). */
+luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* frame, const luz_scene* scene,
+                            const luz_light* lights, uint32_t light_count,
+                            const luz_model* models, uint32_t model_count);
+/* Primary-ray G-buffer: the raster opaque pass (source/Shaders/opaque.vert:21-31,
+ * opaque.frag:21-58; main.cpp:242-258) as closest-hit rays through pixel centres. */
+luz_status luz_gbuffer_primary(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas);
+/* Shadow (light.frag:86-109,137-146) and AO (light.frag:111-135) any-hit rays of
+ * every lit pixel; writes the visibility bit planes. */
+luz_status luz_trace_visibility(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas,
+                                int32_t frame_index);
+/* The same trace with per-ray work counters (a separate kernel build, for
+ * roofline accounting): out[0] rays, out[1] TLAS node visits, out[2] BLAS node
+ * visits, out[3] triangle tests, out[4] instance entries. */
+luz_status luz_trace_visibility_stats(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas,
+                                      int32_t frame_index, uint64_t out[5]);
+/* Per-pixel AO value (mean of the miss bits) into LUZ_PLANE_AO. */
+luz_status luz_ao_resolve(luz_ctx* ctx, luz_frame* frame);
+/* Number of lit pixels (length(N) != 0) of the last G-buffer pass. */
+luz_status luz_frame_lit_count(luz_ctx* ctx, luz_frame* frame, uint32_t* count);
+/* DeferredRenderer::LightPass (source/Graphics/DeferredRenderer.cpp:324-345) running
+ * light.frag main (light.frag:171-235) over the G-buffer and visibility planes.
+ * use_denoised_ao != 0 reads LUZ_PLANE_AO_DENOISED instead of the AO bit planes. */
+luz_status luz_light_pass(luz_ctx* ctx, luz_frame* frame, int32_t use_denoised_ao);
+/* One whole frame: TLAS build, primary G-buffer, visibility, light pass. */
+luz_status luz_render_frame(luz_ctx* ctx, luz_frame* frame, luz_tlas* tlas,
+                            const luz_instance* instances, uint32_t instance_count,
+                            int32_t frame_index);
+/* Size in bytes of one plane of this frame (LUZ_PLANE_*). */
+size_t luz_frame_plane_bytes(const luz_frame* frame, int32_t plane);
+/* Device→host copy of a plane. */
+luz_status luz_frame_read(luz_ctx* ctx, luz_frame* frame, int32_t plane, void* host_dst,
+                          size_t bytes);
+/* Host→device copy into a plane (e.g. to run the light pass on a given G-buffer). */
+luz_status luz_frame_write(luz_ctx* ctx, luz_frame* frame, int32_t plane,
+                           const void* host_src, size_t bytes);
+/* Device pointer of a plane (for zero-copy interop), NULL on error. */
+void* luz_frame_plane_device_ptr(luz_frame* frame, int32_t plane);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LUZ_GB300_H */

@@ -1,0 +1,104 @@
+/*
+ * luz_scene.h — host-side scene layer of the path (C++17 behind a C ABI).
+ *
+ * It stands where the reference's GPUScene::UpdateResources
+ * (source/Graphics/GPUScene.cpp:181-346) and the scene graph math of
+ * source/Resources/AssetManager.cpp sit: it turns a scene description into the
+ * inputs of include/luz.h (meshes, instances with ModelBlocks, LightBlocks and the
+ * SceneBlock constants). It also holds the seeded synthetic scene generators the
+ * benchmarks and tests use. No GPU work happens here.
+ */
+#ifndef LUZ_GB300_SCENE_H
+#define LUZ_GB300_SCENE_H
+
+#include "luz.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* CameraNode (source/Resources/AssetManager.hpp:229-275). mode: 0 = Orbit, 1 = Fly
+ * (CameraNode::GetView, AssetManager.cpp:334-355), 2 = look-at from eye to center. */
+typedef struct luz_camera {
+    int32_t camera_type;      /* 0 perspective, 1 orthographic */
+    int32_t mode;
+    float eye[3];
+    float center[3];
+    float rotation[3];        /* degrees */
+    float zoom;
+    float far_distance;
+    float near_distance;
+    float horizontal_fov;     /* degrees; passed to perspective() as fovy (AssetManager.cpp:368) */
+    float ortho_far_distance;
+    float ortho_near_distance;
+    float extent[2];          /* viewport size in pixels */
+    float jitter[2];          /* NDC jitter (CameraNode::NextJitter); 0 = off */
+} luz_camera;
+
+/* Synthetic scene generators. config:
+ *   1  ground quad 20x20 + 64 unit cubes, 1 directional + 4 point lights, 512x512
+ *   2  64 displaced icospheres (subdivision 6) x 1024 instances in a 200^3 box,
+ *      1 directional + 32 point + 8 spot lights, 1920x1080, 16 AO samples
+ *   3  config 1's generator with a seeded random camera (denoiser training scenes)
+ *   5  config 2's meshes x 4096 instances, 128 point + 1 directional + 16 spot,
+ *      3840x2160, 64 AO samples
+ *   6  one member of the batched workload: triangle budget `triangles`, built from
+ *      config 1/2 primitives
+ * Fields left 0 take the config's default. */
+typedef struct luz_gen_params {
+    int32_t config;
+    uint32_t pad0;
+    uint64_t seed;
+    uint32_t width, height;
+    int32_t ao_samples;       /* -1 = config default */
+    float ao_max;             /* 0 = config default  */
+    int32_t light_samples;    /* 0 = 1               */
+    int32_t sampler;          /* LUZ_SAMPLER_*       */
+    uint32_t meshes, instances, subdivisions;
+    uint32_t point_lights, spot_lights, directional_lights;
+    uint32_t triangles;       /* config 6 */
+    uint32_t pad1;
+} luz_gen_params;
+
+typedef struct luz_host_scene luz_host_scene;
+
+luz_status luz_scene_default_params(int32_t config, luz_gen_params* out);
+luz_status luz_scene_generate(const luz_gen_params* params, luz_host_scene** out);
+void luz_scene_destroy(luz_host_scene* scene);
+
+uint32_t luz_scene_mesh_count(const luz_host_scene* s);
+luz_status luz_scene_mesh(const luz_host_scene* s, uint32_t i, const luz_vertex** vertices,
+                          uint32_t* vertex_count, const uint32_t** indices, uint32_t* index_count);
+uint32_t luz_scene_instance_count(const luz_host_scene* s);
+/* Mesh index of each instance. */
+const uint32_t* luz_scene_instance_mesh(const luz_host_scene* s);
+/* ModelBlock of each instance (custom index i = model i, as GPUScene.cpp:188-191). */
+const luz_model* luz_scene_models(const luz_host_scene* s);
+uint32_t luz_scene_light_count(const luz_host_scene* s);
+const luz_light* luz_scene_lights(const luz_host_scene* s);
+const luz_scene* luz_scene_block(const luz_host_scene* s);
+uint32_t luz_scene_width(const luz_host_scene* s);
+uint32_t luz_scene_height(const luz_host_scene* s);
+/* Instance transforms as VkTransformMatrixKHR rows (VulkanWrapper.cpp:1122-1126):
+ * count*12 floats, row-major 3x4 = the first three rows of modelMat. */
+luz_status luz_scene_instance_transforms(const luz_host_scene* s, float* out);
+luz_status luz_scene_set_camera(luz_host_scene* s, const luz_camera* cam);
+luz_status luz_scene_get_camera(const luz_host_scene* s, luz_camera* cam);
+/* Sample counts: aoSamples/aoMin/aoMax (GPUScene.cpp:333-335) and lightSamples,
+ * which becomes every light's numShadowSamples (GPUScene.cpp:248). */
+luz_status luz_scene_set_sampling(luz_host_scene* s, int32_t ao_samples, float ao_min, float ao_max,
+                                  int32_t light_samples, int32_t sampler);
+
+/* Node::ComposeTransform (AssetManager.cpp:38-43): parent * T * R(quat(radians(rot))) * S.
+ * parent may be NULL (identity). Column-major 4x4 out. */
+void luz_compose_transform(const float pos[3], const float rot_deg[3], const float scale[3],
+                           const float* parent, float out[16]);
+/* CameraNode::GetView and GetProjJittered (AssetManager.cpp:334-377). */
+void luz_camera_matrices(const luz_camera* cam, float view[16], float proj[16]);
+/* Seeded RGBA8 substitute for the missing assets/blue_noise.png. */
+luz_status luz_blue_noise_generate(uint64_t seed, uint32_t size, uint8_t* rgba8);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LUZ_GB300_SCENE_H */

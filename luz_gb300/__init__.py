@@ -1,0 +1,403 @@
+"""luz_gb300 — GB300-native (sm_103a) ray-traced visibility and deferred lighting.
+
+Python face of the C ABI in include/luz.h and include/luz_scene.h. Every compute
+call goes to libluz_gb300.so (hand-written CUDA kernels); there is no CPU or
+PyTorch fallback, and importing the package fails when the library is missing.
+
+The classes mirror the reference renderer's host interface for this path
+(hadryansalles/Luz): ``GPUScene`` follows GPUScene::AddMesh / UpdateResources /
+UpdateResourcesGPU (source/Graphics/GPUScene.cpp:108-366) and ``light_pass``
+follows DeferredRenderer::LightPass (source/Graphics/DeferredRenderer.cpp:324-345).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import (BLUE_NOISE_SIZE, LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_SPOT, PLANE_ALBEDO, PLANE_AO,
+                   PLANE_AO_BITS, PLANE_AO_DENOISED, PLANE_DEPTH, PLANE_DTYPES, PLANE_EMISSION, PLANE_LIGHT,
+                   PLANE_MATERIAL, PLANE_NORMAL, PLANE_PRIMARY_HIT, PLANE_SHADOW_BITS, SAMPLER_PARITY,
+                   SAMPLER_STRATIFIED, SHADOW_RAYTRACING, BlasDesc, Camera, GenParams, Instance, Light, Model,
+                   Scene, Vertex)
+
+lib = _abi.load()
+
+__all__ = ["LuzError", "HostScene", "Context", "GPUScene", "lib", "blue_noise"]
+
+
+class LuzError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"{_abi.STATUS_NAMES.get(status, status)}: {message}")
+
+
+def _check(status: int, ctx_handle=None, what: str = "") -> None:
+    if status != _abi.LUZ_OK:
+        msg = lib.luz_last_error(ctx_handle).decode() if ctx_handle else what
+        raise LuzError(status, f"{what}: {msg}" if what else msg)
+
+
+def blue_noise(seed: int = 7, size: int = BLUE_NOISE_SIZE) -> np.ndarray:
+    """Seeded RGBA8 substitute for the reference's missing assets/blue_noise.png."""
+    out = np.zeros((size, size, 4), np.uint8)
+    _check(lib.luz_blue_noise_generate(seed, size, _abi.ptr(out, _abi.c_u8_p)), what="blue noise")
+    return out
+
+
+# ---------------------------------------------------------------------------- host scenes
+class HostScene:
+    """A generated scene (meshes, instances with ModelBlocks, lights, SceneBlock)."""
+
+    def __init__(self, config: int, seed: int | None = None, width: int | None = None,
+                 height: int | None = None, **overrides):
+        p = GenParams()
+        _check(lib.luz_scene_default_params(config, C.byref(p)), what="default params")
+        if seed is not None:
+            p.seed = seed
+        if width:
+            p.width = width
+        if height:
+            p.height = height
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        self.params = p
+        h = C.c_void_p()
+        _check(lib.luz_scene_generate(C.byref(p), C.byref(h)), what="scene generate")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib.luz_scene_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def width(self) -> int:
+        return lib.luz_scene_width(self._h)
+
+    @property
+    def height(self) -> int:
+        return lib.luz_scene_height(self._h)
+
+    def meshes(self) -> list[tuple[np.ndarray, np.ndarray]]:
+        """[(vertices float32 (nv, 12), indices uint32 (ni,))] — views into the scene."""
+        out = []
+        for i in range(lib.luz_scene_mesh_count(self._h)):
+            vp = C.POINTER(Vertex)()
+            ip = _abi.c_u32_p()
+            nv, ni = C.c_uint32(), C.c_uint32()
+            _check(lib.luz_scene_mesh(self._h, i, C.byref(vp), C.byref(nv), C.byref(ip), C.byref(ni)))
+            v = np.ctypeslib.as_array(C.cast(vp, _abi.c_float_p), shape=(nv.value, 12)) if nv.value else \
+                np.zeros((0, 12), np.float32)
+            idx = np.ctypeslib.as_array(ip, shape=(ni.value,)) if ni.value else np.zeros(0, np.uint32)
+            out.append((v, idx))
+        return out
+
+    @property
+    def instance_count(self) -> int:
+        return lib.luz_scene_instance_count(self._h)
+
+    def instance_mesh(self) -> np.ndarray:
+        n = self.instance_count
+        return np.ctypeslib.as_array(lib.luz_scene_instance_mesh(self._h), shape=(n,)).copy()
+
+    def models(self) -> C.Array:
+        n = self.instance_count
+        arr = (Model * n)()
+        C.memmove(arr, lib.luz_scene_models(self._h), C.sizeof(Model) * n)
+        return arr
+
+    def lights(self) -> C.Array:
+        n = lib.luz_scene_light_count(self._h)
+        arr = (Light * max(n, 1))()
+        if n:
+            C.memmove(arr, lib.luz_scene_lights(self._h), C.sizeof(Light) * n)
+        return arr
+
+    @property
+    def light_count(self) -> int:
+        return lib.luz_scene_light_count(self._h)
+
+    def block(self) -> Scene:
+        s = Scene()
+        C.memmove(C.byref(s), lib.luz_scene_block(self._h), C.sizeof(Scene))
+        return s
+
+    def transforms(self) -> np.ndarray:
+        out = np.zeros((self.instance_count, 3, 4), np.float32)
+        _check(lib.luz_scene_instance_transforms(self._h, _abi.ptr(out, _abi.c_float_p)))
+        return out
+
+    def set_sampling(self, ao_samples: int, ao_min: float | None = None, ao_max: float | None = None,
+                     light_samples: int = 1, sampler: int | None = None) -> None:
+        b = self.block()
+        _check(lib.luz_scene_set_sampling(self._h, ao_samples, b.ao_min if ao_min is None else ao_min,
+                                          b.ao_max if ao_max is None else ao_max, light_samples,
+                                          b.sampler if sampler is None else sampler))
+
+    def camera(self) -> Camera:
+        c = Camera()
+        _check(lib.luz_scene_get_camera(self._h, C.byref(c)))
+        return c
+
+    def set_camera(self, cam: Camera) -> None:
+        _check(lib.luz_scene_set_camera(self._h, C.byref(cam)))
+
+    def triangle_count(self) -> int:
+        per = [len(i) // 3 for _, i in self.meshes()]
+        return int(sum(per[m] for m in self.instance_mesh()))
+
+
+# ---------------------------------------------------------------------------- device objects
+class Blas:
+    def __init__(self, ctx: "Context", handle):
+        self.ctx, self._h = ctx, handle
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def prims(self) -> int:
+        return lib.luz_blas_primitive_count(self._h)
+
+    def download(self):
+        n = self.prims
+        m = max(n, 2) - 1
+        nodes = np.zeros((m, 16), np.float32)
+        tris = np.zeros((max(n, 1), 12), np.float32)
+        mort = np.zeros(max(n, 1), np.uint32)
+        order = np.zeros(max(n, 1), np.uint32)
+        _check(lib.luz_blas_download(self.ctx.handle, self._h, _abi.ptr(nodes), _abi.ptr(tris),
+                                     _abi.ptr(mort, _abi.c_u32_p), _abi.ptr(order, _abi.c_u32_p)),
+               self.ctx.handle, "blas download")
+        return nodes, tris[:n], mort[:n], order[:n]
+
+    def close(self):
+        if self._h:
+            lib.luz_blas_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Tlas:
+    def __init__(self, ctx: "Context", max_instances: int):
+        self.ctx = ctx
+        h = C.c_void_p()
+        _check(lib.luz_tlas_create(ctx.handle, max_instances, C.byref(h)), ctx.handle, "tlas create")
+        self._h = h
+        self._instances = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @staticmethod
+    def make_instances(blas: list[Blas], instance_mesh, transforms: np.ndarray, custom=None, mask=None):
+        n = len(instance_mesh)
+        arr = (Instance * max(n, 1))()
+        for i in range(n):
+            arr[i].blas = blas[int(instance_mesh[i])].handle
+            C.memmove(arr[i].transform, transforms[i].astype(np.float32).ctypes.data, 48)
+            arr[i].custom_index = i if custom is None else int(custom[i])
+            arr[i].mask = 0xFF if mask is None else int(mask[i])
+        return arr, n
+
+    def build(self, instances, count: int) -> None:
+        self._instances = instances   # keep alive until the next build
+        _check(lib.luz_tlas_build(self.ctx.handle, self._h, instances, count), self.ctx.handle, "tlas build")
+
+    def download(self):
+        cnt = C.c_uint32()
+        _check(lib.luz_tlas_download(self.ctx.handle, self._h, None, None, None, C.byref(cnt)))
+        m = cnt.value
+        nodes = np.zeros((max(m, 1), 16), np.float32)
+        n = len(self._instances) if self._instances is not None else 0
+        mort = np.zeros(max(n, 1), np.uint32)
+        order = np.zeros(max(n, 1), np.uint32)
+        _check(lib.luz_tlas_download(self.ctx.handle, self._h, _abi.ptr(nodes), _abi.ptr(mort, _abi.c_u32_p),
+                                     _abi.ptr(order, _abi.c_u32_p), C.byref(cnt)), self.ctx.handle, "tlas download")
+        return nodes[:m], mort, order
+
+    def close(self):
+        if self._h:
+            lib.luz_tlas_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Frame:
+    def __init__(self, ctx: "Context", width: int, height: int):
+        self.ctx, self.width, self.height = ctx, width, height
+        h = C.c_void_p()
+        _check(lib.luz_frame_create(ctx.handle, width, height, C.byref(h)), ctx.handle, "frame create")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def upload(self, scene: Scene, lights, light_count: int, models, model_count: int) -> None:
+        _check(lib.luz_frame_upload(self.ctx.handle, self._h, C.byref(scene), lights, light_count, models,
+                                    model_count), self.ctx.handle, "frame upload")
+
+    def gbuffer(self, tlas: Tlas) -> None:
+        _check(lib.luz_gbuffer_primary(self.ctx.handle, self._h, tlas.handle), self.ctx.handle, "gbuffer")
+
+    def trace(self, tlas: Tlas, frame_index: int = 0) -> None:
+        _check(lib.luz_trace_visibility(self.ctx.handle, self._h, tlas.handle, frame_index), self.ctx.handle,
+               "trace visibility")
+
+    def trace_stats(self, tlas: Tlas, frame_index: int = 0) -> dict:
+        out = (C.c_uint64 * 5)()
+        _check(lib.luz_trace_visibility_stats(self.ctx.handle, self._h, tlas.handle, frame_index, out),
+               self.ctx.handle, "trace stats")
+        return {"rays": out[0], "tlas_nodes": out[1], "blas_nodes": out[2], "tris": out[3], "instances": out[4]}
+
+    def ao_resolve(self) -> None:
+        _check(lib.luz_ao_resolve(self.ctx.handle, self._h), self.ctx.handle, "ao resolve")
+
+    def lit_count(self) -> int:
+        n = C.c_uint32()
+        _check(lib.luz_frame_lit_count(self.ctx.handle, self._h, C.byref(n)), self.ctx.handle, "lit count")
+        return n.value
+
+    def light_pass(self, use_denoised_ao: bool = False) -> None:
+        _check(lib.luz_light_pass(self.ctx.handle, self._h, int(use_denoised_ao)), self.ctx.handle, "light pass")
+
+    def plane_bytes(self, plane: int) -> int:
+        return lib.luz_frame_plane_bytes(self._h, plane)
+
+    def read(self, plane: int) -> np.ndarray:
+        dt, comps = PLANE_DTYPES[plane]
+        nbytes = self.plane_bytes(plane)
+        out = np.zeros(max(nbytes // 4, 1), np.uint32).view(dt)
+        if nbytes:
+            _check(lib.luz_frame_read(self.ctx.handle, self._h, plane, _abi.ptr(out), nbytes), self.ctx.handle,
+                   "frame read")
+        out = out[: nbytes // 4]
+        if plane in (PLANE_SHADOW_BITS, PLANE_AO_BITS):
+            words = (self.width * self.height + 31) // 32
+            return out.reshape(-1, words)
+        if comps > 1:
+            return out.reshape(self.height, self.width, comps)
+        return out.reshape(self.height, self.width)
+
+    def write(self, plane: int, data: np.ndarray) -> None:
+        data = np.ascontiguousarray(data)
+        _check(lib.luz_frame_write(self.ctx.handle, self._h, plane, _abi.ptr(data), data.nbytes), self.ctx.handle,
+               "frame write")
+
+    def close(self):
+        if self._h:
+            lib.luz_frame_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Context:
+    """One CUDA device and stream (the reference's global Vulkan context)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(lib.luz_ctx_create(device, C.byref(h)), what="luz_ctx_create")
+        self._h = h
+        self._children = []
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_blue_noise(self, tex: np.ndarray) -> None:
+        tex = np.ascontiguousarray(tex, np.uint8)
+        _check(lib.luz_ctx_set_blue_noise(self._h, _abi.ptr(tex, _abi.c_u8_p), tex.shape[0]), self._h, "blue noise")
+
+    def build_blas(self, meshes: list[tuple[np.ndarray, np.ndarray]]) -> list[Blas]:
+        descs = (BlasDesc * len(meshes))()
+        keep = []
+        for i, (v, idx) in enumerate(meshes):
+            v = np.ascontiguousarray(v, np.float32)
+            idx = np.ascontiguousarray(idx, np.uint32)
+            keep += [v, idx]
+            descs[i].vertices = v.ctypes.data
+            descs[i].vertex_count = v.shape[0]
+            descs[i].vertex_stride = v.shape[1] * 4 if v.ndim == 2 else 48
+            descs[i].indices = idx.ctypes.data
+            descs[i].index_count = idx.size
+        outs = (C.c_void_p * len(meshes))()
+        _check(lib.luz_blas_build_batch(self._h, len(meshes), descs, outs), self._h, "blas build")
+        return [Blas(self, C.c_void_p(outs[i])) for i in range(len(meshes))]
+
+    def tlas(self, max_instances: int) -> Tlas:
+        return Tlas(self, max_instances)
+
+    def frame(self, width: int, height: int) -> Frame:
+        return Frame(self, width, height)
+
+    def synchronize(self) -> None:
+        _check(lib.luz_ctx_synchronize(self._h), self._h, "synchronize")
+
+    def device_status(self) -> int:
+        bits = C.c_uint32()
+        _check(lib.luz_ctx_device_status(self._h, C.byref(bits)), self._h, "device status")
+        return bits.value
+
+    def launch_count(self) -> int:
+        return lib.luz_ctx_launch_count(self._h)
+
+    def close(self):
+        if self._h:
+            lib.luz_ctx_destroy(self._h)
+            self._h = None
+
+
+# ---------------------------------------------------------------------------- GPUScene mirror
+class GPUScene:
+    """Host orchestration of the path, mirroring the reference's GPUScene
+    (AddMesh / UpdateResources / UpdateResourcesGPU, GPUScene.cpp:108-366) and the
+    frame order of LuzApplication::RenderFrame (main.cpp:223-311): TLAS rebuild,
+    opaque (primary-ray G-buffer) pass, light pass with ray-traced visibility."""
+
+    def __init__(self, ctx: Context, scene: HostScene, blue_noise_seed: int = 7):
+        self.ctx, self.scene = ctx, scene
+        ctx.set_blue_noise(blue_noise(blue_noise_seed))
+        self.blas = ctx.build_blas(scene.meshes())                  # AddMesh for every mesh
+        self.tlas = ctx.tlas(max(scene.instance_count, 1))          # CreateTLAS
+        self.frame = ctx.frame(scene.width, scene.height)           # DeferredRenderer::CreateImages
+        self.update_resources()
+
+    def update_resources(self) -> None:
+        """UpdateResources: pack ModelBlocks, SceneBlock and LightBlocks (host)."""
+        s = self.scene
+        self.models = s.models()
+        self.lights = s.lights()
+        self.block = s.block()
+        self.instances, self.n_instances = Tlas.make_instances(self.blas, s.instance_mesh(), s.transforms())
+
+    def update_resources_gpu(self) -> None:
+        """UpdateResourcesGPU: copy the blocks to the device and rebuild the TLAS."""
+        self.frame.upload(self.block, self.lights, self.scene.light_count, self.models, self.scene.instance_count)
+        self.tlas.build(self.instances, self.n_instances)
+
+    def render(self, frame_index: int = 0, use_denoised_ao: bool = False) -> None:
+        self.update_resources_gpu()
+        self.frame.gbuffer(self.tlas)
+        self.frame.trace(self.tlas, frame_index)
+        self.frame.light_pass(use_denoised_ao)
+
+    def render_frame(self, frame_index: int = 0) -> None:
+        """The whole frame in one C call (TLAS build + G-buffer + visibility + light pass)."""
+        _check(lib.luz_render_frame(self.ctx.handle, self.frame.handle, self.tlas.handle, self.instances,
+                                    self.n_instances, frame_index), self.ctx.handle, "render frame")

@@ -1,0 +1,176 @@
+"""ctypes mirror of include/luz.h and include/luz_scene.h.
+
+The structures below are byte-for-byte the C structs of the C ABI; tests assert
+their sizes against the header's static assertions.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libluz_gb300.so"
+
+c_float_p = C.POINTER(C.c_float)
+c_u32_p = C.POINTER(C.c_uint32)
+c_u8_p = C.POINTER(C.c_uint8)
+
+LUZ_OK = 0
+STATUS_NAMES = {0: "LUZ_OK", 1: "LUZ_ERR_INVALID", 2: "LUZ_ERR_CUDA", 3: "LUZ_ERR_OOM",
+                4: "LUZ_ERR_DEVICE", 5: "LUZ_ERR_LIMIT", 6: "LUZ_ERR_NO_DEVICE"}
+
+LIGHT_POINT, LIGHT_SPOT, LIGHT_DIRECTIONAL = 0, 1, 2
+SHADOW_DISABLED, SHADOW_RAYTRACING, SHADOW_MAP = 0, 1, 2
+SAMPLER_PARITY, SAMPLER_STRATIFIED = 0, 1
+BLUE_NOISE_SIZE = 128
+
+PLANE_ALBEDO, PLANE_NORMAL, PLANE_MATERIAL, PLANE_EMISSION, PLANE_DEPTH, PLANE_LIGHT = range(6)
+PLANE_SHADOW_BITS, PLANE_AO_BITS, PLANE_AO, PLANE_AO_DENOISED, PLANE_PRIMARY_HIT = range(6, 11)
+PLANE_DTYPES = {PLANE_ALBEDO: (np.uint32, 1), PLANE_NORMAL: (np.float32, 4), PLANE_MATERIAL: (np.uint32, 1),
+                PLANE_EMISSION: (np.uint32, 1), PLANE_DEPTH: (np.float32, 1), PLANE_LIGHT: (np.float32, 4),
+                PLANE_SHADOW_BITS: (np.uint32, 1), PLANE_AO_BITS: (np.uint32, 1), PLANE_AO: (np.float32, 1),
+                PLANE_AO_DENOISED: (np.float32, 1), PLANE_PRIMARY_HIT: (np.uint32, 2)}
+
+
+class Vertex(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("normal", C.c_float * 3), ("tangent", C.c_float * 4),
+                ("texcoord", C.c_float * 2)]
+
+
+class Light(C.Structure):
+    _fields_ = [("color", C.c_float * 3), ("intensity", C.c_float), ("position", C.c_float * 3),
+                ("inner_angle", C.c_float), ("direction", C.c_float * 3), ("outer_angle", C.c_float),
+                ("type", C.c_int32), ("num_shadow_samples", C.c_int32), ("radius", C.c_float),
+                ("shadow_map", C.c_int32)]
+
+
+class Model(C.Structure):
+    _fields_ = [("model_mat", C.c_float * 16), ("color", C.c_float * 4), ("emission", C.c_float * 3),
+                ("metallic", C.c_float), ("roughness", C.c_float), ("ao_map", C.c_int32),
+                ("color_map", C.c_int32), ("normal_map", C.c_int32), ("emission_map", C.c_int32),
+                ("metallic_roughness_map", C.c_int32), ("vertex_buffer", C.c_int32),
+                ("index_buffer", C.c_int32)]
+
+
+class Scene(C.Structure):
+    _fields_ = [("ambient_light_color", C.c_float * 3), ("ambient_light_intensity", C.c_float),
+                ("proj", C.c_float * 16), ("view", C.c_float * 16), ("view_proj", C.c_float * 16),
+                ("prev_view_proj", C.c_float * 16), ("inverse_proj", C.c_float * 16),
+                ("inverse_view", C.c_float * 16), ("jitter", C.c_float * 2), ("prev_jitter", C.c_float * 2),
+                ("cam_pos", C.c_float * 3), ("num_lights", C.c_int32), ("ao_min", C.c_float),
+                ("ao_max", C.c_float), ("exposure", C.c_float), ("ao_num_samples", C.c_int32),
+                ("white_texture", C.c_int32), ("black_texture", C.c_int32),
+                ("blue_noise_texture", C.c_int32), ("tlas_rid", C.c_int32), ("shadow_type", C.c_int32),
+                ("sampler", C.c_int32), ("pad", C.c_int32 * 2)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("blas", C.c_void_p), ("transform", (C.c_float * 4) * 3), ("custom_index", C.c_uint32),
+                ("mask", C.c_uint32)]
+
+
+class BlasDesc(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("vertex_count", C.c_uint32), ("vertex_stride", C.c_uint32),
+                ("indices", C.c_void_p), ("index_count", C.c_uint32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("camera_type", C.c_int32), ("mode", C.c_int32), ("eye", C.c_float * 3),
+                ("center", C.c_float * 3), ("rotation", C.c_float * 3), ("zoom", C.c_float),
+                ("far_distance", C.c_float), ("near_distance", C.c_float), ("horizontal_fov", C.c_float),
+                ("ortho_far_distance", C.c_float), ("ortho_near_distance", C.c_float),
+                ("extent", C.c_float * 2), ("jitter", C.c_float * 2)]
+
+
+class GenParams(C.Structure):
+    _fields_ = [("config", C.c_int32), ("pad0", C.c_uint32), ("seed", C.c_uint64), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("ao_samples", C.c_int32), ("ao_max", C.c_float),
+                ("light_samples", C.c_int32), ("sampler", C.c_int32), ("meshes", C.c_uint32),
+                ("instances", C.c_uint32), ("subdivisions", C.c_uint32), ("point_lights", C.c_uint32),
+                ("spot_lights", C.c_uint32), ("directional_lights", C.c_uint32), ("triangles", C.c_uint32),
+                ("pad1", C.c_uint32)]
+
+
+# (name, restype, argtypes) of every entry point declared in include/*.h
+P = C.c_void_p
+SIGNATURES = [
+    ("luz_ctx_create", C.c_int32, [C.c_int, C.POINTER(P)]),
+    ("luz_ctx_destroy", None, [P]),
+    ("luz_last_error", C.c_char_p, [P]),
+    ("luz_ctx_synchronize", C.c_int32, [P]),
+    ("luz_ctx_device_status", C.c_int32, [P, c_u32_p]),
+    ("luz_ctx_launch_count", C.c_uint64, [P]),
+    ("luz_ctx_set_stream", C.c_int32, [P, P]),
+    ("luz_ctx_set_blue_noise", C.c_int32, [P, c_u8_p, C.c_uint32]),
+    ("luz_blas_build", C.c_int32, [P, C.POINTER(BlasDesc), C.POINTER(P)]),
+    ("luz_blas_build_batch", C.c_int32, [P, C.c_uint32, C.POINTER(BlasDesc), C.POINTER(P)]),
+    ("luz_blas_destroy", None, [P]),
+    ("luz_blas_primitive_count", C.c_uint32, [P]),
+    ("luz_blas_download", C.c_int32, [P, P, P, P, c_u32_p, c_u32_p]),
+    ("luz_tlas_create", C.c_int32, [P, C.c_uint32, C.POINTER(P)]),
+    ("luz_tlas_build", C.c_int32, [P, P, C.POINTER(Instance), C.c_uint32]),
+    ("luz_tlas_destroy", None, [P]),
+    ("luz_tlas_download", C.c_int32, [P, P, P, c_u32_p, c_u32_p, c_u32_p]),
+    ("luz_frame_create", C.c_int32, [P, C.c_uint32, C.c_uint32, C.POINTER(P)]),
+    ("luz_frame_destroy", None, [P]),
+    ("luz_frame_upload", C.c_int32, [P, P, C.POINTER(Scene), C.POINTER(Light), C.c_uint32,
+                                     C.POINTER(Model), C.c_uint32]),
+    ("luz_gbuffer_primary", C.c_int32, [P, P, P]),
+    ("luz_trace_visibility", C.c_int32, [P, P, P, C.c_int32]),
+    ("luz_trace_visibility_stats", C.c_int32, [P, P, P, C.c_int32, C.POINTER(C.c_uint64)]),
+    ("luz_ao_resolve", C.c_int32, [P, P]),
+    ("luz_frame_lit_count", C.c_int32, [P, P, c_u32_p]),
+    ("luz_light_pass", C.c_int32, [P, P, C.c_int32]),
+    ("luz_render_frame", C.c_int32, [P, P, P, C.POINTER(Instance), C.c_uint32, C.c_int32]),
+    ("luz_frame_plane_bytes", C.c_size_t, [P, C.c_int32]),
+    ("luz_frame_read", C.c_int32, [P, P, C.c_int32, P, C.c_size_t]),
+    ("luz_frame_write", C.c_int32, [P, P, C.c_int32, P, C.c_size_t]),
+    ("luz_frame_plane_device_ptr", P, [P, C.c_int32]),
+    # luz_scene.h
+    ("luz_scene_default_params", C.c_int32, [C.c_int32, C.POINTER(GenParams)]),
+    ("luz_scene_generate", C.c_int32, [C.POINTER(GenParams), C.POINTER(P)]),
+    ("luz_scene_destroy", None, [P]),
+    ("luz_scene_mesh_count", C.c_uint32, [P]),
+    ("luz_scene_mesh", C.c_int32, [P, C.c_uint32, C.POINTER(C.POINTER(Vertex)), c_u32_p,
+                                   C.POINTER(c_u32_p), c_u32_p]),
+    ("luz_scene_instance_count", C.c_uint32, [P]),
+    ("luz_scene_instance_mesh", c_u32_p, [P]),
+    ("luz_scene_models", C.POINTER(Model), [P]),
+    ("luz_scene_light_count", C.c_uint32, [P]),
+    ("luz_scene_lights", C.POINTER(Light), [P]),
+    ("luz_scene_block", C.POINTER(Scene), [P]),
+    ("luz_scene_width", C.c_uint32, [P]),
+    ("luz_scene_height", C.c_uint32, [P]),
+    ("luz_scene_instance_transforms", C.c_int32, [P, c_float_p]),
+    ("luz_scene_set_camera", C.c_int32, [P, C.POINTER(Camera)]),
+    ("luz_scene_get_camera", C.c_int32, [P, C.POINTER(Camera)]),
+    ("luz_scene_set_sampling", C.c_int32, [P, C.c_int32, C.c_float, C.c_float, C.c_int32, C.c_int32]),
+    ("luz_compose_transform", None, [c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
+    ("luz_camera_matrices", None, [C.POINTER(Camera), c_float_p, c_float_p]),
+    ("luz_blue_noise_generate", C.c_int32, [C.c_uint64, C.c_uint32, c_u8_p]),
+]
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the in-tree libluz_gb300.so. Raises if it was not built: there is no
+    fallback implementation of any entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: run luz_gb300.build.build() (needs nvcc)")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def ptr(a: np.ndarray, t=C.c_void_p):
+    return C.cast(a.ctypes.data, t)

@@ -1,0 +1,466 @@
+// capi.cu — the extern "C" entry points of include/luz.h: context, BLAS/TLAS
+// handles, frames, uploads and read-back.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "internal.cuh"
+
+namespace luz {
+luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* descs, luz_blas** out);
+luz_status tlas_alloc(luz_ctx* ctx, luz_tlas* t);
+luz_status build_tlas(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint32_t n);
+luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t);
+luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int frame_index,
+                             unsigned long long* d_stats);
+luz_status frame_lit_count(luz_ctx* ctx, luz_frame* f, uint32_t* count);
+luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised);
+luz_status launch_ao_resolve(luz_ctx* ctx, luz_frame* f);
+luz_status upload_srgb_lut(luz_ctx* ctx, const float* lut);
+
+luz_status set_error(luz_ctx* ctx, luz_status st, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return st;
+}
+luz_status cuda_error(luz_ctx* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    luz_status st = LUZ_ERR_CUDA;
+    if (e == cudaErrorMemoryAllocation) st = LUZ_ERR_OOM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) st = LUZ_ERR_NO_DEVICE;
+    return set_error(ctx, st, m);
+}
+luz_status check_launch(luz_ctx* ctx, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(ctx, e, what);
+    return LUZ_OK;
+}
+luz_status ensure_scratch(luz_ctx* ctx, size_t bytes) {
+    if (bytes <= ctx->scratch_bytes) return LUZ_OK;
+    if (ctx->d_scratch) {
+        LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->d_scratch);
+        ctx->d_scratch = nullptr;
+        ctx->scratch_bytes = 0;
+    }
+    size_t b = std::max(bytes, (size_t)1 << 20);
+    LUZ_CUDA(ctx, cudaMalloc(&ctx->d_scratch, b));
+    ctx->scratch_bytes = b;
+    return LUZ_OK;
+}
+
+static void free_frame_buffers(luz_frame* f) {
+    void* ptrs[] = {f->albedo, f->normal, f->material, f->emission, f->depth, f->light,
+                    f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->surf,
+                    f->block_counts, f->lit_count, f->d_scene, f->d_lights, f->d_models,
+                    f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+}
+
+// (Re)allocates *p for at least `need` elements when `cap` is short; cap is updated.
+static luz_status grow(luz_ctx* ctx, void** p, uint32_t& cap, uint32_t need, size_t elem) {
+    if (need <= cap && *p) return LUZ_OK;
+    uint32_t n = std::max(need, std::max(cap * 2, 16u));
+    if (*p) {
+        LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    LUZ_CUDA(ctx, cudaMalloc(p, (size_t)n * elem));
+    cap = n;
+    return LUZ_OK;
+}
+
+}  // namespace luz
+
+using namespace luz;
+
+extern "C" {
+
+luz_status luz_ctx_create(int device, luz_ctx** out) {
+    if (!out) return LUZ_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return LUZ_ERR_NO_DEVICE;
+    if (device < 0 || device >= n) return LUZ_ERR_INVALID;
+    luz_ctx* ctx = new luz_ctx();
+    ctx->device = device;
+    auto fail = [&](luz_status s) { luz_ctx_destroy(ctx); return s; };
+    if (cudaSetDevice(device) != cudaSuccess) return fail(LUZ_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(LUZ_ERR_CUDA);
+    ctx->stream = ctx->own_stream;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaMalloc(&ctx->d_status, 4) != cudaSuccess) return fail(LUZ_ERR_OOM);
+    cudaMemset(ctx->d_status, 0, 4);
+    float lut[256];
+    for (int i = 0; i < 256; ++i) lut[i] = (float)std::pow((double)((float)i / 255.0f), 2.2);
+    if (upload_srgb_lut(ctx, lut) != LUZ_OK) return fail(LUZ_ERR_CUDA);
+    // Default substitute blue noise: a flat mid-grey texel (callers upload the seeded one).
+    uint8_t grey[4] = {128, 128, 128, 255};
+    if (luz_ctx_set_blue_noise(ctx, grey, 1) != LUZ_OK) return fail(LUZ_ERR_CUDA);
+    *out = ctx;
+    return LUZ_OK;
+}
+
+void luz_ctx_destroy(luz_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->d_blue_noise) cudaFree(ctx->d_blue_noise);
+    if (ctx->d_scratch) cudaFree(ctx->d_scratch);
+    if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+const char* luz_last_error(const luz_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+luz_status luz_ctx_synchronize(luz_ctx* ctx) {
+    if (!ctx) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LUZ_OK;
+}
+
+luz_status luz_ctx_device_status(luz_ctx* ctx, uint32_t* bits) {
+    if (!ctx || !bits) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    LUZ_CUDA(ctx, cudaMemcpy(bits, ctx->d_status, 4, cudaMemcpyDeviceToHost));
+    LUZ_CUDA(ctx, cudaMemset(ctx->d_status, 0, 4));
+    return LUZ_OK;
+}
+
+uint64_t luz_ctx_launch_count(const luz_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+luz_status luz_ctx_set_stream(luz_ctx* ctx, void* stream) {
+    if (!ctx) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return LUZ_OK;
+}
+
+luz_status luz_ctx_set_blue_noise(luz_ctx* ctx, const uint8_t* rgba8, uint32_t size) {
+    if (!ctx || !rgba8 || size == 0 || size > 4096) return LUZ_ERR_INVALID;
+    if (ctx->d_blue_noise) {
+        LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->d_blue_noise);
+        ctx->d_blue_noise = nullptr;
+    }
+    LUZ_CUDA(ctx, cudaMalloc(&ctx->d_blue_noise, (size_t)size * size * 4));
+    LUZ_CUDA(ctx, cudaMemcpy(ctx->d_blue_noise, rgba8, (size_t)size * size * 4, cudaMemcpyHostToDevice));
+    ctx->blue_noise_size = size;
+    return LUZ_OK;
+}
+
+// ------------------------------------------------------------------ BLAS
+luz_status luz_blas_build(luz_ctx* ctx, const luz_blas_desc* desc, luz_blas** out) {
+    if (!ctx || !desc || !out) return LUZ_ERR_INVALID;
+    return build_blas_batch(ctx, 1, desc, out);
+}
+
+luz_status luz_blas_build_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* descs, luz_blas** out) {
+    if (!ctx || !descs || !out || count == 0) return LUZ_ERR_INVALID;
+    if (count > (1u << 18)) return set_error(ctx, LUZ_ERR_LIMIT, "more than 2^18 BLAS in one batch");
+    return build_blas_batch(ctx, count, descs, out);
+}
+
+void luz_blas_destroy(luz_blas* b) {
+    if (!b) return;
+    if (b->arena && --b->arena->refs == 0) {
+        if (b->ctx && b->ctx->stream) cudaStreamSynchronize(b->ctx->stream);
+        cudaFree(b->arena->base);
+        delete b->arena;
+    }
+    delete b;
+}
+
+uint32_t luz_blas_primitive_count(const luz_blas* b) { return b ? b->prims : 0; }
+
+luz_status luz_blas_download(luz_ctx* ctx, const luz_blas* b, void* nodes, void* tris,
+                             uint32_t* morton_sorted, uint32_t* order) {
+    if (!ctx || !b) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t n = b->prims, m = std::max(n, 2u) - 1;
+    if (nodes) LUZ_CUDA(ctx, cudaMemcpy(nodes, b->nodes, (size_t)m * 64, cudaMemcpyDeviceToHost));
+    if (tris && n) LUZ_CUDA(ctx, cudaMemcpy(tris, b->tris, (size_t)n * 48, cudaMemcpyDeviceToHost));
+    if (morton_sorted && n) LUZ_CUDA(ctx, cudaMemcpy(morton_sorted, b->morton, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    if (order && n) LUZ_CUDA(ctx, cudaMemcpy(order, b->order, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    return LUZ_OK;
+}
+
+// ------------------------------------------------------------------ TLAS
+luz_status luz_tlas_create(luz_ctx* ctx, uint32_t max_instances, luz_tlas** out) {
+    if (!ctx || !out || max_instances == 0) return LUZ_ERR_INVALID;
+    if (max_instances > (1u << 24)) return set_error(ctx, LUZ_ERR_LIMIT, "max_instances above 2^24");
+    luz_tlas* t = new luz_tlas();
+    t->ctx = ctx;
+    t->max_instances = max_instances;
+    luz_status s = tlas_alloc(ctx, t);
+    if (s == LUZ_OK && cudaEventCreateWithFlags(&t->input_copied, cudaEventDisableTiming) != cudaSuccess)
+        s = set_error(ctx, LUZ_ERR_CUDA, "cudaEventCreate");
+    if (s != LUZ_OK) { luz_tlas_destroy(t); return s; }
+    *out = t;
+    return LUZ_OK;
+}
+
+luz_status luz_tlas_build(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint32_t count) {
+    if (!ctx || !t || (count && !inst)) return LUZ_ERR_INVALID;
+    // The pinned staging buffer may still be read by the previous build's copy.
+    LUZ_CUDA(ctx, cudaEventSynchronize(t->input_copied));
+    luz_status s = build_tlas(ctx, t, inst, count);
+    if (s != LUZ_OK) return s;
+    t->node_count = std::max(count, 2u) - 1;
+    LUZ_CUDA(ctx, cudaEventRecord(t->input_copied, ctx->stream));
+    return LUZ_OK;
+}
+
+void luz_tlas_destroy(luz_tlas* t) {
+    if (!t) return;
+    if (t->ctx && t->ctx->stream) cudaStreamSynchronize(t->ctx->stream);
+    if (t->nodes) cudaFree(t->nodes);
+    if (t->instances) cudaFree(t->instances);
+    if (t->shade) cudaFree(t->shade);
+    if (t->d_input) cudaFree(t->d_input);
+    if (t->h_input) cudaFreeHost(t->h_input);
+    if (t->morton) cudaFree(t->morton);
+    if (t->order) cudaFree(t->order);
+    if (t->tmp) cudaFree(t->tmp);
+    if (t->input_copied) cudaEventDestroy(t->input_copied);
+    delete t;
+}
+
+luz_status luz_tlas_download(luz_ctx* ctx, const luz_tlas* t, void* nodes, uint32_t* morton_sorted,
+                             uint32_t* order, uint32_t* node_count) {
+    if (!ctx || !t) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t n = t->count, m = n ? std::max(n, 2u) - 1 : 0;
+    if (node_count) *node_count = m;
+    if (nodes && m) LUZ_CUDA(ctx, cudaMemcpy(nodes, t->nodes, (size_t)m * 64, cudaMemcpyDeviceToHost));
+    if (morton_sorted && n) LUZ_CUDA(ctx, cudaMemcpy(morton_sorted, t->morton, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    if (order && n) LUZ_CUDA(ctx, cudaMemcpy(order, t->order, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    return LUZ_OK;
+}
+
+// ------------------------------------------------------------------ frame
+luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_frame** out) {
+    if (!ctx || !out || width == 0 || height == 0) return LUZ_ERR_INVALID;
+    if ((uint64_t)width * height > (1ull << 27))
+        return set_error(ctx, LUZ_ERR_LIMIT, "frame larger than 2^27 pixels");
+    luz_frame* f = new luz_frame();
+    f->ctx = ctx;
+    f->width = width;
+    f->height = height;
+    f->pixels = width * height;
+    f->words = (f->pixels + 31) / 32;
+    size_t P = f->pixels;
+    uint32_t chunks = (f->pixels + 1023) / 1024;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, std::max(bytes, (size_t)16)); };
+    A((void**)&f->albedo, P * 4);
+    A((void**)&f->normal, P * 16);
+    A((void**)&f->material, P * 4);
+    A((void**)&f->emission, P * 4);
+    A((void**)&f->depth, P * 4);
+    A((void**)&f->light, P * 16);
+    A((void**)&f->primary_hit, P * 8);
+    A((void**)&f->ao, P * 4);
+    A((void**)&f->ao_denoised, P * 4);
+    A((void**)&f->surf, P * 32);
+    A((void**)&f->block_counts, (size_t)chunks * 4);
+    A((void**)&f->lit_count, 4);
+    A((void**)&f->d_scene, sizeof(luz_scene));
+    A((void**)&f->work_counter, 8);
+    if (e != cudaSuccess) {
+        free_frame_buffers(f);
+        delete f;
+        return cuda_error(ctx, e, "cudaMalloc(frame)");
+    }
+    cudaMemset(f->ao_denoised, 0, P * 4);
+    *out = f;
+    return LUZ_OK;
+}
+
+void luz_frame_destroy(luz_frame* f) {
+    if (!f) return;
+    if (f->ctx && f->ctx->stream) cudaStreamSynchronize(f->ctx->stream);
+    free_frame_buffers(f);
+    delete f;
+}
+
+luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, const luz_light* lights,
+                            uint32_t light_count, const luz_model* models, uint32_t model_count) {
+    if (!ctx || !f || !scene || (light_count && !lights) || (model_count && !models))
+        return LUZ_ERR_INVALID;
+    if (scene->shadow_type == LUZ_SHADOW_MAP)
+        return set_error(ctx, LUZ_ERR_INVALID, "shadow maps are not part of the ray-traced path");
+    if (scene->ao_num_samples < 0 || scene->ao_num_samples > LUZ_MAX_AO_SAMPLES)
+        return set_error(ctx, LUZ_ERR_LIMIT, "ao_num_samples outside [0, LUZ_MAX_AO_SAMPLES]");
+    if (light_count > 65535) return set_error(ctx, LUZ_ERR_LIMIT, "more than 65535 lights");
+    // Shadow slots: Σ numShadowSamples (GPUScene.cpp:248), one bit plane each.
+    std::vector<uint32_t> slot_table, light_slot(std::max(light_count, 1u));
+    for (uint32_t l = 0; l < light_count; ++l) {
+        light_slot[l] = (uint32_t)slot_table.size();
+        int ns = scene->shadow_type == LUZ_SHADOW_RAYTRACING ? lights[l].num_shadow_samples : 0;
+        if (ns < 0) ns = 0;
+        if (slot_table.size() + ns > LUZ_MAX_SHADOW_SLOTS)
+            return set_error(ctx, LUZ_ERR_LIMIT, "more than LUZ_MAX_SHADOW_SLOTS shadow samples per pixel");
+        for (int s = 0; s < ns; ++s) slot_table.push_back(l | ((uint32_t)s << 16));
+    }
+    cudaStream_t st = ctx->stream;
+    uint32_t shadow_slots = (uint32_t)slot_table.size();
+    uint32_t ao = (uint32_t)scene->ao_num_samples;
+    uint32_t cap_shadow = f->shadow_planes_cap, cap_ao = f->ao_planes_cap;
+    luz_status s;
+    if ((s = grow(ctx, (void**)&f->shadow_bits, cap_shadow, std::max(shadow_slots, 1u), (size_t)f->words * 4)) != LUZ_OK) return s;
+    if ((s = grow(ctx, (void**)&f->ao_bits, cap_ao, std::max(ao, 1u), (size_t)f->words * 4)) != LUZ_OK) return s;
+    f->shadow_planes_cap = cap_shadow;
+    f->ao_planes_cap = cap_ao;
+    static_assert(sizeof(luz_light) == 64, "luz_light layout");
+    static_assert(sizeof(luz_model) == 128, "luz_model layout");
+    static_assert(sizeof(luz_vertex) == 48, "luz_vertex layout");
+    if (light_count > f->lights_cap || !f->d_lights) {
+        uint32_t cap = 0, cap2 = 0;
+        if ((s = grow(ctx, (void**)&f->d_lights, cap, std::max(light_count, 1u), sizeof(luz_light))) != LUZ_OK) return s;
+        if ((s = grow(ctx, (void**)&f->d_light_slot, cap2, cap, 4)) != LUZ_OK) return s;
+        f->lights_cap = cap;
+    }
+    if (model_count > f->models_cap || !f->d_models) {
+        uint32_t cap = 0, cap2 = 0;
+        if ((s = grow(ctx, (void**)&f->d_models, cap, std::max(model_count, 1u), sizeof(luz_model))) != LUZ_OK) return s;
+        if ((s = grow(ctx, (void**)&f->d_model_skip, cap2, cap, 1)) != LUZ_OK) return s;
+        f->models_cap = cap;
+    }
+    if (!f->d_slot_table) LUZ_CUDA(ctx, cudaMalloc(&f->d_slot_table, (size_t)LUZ_MAX_SHADOW_SLOTS * 4));
+    f->h_slot_table = slot_table;
+    std::vector<uint8_t> skip(std::max(model_count, 1u), 0);
+    for (uint32_t m = 0; m < model_count; ++m)
+        skip[m] = (models[m].color_map < 0 && models[m].color[3] < 0.5f) ? 1 : 0;
+    f->h_scene = *scene;
+    f->light_count = light_count;
+    f->model_count = model_count;
+    f->shadow_slots = shadow_slots;
+    f->ao_samples = ao;
+    LUZ_CUDA(ctx, cudaMemcpyAsync(f->d_scene, scene, sizeof(luz_scene), cudaMemcpyHostToDevice, st));
+    if (light_count) {
+        LUZ_CUDA(ctx, cudaMemcpyAsync(f->d_lights, lights, (size_t)light_count * sizeof(luz_light), cudaMemcpyHostToDevice, st));
+        LUZ_CUDA(ctx, cudaMemcpyAsync(f->d_light_slot, light_slot.data(), (size_t)light_count * 4, cudaMemcpyHostToDevice, st));
+    }
+    if (shadow_slots)
+        LUZ_CUDA(ctx, cudaMemcpyAsync(f->d_slot_table, slot_table.data(), (size_t)shadow_slots * 4, cudaMemcpyHostToDevice, st));
+    if (model_count) {
+        LUZ_CUDA(ctx, cudaMemcpyAsync(f->d_models, models, (size_t)model_count * sizeof(luz_model), cudaMemcpyHostToDevice, st));
+        LUZ_CUDA(ctx, cudaMemcpyAsync(f->d_model_skip, skip.data(), model_count, cudaMemcpyHostToDevice, st));
+    }
+    // Pageable sources: the copies above are staged before returning; the vectors
+    // may go out of scope once the stream has consumed them.
+    LUZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return LUZ_OK;
+}
+
+luz_status luz_gbuffer_primary(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
+    if (!ctx || !f || !t) return LUZ_ERR_INVALID;
+    return launch_gbuffer(ctx, f, t);
+}
+
+luz_status luz_trace_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int32_t frame_index) {
+    if (!ctx || !f || !t) return LUZ_ERR_INVALID;
+    return launch_visibility(ctx, f, t, frame_index, nullptr);
+}
+
+luz_status luz_trace_visibility_stats(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int32_t frame_index,
+                                      uint64_t out[5]) {
+    if (!ctx || !f || !t || !out) return LUZ_ERR_INVALID;
+    unsigned long long* d = nullptr;
+    LUZ_CUDA(ctx, cudaMalloc(&d, 5 * sizeof(unsigned long long)));
+    luz_status s = launch_visibility(ctx, f, t, frame_index, d);
+    if (s == LUZ_OK) {
+        cudaError_t e = cudaMemcpyAsync(out, d, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) s = cuda_error(ctx, e, "stats read-back");
+    }
+    cudaFree(d);
+    return s;
+}
+
+luz_status luz_ao_resolve(luz_ctx* ctx, luz_frame* f) {
+    if (!ctx || !f) return LUZ_ERR_INVALID;
+    return launch_ao_resolve(ctx, f);
+}
+
+luz_status luz_frame_lit_count(luz_ctx* ctx, luz_frame* f, uint32_t* count) {
+    if (!ctx || !f || !count) return LUZ_ERR_INVALID;
+    return frame_lit_count(ctx, f, count);
+}
+
+luz_status luz_light_pass(luz_ctx* ctx, luz_frame* f, int32_t use_denoised_ao) {
+    if (!ctx || !f) return LUZ_ERR_INVALID;
+    return launch_light_pass(ctx, f, use_denoised_ao);
+}
+
+luz_status luz_render_frame(luz_ctx* ctx, luz_frame* f, luz_tlas* t, const luz_instance* instances,
+                            uint32_t instance_count, int32_t frame_index) {
+    if (!ctx || !f || !t) return LUZ_ERR_INVALID;
+    luz_status s;
+    if ((s = luz_tlas_build(ctx, t, instances, instance_count)) != LUZ_OK) return s;
+    if ((s = launch_gbuffer(ctx, f, t)) != LUZ_OK) return s;
+    if ((s = launch_visibility(ctx, f, t, frame_index, nullptr)) != LUZ_OK) return s;
+    return launch_light_pass(ctx, f, 0);
+}
+
+size_t luz_frame_plane_bytes(const luz_frame* f, int32_t plane) {
+    if (!f) return 0;
+    size_t P = f->pixels;
+    switch (plane) {
+        case LUZ_PLANE_ALBEDO: case LUZ_PLANE_MATERIAL: case LUZ_PLANE_EMISSION: case LUZ_PLANE_DEPTH:
+        case LUZ_PLANE_AO: case LUZ_PLANE_AO_DENOISED: return P * 4;
+        case LUZ_PLANE_NORMAL: case LUZ_PLANE_LIGHT: return P * 16;
+        case LUZ_PLANE_PRIMARY_HIT: return P * 8;
+        case LUZ_PLANE_SHADOW_BITS: return (size_t)f->shadow_slots * f->words * 4;
+        case LUZ_PLANE_AO_BITS: return (size_t)f->ao_samples * f->words * 4;
+        default: return 0;
+    }
+}
+
+void* luz_frame_plane_device_ptr(luz_frame* f, int32_t plane) {
+    if (!f) return nullptr;
+    switch (plane) {
+        case LUZ_PLANE_ALBEDO: return f->albedo;
+        case LUZ_PLANE_NORMAL: return f->normal;
+        case LUZ_PLANE_MATERIAL: return f->material;
+        case LUZ_PLANE_EMISSION: return f->emission;
+        case LUZ_PLANE_DEPTH: return f->depth;
+        case LUZ_PLANE_LIGHT: return f->light;
+        case LUZ_PLANE_SHADOW_BITS: return f->shadow_bits;
+        case LUZ_PLANE_AO_BITS: return f->ao_bits;
+        case LUZ_PLANE_AO: return f->ao;
+        case LUZ_PLANE_AO_DENOISED: return f->ao_denoised;
+        case LUZ_PLANE_PRIMARY_HIT: return f->primary_hit;
+        default: return nullptr;
+    }
+}
+
+luz_status luz_frame_read(luz_ctx* ctx, luz_frame* f, int32_t plane, void* dst, size_t bytes) {
+    if (!ctx || !f || !dst) return LUZ_ERR_INVALID;
+    size_t need = luz_frame_plane_bytes(f, plane);
+    void* src = luz_frame_plane_device_ptr(f, plane);
+    if (!src || bytes < need) return set_error(ctx, LUZ_ERR_INVALID, "bad plane or short buffer");
+    if (need == 0) return LUZ_OK;
+    LUZ_CUDA(ctx, cudaMemcpyAsync(dst, src, need, cudaMemcpyDeviceToHost, ctx->stream));
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LUZ_OK;
+}
+
+luz_status luz_frame_write(luz_ctx* ctx, luz_frame* f, int32_t plane, const void* src, size_t bytes) {
+    if (!ctx || !f || !src) return LUZ_ERR_INVALID;
+    size_t need = luz_frame_plane_bytes(f, plane);
+    void* dst = luz_frame_plane_device_ptr(f, plane);
+    if (!dst || bytes != need) return set_error(ctx, LUZ_ERR_INVALID, "bad plane or size mismatch");
+    if (need == 0) return LUZ_OK;
+    LUZ_CUDA(ctx, cudaMemcpyAsync(dst, src, need, cudaMemcpyHostToDevice, ctx->stream));
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LUZ_OK;
+}
+
+}  // extern "C"

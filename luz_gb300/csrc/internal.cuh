@@ -1,0 +1,173 @@
+// internal.cuh — device records, handle structs and error plumbing of libluz_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/luz.h"
+#include "pathmath.cuh"
+
+namespace luz {
+
+// ---------------------------------------------------------------- BVH layout
+// A BVH node holds the boxes of its two children, 64 B = 4 x float4:
+//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   n3 = (child0, child1, 0, 0) as int bits; child >= 0 is an internal node index,
+//        child < 0 is a leaf ~index (a triangle in a BLAS, an instance in a TLAS).
+// A triangle is 48 B = 3 x float4: (v0, prim), (v1, 0), (v2, 0) in object space, in
+// sorted leaf order; `prim` is the original triangle index as int bits.
+constexpr int kNodeF4 = 4;
+constexpr int kTriF4 = 3;
+constexpr int32_t kEmptyChild = (int32_t)0x80000001;  // child slot with an inverted box
+constexpr int32_t kStackMarker = (int32_t)0x80000000; // two-level stack: back to the TLAS
+constexpr int kStackSize = 128;
+
+// One TLAS leaf, in sorted (leaf) order. 80 B, 16-B aligned for vector loads.
+struct __align__(16) DevInstance {
+    float w2o[12];          // world -> object, 3x4 row-major
+    const float4* nodes;    // BLAS nodes
+    const float4* tris;     // BLAS triangles
+    uint32_t custom_index;  // instanceCustomIndex = modelRID
+    uint32_t mask;
+    uint32_t input_index;   // position in the caller's instance array
+    uint32_t blas_prims;    // BLAS primitive count
+};
+static_assert(sizeof(DevInstance) == 80, "DevInstance layout");
+
+// Per-instance data used by the G-buffer kernel, in the caller's instance order.
+struct DevShadeInstance {
+    float normal_mat[9];    // transpose(inverse(model 3x3)), row-major
+    float pad0;
+    const luz_vertex* vertices;
+    const uint32_t* indices;
+};
+
+// Host-side instance as uploaded by luz_tlas_build (64 B + pointers).
+struct DevInstanceInput {
+    float o2w[12];
+    const float4* nodes;
+    const float4* tris;
+    const luz_vertex* vertices;
+    const uint32_t* indices;
+    uint32_t custom_index;
+    uint32_t mask;
+    uint32_t blas_prims;
+    uint32_t pad;
+};
+
+// ---------------------------------------------------------------- handles
+struct Arena {            // one device allocation shared by a batch of BLAS
+    void* base = nullptr;
+    int refs = 0;
+};
+
+}  // namespace luz
+
+struct luz_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    std::string last_error;
+    uint32_t* d_status = nullptr;        // device status word (LUZ_DEV_* bits)
+    uint64_t launches = 0;
+    uint8_t* d_blue_noise = nullptr;     // RGBA8 size*size
+    uint32_t blue_noise_size = 0;
+    // reusable scratch
+    void* d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    void* h_pinned = nullptr;
+    size_t pinned_bytes = 0;
+    int sm_count = 0;
+};
+
+struct luz_blas {
+    luz_ctx* ctx = nullptr;
+    luz::Arena* arena = nullptr;
+    float4* nodes = nullptr;             // max(n-1,1) nodes
+    float4* tris = nullptr;              // n triangles
+    uint32_t* morton = nullptr;          // sorted 30-bit keys (n)
+    uint32_t* order = nullptr;           // sorted primitive order (n)
+    luz_vertex* vertices = nullptr;      // shading copy of the vertex buffer (48-B stride)
+    uint32_t* indices = nullptr;
+    uint32_t prims = 0;
+    uint32_t vertex_count = 0;
+};
+
+struct luz_tlas {
+    luz_ctx* ctx = nullptr;
+    uint32_t max_instances = 0;
+    uint32_t count = 0;
+    float4* nodes = nullptr;             // BFS order, max(n-1,1) nodes
+    luz::DevInstance* instances = nullptr;        // leaf order
+    luz::DevShadeInstance* shade = nullptr;       // input order
+    luz::DevInstanceInput* d_input = nullptr;
+    luz::DevInstanceInput* h_input = nullptr;     // pinned staging
+    uint32_t* morton = nullptr;
+    uint32_t* order = nullptr;
+    uint32_t node_count = 0;
+    cudaEvent_t input_copied = nullptr;           // h_input may be rewritten after this
+    // build temporaries
+    void* tmp = nullptr;
+    size_t tmp_bytes = 0;
+};
+
+struct luz_frame {
+    luz_ctx* ctx = nullptr;
+    uint32_t width = 0, height = 0, pixels = 0, words = 0;  // words per bit plane
+    // G-buffer (DeferredRenderer.cpp:175-248 formats)
+    uint32_t* albedo = nullptr;     // RGBA8
+    float4* normal = nullptr;       // RGBA32F
+    uint32_t* material = nullptr;   // RGBA8
+    uint32_t* emission = nullptr;   // RGBA8
+    float* depth = nullptr;         // F32
+    float4* light = nullptr;        // RGBA32F
+    uint2* primary_hit = nullptr;
+    // visibility
+    uint32_t* shadow_bits = nullptr;
+    uint32_t* ao_bits = nullptr;
+    float* ao = nullptr;
+    float* ao_denoised = nullptr;
+    uint32_t shadow_planes_cap = 0, ao_planes_cap = 0;
+    uint32_t shadow_slots = 0, ao_samples = 0;
+    // compacted lit pixels
+    float4* surf = nullptr;         // 2 float4 per lit pixel: (fragPos, pixel), (N, 0)
+    uint32_t* block_counts = nullptr;
+    uint32_t* lit_count = nullptr;  // device counter
+    uint32_t h_lit_count = 0;
+    // scene constants
+    luz_scene h_scene{};
+    luz_scene* d_scene = nullptr;
+    luz_light* d_lights = nullptr;
+    uint32_t lights_cap = 0, light_count = 0;
+    luz_model* d_models = nullptr;
+    uint32_t models_cap = 0, model_count = 0;
+    uint32_t* d_slot_table = nullptr;  // per shadow slot: light | sample << 16
+    std::vector<uint32_t> h_slot_table;
+    uint32_t* d_light_slot = nullptr;  // per light: first shadow slot
+    uint8_t* d_model_skip = nullptr;   // per model: 1 = discarded by the alpha test
+    unsigned long long* work_counter = nullptr;
+};
+
+// ---------------------------------------------------------------- error plumbing
+namespace luz {
+luz_status set_error(luz_ctx* ctx, luz_status st, const std::string& msg);
+luz_status cuda_error(luz_ctx* ctx, cudaError_t e, const char* what);
+luz_status ensure_scratch(luz_ctx* ctx, size_t bytes);
+luz_status check_launch(luz_ctx* ctx, const char* what);
+}  // namespace luz
+
+#define LUZ_CUDA(ctx, call)                                          \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return luz::cuda_error(ctx, e_, #call); \
+    } while (0)
+
+#define LUZ_LAUNCHED(ctx, name)                                  \
+    do {                                                         \
+        (ctx)->launches++;                                       \
+        luz_status s_ = luz::check_launch(ctx, name);            \
+        if (s_ != LUZ_OK) return s_;                             \
+    } while (0)

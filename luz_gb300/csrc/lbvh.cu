@@ -1,0 +1,912 @@
+// lbvh.cu — device-built two-level LBVH: BLAS over triangles (batched over many
+// meshes as sort segments) and TLAS over instances.
+//
+// Pipeline (each step a kernel on the context stream):
+//   bounds   : centroid bounds per segment (order-preserving uint atomics, exact)
+//   morton   : 64-bit key = segment << 30 | morton30(centroid), value = primitive
+//   sort     : LSD radix sort, 8-bit digits, one upsweep histogram kernel for all
+//              passes + one "onesweep" kernel per pass (tile-local warp multi-split
+//              ranking, decoupled look-back across tiles). Stable.
+//   karras   : T. Karras, "Maximizing Parallelism in the Construction of BVHs,
+//              Octrees, and k-d Trees", HPG 2012 — one thread per internal node,
+//              duplicate codes split by index (delta = 32 + clz(i ^ j)).
+//   emit     : gather triangles / instances into leaf order, padded leaf boxes
+//   refit    : bottom-up, second arrival at a node (atomic flag) merges its children
+//   bfs      : (TLAS) breadth-first relayout so that the top of the tree is a prefix
+//              of the node array, staged into shared memory by the traversal.
+// Replaces the driver builds behind vkw::CmdBuildBLAS / vkw::CmdBuildTLAS
+// (source/Graphics/VulkanWrapper.cpp:1089-1139).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace luz {
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ uint32_t float_to_ordered(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+struct SegDesc {
+    uint32_t prim_off;     // first primitive (global)
+    uint32_t prim_count;
+    uint32_t node_off;     // first internal node (global), max(n-1,1) nodes
+    uint32_t pad;
+    const luz_vertex* vertices;  // device copy, 48-B stride (BLAS only)
+    const uint32_t* indices;
+    float4* nodes;         // output nodes of this segment
+    float4* tris;          // output triangles of this segment
+};
+
+__device__ __forceinline__ int find_seg(const uint32_t* offs, int nseg, uint32_t g) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (offs[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ V3 load_pos(const luz_vertex* v, uint32_t i) {
+    const float* p = v[i].position;
+    return V3{p[0], p[1], p[2]};
+}
+
+__device__ __forceinline__ void tri_box(V3 a, V3 b, V3 c, V3& lo, V3& hi) {
+    lo = V3{fmin_(fmin_(a.x, b.x), c.x), fmin_(fmin_(a.y, b.y), c.y), fmin_(fmin_(a.z, b.z), c.z)};
+    hi = V3{fmax_(fmax_(a.x, b.x), c.x), fmax_(fmax_(a.y, b.y), c.y), fmax_(fmax_(a.z, b.z), c.z)};
+}
+
+// Leaf padding of a triangle box (relative 2^-20 of the coordinate magnitude).
+__device__ __forceinline__ float leaf_pad(float lo, float hi) {
+    return fmax_(fabsf(lo), fabsf(hi)) * 0x1p-20f + 0x1p-100f;
+}
+
+// ---------------------------------------------------------------- bounds + morton
+// seg_bounds: 6 ordered uints per segment (min xyz, max xyz); init min=~0, max=0.
+__global__ void blas_bounds_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
+                                   uint32_t total, uint32_t* seg_bounds) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int s = find_seg(seg_prim_off, nseg, g);
+    const SegDesc sd = segs[s];
+    uint32_t p = g - sd.prim_off;
+    uint32_t i0 = sd.indices[3 * p], i1 = sd.indices[3 * p + 1], i2 = sd.indices[3 * p + 2];
+    V3 lo, hi;
+    tri_box(load_pos(sd.vertices, i0), load_pos(sd.vertices, i1), load_pos(sd.vertices, i2), lo, hi);
+    V3 c = V3{(lo.x + hi.x) * 0.5f + 0.0f, (lo.y + hi.y) * 0.5f + 0.0f, (lo.z + hi.z) * 0.5f + 0.0f};
+    if (!finite3(c)) return;
+    uint32_t* b = seg_bounds + 6 * s;
+    atomicMin(b + 0, float_to_ordered(c.x));
+    atomicMin(b + 1, float_to_ordered(c.y));
+    atomicMin(b + 2, float_to_ordered(c.z));
+    atomicMax(b + 3, float_to_ordered(c.x));
+    atomicMax(b + 4, float_to_ordered(c.y));
+    atomicMax(b + 5, float_to_ordered(c.z));
+}
+
+__device__ __forceinline__ void decode_bounds(const uint32_t* b, V3& cmin, V3& ext) {
+    cmin = V3{ordered_to_float(b[0]), ordered_to_float(b[1]), ordered_to_float(b[2])};
+    V3 cmax = V3{ordered_to_float(b[3]), ordered_to_float(b[4]), ordered_to_float(b[5])};
+    ext = cmax - cmin;
+}
+
+__global__ void blas_morton_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
+                                   uint32_t total, const uint32_t* seg_bounds,
+                                   unsigned long long* keys, uint32_t* vals) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int s = find_seg(seg_prim_off, nseg, g);
+    const SegDesc sd = segs[s];
+    uint32_t p = g - sd.prim_off;
+    uint32_t i0 = sd.indices[3 * p], i1 = sd.indices[3 * p + 1], i2 = sd.indices[3 * p + 2];
+    V3 lo, hi;
+    tri_box(load_pos(sd.vertices, i0), load_pos(sd.vertices, i1), load_pos(sd.vertices, i2), lo, hi);
+    V3 cmin, ext;
+    decode_bounds(seg_bounds + 6 * s, cmin, ext);
+    uint32_t m = morton30(lo, hi, cmin, ext);
+    keys[g] = ((unsigned long long)s << 30) | m;
+    vals[g] = g;
+}
+
+// ---------------------------------------------------------------- onesweep radix sort
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;   // 2048 keys
+constexpr int kRadix = 256;
+constexpr int kMaxPasses = 6;
+constexpr uint32_t kFlagAggregate = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1;
+constexpr uint32_t kLookbackSpinLimit = 1u << 22;
+
+__global__ void sort_histogram_kernel(const unsigned long long* keys, uint32_t n, int passes,
+                                      uint32_t* hist) {
+    __shared__ uint32_t s_hist[kMaxPasses][kRadix];
+    for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += blockDim.x) (&s_hist[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned long long k = keys[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&s_hist[p][(k >> (8 * p)) & 0xFF], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) {
+        uint32_t v = (&s_hist[0][0])[i];
+        if (v) atomicAdd(hist + i, v);
+    }
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim.x == 256).
+__device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* s_tmp /*8*/,
+                                                        uint32_t* total) {
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_tmp[warp] = x;
+    __syncthreads();
+    uint32_t wsum = 0, all = 0;
+    for (int w = 0; w < 8; ++w) {
+        uint32_t t = s_tmp[w];
+        if (w < warp) wsum += t;
+        all += t;
+    }
+    __syncthreads();
+    if (total) *total = all;
+    return wsum + x - v;
+}
+
+__global__ void sort_scan_kernel(const uint32_t* hist, uint32_t* offsets) {
+    __shared__ uint32_t s_tmp[8];
+    int p = blockIdx.x;
+    uint32_t v = hist[p * kRadix + threadIdx.x];
+    offsets[p * kRadix + threadIdx.x] = block_excl_scan_256(v, s_tmp, nullptr);
+}
+
+__device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.volatile.global.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ void st_volatile_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.volatile.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+onesweep_pass_kernel(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
+                     unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, uint32_t n,
+                     int shift, const uint32_t* __restrict__ pass_offsets, uint32_t* tile_status,
+                     uint32_t* tile_counter, uint32_t* dev_status) {
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_warp_hist[kSortWarps][kRadix];
+    __shared__ uint32_t s_digit_excl[kRadix];
+    __shared__ uint32_t s_global_base[kRadix];
+    __shared__ uint32_t s_tmp[8];
+    __shared__ unsigned long long s_keys[kSortTile];
+    __shared__ uint32_t s_vals[kSortTile];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_tile = atomicAdd(tile_counter, 1u);
+    for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) (&s_warp_hist[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * kSortTile;
+
+    unsigned long long key[kSortItems];
+    uint32_t val[kSortItems], dig[kSortItems], rank[kSortItems];
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        uint32_t idx = base + warp * (32 * kSortItems) + k * 32 + lane;
+        bool valid = idx < n;
+        key[k] = valid ? kin[idx] : 0ull;
+        val[k] = valid ? vin[idx] : 0u;
+        dig[k] = valid ? (uint32_t)((key[k] >> shift) & 0xFF) : 256u;
+    }
+    const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        uint32_t d = dig[k];
+        uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+        uint32_t before = peers & lt_mask;
+        uint32_t cnt = (d < 256) ? s_warp_hist[warp][d] : 0u;
+        rank[k] = cnt + __popc(before);
+        __syncwarp();
+        if (d < 256 && before == 0) s_warp_hist[warp][d] = cnt + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // Digit `tid`: exclusive scan across warps and tile total.
+    uint32_t tile_count = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+        uint32_t c = s_warp_hist[w][tid];
+        s_warp_hist[w][tid] = tile_count;
+        tile_count += c;
+    }
+    // Decoupled look-back for digit `tid`.
+    uint32_t* my_status = tile_status + (size_t)tile * kRadix + tid;
+    uint32_t global_base;
+    if (tile == 0) {
+        global_base = pass_offsets[tid];
+        st_volatile_u32(my_status, kFlagPrefix | (global_base + tile_count));
+    } else {
+        st_volatile_u32(my_status, kFlagAggregate | tile_count);
+        uint32_t excl = 0;
+        int j = (int)tile - 1;
+        uint32_t spins = 0;
+        while (j >= 0) {
+            uint32_t s = ld_volatile_u32(tile_status + (size_t)j * kRadix + tid);
+            uint32_t flag = s & ~kValueMask;
+            if (flag == 0) {
+                if (++spins > kLookbackSpinLimit) {
+                    atomicOr(dev_status, (uint32_t)LUZ_DEV_SORT_LOOKBACK_TIMEOUT);
+                    break;
+                }
+                continue;
+            }
+            excl += s & kValueMask;
+            if (flag == kFlagPrefix) break;
+            --j;
+        }
+        global_base = excl;
+        st_volatile_u32(my_status, kFlagPrefix | (excl + tile_count));
+    }
+    s_global_base[tid] = global_base;
+    s_digit_excl[tid] = block_excl_scan_256(tile_count, s_tmp, nullptr);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        uint32_t d = dig[k];
+        if (d < 256) {
+            uint32_t pos = s_digit_excl[d] + s_warp_hist[warp][d] + rank[k];
+            s_keys[pos] = key[k];
+            s_vals[pos] = val[k];
+        }
+    }
+    __syncthreads();
+    uint32_t tile_n = min((uint32_t)kSortTile, n - base);
+    for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
+        unsigned long long k = s_keys[i];
+        uint32_t d = (uint32_t)((k >> shift) & 0xFF);
+        uint32_t out = s_global_base[d] + (i - s_digit_excl[d]);
+        if (out < n) {   // always true unless a look-back timed out (status word raised)
+            kout[out] = k;
+            vout[out] = s_vals[i];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- Karras hierarchy
+__device__ __forceinline__ int kdelta(const unsigned long long* keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint32_t ki = (uint32_t)keys[i] & 0x3FFFFFFFu, kj = (uint32_t)keys[j] & 0x3FFFFFFFu;
+    if (ki != kj) return __clz(ki ^ kj);
+    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+__device__ __forceinline__ void write_inverted_slot(float4* node, int slot) {
+    const float inf = __int_as_float(0x7f800000);
+    if (slot == 0) {
+        node[0] = make_float4(inf, -inf, inf, -inf);
+        node[2].x = inf; node[2].y = -inf;
+    } else {
+        node[1] = make_float4(inf, -inf, inf, -inf);
+        node[2].z = inf; node[2].w = -inf;
+    }
+}
+
+// seg_node_off: first internal node of each segment (global); sorted keys per segment
+// start at seg_prim_off. node_parent / leaf_parent: (local parent << 1) | side.
+__global__ void karras_kernel(const SegDesc* segs, const uint32_t* seg_node_off, int nseg,
+                              uint32_t total_nodes, const unsigned long long* keys,
+                              uint32_t* node_parent, uint32_t* leaf_parent, uint32_t* dev_status) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= total_nodes) return;
+    int s = find_seg(seg_node_off, nseg, q);
+    const SegDesc sd = segs[s];
+    int i = (int)(q - sd.node_off);
+    int n = (int)sd.prim_count;
+    float4* node = sd.nodes + (size_t)i * kNodeF4;
+    if (n <= 1) {
+        // Single node: child0 = leaf 0 (if any), child1 = empty.
+        write_inverted_slot(node, 0);
+        write_inverted_slot(node, 1);
+        int c0 = n == 1 ? ~0 : kEmptyChild;
+        node[3] = make_float4(__int_as_float(c0), __int_as_float(kEmptyChild), 0.f, 0.f);
+        if (n == 1) leaf_parent[sd.prim_off] = 0u;
+        node_parent[sd.node_off] = 0xFFFFFFFFu;
+        return;
+    }
+    const unsigned long long* k = keys + sd.prim_off;
+    int d = (kdelta(k, n, i, i + 1) - kdelta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = kdelta(k, n, i, i - d);
+    int lmax = 2;
+    int guard = 0;
+    while (kdelta(k, n, i, i + lmax * d) > dmin) {
+        lmax <<= 1;
+        if (++guard > 40) { atomicOr(dev_status, (uint32_t)LUZ_DEV_KARRAS_RANGE); return; }
+    }
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = kdelta(k, n, i, j);
+    int split = 0, step = l;
+    do {
+        step = (step + 1) >> 1;
+        if (kdelta(k, n, i, i + (split + step) * d) > dnode) split += step;
+    } while (step > 1);
+    int gamma = i + split * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    int c0, c1;
+    if (lo == gamma) { c0 = ~gamma; leaf_parent[sd.prim_off + gamma] = ((uint32_t)i << 1) | 0u; }
+    else { c0 = gamma; node_parent[sd.node_off + gamma] = ((uint32_t)i << 1) | 0u; }
+    if (hi == gamma + 1) { c1 = ~(gamma + 1); leaf_parent[sd.prim_off + gamma + 1] = ((uint32_t)i << 1) | 1u; }
+    else { c1 = gamma + 1; node_parent[sd.node_off + gamma + 1] = ((uint32_t)i << 1) | 1u; }
+    node[3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
+}
+
+// ---------------------------------------------------------------- leaves + refit
+// BLAS: gather triangles into leaf order; padded leaf boxes; sorted morton/order.
+__global__ void blas_emit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
+                                 uint32_t total, const unsigned long long* keys,
+                                 const uint32_t* vals, float4* leaf_box, uint32_t* morton_out,
+                                 uint32_t* order_out) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int s = find_seg(seg_prim_off, nseg, g);
+    const SegDesc sd = segs[s];
+    uint32_t j = g - sd.prim_off;
+    uint32_t prim = vals[g] - sd.prim_off;
+    morton_out[g] = (uint32_t)keys[g] & 0x3FFFFFFFu;
+    order_out[g] = prim;
+    uint32_t i0 = sd.indices[3 * prim], i1 = sd.indices[3 * prim + 1], i2 = sd.indices[3 * prim + 2];
+    V3 a = load_pos(sd.vertices, i0), b = load_pos(sd.vertices, i1), c = load_pos(sd.vertices, i2);
+    float4* t = sd.tris + (size_t)j * kTriF4;
+    t[0] = make_float4(a.x, a.y, a.z, __int_as_float((int)prim));
+    t[1] = make_float4(b.x, b.y, b.z, 0.f);
+    t[2] = make_float4(c.x, c.y, c.z, 0.f);
+    V3 lo, hi;
+    tri_box(a, b, c, lo, hi);
+    float px = leaf_pad(lo.x, hi.x), py = leaf_pad(lo.y, hi.y), pz = leaf_pad(lo.z, hi.z);
+    leaf_box[2 * g] = make_float4(lo.x - px, lo.y - py, lo.z - pz, 0.f);
+    leaf_box[2 * g + 1] = make_float4(hi.x + px, hi.y + py, hi.z + pz, 0.f);
+}
+
+__device__ __forceinline__ void write_slot(float4* node, int slot, float4 lo, float4 hi) {
+    if (slot == 0) {
+        node[0] = make_float4(lo.x, hi.x, lo.y, hi.y);
+        node[2].x = lo.z; node[2].y = hi.z;
+    } else {
+        node[1] = make_float4(lo.x, hi.x, lo.y, hi.y);
+        node[2].z = lo.z; node[2].w = hi.z;
+    }
+}
+
+__global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
+                             uint32_t total, const float4* leaf_box, const uint32_t* node_parent,
+                             const uint32_t* leaf_parent, uint32_t* flags) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int s = find_seg(seg_prim_off, nseg, g);
+    const SegDesc sd = segs[s];
+    float4 lo = leaf_box[2 * g], hi = leaf_box[2 * g + 1];
+    uint32_t p = leaf_parent[g];
+    const uint32_t node_count = sd.prim_count > 1 ? sd.prim_count - 1 : 1;
+    // Depth is bounded by the node count; the loop always ends at the root.
+    for (uint32_t guard = 0; guard <= sd.prim_count + 1; ++guard) {
+        uint32_t local = p >> 1;
+        if (p == 0xFFFFFFFFu || local >= node_count) return;
+        float4* node = sd.nodes + (size_t)local * kNodeF4;
+        write_slot(node, p & 1, lo, hi);
+        __threadfence();
+        uint32_t old = atomicAdd(flags + sd.node_off + local, 1u);
+        if (old == 0) return;
+        __threadfence();
+        float4 n0 = __ldcg(node + 0), n1 = __ldcg(node + 1), n2 = __ldcg(node + 2);
+        lo = make_float4(fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z), 0.f);
+        hi = make_float4(fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w), 0.f);
+        p = node_parent[sd.node_off + local];
+        if (p == 0xFFFFFFFFu) return;
+    }
+}
+
+// ---------------------------------------------------------------- TLAS
+__global__ void tlas_instance_kernel(const DevInstanceInput* in, uint32_t n, float4* inst_box,
+                                     DevShadeInstance* shade, uint32_t* seg_bounds) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevInstanceInput ii = in[i];
+    float w2o[12];
+    affine_inverse(ii.o2w, w2o);
+    DevShadeInstance sh;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) sh.normal_mat[r * 3 + c] = w2o[c * 4 + r];
+    sh.pad0 = 0.f;
+    sh.vertices = ii.vertices;
+    sh.indices = ii.indices;
+    shade[i] = sh;
+    const float inf = __int_as_float(0x7f800000);
+    V3 wlo = V3{inf, inf, inf}, whi = V3{-inf, -inf, -inf};
+    if (ii.blas_prims > 0) {
+        float4 n0 = ii.nodes[0], n1 = ii.nodes[1], n2 = ii.nodes[2];
+        V3 lo = V3{fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z)};
+        V3 hi = V3{fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w)};
+        for (int c = 0; c < 8; ++c) {
+            V3 p = V3{(c & 1) ? hi.x : lo.x, (c & 2) ? hi.y : lo.y, (c & 4) ? hi.z : lo.z};
+            V3 w = xform_point(ii.o2w, p);
+            wlo = V3{fmin_(wlo.x, w.x), fmin_(wlo.y, w.y), fmin_(wlo.z, w.z)};
+            whi = V3{fmax_(whi.x, w.x), fmax_(whi.y, w.y), fmax_(whi.z, w.z)};
+        }
+        float px = box_pad(wlo.x, whi.x), py = box_pad(wlo.y, whi.y), pz = box_pad(wlo.z, whi.z);
+        wlo = V3{wlo.x - px, wlo.y - py, wlo.z - pz};
+        whi = V3{whi.x + px, whi.y + py, whi.z + pz};
+    }
+    inst_box[2 * i] = make_float4(wlo.x, wlo.y, wlo.z, 0.f);
+    inst_box[2 * i + 1] = make_float4(whi.x, whi.y, whi.z, 0.f);
+    V3 c = V3{(wlo.x + whi.x) * 0.5f + 0.0f, (wlo.y + whi.y) * 0.5f + 0.0f, (wlo.z + whi.z) * 0.5f + 0.0f};
+    if (!finite3(c)) return;
+    atomicMin(seg_bounds + 0, float_to_ordered(c.x));
+    atomicMin(seg_bounds + 1, float_to_ordered(c.y));
+    atomicMin(seg_bounds + 2, float_to_ordered(c.z));
+    atomicMax(seg_bounds + 3, float_to_ordered(c.x));
+    atomicMax(seg_bounds + 4, float_to_ordered(c.y));
+    atomicMax(seg_bounds + 5, float_to_ordered(c.z));
+}
+
+__global__ void tlas_morton_kernel(const float4* inst_box, uint32_t n, const uint32_t* seg_bounds,
+                                   unsigned long long* keys, uint32_t* vals) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 l = inst_box[2 * i], h = inst_box[2 * i + 1];
+    V3 cmin, ext;
+    decode_bounds(seg_bounds, cmin, ext);
+    keys[i] = morton30(V3{l.x, l.y, l.z}, V3{h.x, h.y, h.z}, cmin, ext);
+    vals[i] = i;
+}
+
+__global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_box, uint32_t n,
+                                 const unsigned long long* keys, const uint32_t* vals,
+                                 DevInstance* inst_out, float4* leaf_box, uint32_t* morton_out,
+                                 uint32_t* order_out) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t i = vals[j];
+    morton_out[j] = (uint32_t)keys[j] & 0x3FFFFFFFu;
+    order_out[j] = i;
+    const DevInstanceInput ii = in[i];
+    DevInstance d;
+    affine_inverse(ii.o2w, d.w2o);
+    d.nodes = ii.nodes;
+    d.tris = ii.tris;
+    d.custom_index = ii.custom_index;
+    d.mask = ii.mask;
+    d.input_index = i;
+    d.blas_prims = ii.blas_prims;
+    inst_out[j] = d;
+    leaf_box[2 * j] = inst_box[2 * i];
+    leaf_box[2 * j + 1] = inst_box[2 * i + 1];
+}
+
+// Breadth-first relayout of one tree (single block of 1024 threads). Children of a
+// level keep their parents' order, left before right.
+__global__ void __launch_bounds__(1024)
+bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
+                    uint32_t* newidx) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) { queue[0] = 0; newidx[0] = 0; s_carry = 0; }
+    __syncthreads();
+    uint32_t head = 0, tail = 1;
+    while (head < tail && tail <= m) {
+        uint32_t level_end = tail;
+        for (uint32_t base = head; base < level_end; base += 1024) {
+            uint32_t q = base + tid;
+            int c0 = 0, c1 = 0;
+            uint32_t cnt = 0;
+            if (q < level_end) {
+                uint32_t old = queue[q];
+                float4 n3 = src[(size_t)old * kNodeF4 + 3];
+                c0 = __float_as_int(n3.x);
+                c1 = __float_as_int(n3.y);
+                cnt = (c0 >= 0) + (c1 >= 0);
+            }
+            // block exclusive scan of cnt
+            uint32_t x = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) s_warp[warp] = x;
+            __syncthreads();
+            uint32_t wpre = 0, total = 0;
+            for (int w = 0; w < 32; ++w) {
+                uint32_t t = s_warp[w];
+                if (w < warp) wpre += t;
+                total += t;
+            }
+            uint32_t pos = tail + s_carry + wpre + x - cnt;
+            if (q < level_end) {
+                // A tree has exactly m nodes: positions and child indices stay below m.
+                if (c0 >= 0) {
+                    if (pos < m && (uint32_t)c0 < m) { queue[pos] = (uint32_t)c0; newidx[c0] = pos; }
+                    ++pos;
+                }
+                if (c1 >= 0 && pos < m && (uint32_t)c1 < m) { queue[pos] = (uint32_t)c1; newidx[c1] = pos; }
+            }
+            __syncthreads();
+            if (tid == 0) s_carry += total;
+            __syncthreads();
+        }
+        head = level_end;
+        tail = level_end + s_carry;
+        __syncthreads();
+        if (tid == 0) s_carry = 0;
+        __syncthreads();
+    }
+    for (uint32_t old = tid; old < m; old += 1024) {
+        const float4* s = src + (size_t)old * kNodeF4;
+        float4* d = dst + (size_t)newidx[old] * kNodeF4;
+        float4 n3 = s[3];
+        int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+        if (c0 >= 0) c0 = (int)newidx[c0];
+        if (c1 >= 0) c1 = (int)newidx[c1];
+        d[0] = s[0];
+        d[1] = s[1];
+        d[2] = s[2];
+        d[3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
+    }
+}
+
+// ---------------------------------------------------------------- host drivers
+static inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+static int passes_for(int nseg) {
+    int bits = 30;
+    int sb = 0;
+    while ((1 << sb) < nseg) ++sb;
+    return (bits + sb + 7) / 8;
+}
+
+struct SortBuffers {
+    unsigned long long* keys[2];
+    uint32_t* vals[2];
+    uint32_t* hist;       // passes * 256
+    uint32_t* offsets;    // passes * 256
+    uint32_t* tile_status;  // passes * tiles * 256
+    uint32_t* tile_counter; // passes
+    uint32_t tiles;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Bytes of scratch for a sort of n keys with `passes` passes.
+static size_t sort_scratch_bytes(uint32_t n, int passes) {
+    uint32_t tiles = std::max(1u, cdiv(n, kSortTile));
+    return 2 * align256((size_t)n * 8) + 2 * align256((size_t)n * 4) +
+           2 * align256((size_t)passes * 256 * 4) +
+           align256((size_t)passes * tiles * 256 * 4) + align256((size_t)passes * 4);
+}
+
+static char* carve_sort(char* p, uint32_t n, int passes, SortBuffers& sb) {
+    sb.tiles = std::max(1u, cdiv(n, kSortTile));
+    sb.keys[0] = (unsigned long long*)p; p += align256((size_t)n * 8);
+    sb.keys[1] = (unsigned long long*)p; p += align256((size_t)n * 8);
+    sb.vals[0] = (uint32_t*)p; p += align256((size_t)n * 4);
+    sb.vals[1] = (uint32_t*)p; p += align256((size_t)n * 4);
+    sb.hist = (uint32_t*)p; p += align256((size_t)passes * 256 * 4);
+    sb.offsets = (uint32_t*)p; p += align256((size_t)passes * 256 * 4);
+    sb.tile_status = (uint32_t*)p; p += align256((size_t)passes * sb.tiles * 256 * 4);
+    sb.tile_counter = (uint32_t*)p; p += align256((size_t)passes * 4);
+    return p;
+}
+
+// Sorts sb.keys[0]/vals[0]; returns the index (0/1) of the buffer holding the result.
+static luz_status run_sort(luz_ctx* ctx, SortBuffers& sb, uint32_t n, int passes, int& result) {
+    cudaStream_t st = ctx->stream;
+    LUZ_CUDA(ctx, cudaMemsetAsync(sb.hist, 0, (size_t)passes * 256 * 4, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(sb.tile_status, 0, (size_t)passes * sb.tiles * 256 * 4, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(sb.tile_counter, 0, (size_t)passes * 4, st));
+    uint32_t hblocks = std::min<uint32_t>(std::max(1u, cdiv(n, 256 * 16)), (uint32_t)ctx->sm_count * 4);
+    sort_histogram_kernel<<<hblocks, 256, 0, st>>>(sb.keys[0], n, passes, sb.hist);
+    LUZ_LAUNCHED(ctx, "sort_histogram_kernel");
+    sort_scan_kernel<<<passes, 256, 0, st>>>(sb.hist, sb.offsets);
+    LUZ_LAUNCHED(ctx, "sort_scan_kernel");
+    int cur = 0;
+    for (int p = 0; p < passes; ++p) {
+        onesweep_pass_kernel<<<sb.tiles, kSortThreads, 0, st>>>(
+            sb.keys[cur], sb.vals[cur], sb.keys[cur ^ 1], sb.vals[cur ^ 1], n, 8 * p,
+            sb.offsets + p * 256, sb.tile_status + (size_t)p * sb.tiles * 256, sb.tile_counter + p,
+            ctx->d_status);
+        LUZ_LAUNCHED(ctx, "onesweep_pass_kernel");
+        cur ^= 1;
+    }
+    result = cur;
+    return LUZ_OK;
+}
+
+luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* descs,
+                            luz_blas** out) {
+    // Validate on the host (indices in range, sizes) before any device work.
+    std::vector<SegDesc> segs(count);
+    std::vector<uint32_t> prim_off(count), node_off(count);
+    uint64_t total_prims = 0, total_nodes = 0, total_verts = 0;
+    for (uint32_t s = 0; s < count; ++s) {
+        const luz_blas_desc& d = descs[s];
+        if (d.index_count % 3 != 0)
+            return set_error(ctx, LUZ_ERR_INVALID, "index_count is not a multiple of 3");
+        if (d.vertex_stride < 12 || (d.vertex_count > 0 && !d.vertices) ||
+            (d.index_count > 0 && !d.indices))
+            return set_error(ctx, LUZ_ERR_INVALID, "bad vertex/index buffer description");
+        for (uint32_t k = 0; k < d.index_count; ++k)
+            if (d.indices[k] >= d.vertex_count)
+                return set_error(ctx, LUZ_ERR_INVALID, "index out of range of the vertex buffer");
+        uint32_t n = d.index_count / 3;
+        prim_off[s] = (uint32_t)total_prims;
+        node_off[s] = (uint32_t)total_nodes;
+        total_prims += n;
+        total_nodes += std::max(n, 2u) - 1;
+        total_verts += d.vertex_count;
+    }
+    if (total_prims >= (1ull << 30) - 1)
+        return set_error(ctx, LUZ_ERR_LIMIT, "more than 2^30 triangles in one batch");
+    cudaStream_t st = ctx->stream;
+    // Persistent arena: per BLAS nodes | tris | morton | order | vertices | indices.
+    std::vector<size_t> off_nodes(count), off_tris(count), off_mort(count), off_ord(count),
+        off_vtx(count), off_idx(count);
+    size_t arena_bytes = 0;
+    for (uint32_t s = 0; s < count; ++s) {
+        uint32_t n = descs[s].index_count / 3;
+        uint32_t m = std::max(n, 2u) - 1;
+        off_nodes[s] = arena_bytes; arena_bytes += align256((size_t)m * 64);
+        off_tris[s] = arena_bytes; arena_bytes += align256((size_t)std::max(n, 1u) * 48);
+        off_mort[s] = arena_bytes; arena_bytes += align256((size_t)std::max(n, 1u) * 4);
+        off_ord[s] = arena_bytes; arena_bytes += align256((size_t)std::max(n, 1u) * 4);
+        off_vtx[s] = arena_bytes; arena_bytes += align256((size_t)std::max(descs[s].vertex_count, 1u) * sizeof(luz_vertex));
+        off_idx[s] = arena_bytes; arena_bytes += align256((size_t)std::max(descs[s].index_count, 3u) * 4);
+    }
+    Arena* arena = new Arena();
+    cudaError_t e = cudaMalloc(&arena->base, arena_bytes);
+    if (e != cudaSuccess) { delete arena; return cuda_error(ctx, e, "cudaMalloc(BLAS arena)"); }
+    char* ab = (char*)arena->base;
+    // Upload vertices (repacked to 48-B luz_vertex when the stride differs) and indices.
+    for (uint32_t s = 0; s < count; ++s) {
+        const luz_blas_desc& d = descs[s];
+        luz_vertex* dv = (luz_vertex*)(ab + off_vtx[s]);
+        if (d.vertex_stride == sizeof(luz_vertex)) {
+            if (d.vertex_count)
+                LUZ_CUDA(ctx, cudaMemcpyAsync(dv, d.vertices, (size_t)d.vertex_count * 48,
+                                              cudaMemcpyHostToDevice, st));
+        } else {
+            std::vector<luz_vertex> tmp(d.vertex_count);
+            for (uint32_t v = 0; v < d.vertex_count; ++v) {
+                memset(&tmp[v], 0, sizeof(luz_vertex));
+                memcpy(tmp[v].position, (const char*)d.vertices + (size_t)v * d.vertex_stride, 12);
+                if (d.vertex_stride >= 24)
+                    memcpy(tmp[v].normal, (const char*)d.vertices + (size_t)v * d.vertex_stride + 12, 12);
+            }
+            if (d.vertex_count)
+                LUZ_CUDA(ctx, cudaMemcpy(dv, tmp.data(), (size_t)d.vertex_count * 48,
+                                         cudaMemcpyHostToDevice));
+        }
+        if (d.index_count)
+            LUZ_CUDA(ctx, cudaMemcpyAsync(ab + off_idx[s], d.indices, (size_t)d.index_count * 4,
+                                          cudaMemcpyHostToDevice, st));
+        SegDesc& sd = segs[s];
+        sd.prim_off = prim_off[s];
+        sd.prim_count = d.index_count / 3;
+        sd.node_off = node_off[s];
+        sd.pad = 0;
+        sd.vertices = dv;
+        sd.indices = (const uint32_t*)(ab + off_idx[s]);
+        sd.nodes = (float4*)(ab + off_nodes[s]);
+        sd.tris = (float4*)(ab + off_tris[s]);
+    }
+    // Scratch: segs | prim_off | node_off | bounds | sort | leaf boxes | parents | flags |
+    // sorted morton/order staging.
+    uint32_t N = (uint32_t)total_prims, M = (uint32_t)total_nodes;
+    int passes = passes_for((int)count);
+    size_t need = align256(count * sizeof(SegDesc)) + 2 * align256(count * 4) +
+                  align256(count * 24) + sort_scratch_bytes(std::max(N, 1u), passes) +
+                  align256((size_t)std::max(N, 1u) * 32) + align256((size_t)M * 4) +
+                  align256((size_t)std::max(N, 1u) * 4) + align256((size_t)M * 4) +
+                  2 * align256((size_t)std::max(N, 1u) * 4);
+    luz_status stt = ensure_scratch(ctx, need);
+    if (stt != LUZ_OK) { cudaFree(arena->base); delete arena; return stt; }
+    char* p = (char*)ctx->d_scratch;
+    SegDesc* d_segs = (SegDesc*)p; p += align256(count * sizeof(SegDesc));
+    uint32_t* d_prim_off = (uint32_t*)p; p += align256(count * 4);
+    uint32_t* d_node_off = (uint32_t*)p; p += align256(count * 4);
+    uint32_t* d_bounds = (uint32_t*)p; p += align256(count * 24);
+    SortBuffers sb;
+    p = carve_sort(p, std::max(N, 1u), passes, sb);
+    float4* d_leaf_box = (float4*)p; p += align256((size_t)std::max(N, 1u) * 32);
+    uint32_t* d_node_parent = (uint32_t*)p; p += align256((size_t)M * 4);
+    uint32_t* d_leaf_parent = (uint32_t*)p; p += align256((size_t)std::max(N, 1u) * 4);
+    uint32_t* d_flags = (uint32_t*)p; p += align256((size_t)M * 4);
+    uint32_t* d_mort = (uint32_t*)p; p += align256((size_t)std::max(N, 1u) * 4);
+    uint32_t* d_ord = (uint32_t*)p; p += align256((size_t)std::max(N, 1u) * 4);
+
+    LUZ_CUDA(ctx, cudaMemcpyAsync(d_segs, segs.data(), count * sizeof(SegDesc), cudaMemcpyHostToDevice, st));
+    LUZ_CUDA(ctx, cudaMemcpyAsync(d_prim_off, prim_off.data(), count * 4, cudaMemcpyHostToDevice, st));
+    LUZ_CUDA(ctx, cudaMemcpyAsync(d_node_off, node_off.data(), count * 4, cudaMemcpyHostToDevice, st));
+    std::vector<uint32_t> binit(count * 6);
+    for (uint32_t s = 0; s < count; ++s)
+        for (int k = 0; k < 6; ++k) binit[s * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
+    LUZ_CUDA(ctx, cudaMemcpyAsync(d_bounds, binit.data(), count * 24, cudaMemcpyHostToDevice, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(d_node_parent, 0xFF, (size_t)M * 4, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(d_leaf_parent, 0xFF, (size_t)std::max(N, 1u) * 4, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(d_flags, 0, (size_t)M * 4, st));
+    if (N > 0) {
+        blas_bounds_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, d_bounds);
+        LUZ_LAUNCHED(ctx, "blas_bounds_kernel");
+        blas_morton_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, d_bounds,
+                                                         sb.keys[0], sb.vals[0]);
+        LUZ_LAUNCHED(ctx, "blas_morton_kernel");
+    }
+    int res = 0;
+    if (N > 0) {
+        stt = run_sort(ctx, sb, N, passes, res);
+        if (stt != LUZ_OK) { cudaFree(arena->base); delete arena; return stt; }
+    }
+    // Every segment has at least one node; segments with 0 or 1 primitive get their
+    // single node (empty / one leaf) here without reading keys.
+    karras_kernel<<<cdiv(M, 256), 256, 0, st>>>(d_segs, d_node_off, count, M, sb.keys[res],
+                                                d_node_parent, d_leaf_parent, ctx->d_status);
+    LUZ_LAUNCHED(ctx, "karras_kernel");
+    if (N > 0) {
+        blas_emit_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, sb.keys[res],
+                                                       sb.vals[res], d_leaf_box, d_mort, d_ord);
+        LUZ_LAUNCHED(ctx, "blas_emit_kernel");
+        refit_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, d_leaf_box,
+                                                   d_node_parent, d_leaf_parent, d_flags);
+        LUZ_LAUNCHED(ctx, "refit_kernel");
+    }
+    for (uint32_t s = 0; s < count; ++s) {
+        uint32_t n = segs[s].prim_count;
+        if (n)
+            LUZ_CUDA(ctx, cudaMemcpyAsync(ab + off_mort[s], d_mort + prim_off[s], (size_t)n * 4,
+                                          cudaMemcpyDeviceToDevice, st));
+        if (n)
+            LUZ_CUDA(ctx, cudaMemcpyAsync(ab + off_ord[s], d_ord + prim_off[s], (size_t)n * 4,
+                                          cudaMemcpyDeviceToDevice, st));
+    }
+    LUZ_CUDA(ctx, cudaStreamSynchronize(st));
+    uint32_t bits = 0;
+    LUZ_CUDA(ctx, cudaMemcpy(&bits, ctx->d_status, 4, cudaMemcpyDeviceToHost));
+    if (bits) {
+        cudaFree(arena->base);
+        delete arena;
+        return set_error(ctx, LUZ_ERR_DEVICE, "BLAS build kernel raised the device status word");
+    }
+    for (uint32_t s = 0; s < count; ++s) {
+        luz_blas* b = new luz_blas();
+        b->ctx = ctx;
+        b->arena = arena;
+        arena->refs++;
+        b->nodes = segs[s].nodes;
+        b->tris = segs[s].tris;
+        b->morton = (uint32_t*)(ab + off_mort[s]);
+        b->order = (uint32_t*)(ab + off_ord[s]);
+        b->vertices = (luz_vertex*)(ab + off_vtx[s]);
+        b->indices = (uint32_t*)(ab + off_idx[s]);
+        b->prims = segs[s].prim_count;
+        b->vertex_count = descs[s].vertex_count;
+        out[s] = b;
+    }
+    return LUZ_OK;
+}
+
+// TLAS scratch layout (allocated once per luz_tlas for max_instances).
+static size_t tlas_tmp_bytes(uint32_t cap) {
+    uint32_t m = std::max(cap, 2u) - 1;
+    return align256((size_t)cap * 32) + align256(24) + sort_scratch_bytes(std::max(cap, 1u), 4) +
+           align256((size_t)cap * 32) + align256((size_t)m * 4) + align256((size_t)cap * 4) +
+           align256((size_t)m * 4) + align256((size_t)m * 64) + 2 * align256((size_t)m * 4) +
+           align256(sizeof(SegDesc)) + 2 * align256(4);
+}
+
+luz_status tlas_alloc(luz_ctx* ctx, luz_tlas* t) {
+    uint32_t cap = std::max(t->max_instances, 1u);
+    uint32_t m = std::max(cap, 2u) - 1;
+    LUZ_CUDA(ctx, cudaMalloc(&t->nodes, (size_t)m * 64));
+    LUZ_CUDA(ctx, cudaMalloc(&t->instances, (size_t)cap * sizeof(DevInstance)));
+    LUZ_CUDA(ctx, cudaMalloc(&t->shade, (size_t)cap * sizeof(DevShadeInstance)));
+    LUZ_CUDA(ctx, cudaMalloc(&t->d_input, (size_t)cap * sizeof(DevInstanceInput)));
+    LUZ_CUDA(ctx, cudaMallocHost(&t->h_input, (size_t)cap * sizeof(DevInstanceInput)));
+    LUZ_CUDA(ctx, cudaMalloc(&t->morton, (size_t)cap * 4));
+    LUZ_CUDA(ctx, cudaMalloc(&t->order, (size_t)cap * 4));
+    t->tmp_bytes = tlas_tmp_bytes(cap);
+    LUZ_CUDA(ctx, cudaMalloc(&t->tmp, t->tmp_bytes));
+    return LUZ_OK;
+}
+
+luz_status build_tlas(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint32_t n) {
+    if (n > t->max_instances)
+        return set_error(ctx, LUZ_ERR_LIMIT, "instance count exceeds the TLAS max_instances");
+    for (uint32_t i = 0; i < n; ++i) {
+        const luz_blas* b = inst[i].blas;
+        if (!b) return set_error(ctx, LUZ_ERR_INVALID, "instance without a BLAS");
+        DevInstanceInput& d = t->h_input[i];
+        memcpy(d.o2w, inst[i].transform, 48);
+        d.nodes = b->nodes;
+        d.tris = b->tris;
+        d.vertices = b->vertices;
+        d.indices = b->indices;
+        d.custom_index = inst[i].custom_index;
+        d.mask = inst[i].mask;
+        d.blas_prims = b->prims;
+        d.pad = 0;
+    }
+    cudaStream_t st = ctx->stream;
+    t->count = n;
+    if (n == 0) return LUZ_OK;
+    LUZ_CUDA(ctx, cudaMemcpyAsync(t->d_input, t->h_input, (size_t)n * sizeof(DevInstanceInput),
+                                  cudaMemcpyHostToDevice, st));
+    uint32_t cap = std::max(t->max_instances, 1u);
+    uint32_t mcap = std::max(cap, 2u) - 1;
+    uint32_t m = std::max(n, 2u) - 1;
+    char* p = (char*)t->tmp;
+    float4* inst_box = (float4*)p; p += align256((size_t)cap * 32);
+    uint32_t* bounds = (uint32_t*)p; p += align256(24);
+    SortBuffers sb;
+    p = carve_sort(p, cap, 4, sb);
+    float4* leaf_box = (float4*)p; p += align256((size_t)cap * 32);
+    uint32_t* node_parent = (uint32_t*)p; p += align256((size_t)mcap * 4);
+    uint32_t* leaf_parent = (uint32_t*)p; p += align256((size_t)cap * 4);
+    uint32_t* flags = (uint32_t*)p; p += align256((size_t)mcap * 4);
+    float4* karras_nodes = (float4*)p; p += align256((size_t)mcap * 64);
+    uint32_t* queue = (uint32_t*)p; p += align256((size_t)mcap * 4);
+    uint32_t* newidx = (uint32_t*)p; p += align256((size_t)mcap * 4);
+    SegDesc* d_seg = (SegDesc*)p; p += align256(sizeof(SegDesc));
+    uint32_t* d_zero = (uint32_t*)p; p += align256(4);
+
+    SegDesc sd{};
+    sd.prim_off = 0;
+    sd.prim_count = n;
+    sd.node_off = 0;
+    sd.nodes = karras_nodes;
+    // bounds init + segment descriptor in one small upload via pinned staging
+    struct Small { uint32_t b[6]; uint32_t zero; } small;
+    for (int k = 0; k < 6; ++k) small.b[k] = k < 3 ? 0xFFFFFFFFu : 0u;
+    small.zero = 0;
+    LUZ_CUDA(ctx, cudaMemcpyAsync(bounds, small.b, 24, cudaMemcpyHostToDevice, st));
+    LUZ_CUDA(ctx, cudaMemcpyAsync(d_seg, &sd, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(d_zero, 0, 4, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(node_parent, 0xFF, (size_t)m * 4, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(leaf_parent, 0xFF, (size_t)n * 4, st));
+    LUZ_CUDA(ctx, cudaMemsetAsync(flags, 0, (size_t)m * 4, st));
+
+    tlas_instance_kernel<<<cdiv(n, 128), 128, 0, st>>>(t->d_input, n, inst_box, t->shade, bounds);
+    LUZ_LAUNCHED(ctx, "tlas_instance_kernel");
+    tlas_morton_kernel<<<cdiv(n, 128), 128, 0, st>>>(inst_box, n, bounds, sb.keys[0], sb.vals[0]);
+    LUZ_LAUNCHED(ctx, "tlas_morton_kernel");
+    int res = 0;
+    luz_status s = run_sort(ctx, sb, n, 4, res);
+    if (s != LUZ_OK) return s;
+    karras_kernel<<<cdiv(m, 128), 128, 0, st>>>(d_seg, d_zero, 1, m, sb.keys[res], node_parent,
+                                                leaf_parent, ctx->d_status);
+    LUZ_LAUNCHED(ctx, "karras_kernel");
+    tlas_emit_kernel<<<cdiv(n, 128), 128, 0, st>>>(t->d_input, inst_box, n, sb.keys[res],
+                                                   sb.vals[res], t->instances, leaf_box,
+                                                   t->morton, t->order);
+    LUZ_LAUNCHED(ctx, "tlas_emit_kernel");
+    refit_kernel<<<cdiv(n, 128), 128, 0, st>>>(d_seg, d_zero, 1, n, leaf_box, node_parent,
+                                               leaf_parent, flags);
+    LUZ_LAUNCHED(ctx, "refit_kernel");
+    bfs_relayout_kernel<<<1, 1024, 0, st>>>(karras_nodes, t->nodes, m, queue, newidx);
+    LUZ_LAUNCHED(ctx, "bfs_relayout_kernel");
+    return LUZ_OK;
+}
+
+}  // namespace luz

@@ -1,0 +1,229 @@
+// lightpass.cu — the deferred light pass: light.frag main (light.frag:171-235) over
+// the G-buffer planes and the visibility bit planes, one thread per pixel, with
+// coalesced 128-bit loads of the RGBA32F normal and stores of the RGBA32F output.
+#include <cstring>
+
+#include "internal.cuh"
+
+namespace luz {
+
+// pow(i/255, 2.2) for the albedo decode of light.frag:172, filled by the host.
+__constant__ float c_srgb_lut[256];
+
+luz_status upload_srgb_lut(luz_ctx* ctx, const float* lut) {
+    LUZ_CUDA(ctx, cudaMemcpyToSymbol(c_srgb_lut, lut, 256 * sizeof(float)));
+    return LUZ_OK;
+}
+
+struct LightParams {
+    const uint32_t* albedo;
+    const float4* normal;
+    const uint32_t* material;
+    const uint32_t* emission;
+    const float* depth;
+    const uint32_t* shadow_bits;
+    const uint32_t* ao_bits;
+    const float* ao_denoised;
+    int use_denoised;
+    const luz_light* lights;
+    const uint32_t* light_slot;
+    uint32_t light_count;
+    uint32_t words;
+    uint32_t ao_samples;
+    int shadow_type;
+    float inverse_proj[16], inverse_view[16];
+    float cam[3];
+    float ambient[3];
+    float ambient_intensity;
+    uint32_t width, height;
+    float4* out;
+};
+
+// light.frag:17-26
+__device__ __forceinline__ float distribution_ggx(V3 N, V3 H, float roughness) {
+    float a = roughness * roughness;
+    float a2 = a * a;
+    float NdotH = fmax_(dot(N, H), 0.0f);
+    float NdotH2 = NdotH * NdotH;
+    float nom = a2;
+    float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
+    denom = kPi * denom * denom;
+    return nom / denom;
+}
+// light.frag:28-36
+__device__ __forceinline__ float geometry_schlick_ggx(float NdotV, float roughness) {
+    float r = (roughness + 1.0f);
+    float k = (r * r) / 8.0f;
+    float nom = NdotV;
+    float denom = NdotV * (1.0f - k) + k;
+    return nom / denom;
+}
+// light.frag:38-45
+__device__ __forceinline__ float geometry_smith(V3 N, V3 V, V3 L, float roughness) {
+    float NdotV = fmax_(dot(N, V), 0.0f);
+    float NdotL = fmax_(dot(N, L), 0.0f);
+    float ggx2 = geometry_schlick_ggx(NdotV, roughness);
+    float ggx1 = geometry_schlick_ggx(NdotL, roughness);
+    return ggx1 * ggx2;
+}
+// light.frag:47-49; pow(x, 5.0) evaluated as x^4 * x.
+__device__ __forceinline__ V3 fresnel_schlick(float cos_theta, V3 F0) {
+    float x = clamp01(1.0f - cos_theta);
+    float x2 = x * x;
+    float p5 = (x2 * x2) * x;
+    return F0 + (V3{1.0f, 1.0f, 1.0f} - F0) * p5;
+}
+
+__device__ __forceinline__ float unorm8_to_float(uint32_t b) { return (float)b / 255.0f; }
+
+__device__ __forceinline__ uint32_t bit_at(const uint32_t* __restrict__ planes, uint32_t plane,
+                                           uint32_t words, uint32_t pix) {
+    return (__ldg(planes + (size_t)plane * words + (pix >> 5)) >> (pix & 31)) & 1u;
+}
+
+__global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
+    extern __shared__ luz_light s_lights[];
+    for (uint32_t i = threadIdx.x; i < P.light_count; i += blockDim.x) s_lights[i] = P.lights[i];
+    __syncthreads();
+    uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= P.width * P.height) return;
+    float4 nn = P.normal[pix];
+    V3 N = V3{nn.x, nn.y, nn.z};
+    V3 amb = V3{P.ambient[0], P.ambient[1], P.ambient[2]};
+    if (length(N) == 0.0f) {
+        V3 c = amb * P.ambient_intensity;
+        P.out[pix] = make_float4(c.x, c.y, c.z, 1.0f);
+        return;
+    }
+    uint32_t a8 = P.albedo[pix], m8 = P.material[pix], e8 = P.emission[pix];
+    V3 albedo = V3{c_srgb_lut[a8 & 0xFF], c_srgb_lut[(a8 >> 8) & 0xFF], c_srgb_lut[(a8 >> 16) & 0xFF]};
+    float roughness = unorm8_to_float(m8 & 0xFF);
+    float metallic = unorm8_to_float((m8 >> 8) & 0xFF);
+    float occlusion = unorm8_to_float((m8 >> 16) & 0xFF);
+    V3 emission = V3{unorm8_to_float(e8 & 0xFF), unorm8_to_float((e8 >> 8) & 0xFF),
+                     unorm8_to_float((e8 >> 16) & 0xFF)};
+    uint32_t x = pix % P.width, y = pix / P.width;
+    V3 p = depth_to_world(P.inverse_proj, P.inverse_view, pixel_uv(x, P.width), pixel_uv(y, P.height),
+                          P.depth[pix]);
+    V3 cam = V3{P.cam[0], P.cam[1], P.cam[2]};
+    V3 V = normalize(cam - p);
+    V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + albedo * metallic;
+    V3 Lo = V3{0.0f, 0.0f, 0.0f};
+    for (uint32_t i = 0; i < P.light_count; ++i) {
+        const luz_light& lt = s_lights[i];
+        V3 lpos = V3{lt.position[0], lt.position[1], lt.position[2]};
+        V3 ldir = V3{lt.direction[0], lt.direction[1], lt.direction[2]};
+        V3 L = normalize(lpos - p);
+        float attenuation = 1.0f;
+        if (lt.type == LUZ_LIGHT_DIRECTIONAL) {
+            L = normalize(-ldir);
+        } else if (lt.type == LUZ_LIGHT_SPOT) {
+            float dist = length(lpos - p);
+            attenuation = 1.0f / (dist * dist);
+            float theta = dot(L, normalize(-ldir));
+            float epsilon = lt.inner_angle - lt.outer_angle;
+            attenuation *= clamp01((theta - lt.outer_angle) / epsilon);
+        } else if (lt.type == LUZ_LIGHT_POINT) {
+            float dist = length(lpos - p);
+            attenuation = 1.0f / (dist * dist);
+        }
+        // EvaluateShadow (light.frag:137-169): ray-traced factor = hits / samples.
+        float shadow = 1.0f;
+        if (P.shadow_type == LUZ_SHADOW_RAYTRACING) {
+            int ns = lt.num_shadow_samples;
+            if (ns <= 0) {
+                shadow = 0.0f;
+            } else {
+                uint32_t first = P.light_slot[i];
+                uint32_t hits = 0;
+                for (int s = 0; s < ns; ++s) hits += bit_at(P.shadow_bits, first + s, P.words, pix);
+                shadow = (float)hits / (float)ns;
+            }
+        }
+        V3 color = V3{lt.color[0], lt.color[1], lt.color[2]};
+        V3 radiance = ((color * lt.intensity) * attenuation) * (1.0f - shadow);
+        V3 H = normalize(V + L);
+        float NDF = distribution_ggx(N, H, roughness);
+        float G = geometry_smith(N, V, L, roughness);
+        V3 F = fresnel_schlick(clamp01(dot(H, V)), F0);
+        V3 num = (NDF * G) * F;
+        float denom = (4.0f * fmax_(dot(N, V), 0.0f)) * fmax_(dot(N, L), 0.0f) + 0.0001f;
+        V3 spec = num / denom;
+        V3 kD = (V3{1.0f, 1.0f, 1.0f} - F) * (1.0f - metallic);
+        float NdotL = fmax_(dot(N, L), 0.0f);
+        Lo = Lo + ((kD * albedo) / kPi + spec) * radiance * NdotL;
+    }
+    float ao;
+    if (P.use_denoised) {
+        ao = P.ao_denoised[pix];
+    } else if (P.ao_samples == 0) {
+        ao = 1.0f;
+    } else {
+        uint32_t misses = 0;
+        for (uint32_t s = 0; s < P.ao_samples; ++s) misses += bit_at(P.ao_bits, s, P.words, pix);
+        ao = (float)misses / (float)P.ao_samples;
+    }
+    V3 ambient = (((amb * P.ambient_intensity) * albedo) * occlusion) * ao;
+    V3 c = (ambient + Lo) + emission;
+    P.out[pix] = make_float4(c.x, c.y, c.z, 1.0f);
+}
+
+// AO value per pixel (mean of the miss bits; 0 for background pixels).
+__global__ void __launch_bounds__(256) ao_resolve_kernel(const float4* normal, const uint32_t* ao_bits,
+                                                         uint32_t words, uint32_t samples,
+                                                         uint32_t pixels, float* ao) {
+    uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= pixels) return;
+    float4 nn = normal[pix];
+    if (length(V3{nn.x, nn.y, nn.z}) == 0.0f) { ao[pix] = 0.0f; return; }
+    if (samples == 0) { ao[pix] = 1.0f; return; }
+    uint32_t misses = 0;
+    for (uint32_t s = 0; s < samples; ++s) misses += bit_at(ao_bits, s, words, pix);
+    ao[pix] = (float)misses / (float)samples;
+}
+
+luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
+    LightParams P;
+    P.albedo = f->albedo;
+    P.normal = f->normal;
+    P.material = f->material;
+    P.emission = f->emission;
+    P.depth = f->depth;
+    P.shadow_bits = f->shadow_bits;
+    P.ao_bits = f->ao_bits;
+    P.ao_denoised = f->ao_denoised;
+    P.use_denoised = use_denoised;
+    P.lights = f->d_lights;
+    P.light_slot = f->d_light_slot;
+    P.light_count = f->light_count;
+    P.words = f->words;
+    P.ao_samples = f->ao_samples;
+    P.shadow_type = f->h_scene.shadow_type;
+    memcpy(P.inverse_proj, f->h_scene.inverse_proj, 64);
+    memcpy(P.inverse_view, f->h_scene.inverse_view, 64);
+    memcpy(P.cam, f->h_scene.cam_pos, 12);
+    memcpy(P.ambient, f->h_scene.ambient_light_color, 12);
+    P.ambient_intensity = f->h_scene.ambient_light_intensity;
+    P.width = f->width;
+    P.height = f->height;
+    P.out = f->light;
+    size_t smem = (size_t)f->light_count * sizeof(luz_light);
+    if (smem > 48 * 1024) {
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(light_pass_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    uint32_t blocks = (f->pixels + 255) / 256;
+    light_pass_kernel<<<blocks, 256, smem, ctx->stream>>>(P);
+    LUZ_LAUNCHED(ctx, "light_pass_kernel");
+    return LUZ_OK;
+}
+
+luz_status launch_ao_resolve(luz_ctx* ctx, luz_frame* f) {
+    uint32_t blocks = (f->pixels + 255) / 256;
+    ao_resolve_kernel<<<blocks, 256, 0, ctx->stream>>>(f->normal, f->ao_bits, f->words,
+                                                      f->ao_samples, f->pixels, f->ao);
+    LUZ_LAUNCHED(ctx, "ao_resolve_kernel");
+    return LUZ_OK;
+}
+
+}  // namespace luz

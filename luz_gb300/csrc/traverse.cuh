@@ -1,0 +1,235 @@
+// traverse.cuh — two-level BVH traversal on the SMs (no RT cores are used: the
+// reference's rayQueryProceedEXT loop, light.frag:99-106,125-132, becomes this).
+//
+// * Rays are tested against triangles with the watertight test of S. Woop,
+//   C. Benthin and I. Wald, "Watertight Ray/Triangle Intersection", JCGT 2(1),
+//   2013. Its edge functions are recomputed in FP64 only when an FP32 value is
+//   exactly zero. Triangles are two-sided (instances carry
+//   TRIANGLE_FACING_CULL_DISABLE, source/Graphics/VulkanWrapper.cpp:1119).
+// * Any-hit (gl_RayFlagsTerminateOnFirstHitEXT) returns the OR over all triangles
+//   with t in [tmin, tmax]; closest-hit keeps the smallest t, ties broken by
+//   (instance input index, primitive), so both results are independent of the
+//   traversal order.
+// * Box tests are conservative: leaf boxes are padded and the slab interval is
+//   widened by a relative 2^-18, so no box that holds an accepted hit is culled.
+#pragma once
+#include "internal.cuh"
+
+namespace luz {
+
+constexpr float kSlabEps = 0x1p-18f;
+constexpr uint32_t kTraversalCap = 1u << 24;
+
+__device__ __forceinline__ float comp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+struct WtRay {
+    V3 o;
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+__device__ __forceinline__ WtRay wt_setup(V3 o, V3 d) {
+    WtRay r;
+    r.o = o;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = ax >= ay ? (ax >= az ? 0 : 2) : (ay >= az ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    float dz = comp(d, kz);
+    if (dz < 0.0f) { int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.sx = comp(d, kx) / dz;
+    r.sy = comp(d, ky) / dz;
+    r.sz = 1.0f / dz;
+    return r;
+}
+
+// Returns true with t, (u,v,w) barycentric numerators and det when the ray crosses
+// the triangle (before the [tmin,tmax] check).
+__device__ __forceinline__ bool wt_test(const WtRay& r, V3 v0, V3 v1, V3 v2, float& t, float& U,
+                                        float& V, float& W, float& det) {
+    V3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
+    float akx = comp(A, r.kx), aky = comp(A, r.ky), akz = comp(A, r.kz);
+    float bkx = comp(B, r.kx), bky = comp(B, r.ky), bkz = comp(B, r.kz);
+    float ckx = comp(C, r.kx), cky = comp(C, r.ky), ckz = comp(C, r.kz);
+    float Ax = akx - r.sx * akz, Ay = aky - r.sy * akz;
+    float Bx = bkx - r.sx * bkz, By = bky - r.sy * bkz;
+    float Cx = ckx - r.sx * ckz, Cy = cky - r.sy * ckz;
+    U = Cx * By - Cy * Bx;
+    V = Ax * Cy - Ay * Cx;
+    W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        double CxBy = (double)Cx * (double)By, CyBx = (double)Cy * (double)Bx;
+        U = (float)(CxBy - CyBx);
+        double AxCy = (double)Ax * (double)Cy, AyCx = (double)Ay * (double)Cx;
+        V = (float)(AxCy - AyCx);
+        double BxAy = (double)Bx * (double)Ay, ByAx = (double)By * (double)Ax;
+        W = (float)(BxAy - ByAx);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    det = U + V + W;
+    if (det == 0.0f) return false;
+    float Az = r.sz * akz, Bz = r.sz * bkz, Cz = r.sz * ckz;
+    float T = U * Az + V * Bz + W * Cz;
+    t = T / det;
+    return true;
+}
+
+__device__ __forceinline__ V3 safe_inv(V3 d) {
+    const float tiny = 1e-20f;
+    float x = fabsf(d.x) > tiny ? d.x : copysignf(tiny, d.x);
+    float y = fabsf(d.y) > tiny ? d.y : copysignf(tiny, d.y);
+    float z = fabsf(d.z) > tiny ? d.z : copysignf(tiny, d.z);
+    return V3{1.0f / x, 1.0f / y, 1.0f / z};
+}
+
+__device__ __forceinline__ bool slab(float lx, float hx, float ly, float hy, float lz, float hz,
+                                     V3 o, V3 id, float tmin, float tmax, float& tnear) {
+    float tx0 = (lx - o.x) * id.x, tx1 = (hx - o.x) * id.x;
+    float ty0 = (ly - o.y) * id.y, ty1 = (hy - o.y) * id.y;
+    float tz0 = (lz - o.z) * id.z, tz1 = (hz - o.z) * id.z;
+    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+    tnear = tn;
+    return tn - fabsf(tn) * kSlabEps <= tf + fabsf(tf) * kSlabEps;
+}
+
+struct TlasView {
+    const float4* __restrict__ nodes;    // global, BFS order
+    const float4* smem_nodes;            // first `smem_count` nodes staged in shared memory
+    uint32_t smem_count;
+    const DevInstance* __restrict__ instances;
+    uint32_t count;
+};
+
+struct ClosestHit {
+    float t;
+    uint32_t inst_input;   // instance input index
+    uint32_t prim;
+    uint32_t custom;
+    float b0, b1, b2;      // barycentric weights of v0, v1, v2
+};
+
+// Work counters of one ray (kStats builds only).
+struct TraceCounters {
+    uint32_t tlas_nodes, blas_nodes, tris, instances;
+};
+
+// kClosest = false: any-hit, returns at the first accepted triangle.
+// skip: closest-hit skips instances whose custom index is flagged in `skip`.
+template <bool kClosest, bool kStats = false>
+__device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float tmin, float tmax,
+                                          uint32_t ray_mask, const uint8_t* __restrict__ skip,
+                                          uint32_t skip_count, ClosestHit* hit, uint32_t& err,
+                                          TraceCounters* cnt = nullptr) {
+    if (T.count == 0) return false;
+    if (!finite3(wo) || !finite3(wd) || !(tmin <= tmax)) return false;
+    if (wd.x == 0.0f && wd.y == 0.0f && wd.z == 0.0f) return false;
+    const V3 widir = safe_inv(wd);
+    V3 o = wo, idir = widir;
+    WtRay wt{};
+    int stack[kStackSize];
+    int sp = 0;
+    int node = 0;
+    bool in_blas = false;
+    const float4* __restrict__ nodes = T.nodes;
+    const float4* __restrict__ tris = nullptr;
+    uint32_t inst_input = 0, inst_custom = 0;
+    bool found = false;
+    unsigned long long best_key = ~0ull;
+    for (uint32_t iter = 0;; ++iter) {
+        if (iter > kTraversalCap) { err |= LUZ_DEV_TRAVERSAL_CAP; return false; }
+        bool pop = true;
+        if (node >= 0) {
+            if (kStats) { if (in_blas) cnt->blas_nodes++; else cnt->tlas_nodes++; }
+            float4 n0, n1, n2, n3;
+            if (!in_blas && (uint32_t)node < T.smem_count) {
+                const float4* s = T.smem_nodes + (size_t)node * kNodeF4;
+                n0 = s[0]; n1 = s[1]; n2 = s[2]; n3 = s[3];
+            } else {
+                const float4* g = nodes + (size_t)node * kNodeF4;
+                n0 = __ldg(g); n1 = __ldg(g + 1); n2 = __ldg(g + 2); n3 = __ldg(g + 3);
+            }
+            int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+            float t0, t1;
+            bool h0 = c0 != kEmptyChild && slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, o, idir, tmin, tmax, t0);
+            bool h1 = c1 != kEmptyChild && slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, o, idir, tmin, tmax, t1);
+            if (h0 && h1) {
+                int nearc = c0, farc = c1;
+                if (t1 < t0) { nearc = c1; farc = c0; }
+                if (sp >= kStackSize) { err |= LUZ_DEV_STACK_OVERFLOW; return false; }
+                stack[sp++] = farc;
+                node = nearc;
+                pop = false;
+            } else if (h0) { node = c0; pop = false; }
+            else if (h1) { node = c1; pop = false; }
+        } else if (!in_blas) {
+            if (kStats) cnt->instances++;
+            const DevInstance* I = T.instances + (~node);
+            const float4* wp = reinterpret_cast<const float4*>(I->w2o);
+            float4 r0 = __ldg(wp), r1 = __ldg(wp + 1), r2 = __ldg(wp + 2);
+            const float4* pnodes = I->nodes;
+            const float4* ptris = I->tris;
+            uint4 meta = __ldg(reinterpret_cast<const uint4*>(&I->custom_index));
+            // meta = (custom_index, mask, input_index, blas_prims)
+            bool take = (meta.y & ray_mask) != 0 && meta.w > 0;
+            if (kClosest && take && skip && meta.x < skip_count) take = skip[meta.x] == 0;
+            if (take) {
+                float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
+                V3 oo = xform_point(m, wo);
+                V3 od = xform_dir(m, wd);
+                if (sp >= kStackSize) { err |= LUZ_DEV_STACK_OVERFLOW; return false; }
+                stack[sp++] = kStackMarker;
+                o = oo;
+                idir = safe_inv(od);
+                wt = wt_setup(oo, od);
+                in_blas = true;
+                nodes = pnodes;
+                tris = ptris;
+                inst_input = meta.z;
+                inst_custom = meta.x;
+                node = 0;
+                pop = false;
+            }
+        } else {
+            if (kStats) cnt->tris++;
+            const float4* tp = tris + (size_t)(~node) * kTriF4;
+            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            float t, U, V, W, det;
+            if (wt_test(wt, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, V3{c.x, c.y, c.z}, t, U, V, W, det) &&
+                t >= tmin && t <= tmax) {
+                if (!kClosest) return true;
+                uint32_t prim = (uint32_t)__float_as_int(a.w);
+                unsigned long long key = ((unsigned long long)inst_input << 32) | prim;
+                if (!found || t < tmax || key < best_key) {
+                    found = true;
+                    tmax = t;
+                    best_key = key;
+                    hit->t = t;
+                    hit->inst_input = inst_input;
+                    hit->prim = prim;
+                    hit->custom = inst_custom;
+                    hit->b0 = U / det;
+                    hit->b1 = V / det;
+                    hit->b2 = W / det;
+                }
+            }
+        }
+        if (pop) {
+            for (;;) {
+                if (sp == 0) return found;
+                node = stack[--sp];
+                if (node == kStackMarker) {
+                    in_blas = false;
+                    nodes = T.nodes;
+                    o = wo;
+                    idir = widir;
+                    continue;
+                }
+                break;
+            }
+        }
+    }
+}
+
+}  // namespace luz

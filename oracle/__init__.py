@@ -1,0 +1,196 @@
+"""Python handle on the CPU oracle (oracle/luz_oracle.cpp).
+
+TEST INFRASTRUCTURE: imported only by tests/, the smoke check and the CPU-baseline
+leg of bench.py, as the checker. The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libluz_oracle.so"
+
+P = C.c_void_p
+
+
+def build() -> Path:
+    src = HERE / "luz_oracle.cpp"
+    if not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        sig = {
+            "oracle_blas_build": (C.c_int, [P, C.c_uint32, C.c_uint32, P, C.c_uint32, C.POINTER(P)]),
+            "oracle_blas_prims": (C.c_uint32, [P]),
+            "oracle_blas_get": (None, [P, P, P, P, P]),
+            "oracle_blas_destroy": (None, [P]),
+            "oracle_tlas_build": (C.c_int, [P, P, P, P, C.c_uint32, C.POINTER(P)]),
+            "oracle_tlas_get": (None, [P, P, P, P, P]),
+            "oracle_tlas_destroy": (None, [P]),
+            "oracle_gbuffer": (C.c_int, [P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P, P, P, P, C.c_int,
+                                         C.c_uint32, C.c_uint32]),
+            "oracle_visibility": (C.c_uint64, [P, P, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, C.c_uint32,
+                                               C.c_uint32, C.c_int, P, C.c_uint32, P, P, C.c_int, C.c_int]),
+            "oracle_light_pass": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32, P,
+                                            C.c_int, C.c_uint32, C.c_uint32]),
+            "oracle_light_pass_f64": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32,
+                                                P, C.c_int, C.c_uint32, C.c_uint32]),
+            "oracle_trace_ray": (C.c_int, [P, P, P, C.c_float, C.c_float, C.c_int, C.c_int, P]),
+            "oracle_sincos": (None, [P, P, P, C.c_uint32]),
+            "oracle_disk_sample": (None, [C.c_float, C.c_float, C.c_float, P, P]),
+            "oracle_hemisphere_sample": (None, [C.c_float, C.c_float, P]),
+            "oracle_ggx_terms": (None, [P, P, P, C.c_float, P, P, P, P]),
+            "oracle_depth_to_world": (None, [P, C.c_float, C.c_float, C.c_float, P]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype, f.argtypes = res, args
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def threads() -> int:
+    return max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count() or 1)
+
+
+class OracleBlas:
+    def __init__(self, vertices: np.ndarray, indices: np.ndarray):
+        lib = load()
+        v = np.ascontiguousarray(vertices, np.float32)
+        i = np.ascontiguousarray(indices, np.uint32)
+        h = C.c_void_p()
+        st = lib.oracle_blas_build(_p(v), v.shape[0], v.shape[1] * 4, _p(i), i.size, C.byref(h))
+        if st != 0:
+            raise ValueError(f"oracle_blas_build failed ({st})")
+        self._h = h
+        self.prims = i.size // 3
+
+    @property
+    def handle(self):
+        return self._h
+
+    def arrays(self):
+        n = self.prims
+        m = max(n, 2) - 1
+        nodes = np.zeros((m, 16), np.float32)
+        tris = np.zeros((max(n, 1), 12), np.float32)
+        mort = np.zeros(max(n, 1), np.uint32)
+        order = np.zeros(max(n, 1), np.uint32)
+        load().oracle_blas_get(self._h, _p(nodes), _p(tris), _p(mort), _p(order))
+        return nodes, tris[:n], mort[:n], order[:n]
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.oracle_blas_destroy(self._h)
+            self._h = None
+
+
+class OracleTlas:
+    def __init__(self, blas_per_instance: list[OracleBlas], transforms: np.ndarray, custom=None, mask=None):
+        lib = load()
+        n = len(blas_per_instance)
+        arr = (C.c_void_p * max(n, 1))(*[b.handle.value for b in blas_per_instance])
+        tr = np.ascontiguousarray(transforms, np.float32).reshape(n, 12)
+        cu = None if custom is None else np.ascontiguousarray(custom, np.uint32)
+        ma = None if mask is None else np.ascontiguousarray(mask, np.uint32)
+        h = C.c_void_p()
+        lib.oracle_tlas_build(C.cast(arr, C.c_void_p), _p(tr), _p(cu), _p(ma), n, C.byref(h))
+        self._h = h
+        self.n = n
+        self._keep = blas_per_instance
+
+    @property
+    def handle(self):
+        return self._h
+
+    def arrays(self):
+        lib = load()
+        cnt = C.c_uint32()
+        lib.oracle_tlas_get(self._h, None, None, None, C.byref(cnt))
+        nodes = np.zeros((max(cnt.value, 1), 16), np.float32)
+        mort = np.zeros(max(self.n, 1), np.uint32)
+        order = np.zeros(max(self.n, 1), np.uint32)
+        lib.oracle_tlas_get(self._h, _p(nodes), _p(mort), _p(order), C.byref(cnt))
+        return nodes[: cnt.value], mort[: self.n], order[: self.n]
+
+    def ray(self, o, d, tmin, tmax, closest=False, brute=False):
+        o = np.asarray(o, np.float32)
+        d = np.asarray(d, np.float32)
+        t = C.c_float()
+        r = load().oracle_trace_ray(self._h, _p(o), _p(d), tmin, tmax, int(closest), int(brute), C.byref(t))
+        return bool(r), t.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.oracle_tlas_destroy(self._h)
+            self._h = None
+
+
+def scene_bytes(scene) -> C.c_void_p:
+    return C.cast(C.byref(scene), C.c_void_p)
+
+
+class OracleFrame:
+    """G-buffer, visibility and light pass of one frame on the CPU."""
+
+    def __init__(self, tlas: OracleTlas, scene, lights, n_lights: int, models, n_models: int, width: int,
+                 height: int):
+        self.tlas, self.scene, self.lights, self.nl = tlas, scene, lights, n_lights
+        self.models, self.nm, self.W, self.H = models, n_models, width, height
+        P_ = width * height
+        self.albedo = np.zeros(P_, np.uint32)
+        self.normal = np.zeros((P_, 4), np.float32)
+        self.material = np.zeros(P_, np.uint32)
+        self.emission = np.zeros(P_, np.uint32)
+        self.depth = np.zeros(P_, np.float32)
+        self.primary_hit = np.zeros((P_, 2), np.uint32)
+        self.words = (P_ + 31) // 32
+        ns = sum(max(0, lights[i].num_shadow_samples) for i in range(n_lights)) \
+            if scene.shadow_type == 1 else 0
+        self.shadow_slots = ns
+        self.ao_samples = max(0, scene.ao_num_samples)
+        self.shadow_bits = np.zeros((max(ns, 1), self.words), np.uint32)
+        self.ao_bits = np.zeros((max(self.ao_samples, 1), self.words), np.uint32)
+
+    def gbuffer(self, nthreads=None, y0: int = 0, y1: int | None = None):
+        load().oracle_gbuffer(self.tlas.handle, scene_bytes(self.scene), C.cast(self.models, C.c_void_p), self.nm,
+                              self.W, self.H, _p(self.albedo), _p(self.normal), _p(self.material),
+                              _p(self.emission), _p(self.depth), _p(self.primary_hit), nthreads or threads(),
+                              y0, self.H if y1 is None else y1)
+
+    def visibility(self, frame: int, bn: np.ndarray, y0: int = 0, y1: int | None = None, brute: bool = False,
+                   nthreads=None) -> int:
+        bn = np.ascontiguousarray(bn, np.uint8)
+        y1 = self.H if y1 is None else y1
+        return load().oracle_visibility(self.tlas.handle, scene_bytes(self.scene), C.cast(self.lights, C.c_void_p),
+                                        self.nl, _p(self.normal), _p(self.depth), self.W, self.H, y0, y1, frame,
+                                        _p(bn), bn.shape[0], _p(self.shadow_bits), _p(self.ao_bits),
+                                        nthreads or threads(), int(brute))
+
+    def light_pass(self, ao_override=None, f64=False, nthreads=None, y0: int = 0, y1: int | None = None) -> np.ndarray:
+        P_ = self.W * self.H
+        out = np.zeros((P_, 4), np.float64 if f64 else np.float32)
+        fn = load().oracle_light_pass_f64 if f64 else load().oracle_light_pass
+        ao = None if ao_override is None else np.ascontiguousarray(ao_override, np.float32)
+        fn(scene_bytes(self.scene), C.cast(self.lights, C.c_void_p), self.nl, _p(self.albedo), _p(self.normal),
+           _p(self.material), _p(self.emission), _p(self.depth), _p(self.shadow_bits), _p(self.ao_bits), _p(ao),
+           self.W, self.H, _p(out), nthreads or threads(), y0, self.H if y1 is None else y1)
+        return out.reshape(self.H, self.W, 4)

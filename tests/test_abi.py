@@ -1,0 +1,110 @@
+"""The C ABI library loads without a GPU and exports every declared entry point."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+
+import luz_gb300 as L
+from luz_gb300 import _abi
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*(luz_[a-z0-9_]+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_every_declared_symbol_is_exported():
+    names = declared_functions()
+    assert len(names) > 40
+    lib = C.CDLL(str(_abi.LIB_PATH))
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_signature_table_covers_header():
+    bound = {n for n, _, _ in _abi.SIGNATURES}
+    assert declared_functions() <= bound, declared_functions() - bound
+
+
+def test_struct_layouts():
+    # LuzCommon.h:37-125 (std430): ModelBlock 128 B, the LightBlock fields on the path 64 B.
+    assert C.sizeof(_abi.Light) == 64
+    assert C.sizeof(_abi.Model) == 128
+    assert C.sizeof(_abi.Vertex) == 48
+    assert C.sizeof(_abi.Scene) == 480
+    assert C.sizeof(_abi.Instance) == 64
+    assert _abi.Scene.inverse_proj.offset == 16 + 4 * 64
+    assert _abi.Scene.cam_pos.offset == 16 + 6 * 64 + 16
+
+
+def test_no_device_is_reported_cleanly():
+    h = C.c_void_p()
+    st = L.lib.luz_ctx_create(0, C.byref(h))
+    if st == 0:          # a GPU is present: nothing to check here
+        L.lib.luz_ctx_destroy(h)
+        return
+    assert st == 6       # LUZ_ERR_NO_DEVICE
+
+
+def test_null_arguments_are_rejected():
+    assert L.lib.luz_ctx_create(0, None) == 1
+    assert L.lib.luz_ctx_synchronize(None) == 1
+    assert L.lib.luz_frame_read(None, None, 0, None, 0) == 1
+
+
+def test_scene_generators_are_deterministic():
+    a = L.HostScene(1, width=32, height=32)
+    b = L.HostScene(1, width=32, height=32)
+    assert np.array_equal(a.transforms(), b.transforms())
+    assert bytes(a.models()) == bytes(b.models())
+    assert bytes(a.lights()) == bytes(b.lights())
+    c = L.HostScene(1, seed=99, width=32, height=32)
+    assert not np.array_equal(a.transforms(), c.transforms())
+
+
+def test_config1_scene_shape():
+    s = L.HostScene(1)
+    assert (s.width, s.height) == (512, 512)
+    assert s.instance_count == 65
+    assert s.triangle_count() == 2 + 64 * 12
+    types = [s.lights()[i].type for i in range(s.light_count)]
+    assert types.count(L.LIGHT_DIRECTIONAL) == 1 and types.count(L.LIGHT_POINT) == 4
+    b = s.block()
+    assert b.ao_num_samples == 4 and abs(b.ao_max - 1.0) < 1e-7 and b.shadow_type == L.SHADOW_RAYTRACING
+    for v, _ in s.meshes():
+        assert np.isfinite(v).all()
+
+
+def test_config2_scene_shape_small():
+    s = L.HostScene(2, width=64, height=36, meshes=3, instances=20, subdivisions=3)
+    meshes = s.meshes()
+    assert all(len(i) == 3 * 20 * 4 ** 3 for _, i in meshes)
+    r = np.linalg.norm(meshes[0][0][:, :3], axis=1)
+    assert r.min() > 1.0 - 8 * 0.05 - 1e-5 and r.max() < 1.0 + 8 * 0.05 + 1e-5
+    n = np.linalg.norm(meshes[0][0][:, 3:6], axis=1)
+    assert np.allclose(n, 1.0, atol=1e-5)
+    types = [s.lights()[i].type for i in range(s.light_count)]
+    assert types.count(L.LIGHT_POINT) == 32 and types.count(L.LIGHT_SPOT) == 8
+
+
+def test_icosphere_counts_config2():
+    s = L.HostScene(2, width=16, height=16, meshes=1, instances=1)
+    (v, i), = s.meshes()
+    assert len(i) // 3 == 81920 and len(v) == 40962
+
+
+def test_blue_noise_substitute():
+    t = L.blue_noise(7)
+    assert t.shape == (128, 128, 4) and t.dtype == np.uint8
+    assert np.array_equal(t, L.blue_noise(7))
+    # roughly uniform bytes in R and G
+    for c in range(2):
+        h = np.bincount(t[..., c].ravel(), minlength=256)
+        assert h.max() < 4 * h.mean()

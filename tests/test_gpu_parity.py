@@ -1,0 +1,134 @@
+"""GPU parity: the sm_103a path through the C ABI against the CPU oracle.
+
+Bit-exact: Morton codes, sort order, BVH topology and boxes, G-buffer planes,
+per-ray hit/miss masks. Radiance: within 1e-4 relative per channel.
+"""
+import numpy as np
+import pytest
+
+import luz_gb300 as L
+from tests.pathutil import bits_mismatch, gpu_frame, oracle_frame, oracle_scene
+
+pytestmark = pytest.mark.gpu
+
+RADIANCE_RTOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = L.Context(0)
+    yield c
+    c.close()
+
+
+def _cfg1(w=512, h=512, **kw):
+    return L.HostScene(1, width=w, height=h, **kw)
+
+
+def test_blas_bit_exact(ctx):
+    s = _cfg1(64, 64)
+    meshes = s.meshes()
+    gb = ctx.build_blas(meshes)
+    ob, _ = oracle_scene(s)
+    for g, o in zip(gb, ob):
+        gn, gt, gm, go = g.download()
+        on, ot, om, oo = o.arrays()
+        assert np.array_equal(gm, om), "morton codes"
+        assert np.array_equal(go, oo), "sort order"
+        assert np.array_equal(gn.view(np.uint32), on.view(np.uint32)), "nodes (topology + boxes)"
+        assert np.array_equal(gt.view(np.uint32), ot.view(np.uint32)), "triangles"
+
+
+def test_blas_batch_icospheres_bit_exact(ctx):
+    s = L.HostScene(2, width=64, height=36, meshes=6, instances=32, subdivisions=4)
+    meshes = s.meshes()
+    gb = ctx.build_blas(meshes)
+    ob, _ = oracle_scene(s)
+    for g, o in zip(gb, ob):
+        gn, gt, gm, go = g.download()
+        on, ot, om, oo = o.arrays()
+        assert np.array_equal(gm, om)
+        assert np.array_equal(go, oo)
+        assert np.array_equal(gn.view(np.uint32), on.view(np.uint32))
+        assert np.array_equal(gt.view(np.uint32), ot.view(np.uint32))
+
+
+def test_tlas_bit_exact(ctx):
+    s = L.HostScene(2, width=64, height=36, meshes=4, instances=300, subdivisions=3)
+    g = L.GPUScene(ctx, s)
+    g.update_resources_gpu()
+    gn, gm, go = g.tlas.download()
+    _, tl = oracle_scene(s)
+    on, om, oo = tl.arrays()
+    assert np.array_equal(gm[: s.instance_count], om)
+    assert np.array_equal(go[: s.instance_count], oo)
+    assert np.array_equal(gn.view(np.uint32), on.view(np.uint32))
+
+
+@pytest.mark.parametrize("sampler", [L.SAMPLER_PARITY, L.SAMPLER_STRATIFIED])
+def test_config1_frame_parity(ctx, sampler):
+    s = _cfg1(sampler=sampler)
+    g = gpu_frame(ctx, s)
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    fr = g.frame
+    # G-buffer planes, bit for bit
+    assert np.array_equal(fr.read(L.PLANE_ALBEDO).ravel(), f.albedo)
+    assert np.array_equal(fr.read(L.PLANE_MATERIAL).ravel(), f.material)
+    assert np.array_equal(fr.read(L.PLANE_EMISSION).ravel(), f.emission)
+    assert np.array_equal(fr.read(L.PLANE_DEPTH).ravel().view(np.uint32), f.depth.view(np.uint32))
+    assert np.array_equal(fr.read(L.PLANE_NORMAL).reshape(-1, 4).view(np.uint32), f.normal.view(np.uint32))
+    assert np.array_equal(fr.read(L.PLANE_PRIMARY_HIT).reshape(-1, 2), f.primary_hit)
+    # hit / miss masks, bit for bit
+    assert bits_mismatch(fr.read(L.PLANE_SHADOW_BITS), f.shadow_bits[: f.shadow_slots]) == 0
+    assert bits_mismatch(fr.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+    # radiance within 1e-4 relative per channel
+    gl = fr.read(L.PLANE_LIGHT)
+    ol = f.light_pass()
+    rel = np.abs(gl - ol) / np.maximum(np.abs(ol), 1e-6)
+    assert rel.max() <= RADIANCE_RTOL, rel.max()
+
+
+def test_config1_masks_match_bruteforce(ctx):
+    s = _cfg1(256, 256)
+    g = gpu_frame(ctx, s)
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl, brute=True)
+    assert bits_mismatch(g.frame.read(L.PLANE_SHADOW_BITS), f.shadow_bits[: f.shadow_slots]) == 0
+    assert bits_mismatch(g.frame.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+
+
+def test_config2_reduced_resolution_parity(ctx):
+    s = L.HostScene(2, width=240, height=136, meshes=8, instances=256, subdivisions=5)
+    g = gpu_frame(ctx, s)
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    fr = g.frame
+    assert np.array_equal(fr.read(L.PLANE_NORMAL).reshape(-1, 4).view(np.uint32), f.normal.view(np.uint32))
+    assert np.array_equal(fr.read(L.PLANE_DEPTH).ravel().view(np.uint32), f.depth.view(np.uint32))
+    assert bits_mismatch(fr.read(L.PLANE_SHADOW_BITS), f.shadow_bits[: f.shadow_slots]) == 0
+    assert bits_mismatch(fr.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+    gl = fr.read(L.PLANE_LIGHT)
+    ol = f.light_pass()
+    rel = np.abs(gl - ol) / np.maximum(np.abs(ol), 1e-6)
+    assert rel.max() <= RADIANCE_RTOL, rel.max()
+
+
+def test_render_frame_single_call_matches_stages(ctx):
+    s = _cfg1(128, 128)
+    g = gpu_frame(ctx, s)
+    staged = g.frame.read(L.PLANE_LIGHT).copy()
+    g.render_frame(0)
+    ctx.synchronize()
+    assert np.array_equal(g.frame.read(L.PLANE_LIGHT).view(np.uint32), staged.view(np.uint32))
+
+
+def test_deterministic_rebuild(ctx):
+    s = _cfg1(128, 128)
+    g1 = gpu_frame(ctx, s)
+    a = g1.frame.read(L.PLANE_AO_BITS).copy()
+    n1 = g1.tlas.download()[0].copy()
+    g1.render(0)
+    ctx.synchronize()
+    assert np.array_equal(a, g1.frame.read(L.PLANE_AO_BITS))
+    assert np.array_equal(n1.view(np.uint32), g1.tlas.download()[0].view(np.uint32))
