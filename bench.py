@@ -202,8 +202,10 @@ def run_ours(args, rank, world, local):
     dev = torch.device("cuda", local)
     scene = L.HostScene(2)
     ctx = L.Context(local)
-    stream = torch.cuda.current_stream(dev)
-    L.lib.luz_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream))
+    # One explicit stream for the library's kernels, the L2 flush and the events.
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
     g = L.GPUScene(ctx, scene)
     g.update_resources_gpu()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)

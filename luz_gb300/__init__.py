@@ -12,7 +12,7 @@ follows DeferredRenderer::LightPass (source/Graphics/DeferredRenderer.cpp:324-34
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass
+import weakref
 
 import numpy as np
 
@@ -314,7 +314,11 @@ class Context:
         h = C.c_void_p()
         _check(lib.luz_ctx_create(device, C.byref(h)), what="luz_ctx_create")
         self._h = h
-        self._children = []
+        self._children = weakref.WeakSet()   # handles that must be destroyed before the context
+
+    def _adopt(self, obj):
+        self._children.add(obj)
+        return obj
 
     @property
     def handle(self):
@@ -338,13 +342,20 @@ class Context:
             descs[i].index_count = idx.size
         outs = (C.c_void_p * len(meshes))()
         _check(lib.luz_blas_build_batch(self._h, len(meshes), descs, outs), self._h, "blas build")
-        return [Blas(self, C.c_void_p(outs[i])) for i in range(len(meshes))]
+        return [self._adopt(Blas(self, C.c_void_p(outs[i]))) for i in range(len(meshes))]
 
     def tlas(self, max_instances: int) -> Tlas:
-        return Tlas(self, max_instances)
+        return self._adopt(Tlas(self, max_instances))
 
     def frame(self, width: int, height: int) -> Frame:
-        return Frame(self, width, height)
+        return self._adopt(Frame(self, width, height))
+
+    def set_stream(self, cuda_stream: int) -> None:
+        """Runs all later work on `cuda_stream` (a cudaStream_t value, not 0: the
+        legacy default stream would not order against the context's own stream)."""
+        if not cuda_stream:
+            raise ValueError("pass an explicit (non-default) CUDA stream")
+        _check(lib.luz_ctx_set_stream(self._h, C.c_void_p(cuda_stream)), self._h, "set stream")
 
     def synchronize(self) -> None:
         _check(lib.luz_ctx_synchronize(self._h), self._h, "synchronize")
@@ -359,8 +370,13 @@ class Context:
 
     def close(self):
         if self._h:
+            for child in list(self._children):
+                child.close()
             lib.luz_ctx_destroy(self._h)
             self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 # ---------------------------------------------------------------------------- GPUScene mirror

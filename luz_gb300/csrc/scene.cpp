@@ -549,7 +549,9 @@ void gen_spheres(luz_host_scene* s, const luz_gen_params& p, Rng& rng, uint32_t 
         F3 col = {rng.uniform(0.5f, 1.0f), rng.uniform(0.5f, 1.0f), rng.uniform(0.5f, 1.0f)};
         s->lights.push_back(make_light(LUZ_LIGHT_SPOT, pos, dir, col, rng.uniform(100.0f, 1000.0f), ls));
     }
-    s->camera = look_camera({0.0f, 0.0f, -273.0f}, {0.0f, 0.0f, 0.0f}, 60.0f, s->width, s->height, 0.1f, 2000.0f);
+    // Camera at the centre of the instance cloud looking along +z (about 23% of the
+    // pixels see geometry; from outside the box only about 4% would).
+    s->camera = look_camera({0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 100.0f}, 60.0f, s->width, s->height, 0.1f, 2000.0f);
 }
 
 // One scene of the batched workload: a triangle budget filled either with cubes on a
