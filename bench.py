@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-rows", type=int, default=24, help="rows of the CPU baseline sample")
+    ap.add_argument("--width", type=int, default=1920, help="smaller sizes only for profiling captures")
+    ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -173,7 +175,7 @@ def run_reference(args, rank):
     if rank != 0:
         return
     import luz_gb300 as L
-    scene = L.HostScene(2)
+    scene = L.HostScene(2, width=args.width, height=args.height)
     K = args.steps
     res, times = cpu_baseline(scene, args.cpu_rows, repeats=max(1, args.warmup) + K)
     times = times[max(1, args.warmup):]
@@ -200,7 +202,7 @@ def run_ours(args, rank, world, local):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     dev = torch.device("cuda", local)
-    scene = L.HostScene(2)
+    scene = L.HostScene(2, width=args.width, height=args.height)
     ctx = L.Context(local)
     # One explicit stream for the library's kernels, the L2 flush and the events.
     stream = torch.cuda.Stream(dev)
@@ -331,8 +333,11 @@ def run_ours(args, rank, world, local):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator)",
-                "config": dict(CONFIG, parallelism=f"replicas{world}" if world > 1 else "single"),
+                "config": dict(CONFIG, width=args.width, height=args.height,
+                               parallelism=f"replicas{world}" if world > 1 else "single"),
                 "rays_per_frame": rays_per_frame, "lit_pixels": lit, "stage_ms": stage_ms,
+                "blas_build": {"ms": g.blas_build_ms, "triangles": g.blas_prims, "meshes": len(g.blas),
+                               "note": "one batched device build, host->device vertex/index copies included"},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk}
         print(json.dumps(line), flush=True)

@@ -12,6 +12,7 @@ follows DeferredRenderer::LightPass (source/Graphics/DeferredRenderer.cpp:324-34
 from __future__ import annotations
 
 import ctypes as C
+import time
 import weakref
 
 import numpy as np
@@ -389,7 +390,11 @@ class GPUScene:
     def __init__(self, ctx: Context, scene: HostScene, blue_noise_seed: int = 7):
         self.ctx, self.scene = ctx, scene
         ctx.set_blue_noise(blue_noise(blue_noise_seed))
-        self.blas = ctx.build_blas(scene.meshes())                  # AddMesh for every mesh
+        meshes = scene.meshes()
+        t0 = time.perf_counter()
+        self.blas = ctx.build_blas(meshes)                          # AddMesh for every mesh
+        self.blas_build_ms = (time.perf_counter() - t0) * 1e3       # synchronous, host copies included
+        self.blas_prims = sum(len(i) // 3 for _, i in meshes)
         self.tlas = ctx.tlas(max(scene.instance_count, 1))          # CreateTLAS
         self.frame = ctx.frame(scene.width, scene.height)           # DeferredRenderer::CreateImages
         self.update_resources()

@@ -70,25 +70,44 @@ __device__ __forceinline__ float leaf_pad(float lo, float hi) {
 
 // ---------------------------------------------------------------- bounds + morton
 // seg_bounds: 6 ordered uints per segment (min xyz, max xyz); init min=~0, max=0.
+// Min/max of the ordered centroid keys: reduced across the warp (redux.sync) when
+// all of its lanes belong to one segment, so one lane issues the six atomics.
 __global__ void blas_bounds_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                                    uint32_t total, uint32_t* seg_bounds) {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= total) return;
-    int s = find_seg(seg_prim_off, nseg, g);
-    const SegDesc sd = segs[s];
-    uint32_t p = g - sd.prim_off;
-    uint32_t i0 = sd.indices[3 * p], i1 = sd.indices[3 * p + 1], i2 = sd.indices[3 * p + 2];
-    V3 lo, hi;
-    tri_box(load_pos(sd.vertices, i0), load_pos(sd.vertices, i1), load_pos(sd.vertices, i2), lo, hi);
-    V3 c = V3{(lo.x + hi.x) * 0.5f + 0.0f, (lo.y + hi.y) * 0.5f + 0.0f, (lo.z + hi.z) * 0.5f + 0.0f};
-    if (!finite3(c)) return;
-    uint32_t* b = seg_bounds + 6 * s;
-    atomicMin(b + 0, float_to_ordered(c.x));
-    atomicMin(b + 1, float_to_ordered(c.y));
-    atomicMin(b + 2, float_to_ordered(c.z));
-    atomicMax(b + 3, float_to_ordered(c.x));
-    atomicMax(b + 4, float_to_ordered(c.y));
-    atomicMax(b + 5, float_to_ordered(c.z));
+    bool in = g < total;
+    int s = in ? find_seg(seg_prim_off, nseg, g) : -1;
+    uint32_t k[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+    if (in) {
+        const SegDesc sd = segs[s];
+        uint32_t p = g - sd.prim_off;
+        uint32_t i0 = sd.indices[3 * p], i1 = sd.indices[3 * p + 1], i2 = sd.indices[3 * p + 2];
+        V3 lo, hi;
+        tri_box(load_pos(sd.vertices, i0), load_pos(sd.vertices, i1), load_pos(sd.vertices, i2), lo, hi);
+        V3 c = V3{(lo.x + hi.x) * 0.5f + 0.0f, (lo.y + hi.y) * 0.5f + 0.0f, (lo.z + hi.z) * 0.5f + 0.0f};
+        if (finite3(c)) {
+            k[0] = k[3] = float_to_ordered(c.x);
+            k[1] = k[4] = float_to_ordered(c.y);
+            k[2] = k[5] = float_to_ordered(c.z);
+        }
+    }
+    const uint32_t full = 0xFFFFFFFFu;
+    int s0 = __shfl_sync(full, s, 0);
+    bool uniform = __all_sync(full, s == s0 || s < 0);
+    if (uniform) {
+        uint32_t r[6];
+        for (int a = 0; a < 3; ++a) r[a] = __reduce_min_sync(full, k[a]);
+        for (int a = 3; a < 6; ++a) r[a] = __reduce_max_sync(full, k[a]);
+        if ((threadIdx.x & 31) == 0 && s0 >= 0) {
+            uint32_t* b = seg_bounds + 6 * s0;
+            for (int a = 0; a < 3; ++a) if (r[a] != 0xFFFFFFFFu) atomicMin(b + a, r[a]);
+            for (int a = 3; a < 6; ++a) if (r[a] != 0u) atomicMax(b + a, r[a]);
+        }
+    } else if (s >= 0 && k[0] != 0xFFFFFFFFu) {
+        uint32_t* b = seg_bounds + 6 * s;
+        for (int a = 0; a < 3; ++a) atomicMin(b + a, k[a]);
+        for (int a = 3; a < 6; ++a) atomicMax(b + a, k[a]);
+    }
 }
 
 __device__ __forceinline__ void decode_bounds(const uint32_t* b, V3& cmin, V3& ext) {
