@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "internal.cuh"
+#include "lbvh_kernels.cuh"
 
 namespace luz {
 
@@ -32,17 +33,6 @@ __device__ __forceinline__ uint32_t float_to_ordered(float f) {
 __device__ __forceinline__ float ordered_to_float(uint32_t u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
 }
-
-struct SegDesc {
-    uint32_t prim_off;     // first primitive (global)
-    uint32_t prim_count;
-    uint32_t node_off;     // first internal node (global), max(n-1,1) nodes
-    uint32_t pad;
-    const luz_vertex* vertices;  // device copy, 48-B stride (BLAS only)
-    const uint32_t* indices;
-    float4* nodes;         // output nodes of this segment
-    float4* tris;          // output triangles of this segment
-};
 
 __device__ __forceinline__ int find_seg(const uint32_t* offs, int nseg, uint32_t g) {
     int lo = 0, hi = nseg - 1;
@@ -135,17 +125,6 @@ __global__ void blas_morton_kernel(const SegDesc* segs, const uint32_t* seg_prim
 }
 
 // ---------------------------------------------------------------- onesweep radix sort
-constexpr int kSortThreads = 256;
-constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 8;
-constexpr int kSortTile = kSortThreads * kSortItems;   // 2048 keys
-constexpr int kRadix = 256;
-constexpr int kMaxPasses = 6;
-constexpr uint32_t kFlagAggregate = 1u << 30;
-constexpr uint32_t kFlagPrefix = 2u << 30;
-constexpr uint32_t kValueMask = (1u << 30) - 1;
-constexpr uint32_t kLookbackSpinLimit = 1u << 22;
-
 __global__ void sort_histogram_kernel(const unsigned long long* keys, uint32_t n, int passes,
                                       uint32_t* hist) {
     __shared__ uint32_t s_hist[kMaxPasses][kRadix];
