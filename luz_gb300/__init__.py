@@ -87,16 +87,16 @@ class HostScene:
         return lib.luz_scene_height(self._h)
 
     def meshes(self) -> list[tuple[np.ndarray, np.ndarray]]:
-        """[(vertices float32 (nv, 12), indices uint32 (ni,))] — views into the scene."""
+        """[(vertices float32 (nv, 12), indices uint32 (ni,))], copies owned by the caller."""
         out = []
         for i in range(lib.luz_scene_mesh_count(self._h)):
             vp = C.POINTER(Vertex)()
             ip = _abi.c_u32_p()
             nv, ni = C.c_uint32(), C.c_uint32()
             _check(lib.luz_scene_mesh(self._h, i, C.byref(vp), C.byref(nv), C.byref(ip), C.byref(ni)))
-            v = np.ctypeslib.as_array(C.cast(vp, _abi.c_float_p), shape=(nv.value, 12)) if nv.value else \
+            v = np.ctypeslib.as_array(C.cast(vp, _abi.c_float_p), shape=(nv.value, 12)).copy() if nv.value else \
                 np.zeros((0, 12), np.float32)
-            idx = np.ctypeslib.as_array(ip, shape=(ni.value,)) if ni.value else np.zeros(0, np.uint32)
+            idx = np.ctypeslib.as_array(ip, shape=(ni.value,)).copy() if ni.value else np.zeros(0, np.uint32)
             out.append((v, idx))
         return out
 
