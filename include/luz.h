@@ -40,7 +40,8 @@ enum {
     LUZ_DEV_STACK_OVERFLOW = 1u << 1,
     LUZ_DEV_TRAVERSAL_CAP = 1u << 2,
     LUZ_DEV_KARRAS_RANGE = 1u << 3,
-    LUZ_DEV_BATCH_QUEUE = 1u << 4
+    LUZ_DEV_BATCH_QUEUE = 1u << 4,
+    LUZ_DEV_BAD_INDEX = 1u << 5
 };
 
 /* ------------------------------------------------------------------ limits */
@@ -201,6 +202,39 @@ luz_status luz_blas_build_batch(luz_ctx* ctx, uint32_t count, const luz_blas_des
                                 luz_blas** out);
 void luz_blas_destroy(luz_blas* blas);
 uint32_t luz_blas_primitive_count(const luz_blas* blas);
+
+/* luz_blas_build_noalloc — builds one BLAS and allocates nothing. This entry point
+ * has no counterpart in the reference renderer.
+ *
+ * For callers that cannot allocate device memory while they build: a renderer that
+ * takes all of its device memory from one up-front budget, code that must not pay
+ * the implicit synchronisation of cudaMalloc/cudaFree inside a frame, or a host that
+ * owns every device allocation through its own pool. The caller passes device
+ * buffers: vertices (luz_vertex, 48-B stride) and u32 indices as input; as output
+ * nodes (max(n-1,1) x 64 B), triangles (n x 48 B), sorted Morton codes and sorted
+ * primitive order (n x 4 B each), n = index_count / 3. The result is byte-identical
+ * to luz_blas_build's (same layouts as luz_blas_download).
+ *
+ * Every temporary lives in one file-scope device array of LUZ_NOALLOC_SCRATCH_BYTES
+ * (about 10.3 MiB), which every GPU that loads the library holds until the process
+ * exits. n above LUZ_NOALLOC_MAX_TRIANGLES returns LUZ_ERR_LIMIT before any GPU
+ * work. No cudaMalloc, cudaFree or allocating library routine is called.
+ *
+ * `stream` is a cudaStream_t (NULL = the legacy default stream); the call waits for
+ * its own work on that stream before it returns. The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device current; make
+ * that first call before any stream capture. All calls share the one array and it
+ * keeps the last call's contents (each call resets what it reads before writing):
+ * calls that overlap on the GPU, from several host threads or streams, race.
+ * Returns LUZ_ERR_INVALID for bad arguments or an index outside the vertex buffer
+ * (checked on the device, the bad index is never dereferenced), LUZ_ERR_DEVICE if a
+ * kernel raised its status word, LUZ_ERR_CUDA if a CUDA call failed. */
+#define LUZ_NOALLOC_MAX_TRIANGLES (1u << 17)
+#define LUZ_NOALLOC_SCRATCH_BYTES 10756608u
+luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint32_t vertex_count,
+                                  const uint32_t* d_indices, uint32_t index_count,
+                                  void* d_nodes, void* d_tris, uint32_t* d_morton,
+                                  uint32_t* d_order, void* stream);
 /* Copies the built BLAS to host memory: nodes (64 B each, count = max(n-1,1)),
  * triangles (48 B each, sorted leaf order), the sorted Morton keys (u32) and the
  * sorted primitive order (u32). Any pointer may be NULL. For parity tests. */

@@ -109,6 +109,7 @@ SIGNATURES = [
     ("luz_blas_destroy", None, [P]),
     ("luz_blas_primitive_count", C.c_uint32, [P]),
     ("luz_blas_download", C.c_int32, [P, P, P, P, c_u32_p, c_u32_p]),
+    ("luz_blas_build_noalloc", C.c_int32, [P, C.c_uint32, P, C.c_uint32, P, P, P, P, P]),
     ("luz_tlas_create", C.c_int32, [P, C.c_uint32, C.POINTER(P)]),
     ("luz_tlas_build", C.c_int32, [P, P, C.POINTER(Instance), C.c_uint32]),
     ("luz_tlas_destroy", None, [P]),
