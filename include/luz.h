@@ -192,6 +192,19 @@ luz_status luz_ctx_set_stream(luz_ctx* ctx, void* stream);
 /* Uploads the substitute blue-noise texture (RGBA8, size*size texels). */
 luz_status luz_ctx_set_blue_noise(luz_ctx* ctx, const uint8_t* rgba8, uint32_t size);
 
+/* Launch shape of the persistent visibility kernel (no counterpart in the reference,
+ * whose traversal is the driver's): TLAS nodes staged in shared memory per CTA
+ * (0..2048), idle lanes that trigger a warp's refill (1..32), traversal steps between
+ * refill checks (1..1024), CTAs per SM (1..16). All zero restores the defaults. */
+typedef struct luz_vis_tuning {
+    uint32_t smem_nodes;
+    uint32_t refill;
+    uint32_t steps;
+    uint32_t ctas_per_sm;
+} luz_vis_tuning;
+luz_status luz_ctx_set_vis_tuning(luz_ctx* ctx, const luz_vis_tuning* tuning);
+luz_status luz_ctx_get_vis_tuning(const luz_ctx* ctx, luz_vis_tuning* tuning);
+
 /* ------------------------------------------------------------------ BLAS
  * Replaces vkw::CreateBLAS + vkw::CmdBuildBLAS (source/Graphics/VulkanWrapper.h:236,
  * :229; VulkanWrapper.cpp:743-836, 1089-1104) as called by GPUScene::AddMesh

@@ -351,6 +351,16 @@ class Context:
     def frame(self, width: int, height: int) -> Frame:
         return self._adopt(Frame(self, width, height))
 
+    def set_vis_tuning(self, smem_nodes: int = 0, refill: int = 0, steps: int = 0, ctas_per_sm: int = 0) -> None:
+        """Launch shape of the visibility kernel; all zero restores the defaults."""
+        arr = (C.c_uint32 * 4)(smem_nodes, refill, steps, ctas_per_sm)
+        _check(lib.luz_ctx_set_vis_tuning(self._h, C.byref(arr)), self._h, "vis tuning")
+
+    def vis_tuning(self) -> dict:
+        arr = (C.c_uint32 * 4)()
+        _check(lib.luz_ctx_get_vis_tuning(self._h, C.byref(arr)), self._h, "vis tuning")
+        return dict(zip(("smem_nodes", "refill", "steps", "ctas_per_sm"), list(arr)))
+
     def set_stream(self, cuda_stream: int) -> None:
         """Runs all later work on `cuda_stream` (a cudaStream_t value, not 0: the
         legacy default stream would not order against the context's own stream)."""

@@ -21,7 +21,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libluz_gb300.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CUDA_TUS = ["lbvh.cu", "trace.cu", "lightpass.cu", "capi.cu", "blas_noalloc.cu"]
+CUDA_TUS = ["lbvh.cu", "trace.cu", "visibility.cu", "lightpass.cu", "capi.cu", "blas_noalloc.cu"]
 HOST_TUS = ["scene.cpp"]
 
 

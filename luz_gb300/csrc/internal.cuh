@@ -64,6 +64,15 @@ struct Arena {            // one device allocation shared by a batch of BLAS
     int refs = 0;
 };
 
+// Launch shape of the visibility kernel (chosen by the autotuner, or defaults).
+struct VisTuning {
+    uint32_t smem_nodes;    // TLAS nodes staged in shared memory per CTA
+    uint32_t refill;        // idle lanes that trigger a refill (1..32)
+    uint32_t steps;         // traversal steps between refill checks
+    uint32_t ctas_per_sm;
+    uint32_t set;           // 0 = use the library defaults
+};
+
 }  // namespace luz
 
 struct luz_ctx {
@@ -81,6 +90,7 @@ struct luz_ctx {
     void* h_pinned = nullptr;
     size_t pinned_bytes = 0;
     int sm_count = 0;
+    luz::VisTuning vis_tuning{0, 0, 0, 0, 0};   // set == 0: library defaults
 };
 
 struct luz_blas {

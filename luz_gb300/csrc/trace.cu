@@ -1,58 +1,15 @@
-// trace.cu — primary-ray G-buffer, lit-pixel compaction and the persistent any-hit
-// visibility kernel (shadow + AO rays of light.frag).
+// trace.cu — primary-ray G-buffer and the compaction of lit pixels (the inputs of
+// the visibility kernel in visibility.cu).
 #include <algorithm>
 #include <cstddef>
 #include <cstring>
 
+#include "raygen.cuh"
 #include "traverse.cuh"
 
 namespace luz {
 
 constexpr int kSmemTlasNodes = 1024;   // 64 KB of TLAS top levels per CTA
-
-// ---------------------------------------------------------------- ray generation
-// EvaluateShadow (light.frag:137-146) + TraceShadowRay (light.frag:86-109) for one
-// sample: origin, direction and tMax of the shadow ray; tMin is 0.001.
-__device__ __forceinline__ void shadow_ray(const luz_light& lt, V3 p, V3 N, V3 cam, float rx,
-                                           float ry, V3& O, V3& dir, float& tmax) {
-    V3 lpos = V3{lt.position[0], lt.position[1], lt.position[2]};
-    V3 ldir = V3{lt.direction[0], lt.direction[1], lt.direction[2]};
-    V3 L = normalize(lpos - p);
-    if (lt.type == LUZ_LIGHT_DIRECTIONAL) L = normalize(-ldir);
-    float bias = fmax_(length(p - cam) * 0.01f, 0.05f);
-    O = p + N * bias;
-    float dist = length(lpos - p);
-    V3 Lv = (lt.type == LUZ_LIGHT_DIRECTIONAL) ? (ldir * dot(ldir, L)) * dist : L * dist;
-    V3 T = normalize(cross(Lv, V3{0.0f, 1.0f, 0.0f}));
-    V3 B = normalize(cross(T, Lv));
-    float dx, dy;
-    disk_sample(rx, ry, lt.radius, &dx, &dy);
-    tmax = length(Lv);
-    dir = normalize((Lv + dx * T) + dy * B);
-}
-
-// TraceAORays (light.frag:111-135) for one sample, with the AO origin of
-// light.frag:229-230 (bias without the 0.05 floor).
-__device__ __forceinline__ void ao_ray(V3 p, V3 N, V3 cam, float rx, float ry, V3& O, V3& dir) {
-    float bias = length(p - cam) * 0.01f;
-    O = p + N * bias;
-    V3 T = fabsf(N.z) > 0.5f ? V3{0.0f, -N.z, N.y} : V3{-N.y, N.x, 0.0f};
-    V3 B = cross(N, T);
-    V3 h = hemisphere_sample(rx, ry);
-    dir = (T * h.x + B * h.y) + N * h.z;
-}
-
-__device__ __forceinline__ void sample_rg(const uint8_t* __restrict__ bn, uint32_t bn_size,
-                                          int sampler, uint32_t px, uint32_t py, int i, int frame,
-                                          uint32_t stream, float* rx, float* ry) {
-    if (sampler == LUZ_SAMPLER_STRATIFIED) {
-        stratified_rg(px, py, i, frame, stream, rx, ry);
-    } else {
-        uint32_t tx = px % bn_size, ty = py % bn_size;
-        uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(bn) + ty * bn_size + tx);
-        blue_noise_rg(w & 0xFF, (w >> 8) & 0xFF, i, frame, rx, ry);
-    }
-}
 
 __device__ __forceinline__ uint32_t unorm8(float x) {
     return (uint32_t)(clamp01(x) * 255.0f + 0.5f);
@@ -255,100 +212,6 @@ __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, co
     }
 }
 
-// ---------------------------------------------------------------- visibility
-struct VisParams {
-    const float4* tlas_nodes;
-    uint32_t tlas_node_count;
-    const DevInstance* instances;
-    uint32_t instance_count;
-    const float4* surf;
-    const uint32_t* lit_count;
-    const luz_light* lights;
-    const uint32_t* slot_table;
-    uint32_t shadow_slots, ao_samples;
-    float cam[3];
-    float ao_min, ao_max;
-    int sampler, frame;
-    const uint8_t* blue_noise;
-    uint32_t bn_size;
-    uint32_t width;
-    uint32_t words;
-    uint32_t* shadow_bits;
-    uint32_t* ao_bits;
-    unsigned long long* work_counter;
-    uint32_t* status;
-};
-
-// Persistent kernel: each warp takes 32 consecutive work items with one atomic,
-// item = slot * lit + j (slot-major, so a warp's rays share a light and lie in
-// neighbouring pixels). Shadow slots record hits, AO samples record misses.
-template <bool kStats>
-__global__ void __launch_bounds__(256, 2) visibility_kernel(VisParams P, unsigned long long* stats) {
-    extern __shared__ float4 s_nodes[];
-    TraceCounters cnt{0, 0, 0, 0};
-    uint32_t rays = 0;
-    uint32_t staged;
-    stage_tlas(P.tlas_nodes, P.tlas_node_count, s_nodes, staged);
-    TlasView T{P.tlas_nodes, s_nodes, staged, P.instances, P.instance_count};
-    const uint32_t lit = *P.lit_count;
-    const unsigned long long total = (unsigned long long)lit * (P.shadow_slots + P.ao_samples);
-    const int lane = threadIdx.x & 31;
-    const V3 cam = V3{P.cam[0], P.cam[1], P.cam[2]};
-    uint32_t err = 0;
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(P.work_counter, 32ull);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= total) break;
-        unsigned long long item = base + lane;
-        if (item >= total) continue;
-        uint32_t slot = (uint32_t)(item / lit);
-        uint32_t j = (uint32_t)(item - (unsigned long long)slot * lit);
-        float4 s0 = __ldg(P.surf + 2 * (size_t)j), s1 = __ldg(P.surf + 2 * (size_t)j + 1);
-        V3 p = V3{s0.x, s0.y, s0.z}, N = V3{s1.x, s1.y, s1.z};
-        uint32_t pix = __float_as_uint(s0.w);
-        uint32_t px = pix % P.width, py = pix / P.width;
-        V3 O, dir;
-        float tmin, tmax;
-        uint32_t plane_word;
-        uint32_t* bits;
-        bool record_hit;
-        if (slot < P.shadow_slots) {
-            uint32_t e = __ldg(P.slot_table + slot);
-            uint32_t li = e & 0xFFFFu, si = e >> 16;
-            luz_light lt = P.lights[li];
-            float rx, ry;
-            sample_rg(P.blue_noise, P.bn_size, P.sampler, px, py, (int)si, P.frame, li + 1, &rx, &ry);
-            shadow_ray(lt, p, N, cam, rx, ry, O, dir, tmax);
-            tmin = 0.001f;
-            bits = P.shadow_bits;
-            plane_word = slot * P.words + (pix >> 5);
-            record_hit = true;
-        } else {
-            uint32_t a = slot - P.shadow_slots;
-            float rx, ry;
-            sample_rg(P.blue_noise, P.bn_size, P.sampler, px, py, (int)a, P.frame, 0u, &rx, &ry);
-            ao_ray(p, N, cam, rx, ry, O, dir);
-            tmin = P.ao_min;
-            tmax = P.ao_max;
-            bits = P.ao_bits;
-            plane_word = a * P.words + (pix >> 5);
-            record_hit = false;
-        }
-        bool hit = trace_ray<false, kStats>(T, O, dir, tmin, tmax, 0xFFu, nullptr, 0u, nullptr, err, &cnt);
-        if (kStats) ++rays;
-        if (hit == record_hit) atomicOr(bits + plane_word, 1u << (pix & 31));
-    }
-    if (err) atomicOr(P.status, err);
-    if (kStats) {
-        atomicAdd(stats + 0, (unsigned long long)rays);
-        atomicAdd(stats + 1, (unsigned long long)cnt.tlas_nodes);
-        atomicAdd(stats + 2, (unsigned long long)cnt.blas_nodes);
-        atomicAdd(stats + 3, (unsigned long long)cnt.tris);
-        atomicAdd(stats + 4, (unsigned long long)cnt.instances);
-    }
-}
-
 // ---------------------------------------------------------------- host launchers
 luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
     GbufParams G;
@@ -395,71 +258,6 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
                                                       (const float*)((const char*)f->d_scene + offsetof(luz_scene, inverse_view)),
                                                       f->surf);
     LUZ_LAUNCHED(ctx, "lit_write_kernel");
-    return LUZ_OK;
-}
-
-luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int frame_index,
-                             unsigned long long* d_stats) {
-    uint32_t S = f->shadow_slots + f->ao_samples;
-    cudaStream_t st = ctx->stream;
-    if (f->shadow_slots)
-        LUZ_CUDA(ctx, cudaMemsetAsync(f->shadow_bits, 0, (size_t)f->shadow_slots * f->words * 4, st));
-    if (f->ao_samples)
-        LUZ_CUDA(ctx, cudaMemsetAsync(f->ao_bits, 0, (size_t)f->ao_samples * f->words * 4, st));
-    if (S == 0 || t->count == 0) return LUZ_OK;
-    LUZ_CUDA(ctx, cudaMemsetAsync(f->work_counter, 0, 8, st));
-    VisParams P;
-    P.tlas_nodes = t->nodes;
-    P.tlas_node_count = t->node_count;
-    P.instances = t->instances;
-    P.instance_count = t->count;
-    P.surf = f->surf;
-    P.lit_count = f->lit_count;
-    P.lights = f->d_lights;
-    P.slot_table = f->d_slot_table;
-    P.shadow_slots = f->shadow_slots;
-    P.ao_samples = f->ao_samples;
-    memcpy(P.cam, f->h_scene.cam_pos, 12);
-    P.ao_min = f->h_scene.ao_min;
-    P.ao_max = f->h_scene.ao_max;
-    P.sampler = f->h_scene.sampler;
-    P.frame = frame_index;
-    P.blue_noise = ctx->d_blue_noise;
-    P.bn_size = ctx->blue_noise_size;
-    P.width = f->width;
-    P.words = f->words;
-    P.shadow_bits = f->shadow_bits;
-    P.ao_bits = f->ao_bits;
-    P.work_counter = f->work_counter;
-    P.status = ctx->d_status;
-    uint32_t staged = std::min<uint32_t>(t->node_count, kSmemTlasNodes);
-    size_t smem = (size_t)staged * 64;
-    static bool attr_set = false;
-    if (!attr_set) {
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<false>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           kSmemTlasNodes * 64));
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<true>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           kSmemTlasNodes * 64));
-        attr_set = true;
-    }
-    uint32_t grid = (uint32_t)ctx->sm_count * 2;
-    if (d_stats) {
-        LUZ_CUDA(ctx, cudaMemsetAsync(d_stats, 0, 5 * sizeof(unsigned long long), st));
-        visibility_kernel<true><<<grid, 256, smem, st>>>(P, d_stats);
-        LUZ_LAUNCHED(ctx, "visibility_kernel<stats>");
-    } else {
-        visibility_kernel<false><<<grid, 256, smem, st>>>(P, nullptr);
-        LUZ_LAUNCHED(ctx, "visibility_kernel");
-    }
-    return LUZ_OK;
-}
-
-luz_status frame_lit_count(luz_ctx* ctx, luz_frame* f, uint32_t* count) {
-    LUZ_CUDA(ctx, cudaMemcpyAsync(&f->h_lit_count, f->lit_count, 4, cudaMemcpyDeviceToHost, ctx->stream));
-    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    *count = f->h_lit_count;
     return LUZ_OK;
 }
 
