@@ -175,7 +175,9 @@ enum {
     LUZ_PLANE_AO = 8,           /* F32 per-pixel AO value (mean of misses)            */
     LUZ_PLANE_AO_DENOISED = 9,  /* F32 per-pixel denoised AO                          */
     LUZ_PLANE_PRIMARY_HIT = 10, /* u32x2 per pixel: (instance custom index, prim id), ~0 = miss */
-    LUZ_PLANE_COUNT = 11
+    LUZ_PLANE_FEATURES = 11,    /* 8 x bf16 per pixel: denoiser input channels           */
+    LUZ_PLANE_LIN_DEPTH = 12,   /* F32 distance to the camera, 0 for background          */
+    LUZ_PLANE_COUNT = 13
 };
 
 /* ------------------------------------------------------------------ context */
@@ -312,6 +314,45 @@ luz_status luz_frame_write(luz_ctx* ctx, luz_frame* frame, int32_t plane,
                            const void* host_src, size_t bytes);
 /* Device pointer of a plane (for zero-copy interop), NULL on error. */
 void* luz_frame_plane_device_ptr(luz_frame* frame, int32_t plane);
+
+/* ------------------------------------------------------------------ denoiser
+ * Learned kernel-predicting AO denoiser; no counterpart in the reference, which
+ * integrates AO with aoSamples rays per pixel (light.frag:111-135). Per pixel an MLP
+ * 72 -> 64 -> 64 -> 64 -> 49 (BF16 tensor cores, FP32 accumulation) reads 8 channels
+ * over a 3x3 neighbourhood (noisy AO, noisy shadow lit fraction, normal, relative
+ * depth, roughness, albedo luminance) and predicts softmax weights of a 7x7 filter
+ * applied to the noisy AO. Parameters: LUZ_DENOISER_PARAMS FP32 values, row-major
+ * [out][in] weights then biases per layer: W1[64][72] b1[64] W2[64][64] b2[64]
+ * W3[64][64] b3[64] W4[49][64] b4[49]. */
+#define LUZ_DENOISER_PARAMS 16177
+typedef struct luz_denoiser luz_denoiser;
+/* A batch of images in device memory: features (LUZ_PLANE_FEATURES layout),
+ * distances (LUZ_PLANE_LIN_DEPTH), noisy AO, and for training the target AO;
+ * `images` images of width x height stored one after the other. */
+typedef struct luz_denoise_batch {
+    const void* features;
+    const float* lin_depth;
+    const float* noisy_ao;
+    const float* target_ao;
+    uint32_t width, height, images;
+} luz_denoise_batch;
+luz_status luz_denoiser_create(luz_ctx* ctx, uint64_t seed, luz_denoiser** out);
+void luz_denoiser_destroy(luz_denoiser* d);
+/* Sets / reads the FP32 parameters (resets the Adam moments). */
+luz_status luz_denoiser_set_weights(luz_ctx* ctx, luz_denoiser* d, const float* params);
+luz_status luz_denoiser_get_weights(luz_ctx* ctx, luz_denoiser* d, float* params);
+/* Computes the features, distances and noisy AO planes of a traced frame. */
+luz_status luz_denoise_features(luz_ctx* ctx, luz_frame* frame);
+/* Features + network + filter: writes LUZ_PLANE_AO_DENOISED. */
+luz_status luz_denoise(luz_ctx* ctx, luz_denoiser* d, luz_frame* frame);
+luz_status luz_denoise_batch_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* d_out);
+/* Mean squared error against target_ao and its gradient (host array of
+ * LUZ_DENOISER_PARAMS, may be NULL); deterministic. */
+luz_status luz_denoiser_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* grad,
+                                 float* loss);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on the batch; loss may be NULL. */
+luz_status luz_denoiser_train_step(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float lr,
+                                   float* loss);
 
 #ifdef __cplusplus
 }

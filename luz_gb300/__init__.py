@@ -276,6 +276,12 @@ class Frame:
     def light_pass(self, use_denoised_ao: bool = False) -> None:
         _check(lib.luz_light_pass(self.ctx.handle, self._h, int(use_denoised_ao)), self.ctx.handle, "light pass")
 
+    def device_ptr(self, plane: int) -> int:
+        return lib.luz_frame_plane_device_ptr(self._h, plane) or 0
+
+    def denoise_features(self) -> None:
+        _check(lib.luz_denoise_features(self.ctx.handle, self._h), self.ctx.handle, "denoise features")
+
     def plane_bytes(self, plane: int) -> int:
         return lib.luz_frame_plane_bytes(self._h, plane)
 
@@ -290,6 +296,8 @@ class Frame:
         if plane in (PLANE_SHADOW_BITS, PLANE_AO_BITS):
             words = (self.width * self.height + 31) // 32
             return out.reshape(-1, words)
+        if plane == _abi.PLANE_FEATURES:
+            return out.view(np.uint16)[: self.width * self.height * 8].reshape(self.height, self.width, 8)
         if comps > 1:
             return out.reshape(self.height, self.width, comps)
         return out.reshape(self.height, self.width)

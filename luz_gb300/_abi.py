@@ -93,6 +93,17 @@ class GenParams(C.Structure):
                 ("pad1", C.c_uint32)]
 
 
+class DenoiseBatch(C.Structure):
+    _fields_ = [("features", C.c_void_p), ("lin_depth", C.c_void_p), ("noisy_ao", C.c_void_p),
+                ("target_ao", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("images", C.c_uint32)]
+
+
+DENOISER_PARAMS = 16177
+PLANE_FEATURES, PLANE_LIN_DEPTH = 11, 12
+PLANE_DTYPES[PLANE_FEATURES] = (np.uint16, 8)
+PLANE_DTYPES[PLANE_LIN_DEPTH] = (np.float32, 1)
+
+
 # (name, restype, argtypes) of every entry point declared in include/*.h
 P = C.c_void_p
 SIGNATURES = [
@@ -131,6 +142,15 @@ SIGNATURES = [
     ("luz_frame_read", C.c_int32, [P, P, C.c_int32, P, C.c_size_t]),
     ("luz_frame_write", C.c_int32, [P, P, C.c_int32, P, C.c_size_t]),
     ("luz_frame_plane_device_ptr", P, [P, C.c_int32]),
+    ("luz_denoiser_create", C.c_int32, [P, C.c_uint64, C.POINTER(P)]),
+    ("luz_denoiser_destroy", None, [P]),
+    ("luz_denoiser_set_weights", C.c_int32, [P, P, c_float_p]),
+    ("luz_denoiser_get_weights", C.c_int32, [P, P, c_float_p]),
+    ("luz_denoise_features", C.c_int32, [P, P]),
+    ("luz_denoise", C.c_int32, [P, P, P]),
+    ("luz_denoise_batch_infer", C.c_int32, [P, P, C.POINTER(DenoiseBatch), P]),
+    ("luz_denoiser_gradient", C.c_int32, [P, P, C.POINTER(DenoiseBatch), c_float_p, c_float_p]),
+    ("luz_denoiser_train_step", C.c_int32, [P, P, C.POINTER(DenoiseBatch), C.c_float, c_float_p]),
     # luz_scene.h
     ("luz_scene_default_params", C.c_int32, [C.c_int32, C.POINTER(GenParams)]),
     ("luz_scene_generate", C.c_int32, [C.POINTER(GenParams), C.POINTER(P)]),

@@ -21,7 +21,9 @@ BUILD = PKG / "_build"
 LIB = PKG / "libluz_gb300.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CUDA_TUS = ["lbvh.cu", "trace.cu", "visibility.cu", "lightpass.cu", "capi.cu", "blas_noalloc.cu"]
+CUDA_TUS = ["lbvh.cu", "trace.cu", "visibility.cu", "lightpass.cu", "capi.cu", "blas_noalloc.cu",
+            "denoise.cu"]
+FMA_TUS = {"denoise.cu"}
 HOST_TUS = ["scene.cpp"]
 
 
@@ -52,7 +54,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     objs = []
     for tu in CUDA_TUS:
         obj = BUILD / (tu + ".o")
-        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true",
+        # The denoiser is not on the bit-exact ray path: FMA contraction is allowed there.
+        fmad = "-fmad=true" if tu in FMA_TUS else "-fmad=false"
+        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", fmad, "-prec-div=true",
                "-prec-sqrt=true", "-ftz=false", "-Xptxas", "-warn-spills",
                "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", str(INCLUDE),
                "-c", str(CSRC / tu), "-o", str(obj)]

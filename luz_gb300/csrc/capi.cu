@@ -52,6 +52,7 @@ luz_status ensure_scratch(luz_ctx* ctx, size_t bytes) {
 static void free_frame_buffers(luz_frame* f) {
     void* ptrs[] = {f->albedo, f->normal, f->material, f->emission, f->depth, f->light,
                     f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->surf,
+                    f->features, f->lin_depth,
                     f->block_counts, f->lit_count, f->d_scene, f->d_lights, f->d_models,
                     f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter};
     for (void* p : ptrs)
@@ -267,6 +268,8 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     A((void**)&f->primary_hit, P * 8);
     A((void**)&f->ao, P * 4);
     A((void**)&f->ao_denoised, P * 4);
+    A((void**)&f->features, P * 16);
+    A((void**)&f->lin_depth, P * 4);
     A((void**)&f->surf, P * 32);
     A((void**)&f->block_counts, (size_t)chunks * 4);
     A((void**)&f->lit_count, 4);
@@ -414,8 +417,8 @@ size_t luz_frame_plane_bytes(const luz_frame* f, int32_t plane) {
     size_t P = f->pixels;
     switch (plane) {
         case LUZ_PLANE_ALBEDO: case LUZ_PLANE_MATERIAL: case LUZ_PLANE_EMISSION: case LUZ_PLANE_DEPTH:
-        case LUZ_PLANE_AO: case LUZ_PLANE_AO_DENOISED: return P * 4;
-        case LUZ_PLANE_NORMAL: case LUZ_PLANE_LIGHT: return P * 16;
+        case LUZ_PLANE_AO: case LUZ_PLANE_AO_DENOISED: case LUZ_PLANE_LIN_DEPTH: return P * 4;
+        case LUZ_PLANE_NORMAL: case LUZ_PLANE_LIGHT: case LUZ_PLANE_FEATURES: return P * 16;
         case LUZ_PLANE_PRIMARY_HIT: return P * 8;
         case LUZ_PLANE_SHADOW_BITS: return (size_t)f->shadow_slots * f->words * 4;
         case LUZ_PLANE_AO_BITS: return (size_t)f->ao_samples * f->words * 4;
@@ -437,6 +440,8 @@ void* luz_frame_plane_device_ptr(luz_frame* f, int32_t plane) {
         case LUZ_PLANE_AO: return f->ao;
         case LUZ_PLANE_AO_DENOISED: return f->ao_denoised;
         case LUZ_PLANE_PRIMARY_HIT: return f->primary_hit;
+        case LUZ_PLANE_FEATURES: return f->features;
+        case LUZ_PLANE_LIN_DEPTH: return f->lin_depth;
         default: return nullptr;
     }
 }

@@ -1,0 +1,852 @@
+// denoise.cu — learned kernel-predicting AO denoiser (no counterpart in the
+// reference renderer): per pixel, 72 features (8 channels over a 3x3 neighbourhood)
+// → 64 → 64 → 64 (ReLU) → 49 logits → softmax → 7x7 filter of the noisy AO.
+//
+// BF16 tensor-core matrix products (mma.sync m16n8k16, FP32 accumulation). A warp
+// owns 16 pixels; activations stay in registers from layer to layer (the FP32
+// accumulator fragment of one layer is the BF16 A fragment of the next). Weights are
+// staged in shared memory, n-major with padded strides (conflict-free fragments).
+//
+// Training: one persistent kernel runs forward and backward over fixed pixel tiles;
+// every CTA accumulates its weight gradients with tensor-core products over the
+// tile's pixels (activations and gradients stored transposed in shared memory) in a
+// fixed order, writes one partial per CTA, and a second kernel sums the partials in
+// CTA order — the gradient is deterministic. Adam keeps FP32 master weights.
+//
+// Feature channels per pixel: 0 noisy AO, 1 noisy shadow (mean lit fraction over the
+// shadow samples), 2-4 normal, 5 depth relative to the centre pixel
+// ((d_q - d_p)/d_p, clamped to [-1,1]), 6 roughness, 7 albedo luminance.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace luz {
+namespace dn {
+
+constexpr int kParams = 16177;
+constexpr int oW1 = 0, ob1 = 4608, oW2 = 4672, ob2 = 8768, oW3 = 8832, ob3 = 12928, oW4 = 12992, ob4 = 16128;
+// packed BF16 weights (elements), n-major with padded k strides
+constexpr int sW1 = 88, sW = 72;
+constexpr int pW1 = 0;
+constexpr int pW2 = pW1 + 64 * sW1;
+constexpr int pW3 = pW2 + 64 * sW;
+constexpr int pW4 = pW3 + 64 * sW;
+constexpr int pW2T = pW4 + 56 * sW;     // transposed copies for the backward pass: [in][out]
+constexpr int pW3T = pW2T + 64 * sW;
+constexpr int pW4T = pW3T + 64 * sW;
+constexpr int pFwdEnd = pW2T;           // what inference needs
+constexpr int pEnd = pW4T + 64 * sW;
+constexpr int kBias = 64 + 64 + 64 + 56;   // b1 | b2 | b3 | b4 (padded)
+constexpr int kTile = 128;                 // pixels per CTA tile (8 warps x 16)
+constexpr int sT = kTile + 8;              // stride of the transposed activation tiles
+
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+__device__ __forceinline__ float bf(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// ---------------------------------------------------------------- features
+struct FeatParams {
+    const uint32_t* albedo;
+    const float4* normal;
+    const uint32_t* material;
+    const float* depth;
+    const uint32_t* shadow_bits;
+    const uint32_t* ao_bits;
+    uint32_t shadow_slots, ao_samples, words;
+    uint32_t width, height;
+    float inverse_proj[16], inverse_view[16];
+    float cam[3];
+    uint4* feat;       // 8 x bf16 per pixel
+    float* lin_depth;  // distance to the camera (0 = background)
+    float* ao;         // noisy AO value
+};
+
+__constant__ float c_lin_lut[256];   // pow(i/255, 2.2)
+
+__global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
+    uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= F.width * F.height) return;
+    float4 n = F.normal[pix];
+    if (length(V3{n.x, n.y, n.z}) == 0.0f) {
+        F.feat[pix] = make_uint4(0, 0, 0, 0);
+        F.lin_depth[pix] = 0.0f;
+        F.ao[pix] = 0.0f;
+        return;
+    }
+    uint32_t w = pix >> 5, bit = 1u << (pix & 31);
+    float ao = 1.0f;
+    if (F.ao_samples) {
+        uint32_t m = 0;
+        for (uint32_t s = 0; s < F.ao_samples; ++s) m += (F.ao_bits[(size_t)s * F.words + w] & bit) ? 1u : 0u;
+        ao = (float)m / (float)F.ao_samples;
+    }
+    float lit = 1.0f;
+    if (F.shadow_slots) {
+        uint32_t h = 0;
+        for (uint32_t s = 0; s < F.shadow_slots; ++s) h += (F.shadow_bits[(size_t)s * F.words + w] & bit) ? 1u : 0u;
+        lit = 1.0f - (float)h / (float)F.shadow_slots;
+    }
+    uint32_t a8 = F.albedo[pix], m8 = F.material[pix];
+    float lum = 0.2127f * c_lin_lut[a8 & 0xFF] + 0.7152f * c_lin_lut[(a8 >> 8) & 0xFF] +
+                0.0722f * c_lin_lut[(a8 >> 16) & 0xFF];
+    float rough = (float)(m8 & 0xFF) / 255.0f;
+    uint32_t x = pix % F.width, y = pix / F.width;
+    V3 p = depth_to_world(F.inverse_proj, F.inverse_view, pixel_uv(x, F.width), pixel_uv(y, F.height), F.depth[pix]);
+    float d = length(p - V3{F.cam[0], F.cam[1], F.cam[2]});
+    uint4 v;
+    v.x = pack2(ao, lit);
+    v.y = pack2(n.x, n.y);
+    v.z = pack2(n.z, 0.0f);
+    v.w = pack2(rough, lum);
+    F.feat[pix] = v;
+    F.lin_depth[pix] = d;
+    F.ao[pix] = ao;
+}
+
+// ---------------------------------------------------------------- shared pieces
+struct ImageGeom {
+    uint32_t width, height, pixels;   // one image
+    uint32_t images;
+};
+
+// Gathers the 16 x 80 feature tile of a warp into `stage` ([16][sW1] bf16) for the
+// pixels base..base+15 (global index over images). Invalid pixels get zeros.
+__device__ __forceinline__ void gather_tile(const uint4* __restrict__ feat, const float* __restrict__ ld,
+                                            const ImageGeom& G, uint32_t base, __nv_bfloat16* stage,
+                                            uint32_t& valid_mask) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t total = G.pixels * G.images;
+    valid_mask = 0;
+    for (int e = lane; e < 16 * 9; e += 32) {
+        int r = e / 9, tap = e % 9;
+        uint32_t gp = base + r;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (gp < total) {
+            uint32_t img = gp / G.pixels, local = gp - img * G.pixels;
+            int x = (int)(local % G.width), y = (int)(local / G.width);
+            float dc = ld[gp];
+            if (dc > 0.0f) {
+                int qx = min(max(x + tap % 3 - 1, 0), (int)G.width - 1);
+                int qy = min(max(y + tap / 3 - 1, 0), (int)G.height - 1);
+                uint32_t q = img * G.pixels + (uint32_t)qy * G.width + (uint32_t)qx;
+                v = feat[q];
+                float dq = ld[q];
+                float rel = dq > 0.0f ? fminf(fmaxf((dq - dc) / dc, -1.0f), 1.0f) : 0.0f;
+                // channel 5 (upper half of v.z) carries the relative depth
+                v.z = (v.z & 0xFFFFu) | (pack2(0.0f, rel) & 0xFFFF0000u);
+            }
+        }
+        *reinterpret_cast<uint4*>(stage + r * sW1 + tap * 8) = v;
+    }
+    for (int e = lane; e < 16; e += 32)
+        *reinterpret_cast<uint4*>(stage + e * sW1 + 72) = make_uint4(0, 0, 0, 0);
+    for (int r = 0; r < 16; ++r) {
+        uint32_t gp = base + r;
+        if (gp < total && ld[gp] > 0.0f) valid_mask |= 1u << r;
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ void load_a(const __nv_bfloat16* stage, int stride, int kk, uint32_t a[4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    a[0] = ld32(stage + g * stride + 16 * kk + 2 * t);
+    a[1] = ld32(stage + (g + 8) * stride + 16 * kk + 2 * t);
+    a[2] = ld32(stage + g * stride + 16 * kk + 2 * t + 8);
+    a[3] = ld32(stage + (g + 8) * stride + 16 * kk + 2 * t + 8);
+}
+
+// c[NT][4] = A[16 x 16*KS] * W^T (+ bias), W n-major [NT*8][stride] in shared memory.
+template <int KS, int NT>
+__device__ __forceinline__ void layer(const uint32_t a[KS][4], const __nv_bfloat16* W, int stride, const float* bias,
+                                      float c[NT][4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        float b0 = bias ? bias[nt * 8 + 2 * t] : 0.f, b1 = bias ? bias[nt * 8 + 2 * t + 1] : 0.f;
+        c[nt][0] = b0; c[nt][1] = b1; c[nt][2] = b0; c[nt][3] = b1;
+        const __nv_bfloat16* wr = W + (nt * 8 + g) * stride + 2 * t;
+#pragma unroll
+        for (int kk = 0; kk < KS; ++kk) mma16816(c[nt], a[kk], ld32(wr + 16 * kk), ld32(wr + 16 * kk + 8));
+    }
+}
+
+// ReLU + BF16: accumulator fragments of 2*KS n-tiles → A fragments of KS k-steps.
+template <int KS>
+__device__ __forceinline__ void to_a_relu(const float c[2 * KS][4], uint32_t a[KS][4]) {
+#pragma unroll
+    for (int kk = 0; kk < KS; ++kk) {
+        a[kk][0] = pack2(fmaxf(c[2 * kk][0], 0.f), fmaxf(c[2 * kk][1], 0.f));
+        a[kk][1] = pack2(fmaxf(c[2 * kk][2], 0.f), fmaxf(c[2 * kk][3], 0.f));
+        a[kk][2] = pack2(fmaxf(c[2 * kk + 1][0], 0.f), fmaxf(c[2 * kk + 1][1], 0.f));
+        a[kk][3] = pack2(fmaxf(c[2 * kk + 1][2], 0.f), fmaxf(c[2 * kk + 1][3], 0.f));
+    }
+}
+
+// Softmax over the 49 logits of rows g and g+8 (4 lanes share a row) and the 7x7
+// filter of the noisy AO. w[7][4] receives the weights; returns y for both rows.
+__device__ __forceinline__ void softmax_filter(float z[7][4], const float* __restrict__ ao, const ImageGeom& G,
+                                               uint32_t base, float y[2], float aok[7][4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const uint32_t total = G.pixels * G.images;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float m = -3.0e38f;
+#pragma unroll
+        for (int nt = 0; nt < 7; ++nt)
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+                if (nt * 8 + 2 * t + j < 49) m = fmaxf(m, z[nt][2 * h + j]);
+        m = fmaxf(m, __shfl_xor_sync(0xFFFFFFFFu, m, 1));
+        m = fmaxf(m, __shfl_xor_sync(0xFFFFFFFFu, m, 2));
+        float s = 0.f;
+#pragma unroll
+        for (int nt = 0; nt < 7; ++nt)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                float e = (nt * 8 + 2 * t + j < 49) ? __expf(z[nt][2 * h + j] - m) : 0.f;
+                z[nt][2 * h + j] = e;
+                s += e;
+            }
+        s += __shfl_xor_sync(0xFFFFFFFFu, s, 1);
+        s += __shfl_xor_sync(0xFFFFFFFFu, s, 2);
+        float inv = 1.0f / s;
+        uint32_t gp = base + g + 8 * h;
+        float acc = 0.f;
+        uint32_t img = 0, local = 0;
+        int x = 0, yy = 0;
+        bool ok = gp < total;
+        if (ok) {
+            img = gp / G.pixels;
+            local = gp - img * G.pixels;
+            x = (int)(local % G.width);
+            yy = (int)(local / G.width);
+        }
+#pragma unroll
+        for (int nt = 0; nt < 7; ++nt)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                int k = nt * 8 + 2 * t + j;
+                float wk = z[nt][2 * h + j] * inv;
+                z[nt][2 * h + j] = wk;
+                float a = 0.f;
+                if (k < 49 && ok) {
+                    int qx = min(max(x + k % 7 - 3, 0), (int)G.width - 1);
+                    int qy = min(max(yy + k / 7 - 3, 0), (int)G.height - 1);
+                    a = __ldg(ao + img * G.pixels + (uint32_t)qy * G.width + (uint32_t)qx);
+                }
+                aok[nt][2 * h + j] = a;
+                acc += wk * a;
+            }
+        acc += __shfl_xor_sync(0xFFFFFFFFu, acc, 1);
+        acc += __shfl_xor_sync(0xFFFFFFFFu, acc, 2);
+        y[h] = acc;
+    }
+}
+
+// ---------------------------------------------------------------- inference
+struct InferParams {
+    const __nv_bfloat16* wpack;
+    const float* bias;
+    const uint4* feat;
+    const float* lin_depth;
+    const float* ao;
+    ImageGeom G;
+    float* out;
+};
+
+__global__ void __launch_bounds__(256) denoise_infer_kernel(InferParams P) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(sm_raw);
+    float* sbias = reinterpret_cast<float*>(sm_raw + pFwdEnd * 2);
+    __nv_bfloat16* stage_all = reinterpret_cast<__nv_bfloat16*>(sm_raw + pFwdEnd * 2 + kBias * 4);
+    for (int i = threadIdx.x; i < pFwdEnd / 8; i += blockDim.x)
+        reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(P.wpack)[i];
+    for (int i = threadIdx.x; i < kBias; i += blockDim.x) sbias[i] = P.bias[i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    __nv_bfloat16* stage = stage_all + warp * 16 * sW1;
+    const uint32_t total = P.G.pixels * P.G.images;
+    const uint32_t tiles = (total + kTile - 1) / kTile;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        uint32_t base = tile * kTile + warp * 16;
+        uint32_t valid;
+        gather_tile(P.feat, P.lin_depth, P.G, base, stage, valid);
+        uint32_t a0[5][4];
+#pragma unroll
+        for (int kk = 0; kk < 5; ++kk) load_a(stage, sW1, kk, a0[kk]);
+        float c[8][4];
+        layer<5, 8>(a0, sw + pW1, sW1, sbias, c);
+        uint32_t a1[4][4];
+        to_a_relu<4>(c, a1);
+        layer<4, 8>(a1, sw + pW2, sW, sbias + 64, c);
+        to_a_relu<4>(c, a1);
+        layer<4, 8>(a1, sw + pW3, sW, sbias + 128, c);
+        to_a_relu<4>(c, a1);
+        float z[7][4], aok[7][4], y[2];
+        layer<4, 7>(a1, sw + pW4, sW, sbias + 192, z);
+        softmax_filter(z, P.ao, P.G, base, y, aok);
+        if (t == 0) {
+            for (int h = 0; h < 2; ++h) {
+                uint32_t gp = base + g + 8 * h;
+                if (gp < total) P.out[gp] = ((valid >> (g + 8 * h)) & 1u) ? y[h] : 0.0f;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- training
+struct TrainParams {
+    const __nv_bfloat16* wpack;
+    const float* bias;
+    const uint4* feat;
+    const float* lin_depth;
+    const float* ao;
+    const float* target;
+    ImageGeom G;
+    float grad_scale;          // 2 / number of pixels (mean squared error)
+    float* partial;            // [gridDim.x][kParams]
+    float* partial_loss;       // [gridDim.x]
+};
+
+constexpr int kDwTiles = 40 + 36 * 3;    // (layer, 16-row, 8-col) tiles of dW (bias as an extra column)
+constexpr int kDwPerWarp = (kDwTiles + 7) / 8;
+
+struct TrainSmem {
+    // transposed tiles: [unit][pixel]
+    __nv_bfloat16 xT[80][sT];     // features, row 72 = ones (bias column of dW1)
+    __nv_bfloat16 h1T[72][sT];    // rows 64 = ones, 65..71 = 0
+    __nv_bfloat16 h2T[72][sT];
+    __nv_bfloat16 h3T[72][sT];
+    __nv_bfloat16 d4T[64][sT];    // rows 49..63 = 0
+    __nv_bfloat16 d3T[64][sT];
+    __nv_bfloat16 d2T[64][sT];
+    __nv_bfloat16 d1T[64][sT];
+};
+
+// dW tile t -> (layer, m-tile, n-tile, A rows, B rows)
+__device__ __forceinline__ void dw_tile(int id, int& l, int& mt, int& nt) {
+    if (id < 40) { l = 0; mt = id / 10; nt = id % 10; return; }
+    id -= 40;
+    l = 1 + id / 36;
+    id %= 36;
+    mt = id / 9;
+    nt = id % 9;
+}
+
+__global__ void __launch_bounds__(256, 1) denoise_train_kernel(TrainParams P) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(sm_raw);
+    float* sbias = reinterpret_cast<float*>(sm_raw + pEnd * 2);
+    TrainSmem& S = *reinterpret_cast<TrainSmem*>(sm_raw + pEnd * 2 + kBias * 4);
+    // The per-warp feature tiles live in d3T/d2T, which are written only after every
+    // warp has loaded its features (barrier below).
+    __nv_bfloat16* stage_all = &S.d3T[0][0];
+    static_assert(2 * sizeof(S.d3T) >= 8 * 16 * sW1 * 2, "staging tiles must fit in d3T+d2T");
+    for (int i = threadIdx.x; i < pEnd / 8; i += blockDim.x)
+        reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(P.wpack)[i];
+    for (int i = threadIdx.x; i < kBias; i += blockDim.x) sbias[i] = P.bias[i];
+    // constant rows: ones for the bias columns, zeros for padding
+    for (int i = threadIdx.x; i < sT; i += blockDim.x) {
+        __nv_bfloat16 one = __float2bfloat16(1.0f), zero = __float2bfloat16(0.0f);
+        S.xT[72][i] = one;
+        for (int r = 73; r < 80; ++r) S.xT[r][i] = zero;
+        S.h1T[64][i] = one; S.h2T[64][i] = one; S.h3T[64][i] = one;
+        for (int r = 65; r < 72; ++r) { S.h1T[r][i] = zero; S.h2T[r][i] = zero; S.h3T[r][i] = zero; }
+        for (int r = 49; r < 64; ++r) S.d4T[r][i] = zero;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    __nv_bfloat16* stage = stage_all + warp * 16 * sW1;
+    const uint32_t total = P.G.pixels * P.G.images;
+    const uint32_t tiles = (total + kTile - 1) / kTile;
+    float dw[kDwPerWarp][4];
+#pragma unroll
+    for (int i = 0; i < kDwPerWarp; ++i) dw[i][0] = dw[i][1] = dw[i][2] = dw[i][3] = 0.f;
+    float loss = 0.f;
+    const int px0 = warp * 16;   // this warp's pixel rows inside the tile
+
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        uint32_t base = tile * kTile + px0;
+        uint32_t valid;
+        gather_tile(P.feat, P.lin_depth, P.G, base, stage, valid);
+        // xT: features transposed (rows 0..71)
+        for (int e = lane; e < 16 * 72; e += 32) {
+            int r = e / 72, k = e % 72;
+            S.xT[k][px0 + r] = stage[r * sW1 + k];
+        }
+        uint32_t a0[5][4];
+#pragma unroll
+        for (int kk = 0; kk < 5; ++kk) load_a(stage, sW1, kk, a0[kk]);
+        __syncthreads();   // every warp's staging tile is consumed before d3T/d2T are written
+        float c[8][4];
+        uint32_t a1[4][4];
+        // ---- forward, keeping h1..h3 (post-ReLU, BF16) transposed in shared memory
+        layer<5, 8>(a0, sw + pW1, sW1, sbias, c);
+        to_a_relu<4>(c, a1);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                S.h1T[nt * 8 + 2 * t + (j & 1)][px0 + g + 8 * (j >> 1)] = __float2bfloat16(fmaxf(c[nt][j], 0.f));
+        layer<4, 8>(a1, sw + pW2, sW, sbias + 64, c);
+        to_a_relu<4>(c, a1);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                S.h2T[nt * 8 + 2 * t + (j & 1)][px0 + g + 8 * (j >> 1)] = __float2bfloat16(fmaxf(c[nt][j], 0.f));
+        layer<4, 8>(a1, sw + pW3, sW, sbias + 128, c);
+        to_a_relu<4>(c, a1);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                S.h3T[nt * 8 + 2 * t + (j & 1)][px0 + g + 8 * (j >> 1)] = __float2bfloat16(fmaxf(c[nt][j], 0.f));
+        float z[7][4], aok[7][4], y[2];
+        layer<4, 7>(a1, sw + pW4, sW, sbias + 192, z);
+        softmax_filter(z, P.ao, P.G, base, y, aok);   // z now holds the softmax weights
+        // ---- loss and dL/dz (softmax + filter backward)
+        float dz[8][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            uint32_t gp = base + g + 8 * h;
+            bool ok = ((valid >> (g + 8 * h)) & 1u) != 0;
+            float tgt = ok ? P.target[gp] : 0.f;
+            float err = ok ? (y[h] - tgt) : 0.f;
+            if (t == 0) loss += err * err * (0.5f * P.grad_scale);   // mean over the batch's pixels
+            float dy = err * P.grad_scale;
+            float sdot = 0.f;
+#pragma unroll
+            for (int nt = 0; nt < 7; ++nt)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) sdot += z[nt][2 * h + j] * (dy * aok[nt][2 * h + j]);
+            sdot += __shfl_xor_sync(0xFFFFFFFFu, sdot, 1);
+            sdot += __shfl_xor_sync(0xFFFFFFFFu, sdot, 2);
+#pragma unroll
+            for (int nt = 0; nt < 7; ++nt)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    int k = nt * 8 + 2 * t + j;
+                    float w = z[nt][2 * h + j];
+                    dz[nt][2 * h + j] = (k < 49) ? w * (dy * aok[nt][2 * h + j] - sdot) : 0.f;
+                }
+            dz[7][2 * h] = dz[7][2 * h + 1] = 0.f;
+        }
+#pragma unroll
+        for (int nt = 0; nt < 7; ++nt)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                int col = nt * 8 + 2 * t + (j & 1);
+                if (col < 49) S.d4T[col][px0 + g + 8 * (j >> 1)] = __float2bfloat16(dz[nt][j]);
+            }
+        // ---- back through layers 4..2: dH = dZ * W, masked by ReLU'
+        uint32_t ad[4][4];
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            ad[kk][0] = pack2(dz[2 * kk][0], dz[2 * kk][1]);
+            ad[kk][1] = pack2(dz[2 * kk][2], dz[2 * kk][3]);
+            ad[kk][2] = pack2(dz[2 * kk + 1][0], dz[2 * kk + 1][1]);
+            ad[kk][3] = pack2(dz[2 * kk + 1][2], dz[2 * kk + 1][3]);
+        }
+        __nv_bfloat16(*hT[3])[sT] = {S.h3T, S.h2T, S.h1T};
+        __nv_bfloat16(*dT[3])[sT] = {S.d3T, S.d2T, S.d1T};
+        const int wT[3] = {pW4T, pW3T, pW2T};
+#pragma unroll
+        for (int L = 0; L < 3; ++L) {
+            float dh[8][4];
+            layer<4, 8>(ad, sw + wT[L], sW, nullptr, dh);
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    int unit = nt * 8 + 2 * t + (j & 1), px = px0 + g + 8 * (j >> 1);
+                    float hv = bf(hT[L][unit][px]);
+                    float d = hv > 0.f ? dh[nt][j] : 0.f;
+                    dh[nt][j] = d;
+                    dT[L][unit][px] = __float2bfloat16(d);
+                }
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                ad[kk][0] = pack2(dh[2 * kk][0], dh[2 * kk][1]);
+                ad[kk][1] = pack2(dh[2 * kk][2], dh[2 * kk][3]);
+                ad[kk][2] = pack2(dh[2 * kk + 1][0], dh[2 * kk + 1][1]);
+                ad[kk][3] = pack2(dh[2 * kk + 1][2], dh[2 * kk + 1][3]);
+            }
+        }
+        __syncthreads();
+        // ---- dW += dZ^T * H over the tile's 128 pixels (fixed order)
+#pragma unroll
+        for (int i = 0; i < kDwPerWarp; ++i) {
+            int id = warp + 8 * i;
+            if (id >= kDwTiles) break;
+            int l, mt, nt;
+            dw_tile(id, l, mt, nt);
+            const __nv_bfloat16* A;
+            const __nv_bfloat16* B;
+            if (l == 0) { A = &S.d1T[0][0]; B = &S.xT[0][0]; }
+            else if (l == 1) { A = &S.d2T[0][0]; B = &S.h1T[0][0]; }
+            else if (l == 2) { A = &S.d3T[0][0]; B = &S.h2T[0][0]; }
+            else { A = &S.d4T[0][0]; B = &S.h3T[0][0]; }
+#pragma unroll
+            for (int kk = 0; kk < kTile / 16; ++kk) {
+                uint32_t a[4];
+                const __nv_bfloat16* ar = A + (mt * 16 + g) * sT + 16 * kk + 2 * t;
+                a[0] = ld32(ar);
+                a[1] = ld32(ar + 8 * sT);
+                a[2] = ld32(ar + 8);
+                a[3] = ld32(ar + 8 * sT + 8);
+                const __nv_bfloat16* br = B + (nt * 8 + g) * sT + 16 * kk + 2 * t;
+                mma16816(dw[i], a, ld32(br), ld32(br + 8));
+            }
+        }
+        __syncthreads();
+    }
+    // ---- write this CTA's partial gradient in the FP32 parameter layout
+    float* out = P.partial + (size_t)blockIdx.x * kParams;
+#pragma unroll
+    for (int i = 0; i < kDwPerWarp; ++i) {
+        int id = warp + 8 * i;
+        if (id >= kDwTiles) break;
+        int l, mt, nt;
+        dw_tile(id, l, mt, nt);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            int row = mt * 16 + g + 8 * (j >> 1), col = nt * 8 + 2 * t + (j & 1);
+            int nin = l == 0 ? 72 : 64, nout = l == 3 ? 49 : 64;
+            int ow = l == 0 ? oW1 : (l == 1 ? oW2 : (l == 2 ? oW3 : oW4));
+            int ob = l == 0 ? ob1 : (l == 1 ? ob2 : (l == 2 ? ob3 : ob4));
+            if (row >= nout) continue;
+            if (col < nin) out[ow + row * nin + col] = dw[i][j];
+            else if (col == nin) out[ob + row] = dw[i][j];
+        }
+    }
+    loss += __shfl_xor_sync(0xFFFFFFFFu, loss, 4);
+    loss += __shfl_xor_sync(0xFFFFFFFFu, loss, 8);
+    loss += __shfl_xor_sync(0xFFFFFFFFu, loss, 16);
+    __shared__ float s_loss[8];
+    if (lane == 0) s_loss[warp] = loss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.f;
+        for (int w = 0; w < 8; ++w) s += s_loss[w];
+        P.partial_loss[blockIdx.x] = s;
+    }
+}
+
+// Sums the per-CTA partials in CTA order (deterministic).
+__global__ void reduce_partials_kernel(const float* partial, int ctas, float* grad, const float* partial_loss,
+                                       float* loss) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kParams) {
+        float s = 0.f;
+        for (int c = 0; c < ctas; ++c) s += partial[(size_t)c * kParams + i];
+        grad[i] = s;
+    }
+    if (i == 0) {
+        float s = 0.f;
+        for (int c = 0; c < ctas; ++c) s += partial_loss[c];
+        *loss = s;
+    }
+}
+
+// Adam on the FP32 master weights.
+__global__ void adam_kernel(float* w, float* m, float* v, const float* grad, float lr, float b1, float b2,
+                            float eps, float bc1, float bc2) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kParams) return;
+    float g = grad[i];
+    float mi = b1 * m[i] + (1.f - b1) * g;
+    float vi = b2 * v[i] + (1.f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
+// FP32 master → packed BF16 weights (n-major + transposed copies) and padded biases.
+__global__ void pack_kernel(const float* w, __nv_bfloat16* pk, float* bias) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < pEnd) {
+        float v = 0.f;
+        if (i < pW2) { int n = i / sW1, k = i % sW1; v = k < 72 ? w[oW1 + n * 72 + k] : 0.f; }
+        else if (i < pW3) { int j = i - pW2, n = j / sW, k = j % sW; v = k < 64 ? w[oW2 + n * 64 + k] : 0.f; }
+        else if (i < pW4) { int j = i - pW3, n = j / sW, k = j % sW; v = k < 64 ? w[oW3 + n * 64 + k] : 0.f; }
+        else if (i < pW2T) { int j = i - pW4, n = j / sW, k = j % sW; v = (k < 64 && n < 49) ? w[oW4 + n * 64 + k] : 0.f; }
+        else if (i < pW3T) { int j = i - pW2T, n = j / sW, k = j % sW; v = k < 64 ? w[oW2 + k * 64 + n] : 0.f; }
+        else if (i < pW4T) { int j = i - pW3T, n = j / sW, k = j % sW; v = k < 64 ? w[oW3 + k * 64 + n] : 0.f; }
+        else { int j = i - pW4T, n = j / sW, k = j % sW; v = k < 49 ? w[oW4 + k * 64 + n] : 0.f; }
+        pk[i] = __float2bfloat16(v);
+    }
+    if (i < kBias) {
+        float b;
+        if (i < 64) b = w[ob1 + i];
+        else if (i < 128) b = w[ob2 + i - 64];
+        else if (i < 192) b = w[ob3 + i - 128];
+        else b = (i - 192) < 49 ? w[ob4 + i - 192] : 0.f;
+        bias[i] = b;
+    }
+}
+
+}  // namespace dn
+}  // namespace luz
+
+// ---------------------------------------------------------------- host API
+struct luz_denoiser {
+    luz_ctx* ctx = nullptr;
+    float* w = nullptr;          // FP32 master weights
+    float* m = nullptr;
+    float* v = nullptr;
+    float* grad = nullptr;
+    __nv_bfloat16* pack = nullptr;
+    float* bias = nullptr;
+    float* partial = nullptr;    // [ctas][kParams]
+    float* partial_loss = nullptr;
+    float* loss = nullptr;
+    int ctas = 0;
+    uint64_t step = 0;
+};
+
+namespace luz {
+namespace dn {
+
+static luz_status upload_lut(luz_ctx* ctx) {
+    static bool done = false;
+    if (done) return LUZ_OK;
+    float lut[256];
+    for (int i = 0; i < 256; ++i) lut[i] = (float)std::pow((double)((float)i / 255.0f), 2.2);
+    LUZ_CUDA(ctx, cudaMemcpyToSymbol(c_lin_lut, lut, sizeof(lut)));
+    done = true;
+    return LUZ_OK;
+}
+
+static luz_status repack(luz_ctx* ctx, luz_denoiser* d) {
+    pack_kernel<<<(pEnd + 255) / 256, 256, 0, ctx->stream>>>(d->w, d->pack, d->bias);
+    LUZ_LAUNCHED(ctx, "denoise_pack_kernel");
+    return LUZ_OK;
+}
+
+static size_t infer_smem() { return (size_t)pFwdEnd * 2 + kBias * 4 + 8 * 16 * sW1 * 2; }
+static size_t train_smem() { return (size_t)pEnd * 2 + kBias * 4 + sizeof(TrainSmem); }
+
+static luz_status check_batch(luz_ctx* ctx, const luz_denoise_batch* b) {
+    if (!b || !b->features || !b->lin_depth || !b->noisy_ao || b->width == 0 || b->height == 0 || b->images == 0)
+        return set_error(ctx, LUZ_ERR_INVALID, "incomplete denoiser batch");
+    if ((uint64_t)b->width * b->height * b->images >= (1ull << 31))
+        return set_error(ctx, LUZ_ERR_LIMIT, "denoiser batch larger than 2^31 pixels");
+    return LUZ_OK;
+}
+
+static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* out) {
+    static bool attr = false;
+    if (!attr) {
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)infer_smem()));
+        attr = true;
+    }
+    InferParams P;
+    P.wpack = d->pack;
+    P.bias = d->bias;
+    P.feat = (const uint4*)b->features;
+    P.lin_depth = b->lin_depth;
+    P.ao = b->noisy_ao;
+    P.G = ImageGeom{b->width, b->height, b->width * b->height, b->images};
+    P.out = out;
+    uint32_t tiles = (P.G.pixels * P.G.images + kTile - 1) / kTile;
+    uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)ctx->sm_count * 3);
+    denoise_infer_kernel<<<grid, 256, infer_smem(), ctx->stream>>>(P);
+    LUZ_LAUNCHED(ctx, "denoise_infer_kernel");
+    return LUZ_OK;
+}
+
+static luz_status run_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b) {
+    if (!b->target_ao) return set_error(ctx, LUZ_ERR_INVALID, "training batch without targets");
+    static bool attr = false;
+    if (!attr) {
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)train_smem()));
+        attr = true;
+    }
+    TrainParams P;
+    P.wpack = d->pack;
+    P.bias = d->bias;
+    P.feat = (const uint4*)b->features;
+    P.lin_depth = b->lin_depth;
+    P.ao = b->noisy_ao;
+    P.target = b->target_ao;
+    P.G = ImageGeom{b->width, b->height, b->width * b->height, b->images};
+    P.grad_scale = 2.0f / (float)((double)P.G.pixels * P.G.images);
+    P.partial = d->partial;
+    P.partial_loss = d->partial_loss;
+    LUZ_CUDA(ctx, cudaMemsetAsync(d->partial, 0, (size_t)d->ctas * kParams * 4, ctx->stream));
+    denoise_train_kernel<<<d->ctas, 256, train_smem(), ctx->stream>>>(P);
+    LUZ_LAUNCHED(ctx, "denoise_train_kernel");
+    reduce_partials_kernel<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(d->partial, d->ctas, d->grad,
+                                                                          d->partial_loss, d->loss);
+    LUZ_LAUNCHED(ctx, "denoise_reduce_kernel");
+    return LUZ_OK;
+}
+
+}  // namespace dn
+}  // namespace luz
+
+using namespace luz;
+using namespace luz::dn;
+
+extern "C" {
+
+luz_status luz_denoiser_create(luz_ctx* ctx, uint64_t seed, luz_denoiser** out) {
+    if (!ctx || !out) return LUZ_ERR_INVALID;
+    luz_status s = upload_lut(ctx);
+    if (s != LUZ_OK) return s;
+    luz_denoiser* d = new luz_denoiser();
+    d->ctx = ctx;
+    d->ctas = ctx->sm_count;
+    cudaError_t e = cudaSuccess;
+    auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, bytes); };
+    A((void**)&d->w, kParams * 4);
+    A((void**)&d->m, kParams * 4);
+    A((void**)&d->v, kParams * 4);
+    A((void**)&d->grad, kParams * 4);
+    A((void**)&d->pack, (size_t)pEnd * 2);
+    A((void**)&d->bias, kBias * 4);
+    A((void**)&d->partial, (size_t)d->ctas * kParams * 4);
+    A((void**)&d->partial_loss, (size_t)d->ctas * 4);
+    A((void**)&d->loss, 4);
+    if (e != cudaSuccess) { luz_denoiser_destroy(d); return cuda_error(ctx, e, "cudaMalloc(denoiser)"); }
+    // He-uniform initialisation from a SplitMix64 stream.
+    std::vector<float> w(kParams, 0.0f);
+    uint64_t st = seed * 0x9E3779B97F4A7C15ull + 1;
+    auto next = [&]() {
+        uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return (float)((z ^ (z >> 31)) >> 40) * (1.0f / 16777216.0f);
+    };
+    const int offs[4] = {oW1, oW2, oW3, oW4}, fan_in[4] = {72, 64, 64, 64}, fan_out[4] = {64, 64, 64, 49};
+    for (int l = 0; l < 4; ++l) {
+        float lim = std::sqrt(6.0f / (float)fan_in[l]) * (l == 3 ? 0.1f : 1.0f);
+        for (int k = 0; k < fan_in[l] * fan_out[l]; ++k) w[offs[l] + k] = (2.0f * next() - 1.0f) * lim;
+    }
+    s = luz_denoiser_set_weights(ctx, d, w.data());
+    if (s != LUZ_OK) { luz_denoiser_destroy(d); return s; }
+    *out = d;
+    return LUZ_OK;
+}
+
+void luz_denoiser_destroy(luz_denoiser* d) {
+    if (!d) return;
+    if (d->ctx && d->ctx->stream) cudaStreamSynchronize(d->ctx->stream);
+    void* p[] = {d->w, d->m, d->v, d->grad, d->pack, d->bias, d->partial, d->partial_loss, d->loss};
+    for (void* x : p)
+        if (x) cudaFree(x);
+    delete d;
+}
+
+luz_status luz_denoiser_set_weights(luz_ctx* ctx, luz_denoiser* d, const float* params) {
+    if (!ctx || !d || !params) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaMemcpyAsync(d->w, params, kParams * 4, cudaMemcpyHostToDevice, ctx->stream));
+    LUZ_CUDA(ctx, cudaMemsetAsync(d->m, 0, kParams * 4, ctx->stream));
+    LUZ_CUDA(ctx, cudaMemsetAsync(d->v, 0, kParams * 4, ctx->stream));
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    d->step = 0;
+    return repack(ctx, d);
+}
+
+luz_status luz_denoiser_get_weights(luz_ctx* ctx, luz_denoiser* d, float* params) {
+    if (!ctx || !d || !params) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaMemcpyAsync(params, d->w, kParams * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LUZ_OK;
+}
+
+luz_status luz_denoiser_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* grad,
+                                 float* loss) {
+    if (!ctx || !d) return LUZ_ERR_INVALID;
+    luz_status s = check_batch(ctx, b);
+    if (s == LUZ_OK) s = run_gradient(ctx, d, b);
+    if (s != LUZ_OK) return s;
+    if (grad) LUZ_CUDA(ctx, cudaMemcpyAsync(grad, d->grad, kParams * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (loss) LUZ_CUDA(ctx, cudaMemcpyAsync(loss, d->loss, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return LUZ_OK;
+}
+
+luz_status luz_denoiser_train_step(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float lr,
+                                   float* loss) {
+    if (!ctx || !d) return LUZ_ERR_INVALID;
+    luz_status s = check_batch(ctx, b);
+    if (s == LUZ_OK) s = run_gradient(ctx, d, b);
+    if (s != LUZ_OK) return s;
+    d->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    float bc1 = 1.0f - (float)std::pow(b1, (double)d->step), bc2 = 1.0f - (float)std::pow(b2, (double)d->step);
+    adam_kernel<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(d->w, d->m, d->v, d->grad, lr, b1, b2, 1e-8f, bc1,
+                                                                bc2);
+    LUZ_LAUNCHED(ctx, "adam_kernel");
+    if ((s = repack(ctx, d)) != LUZ_OK) return s;
+    if (loss) {
+        LUZ_CUDA(ctx, cudaMemcpyAsync(loss, d->loss, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return LUZ_OK;
+}
+
+luz_status luz_denoise_batch_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* d_out) {
+    if (!ctx || !d || !d_out) return LUZ_ERR_INVALID;
+    luz_status s = check_batch(ctx, b);
+    if (s != LUZ_OK) return s;
+    return run_infer(ctx, d, b, d_out);
+}
+
+luz_status luz_denoise_features(luz_ctx* ctx, luz_frame* f) {
+    if (!ctx || !f) return LUZ_ERR_INVALID;
+    luz_status s = upload_lut(ctx);
+    if (s != LUZ_OK) return s;
+    FeatParams F;
+    F.albedo = f->albedo;
+    F.normal = f->normal;
+    F.material = f->material;
+    F.depth = f->depth;
+    F.shadow_bits = f->shadow_bits;
+    F.ao_bits = f->ao_bits;
+    F.shadow_slots = f->shadow_slots;
+    F.ao_samples = f->ao_samples;
+    F.words = f->words;
+    F.width = f->width;
+    F.height = f->height;
+    memcpy(F.inverse_proj, f->h_scene.inverse_proj, 64);
+    memcpy(F.inverse_view, f->h_scene.inverse_view, 64);
+    memcpy(F.cam, f->h_scene.cam_pos, 12);
+    F.feat = (uint4*)f->features;
+    F.lin_depth = f->lin_depth;
+    F.ao = f->ao;
+    features_kernel<<<(f->pixels + 255) / 256, 256, 0, ctx->stream>>>(F);
+    LUZ_LAUNCHED(ctx, "denoise_features_kernel");
+    return LUZ_OK;
+}
+
+luz_status luz_denoise(luz_ctx* ctx, luz_denoiser* d, luz_frame* f) {
+    if (!ctx || !d || !f) return LUZ_ERR_INVALID;
+    luz_status s = luz_denoise_features(ctx, f);
+    if (s != LUZ_OK) return s;
+    luz_denoise_batch b{f->features, f->lin_depth, f->ao, nullptr, f->width, f->height, 1};
+    return run_infer(ctx, d, &b, f->ao_denoised);
+}
+
+}  // extern "C"

@@ -140,6 +140,8 @@ struct luz_frame {
     uint32_t* ao_bits = nullptr;
     float* ao = nullptr;
     float* ao_denoised = nullptr;
+    void* features = nullptr;       // 8 x bf16 per pixel (denoiser input)
+    float* lin_depth = nullptr;
     uint32_t shadow_planes_cap = 0, ao_planes_cap = 0;
     uint32_t shadow_slots = 0, ao_samples = 0;
     // compacted lit pixels
