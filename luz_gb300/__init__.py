@@ -288,16 +288,14 @@ class Frame:
     def read(self, plane: int) -> np.ndarray:
         dt, comps = PLANE_DTYPES[plane]
         nbytes = self.plane_bytes(plane)
-        out = np.zeros(max(nbytes // 4, 1), np.uint32).view(dt)
+        raw = np.zeros(max(nbytes, 16), np.uint8)
         if nbytes:
-            _check(lib.luz_frame_read(self.ctx.handle, self._h, plane, _abi.ptr(out), nbytes), self.ctx.handle,
+            _check(lib.luz_frame_read(self.ctx.handle, self._h, plane, _abi.ptr(raw), nbytes), self.ctx.handle,
                    "frame read")
-        out = out[: nbytes // 4]
+        out = raw[:nbytes].view(dt)
         if plane in (PLANE_SHADOW_BITS, PLANE_AO_BITS):
             words = (self.width * self.height + 31) // 32
             return out.reshape(-1, words)
-        if plane == _abi.PLANE_FEATURES:
-            return out.view(np.uint16)[: self.width * self.height * 8].reshape(self.height, self.width, 8)
         if comps > 1:
             return out.reshape(self.height, self.width, comps)
         return out.reshape(self.height, self.width)

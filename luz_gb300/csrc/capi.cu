@@ -170,7 +170,7 @@ luz_status luz_blas_build_batch(luz_ctx* ctx, uint32_t count, const luz_blas_des
 void luz_blas_destroy(luz_blas* b) {
     if (!b) return;
     if (b->arena && --b->arena->refs == 0) {
-        if (b->ctx && b->ctx->stream) cudaStreamSynchronize(b->ctx->stream);
+        cudaDeviceSynchronize();   // the handle may outlive its context: do not touch it
         cudaFree(b->arena->base);
         delete b->arena;
     }
@@ -219,7 +219,7 @@ luz_status luz_tlas_build(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, u
 
 void luz_tlas_destroy(luz_tlas* t) {
     if (!t) return;
-    if (t->ctx && t->ctx->stream) cudaStreamSynchronize(t->ctx->stream);
+    cudaDeviceSynchronize();   // the handle may outlive its context: do not touch it
     if (t->nodes) cudaFree(t->nodes);
     if (t->instances) cudaFree(t->instances);
     if (t->shade) cudaFree(t->shade);
@@ -287,7 +287,7 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
 
 void luz_frame_destroy(luz_frame* f) {
     if (!f) return;
-    if (f->ctx && f->ctx->stream) cudaStreamSynchronize(f->ctx->stream);
+    cudaDeviceSynchronize();   // the handle may outlive its context: do not touch it
     free_frame_buffers(f);
     delete f;
 }

@@ -751,7 +751,7 @@ luz_status luz_denoiser_create(luz_ctx* ctx, uint64_t seed, luz_denoiser** out) 
 
 void luz_denoiser_destroy(luz_denoiser* d) {
     if (!d) return;
-    if (d->ctx && d->ctx->stream) cudaStreamSynchronize(d->ctx->stream);
+    cudaDeviceSynchronize();   // the handle may outlive its context: do not touch it
     void* p[] = {d->w, d->m, d->v, d->grad, d->pack, d->bias, d->partial, d->partial_loss, d->loss};
     for (void* x : p)
         if (x) cudaFree(x);
