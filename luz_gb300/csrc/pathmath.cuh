@@ -122,8 +122,11 @@ LUZ_HD void blue_noise_rg(uint32_t texel_r, uint32_t texel_g, int i, int frame, 
 }
 
 // Stratified sequence: R2 (the 2-D Kronecker sequence of the plastic number,
-// M. Roberts 2018) with a per-pixel Cranley–Patterson rotation taken from the
-// texel, in 32-bit fixed point so that sample i of 1024+ stays exact.
+// M. Roberts 2018) in 32-bit fixed point, so that sample i of 1024+ stays exact.
+// The 64 pixels of an 8x8 block share one Cranley–Patterson rotation and take
+// interleaved points of one sequence (sample i of in-block pixel j is point 64 i + j):
+// the single samples of neighbouring pixels are stratified over the hemisphere,
+// which is what a spatial filter over 1-sample estimates needs.
 constexpr uint32_t kR2a = 0xC13FA9A9u;   // 2^32 / plastic number
 constexpr uint32_t kR2b = 0x91E10DA5u;   // 2^32 / plastic number^2
 LUZ_HD uint32_t hash32(uint32_t x) {
@@ -134,11 +137,12 @@ LUZ_HD uint32_t hash32(uint32_t x) {
 }
 LUZ_HD void stratified_rg(uint32_t px, uint32_t py, int i, int frame, uint32_t stream,
                           float* rx, float* ry) {
-    uint32_t h = hash32(px * 0x9E3779B1u ^ hash32(py + 0x632BE5ABu * (uint32_t)(frame + 1)) ^
+    uint32_t h = hash32((px >> 3) * 0x9E3779B1u ^ hash32((py >> 3) + 0x632BE5ABu * (uint32_t)(frame + 1)) ^
                         (stream * 0x85EBCA77u));
     uint32_t h2 = hash32(h ^ 0x27D4EB2Fu);
-    uint32_t ux = h + (uint32_t)i * kR2a;
-    uint32_t uy = h2 + (uint32_t)i * kR2b;
+    uint32_t k = (uint32_t)i * 64u + (((py & 7u) << 3) | (px & 7u));
+    uint32_t ux = h + k * kR2a;
+    uint32_t uy = h2 + k * kR2b;
     *rx = (float)(ux >> 8) * (1.0f / 16777216.0f);
     *ry = (float)(uy >> 8) * (1.0f / 16777216.0f);
 }

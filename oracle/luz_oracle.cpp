@@ -125,12 +125,15 @@ static uint32_t hash32(uint32_t x) {
     x ^= x >> 16;
     return x;
 }
-// Stratified: R2 sequence with a per-pixel rotation, 32-bit fixed point.
+// Stratified: R2 sequence in 32-bit fixed point; the 64 pixels of an 8x8 block
+// share one rotation and take interleaved points (sample i of pixel j: point 64 i + j).
 static void StratifiedSample(uint32_t px, uint32_t py, int i, int frame, uint32_t stream, float* rx, float* ry) {
-    uint32_t h = hash32(px * 0x9E3779B1u ^ hash32(py + 0x632BE5ABu * (uint32_t)(frame + 1)) ^ (stream * 0x85EBCA77u));
+    uint32_t h = hash32((px >> 3) * 0x9E3779B1u ^ hash32((py >> 3) + 0x632BE5ABu * (uint32_t)(frame + 1)) ^
+                        (stream * 0x85EBCA77u));
     uint32_t h2 = hash32(h ^ 0x27D4EB2Fu);
-    uint32_t ux = h + (uint32_t)i * 0xC13FA9A9u;
-    uint32_t uy = h2 + (uint32_t)i * 0x91E10DA5u;
+    uint32_t k = (uint32_t)i * 64u + (((py & 7u) << 3) | (px & 7u));
+    uint32_t ux = h + k * 0xC13FA9A9u;
+    uint32_t uy = h2 + k * 0x91E10DA5u;
     *rx = (float)(ux >> 8) * (1.0f / 16777216.0f);
     *ry = (float)(uy >> 8) * (1.0f / 16777216.0f);
 }
