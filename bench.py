@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-denoise", action="store_true")
     return ap.parse_args()
 
 
@@ -187,6 +188,121 @@ def run_reference(args, rank):
             "cpu_baseline": res, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                                          "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------- denoised vs plain
+def denoised_vs_plain(g, ctx, stream, flush, K, W):
+    """AO RMSE against 1024 samples (lit pixels, stratified samples) for the denoised
+    single sample and the plain path; the smallest plain sample count with an RMSE at
+    or below the denoised one; ms/frame of both frames (1 shadow ray per light each)."""
+    import numpy as np
+    import torch
+
+    import luz_gb300 as L
+    from luz_gb300 import denoiser as D
+
+    if not D.DEFAULT_WEIGHTS.exists():
+        return None
+    den = D.Denoiser(ctx)
+    den.load(D.DEFAULT_WEIGHTS)
+    fr, tl, sc = g.frame, g.tlas, g.scene
+    shadow_spp = 1
+
+    def setup(ao, light):
+        sc.set_sampling(ao, light_samples=light, sampler=L.SAMPLER_STRATIFIED)
+        fr.upload(sc.block(), sc.lights(), sc.light_count, sc.models(), sc.instance_count)
+
+    tl.build(g.instances, g.n_instances)
+    fr.gbuffer(tl)
+    lit = np.linalg.norm(fr.read(L.PLANE_NORMAL)[..., :3], axis=-1) > 0
+    setup(1024, 0)
+    fr.trace(tl, 1_000_007)
+    fr.ao_resolve()
+    target = fr.read(L.PLANE_AO).copy()
+
+    def plain_rmse(n):
+        setup(n, 0)
+        fr.trace(tl, 7)
+        fr.ao_resolve()
+        return D.lit_rmse(fr.read(L.PLANE_AO), target, lit)
+
+    curve = {n: plain_rmse(n) for n in (1, 2, 4, 8, 16, 32, 64, 128, 256)}
+    setup(1, shadow_spp)
+    fr.trace(tl, 7)
+    den.denoise(fr)
+    r_den = D.lit_rmse(fr.read(L.PLANE_AO_DENOISED), target, lit)
+    # smallest N with plain RMSE <= denoised: bracket on the measured curve, then walk up
+    ns = sorted(curve)
+    n_star = ns[-1]
+    for a, b in zip(ns, ns[1:]):
+        if curve[b] <= r_den:
+            slope = np.log(curve[a] / curve[b]) / np.log(b / a)
+            n_star = max(a, int(np.floor(a * (curve[a] / r_den) ** (1.0 / max(slope, 1e-3)))))
+            break
+    while n_star < 4096:
+        r = curve.get(n_star) if n_star in curve else plain_rmse(n_star)
+        curve[n_star] = r
+        if r <= r_den:
+            break
+        n_star += 1
+
+    def timed(fn):
+        for w in range(W):
+            fn(w)
+        ts = []
+        for k in range(K):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn(100 + k)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.mean(ts)
+
+    def frame_denoised(fi):
+        tl.build(g.instances, g.n_instances)
+        fr.gbuffer(tl)
+        fr.trace(tl, fi)
+        den.denoise(fr)
+        fr.light_pass(True)
+
+    def frame_plain(fi):
+        tl.build(g.instances, g.n_instances)
+        fr.gbuffer(tl)
+        fr.trace(tl, fi)
+        fr.light_pass(False)
+
+    def ao_denoised(fi):
+        fr.trace(tl, fi)
+        den.denoise(fr)
+
+    def ao_plain(fi):
+        fr.trace(tl, fi)
+
+    setup(1, shadow_spp)
+    ms_den = timed(frame_denoised)
+    ms_denoise_only = timed(lambda fi: den.denoise(fr))
+    setup(n_star, shadow_spp)
+    ms_plain = timed(frame_plain)
+    setup(1, 0)
+    ms_ao_den = timed(ao_denoised)
+    setup(n_star, 0)
+    ms_ao_plain = timed(ao_plain)
+    setup(16, shadow_spp)   # back to the benchmark's sampling
+    sc.set_sampling(16, light_samples=1, sampler=L.SAMPLER_PARITY)
+    fr.upload(sc.block(), sc.lights(), sc.light_count, sc.models(), sc.instance_count)
+    flops = 2.0 * (72 * 64 + 64 * 64 + 64 * 64 + 64 * 49) * fr.width * fr.height
+    return {"rmse_vs_1024spp": {"denoised_1spp": r_den, "plain": {str(k): v for k, v in sorted(curve.items())}},
+            "equal_rmse_spp": n_star,
+            "ms_per_frame_denoised": ms_den, "ms_per_frame_plain_equal_rmse": ms_plain,
+            "frame_speedup": ms_plain / ms_den,
+            "ao_only": {"ms_denoised_1spp": ms_ao_den, "ms_plain_equal_rmse": ms_ao_plain,
+                        "speedup": ms_ao_plain / ms_ao_den},
+            "denoiser_ms": ms_denoise_only,
+            "denoiser_tflops_bf16": flops / (ms_denoise_only * 1e-3) / 1e12,
+            "shadow_rays_per_light": shadow_spp, "sampler": "stratified (8x8-block R2)",
+            "weights": D.DEFAULT_WEIGHTS.name}
 
 
 # ---------------------------------------------------------------------------- GPU arm
@@ -325,6 +441,12 @@ def run_ours(args, rank, world, local):
         e2e = {"value": world * rays_per_frame / e2e_s / 1e9, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nbytes)}
 
+    denoised = None
+    if not args.no_denoise:
+        denoised = denoised_vs_plain(g, ctx, stream, flush, K, args.warmup)
+        if ctx.device_status() != 0:
+            raise RuntimeError("device status word raised during the denoised comparison")
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, _ = cpu_baseline(scene, args.cpu_rows)
@@ -339,7 +461,7 @@ def run_ours(args, rank, world, local):
                 "blas_build": {"ms": g.blas_build_ms, "triangles": g.blas_prims, "meshes": len(g.blas),
                                "note": "one batched device build, host->device vertex/index copies included"},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk}
+                "clocks": clk, "denoised_vs_plain": denoised}
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
