@@ -287,6 +287,11 @@ __global__ void __launch_bounds__(256) denoise_infer_kernel(InferParams P) {
         uint32_t base = tile * kTile + warp * 16;
         uint32_t valid;
         gather_tile(P.feat, P.lin_depth, P.G, base, stage, valid);
+        if (valid == 0) {   // no lit pixel in this warp's 16: nothing to filter (warp-uniform)
+            if (lane < 16 && base + lane < total) P.out[base + lane] = 0.0f;
+            __syncwarp();
+            continue;
+        }
         uint32_t a0[5][4];
 #pragma unroll
         for (int kk = 0; kk < 5; ++kk) load_a(stage, sW1, kk, a0[kk]);
