@@ -50,6 +50,8 @@ def load() -> C.CDLL:
             "oracle_light_pass_f64": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32,
                                                 P, C.c_int, C.c_uint32, C.c_uint32]),
             "oracle_trace_ray": (C.c_int, [P, P, P, C.c_float, C.c_float, C.c_int, C.c_int, P]),
+            "oracle_generate_rays": (C.c_uint64, [P, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, C.c_int, P,
+                                                  C.c_uint32, P, C.c_uint64]),
             "oracle_sincos": (None, [P, P, P, C.c_uint32]),
             "oracle_disk_sample": (None, [C.c_float, C.c_float, C.c_float, P, P]),
             "oracle_hemisphere_sample": (None, [C.c_float, C.c_float, P]),
@@ -65,6 +67,22 @@ def load() -> C.CDLL:
 
 def _p(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+REF_LIB = HERE / "_ref" / "libluz_ref_shaders.so"
+
+
+def load_ref():
+    """The reference's own light-pass shader compiled for the CPU (oracle/_ref), or
+    None where the reference tree was not available to build it."""
+    if not REF_LIB.exists():
+        return None
+    lib = C.CDLL(str(REF_LIB))
+    f = lib.ref_light_pass
+    f.restype = C.c_int
+    f.argtypes = [P, P, C.c_int, P, P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, P, C.c_uint64,
+                  C.POINTER(C.c_uint64)]
+    return lib
 
 
 def threads() -> int:

@@ -1014,6 +1014,48 @@ int oracle_light_pass_f64(const luz_scene* S, const luz_light* lights, uint32_t 
     return LUZ_OK;
 }
 
+// The shadow and AO rays of every lit pixel in the order light.frag main issues them
+// (lights in order, their samples, then the AO samples): 8 floats per ray (o, tmin,
+// d, tmax). Returns the number of rays (written up to cap).
+uint64_t oracle_generate_rays(const luz_scene* S, const luz_light* lights, uint32_t nl, const float* normal,
+                              const float* depth, uint32_t W, uint32_t H, int frame, const uint8_t* bn,
+                              uint32_t bn_size, float* out, uint64_t cap) {
+    Sampler smp{S->sampler, bn, bn_size, frame};
+    v3 cam = {S->cam_pos[0], S->cam_pos[1], S->cam_pos[2]};
+    uint64_t n = 0;
+    auto put = [&](v3 o, float tmin, v3 d, float tmax) {
+        if (n < cap) {
+            float* r = out + 8 * n;
+            r[0] = o.x; r[1] = o.y; r[2] = o.z; r[3] = tmin; r[4] = d.x; r[5] = d.y; r[6] = d.z; r[7] = tmax;
+        }
+        ++n;
+    };
+    for (uint32_t pix = 0; pix < W * H; ++pix) {
+        v3 N = {normal[4 * pix], normal[4 * pix + 1], normal[4 * pix + 2]};
+        if (length(N) == 0.0f) continue;
+        uint32_t x = pix % W, y = pix / W;
+        v3 p = DepthToWorld(*S, pixel_uv(x, W), pixel_uv(y, H), depth[pix]);
+        for (uint32_t l = 0; l < nl; ++l) {
+            int ns = S->shadow_type == LUZ_SHADOW_RAYTRACING ? lights[l].num_shadow_samples : 0;
+            for (int s = 0; s < ns; ++s) {
+                float rx, ry, tMax;
+                smp.rg(x, y, s, l + 1, &rx, &ry);
+                v3 O, dir;
+                ShadowRay(lights[l], p, N, cam, rx, ry, O, dir, tMax);
+                put(O, 0.001f, dir, tMax);
+            }
+        }
+        for (int s = 0; s < S->ao_num_samples; ++s) {
+            float rx, ry;
+            smp.rg(x, y, s, 0u, &rx, &ry);
+            v3 O, dir;
+            AORay(p, N, cam, rx, ry, O, dir);
+            put(O, S->ao_min, dir, S->ao_max);
+        }
+    }
+    return n;
+}
+
 // Single rays, for known-answer tests: any-hit (closest = 0) or closest-hit t.
 int oracle_trace_ray(const oracle_tlas* ot, const float o[3], const float d[3], float tmin, float tmax, int closest,
                      int brute, float* t_out) {
