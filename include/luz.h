@@ -315,6 +315,40 @@ luz_status luz_frame_write(luz_ctx* ctx, luz_frame* frame, int32_t plane,
 /* Device pointer of a plane (for zero-copy interop), NULL on error. */
 void* luz_frame_plane_device_ptr(luz_frame* frame, int32_t plane);
 
+/* ------------------------------------------------------------------ batches
+ * Many independent scenes of uneven size as one unit (no counterpart in the
+ * reference, which renders one scene per frame): every TLAS build and G-buffer pass,
+ * ONE persistent visibility launch over the shadow/AO rays of all scenes, every light
+ * pass. Scene constants and instances are uploaded / packed once at creation (the
+ * arrays may be freed after luz_batch_create); luz_batch_capture records a render as
+ * one CUDA graph that luz_batch_replay launches; luz_batch_autotune picks the
+ * visibility launch shape (ray-batch refill size, steps between refills, CTAs per SM)
+ * by timing the batch's own launch. */
+typedef struct luz_batch luz_batch;
+typedef struct luz_batch_scene {
+    const luz_instance* instances;
+    uint32_t instance_count;
+    const luz_scene* scene;
+    const luz_light* lights;
+    uint32_t light_count;
+    const luz_model* models;
+    uint32_t model_count;
+    uint32_t width, height;
+} luz_batch_scene;
+luz_status luz_batch_create(luz_ctx* ctx, uint32_t count, const luz_batch_scene* scenes, luz_batch** out);
+void luz_batch_destroy(luz_batch* b);
+uint32_t luz_batch_count(const luz_batch* b);
+/* The frame of scene i (planes readable with luz_frame_read). */
+luz_frame* luz_batch_frame(luz_batch* b, uint32_t i);
+luz_status luz_batch_render(luz_ctx* ctx, luz_batch* b, int32_t frame_index);
+/* A render with the counting visibility kernel: out[0..4] as luz_trace_visibility_stats. */
+luz_status luz_batch_stats(luz_ctx* ctx, luz_batch* b, int32_t frame_index, uint64_t out[5]);
+/* Records one render (on the context's explicit stream) into a CUDA graph. */
+luz_status luz_batch_capture(luz_ctx* ctx, luz_batch* b, int32_t frame_index);
+luz_status luz_batch_replay(luz_ctx* ctx, luz_batch* b);
+luz_status luz_batch_autotune(luz_ctx* ctx, luz_batch* b, uint32_t reps, luz_vis_tuning* chosen,
+                              float* best_ms);
+
 /* ------------------------------------------------------------------ denoiser
  * Learned kernel-predicting AO denoiser; no counterpart in the reference, which
  * integrates AO with aoSamples rays per pixel (light.frag:111-135). Per pixel an MLP

@@ -396,6 +396,88 @@ class Context:
         self.close()
 
 
+class _BorrowedFrame(Frame):
+    """A frame owned by a batch (not destroyed by this handle)."""
+
+    def __init__(self, ctx: "Context", handle, width: int, height: int):
+        self.ctx, self.width, self.height, self._h = ctx, width, height, handle
+
+    def close(self):
+        self._h = None
+
+
+class Batch:
+    """Many scenes rendered as one unit (luz_batch_*): one batched BLAS build over the
+    meshes of every scene, then per render every TLAS and G-buffer, one visibility
+    launch for all scenes, every light pass; optionally as one CUDA graph."""
+
+    def __init__(self, ctx: "Context", scenes: list[HostScene]):
+        self.ctx, self.scenes = ctx, scenes
+        meshes, first = [], []
+        for sc in scenes:
+            first.append(len(meshes))
+            meshes += sc.meshes()
+        self.blas = ctx.build_blas(meshes)
+        self.triangles = sum(sc.triangle_count() for sc in scenes)
+        n = len(scenes)
+        descs = (_abi.BatchScene * n)()
+        keep = []
+        for i, sc in enumerate(scenes):
+            nm = lib.luz_scene_mesh_count(sc.handle)
+            inst, cnt = Tlas.make_instances(self.blas[first[i]:first[i] + nm], sc.instance_mesh(), sc.transforms())
+            models, lights, block = sc.models(), sc.lights(), sc.block()
+            keep += [inst, models, lights, block]
+            descs[i].instances = C.addressof(inst)
+            descs[i].instance_count = cnt
+            descs[i].scene = C.addressof(block)
+            descs[i].lights = C.addressof(lights)
+            descs[i].light_count = sc.light_count
+            descs[i].models = C.addressof(models)
+            descs[i].model_count = sc.instance_count
+            descs[i].width, descs[i].height = sc.width, sc.height
+        h = C.c_void_p()
+        _check(lib.luz_batch_create(ctx.handle, n, descs, C.byref(h)), ctx.handle, "batch create")
+        self._h = h
+        ctx._adopt(self)
+        self.frames = [_BorrowedFrame(ctx, C.c_void_p(lib.luz_batch_frame(h, i)), sc.width, sc.height)
+                       for i, sc in enumerate(scenes)]
+
+    @property
+    def handle(self):
+        return self._h
+
+    def render(self, frame_index: int = 0) -> None:
+        _check(lib.luz_batch_render(self.ctx.handle, self._h, frame_index), self.ctx.handle, "batch render")
+
+    def stats(self, frame_index: int = 0) -> dict:
+        out = (C.c_uint64 * 5)()
+        _check(lib.luz_batch_stats(self.ctx.handle, self._h, frame_index, out), self.ctx.handle, "batch stats")
+        return {"rays": out[0], "tlas_nodes": out[1], "blas_nodes": out[2], "tris": out[3], "instances": out[4]}
+
+    def capture(self, frame_index: int = 0) -> None:
+        _check(lib.luz_batch_capture(self.ctx.handle, self._h, frame_index), self.ctx.handle, "batch capture")
+
+    def replay(self) -> None:
+        _check(lib.luz_batch_replay(self.ctx.handle, self._h), self.ctx.handle, "batch replay")
+
+    def autotune(self, reps: int = 3):
+        arr = (C.c_uint32 * 4)()
+        ms = C.c_float()
+        _check(lib.luz_batch_autotune(self.ctx.handle, self._h, reps, C.byref(arr), C.byref(ms)), self.ctx.handle,
+               "batch autotune")
+        return dict(zip(("smem_nodes", "refill", "steps", "ctas_per_sm"), list(arr))), ms.value
+
+    def close(self):
+        if self._h:
+            for f in self.frames:
+                f.close()
+            lib.luz_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 # ---------------------------------------------------------------------------- GPUScene mirror
 class GPUScene:
     """Host orchestration of the path, mirroring the reference's GPUScene

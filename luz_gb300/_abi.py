@@ -93,6 +93,12 @@ class GenParams(C.Structure):
                 ("pad1", C.c_uint32)]
 
 
+class BatchScene(C.Structure):
+    _fields_ = [("instances", C.c_void_p), ("instance_count", C.c_uint32), ("scene", C.c_void_p),
+                ("lights", C.c_void_p), ("light_count", C.c_uint32), ("models", C.c_void_p),
+                ("model_count", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
 class DenoiseBatch(C.Structure):
     _fields_ = [("features", C.c_void_p), ("lin_depth", C.c_void_p), ("noisy_ao", C.c_void_p),
                 ("target_ao", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("images", C.c_uint32)]
@@ -142,6 +148,15 @@ SIGNATURES = [
     ("luz_frame_read", C.c_int32, [P, P, C.c_int32, P, C.c_size_t]),
     ("luz_frame_write", C.c_int32, [P, P, C.c_int32, P, C.c_size_t]),
     ("luz_frame_plane_device_ptr", P, [P, C.c_int32]),
+    ("luz_batch_create", C.c_int32, [P, C.c_uint32, C.POINTER(BatchScene), C.POINTER(P)]),
+    ("luz_batch_destroy", None, [P]),
+    ("luz_batch_count", C.c_uint32, [P]),
+    ("luz_batch_frame", P, [P, C.c_uint32]),
+    ("luz_batch_render", C.c_int32, [P, P, C.c_int32]),
+    ("luz_batch_stats", C.c_int32, [P, P, C.c_int32, C.POINTER(C.c_uint64)]),
+    ("luz_batch_capture", C.c_int32, [P, P, C.c_int32]),
+    ("luz_batch_replay", C.c_int32, [P, P]),
+    ("luz_batch_autotune", C.c_int32, [P, P, C.c_uint32, C.POINTER(C.c_uint32 * 4), C.POINTER(C.c_float)]),
     ("luz_denoiser_create", C.c_int32, [P, C.c_uint64, C.POINTER(P)]),
     ("luz_denoiser_destroy", None, [P]),
     ("luz_denoiser_set_weights", C.c_int32, [P, P, c_float_p]),

@@ -814,6 +814,8 @@ static size_t tlas_tmp_bytes(uint32_t cap) {
            align256(sizeof(SegDesc)) + 2 * align256(4);
 }
 
+luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t);
+
 luz_status tlas_alloc(luz_ctx* ctx, luz_tlas* t) {
     uint32_t cap = std::max(t->max_instances, 1u);
     uint32_t m = std::max(cap, 2u) - 1;
@@ -829,7 +831,9 @@ luz_status tlas_alloc(luz_ctx* ctx, luz_tlas* t) {
     return LUZ_OK;
 }
 
-luz_status build_tlas(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint32_t n) {
+// Host part of a TLAS build: validates the instances and packs them into the pinned
+// staging buffer (the buffer must not be in use by an earlier build's copy).
+luz_status pack_tlas_input(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint32_t n) {
     if (n > t->max_instances)
         return set_error(ctx, LUZ_ERR_LIMIT, "instance count exceeds the TLAS max_instances");
     for (uint32_t i = 0; i < n; ++i) {
@@ -846,8 +850,22 @@ luz_status build_tlas(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint3
         d.blas_prims = b->prims;
         d.pad = 0;
     }
-    cudaStream_t st = ctx->stream;
     t->count = n;
+    t->node_count = std::max(n, 2u) - 1;
+    return LUZ_OK;
+}
+
+luz_status build_tlas(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint32_t n) {
+    luz_status s = pack_tlas_input(ctx, t, inst, n);
+    if (s != LUZ_OK) return s;
+    return launch_tlas_build(ctx, t);
+}
+
+// Device part of a TLAS build from the packed staging buffer: one host-to-device copy
+// from pinned memory and the LBVH kernels; no host synchronisation (graph-capturable).
+luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t) {
+    cudaStream_t st = ctx->stream;
+    const uint32_t n = t->count;
     if (n == 0) return LUZ_OK;
     LUZ_CUDA(ctx, cudaMemcpyAsync(t->d_input, t->h_input, (size_t)n * sizeof(DevInstanceInput),
                                   cudaMemcpyHostToDevice, st));

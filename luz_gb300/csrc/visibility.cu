@@ -1,94 +1,204 @@
 // visibility.cu — the persistent wavefront kernel that traces every shadow and AO ray
-// of a frame (light.frag:86-135) and writes the hit/miss bit planes.
+// of a frame (light.frag:86-135) and writes the hit/miss bit planes; and its batched
+// form, one launch over the rays of many scenes.
 //
 // Work items are (slot, lit pixel) pairs, slot-major, so neighbouring items share a
 // light and lie in neighbouring pixels. Each lane holds one ray as an explicit
 // traversal state. After every few traversal steps the warp counts its idle lanes
 // with a ballot; when enough are idle, one lane takes that many items with a single
 // atomic and the idle lanes pick theirs by rank (popc of the lower lanes' ballot
-// bits), then generate their rays while the others keep traversing. Lanes are never
-// left idle for a whole ray of a slow neighbour.
+// bits), then generate their rays while the others keep traversing.
 //
-// Traversal: the TLAS top (breadth-first prefix) is staged in shared memory; BLAS
-// nodes and triangles come through 16-B vector loads; the stack is warp-interleaved
-// in shared memory (entry k of lane l at [k][l]) with a local-memory tail for rare
-// deep paths.
+// Traversal: the TLAS top (breadth-first prefix) is staged in shared memory (single
+// scene); BLAS nodes and triangles come through 16-B vector loads; the stack is
+// warp-interleaved in shared memory (entry k of lane l at [k][l]) with a
+// local-memory tail for rare deep paths.
 #include <algorithm>
 #include <cstring>
 
 #include "raygen.cuh"
 #include "traverse.cuh"
+#include "visibility.cuh"
 
 namespace luz {
-
-struct VisParams {
-    const float4* tlas_nodes;
-    uint32_t tlas_node_count;
-    uint32_t smem_nodes;         // TLAS nodes staged in shared memory
-    const DevInstance* instances;
-    uint32_t instance_count;
-    const float4* surf;
-    const uint32_t* lit_count;
-    const luz_light* lights;
-    const uint32_t* slot_table;
-    uint32_t shadow_slots, ao_samples;
-    float cam[3];
-    float ao_min, ao_max;
-    int sampler, frame;
-    const uint8_t* blue_noise;
-    uint32_t bn_size;
-    uint32_t width;
-    uint32_t words;
-    uint32_t* shadow_bits;
-    uint32_t* ao_bits;
-    unsigned long long* work_counter;
-    uint32_t* status;
-    uint32_t refill;             // refill when at least this many lanes are idle
-    uint32_t steps;              // traversal steps between refill checks
-};
 
 constexpr int kSmemStack = 16;                      // shared-memory stack entries per lane
 constexpr int kLocalStack = kStackSize - kSmemStack;
 constexpr uint32_t kRayStepCap = 1u << 22;
 
+struct LaneRay {
+    V3 wo, wd, widir, idir;
+    WtRay wt;
+    float tmin, tmax;
+    int node, sp;
+    bool in_blas, record_hit;
+    const float4* bn;
+    const float4* bt;
+    const float4* tlas;
+    const DevInstance* insts;
+    uint32_t* out;
+    uint32_t out_bit, budget;
+};
+
+// Generates the ray of item (slot, j) of scene S. Returns false when there is
+// nothing to trace; the miss (AO) has then already been recorded.
+__device__ __forceinline__ bool setup_ray(LaneRay& r, const SceneVis& S, const VisCommon& C, uint32_t slot,
+                                          uint32_t j) {
+    float4 s0 = __ldg(S.surf + 2 * (size_t)j), s1 = __ldg(S.surf + 2 * (size_t)j + 1);
+    V3 p = V3{s0.x, s0.y, s0.z}, N = V3{s1.x, s1.y, s1.z};
+    uint32_t pix = __float_as_uint(s0.w);
+    uint32_t px = pix % S.width, py = pix / S.width;
+    V3 cam = V3{S.cam[0], S.cam[1], S.cam[2]};
+    float rx, ry;
+    if (slot < S.shadow_slots) {
+        uint32_t e = __ldg(S.slot_table + slot);
+        uint32_t li = e & 0xFFFFu, si = e >> 16;
+        sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)si, S.frame, li + 1, &rx, &ry);
+        shadow_ray(S.lights[li], p, N, cam, rx, ry, r.wo, r.wd, r.tmax);
+        r.tmin = 0.001f;
+        r.out = S.shadow_bits + (size_t)slot * S.words + (pix >> 5);
+        r.record_hit = true;
+    } else {
+        uint32_t a = slot - S.shadow_slots;
+        sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)a, S.frame, 0u, &rx, &ry);
+        ao_ray(p, N, cam, rx, ry, r.wo, r.wd);
+        r.tmin = S.ao_min;
+        r.tmax = S.ao_max;
+        r.out = S.ao_bits + (size_t)a * S.words + (pix >> 5);
+        r.record_hit = false;
+    }
+    r.out_bit = 1u << (pix & 31);
+    bool ok = S.instance_count > 0 && finite3(r.wo) && finite3(r.wd) && (r.tmin <= r.tmax) &&
+              !(r.wd.x == 0.0f && r.wd.y == 0.0f && r.wd.z == 0.0f);
+    if (!ok) {
+        if (!r.record_hit) atomicOr(r.out, r.out_bit);   // no ray: a miss
+        return false;
+    }
+    r.widir = safe_inv(r.wd);
+    r.idir = r.widir;
+    r.wt.o = r.wo;
+    r.node = 0;
+    r.sp = 0;
+    r.in_blas = false;
+    r.budget = 0;
+    r.tlas = S.tlas_nodes;
+    r.insts = S.instances;
+    return true;
+}
+
+// Up to `steps` traversal steps of one lane's ray; clears `active` when it ends.
 template <bool kStats>
-__global__ void __launch_bounds__(256, 3) visibility_kernel(VisParams P, unsigned long long* stats) {
+__device__ __forceinline__ void run_steps(LaneRay& r, bool& active, const float4* smem_tlas, uint32_t staged,
+                                          uint32_t* s_stack, int* lstack, uint32_t steps, uint32_t& err,
+                                          TraceCounters& cnt) {
+    for (uint32_t s = 0; s < steps && active; ++s) {
+        bool finished = false, hit = false;
+        if (++r.budget > kRayStepCap) { err |= LUZ_DEV_TRAVERSAL_CAP; finished = true; }
+        else if (r.node >= 0) {
+            if (kStats) { if (r.in_blas) cnt.blas_nodes++; else cnt.tlas_nodes++; }
+            const float4* np = r.in_blas ? r.bn : ((uint32_t)r.node < staged ? smem_tlas : r.tlas);
+            np += (size_t)r.node * kNodeF4;
+            float4 n0 = np[0], n1 = np[1], n2 = np[2], n3 = np[3];
+            const V3 o = r.in_blas ? r.wt.o : r.wo;
+            int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
+            float t0, t1;
+            bool h0 = c0 != kEmptyChild && slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, o, r.idir, r.tmin, r.tmax, t0);
+            bool h1 = c1 != kEmptyChild && slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, o, r.idir, r.tmin, r.tmax, t1);
+            if (h0 && h1) {
+                int nearc = t1 < t0 ? c1 : c0, farc = t1 < t0 ? c0 : c1;
+                if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)farc;
+                else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = farc;
+                else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
+                ++r.sp;
+                r.node = nearc;
+                if (!finished) continue;
+            } else if (h0 || h1) {
+                r.node = h0 ? c0 : c1;
+                continue;
+            }
+        } else if (!r.in_blas) {
+            if (kStats) cnt.instances++;
+            const DevInstance* I = r.insts + (~r.node);
+            const float4* wp = reinterpret_cast<const float4*>(I->w2o);
+            uint4 meta = __ldg(reinterpret_cast<const uint4*>(&I->custom_index));
+            if ((meta.y & 0xFFu) != 0 && meta.w > 0) {
+                float4 q0 = __ldg(wp), q1 = __ldg(wp + 1), q2 = __ldg(wp + 2);
+                float m[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+                V3 od = xform_dir(m, r.wd);
+                r.wt = wt_setup(xform_point(m, r.wo), od);
+                r.idir = safe_inv(od);
+                r.bn = I->nodes;
+                r.bt = I->tris;
+                if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)kStackMarker;
+                else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = kStackMarker;
+                else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
+                ++r.sp;
+                r.in_blas = true;
+                r.node = 0;
+                if (!finished) continue;
+            }
+        } else {
+            if (kStats) cnt.tris++;
+            const float4* tp = r.bt + (size_t)(~r.node) * kTriF4;
+            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            float t, U, V, W, det;
+            if (wt_test(r.wt, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, V3{c.x, c.y, c.z}, t, U, V, W, det) &&
+                t >= r.tmin && t <= r.tmax) {
+                finished = true;
+                hit = true;
+            }
+        }
+        // pop (at most one TLAS marker lies between two nodes)
+        while (!finished) {
+            if (r.sp == 0) { finished = true; break; }
+            --r.sp;
+            int v = r.sp < kSmemStack ? (int)s_stack[r.sp * 32] : lstack[r.sp - kSmemStack];
+            if (v == kStackMarker) {
+                r.in_blas = false;
+                r.idir = r.widir;
+                continue;
+            }
+            r.node = v;
+            break;
+        }
+        if (finished) {
+            if (hit == r.record_hit) atomicOr(r.out, r.out_bit);
+            active = false;
+        }
+    }
+}
+
+__device__ __forceinline__ void flush_stats(unsigned long long* stats, uint32_t rays, const TraceCounters& cnt) {
+    atomicAdd(stats + 0, (unsigned long long)rays);
+    atomicAdd(stats + 1, (unsigned long long)cnt.tlas_nodes);
+    atomicAdd(stats + 2, (unsigned long long)cnt.blas_nodes);
+    atomicAdd(stats + 3, (unsigned long long)cnt.tris);
+    atomicAdd(stats + 4, (unsigned long long)cnt.instances);
+}
+
+// One scene, TLAS top staged in shared memory.
+template <bool kStats>
+__global__ void __launch_bounds__(256, 3) visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
     extern __shared__ float4 smem[];
-    const uint32_t staged = min(P.tlas_node_count, P.smem_nodes);
-    for (uint32_t i = threadIdx.x; i < staged * kNodeF4; i += blockDim.x) smem[i] = __ldg(P.tlas_nodes + i);
+    const uint32_t staged = min(S.tlas_node_count, C.smem_nodes);
+    for (uint32_t i = threadIdx.x; i < staged * kNodeF4; i += blockDim.x) smem[i] = __ldg(S.tlas_nodes + i);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t* s_stack = reinterpret_cast<uint32_t*>(smem + staged * kNodeF4) + warp * (kSmemStack * 32) + lane;
     int lstack[kLocalStack];
     __syncthreads();
-
-    const uint32_t full = 0xFFFFFFFFu;
-    const uint32_t lit = *P.lit_count;
-    const unsigned long long total = (unsigned long long)lit * (P.shadow_slots + P.ao_samples);
-    const V3 cam = V3{P.cam[0], P.cam[1], P.cam[2]};
-    const uint32_t lt_mask = (1u << lane) - 1u;
-    uint32_t err = 0;
+    const uint32_t full = 0xFFFFFFFFu, lt_mask = (1u << lane) - 1u;
+    const uint32_t lit = *S.lit_count;
+    const unsigned long long total = (unsigned long long)lit * (S.shadow_slots + S.ao_samples);
+    uint32_t err = 0, rays = 0;
     TraceCounters cnt{0, 0, 0, 0};
-    uint32_t rays = 0;
-
-    // per-lane ray state
+    LaneRay r{};
     bool active = false, exhausted = false;
-    V3 wo{}, wd{}, widir{}, idir{};
-    WtRay wt{};
-    float tmin = 0.f, tmax = 0.f;
-    int node = 0, sp = 0;
-    bool in_blas = false;
-    const float4* bn = nullptr;
-    const float4* bt = nullptr;
-    uint32_t out_word = 0, out_bit = 0, budget = 0;
-    bool record_hit = false;
-
-    // Items with nothing to trace (empty TLAS, invalid rays) still owe their bit.
     for (;;) {
         uint32_t idle = __ballot_sync(full, !active);
-        if (!exhausted && __popc(idle) >= (int)P.refill) {
+        if (!exhausted && __popc(idle) >= (int)C.refill) {
             int leader = __ffs(idle) - 1;
             unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(P.work_counter, (unsigned long long)__popc(idle));
+            if (lane == leader) base = atomicAdd(C.work_counter, (unsigned long long)__popc(idle));
             base = __shfl_sync(full, base, leader);
             if (base + __popc(idle) >= total) exhausted = true;
             if (!active) {
@@ -96,187 +206,143 @@ __global__ void __launch_bounds__(256, 3) visibility_kernel(VisParams P, unsigne
                 if (item < total) {
                     uint32_t slot = (uint32_t)(item / lit);
                     uint32_t j = (uint32_t)(item - (unsigned long long)slot * lit);
-                    float4 s0 = __ldg(P.surf + 2 * (size_t)j), s1 = __ldg(P.surf + 2 * (size_t)j + 1);
-                    V3 p = V3{s0.x, s0.y, s0.z}, N = V3{s1.x, s1.y, s1.z};
-                    uint32_t pix = __float_as_uint(s0.w);
-                    uint32_t px = pix % P.width, py = pix / P.width;
-                    float rx, ry;
-                    if (slot < P.shadow_slots) {
-                        uint32_t e = __ldg(P.slot_table + slot);
-                        uint32_t li = e & 0xFFFFu, si = e >> 16;
-                        sample_rg(P.blue_noise, P.bn_size, P.sampler, px, py, (int)si, P.frame, li + 1, &rx, &ry);
-                        shadow_ray(P.lights[li], p, N, cam, rx, ry, wo, wd, tmax);
-                        tmin = 0.001f;
-                        out_word = slot * P.words + (pix >> 5);
-                        record_hit = true;
-                    } else {
-                        uint32_t a = slot - P.shadow_slots;
-                        sample_rg(P.blue_noise, P.bn_size, P.sampler, px, py, (int)a, P.frame, 0u, &rx, &ry);
-                        ao_ray(p, N, cam, rx, ry, wo, wd);
-                        tmin = P.ao_min;
-                        tmax = P.ao_max;
-                        out_word = (P.shadow_slots + a) * P.words + (pix >> 5);
-                        record_hit = false;
-                    }
-                    out_bit = 1u << (pix & 31);
                     if (kStats) ++rays;
-                    bool ok = P.instance_count > 0 && finite3(wo) && finite3(wd) && (tmin <= tmax) &&
-                              !(wd.x == 0.0f && wd.y == 0.0f && wd.z == 0.0f);
-                    if (ok) {
-                        widir = safe_inv(wd);
-                        idir = widir;
-                        wt.o = wo;
-                        node = 0;
-                        sp = 0;
-                        in_blas = false;
-                        budget = 0;
-                        active = true;
-                    } else if (!record_hit) {
-                        // no ray: a miss (AO counts misses; shadow records nothing)
-                        uint32_t* w = out_word < P.shadow_slots * P.words ? P.shadow_bits + out_word
-                                                                          : P.ao_bits + (out_word - P.shadow_slots * P.words);
-                        atomicOr(w, out_bit);
-                    }
+                    active = setup_ray(r, S, C, slot, j);
                 }
             }
         }
         if (exhausted && __ballot_sync(full, active) == 0) break;
-        for (uint32_t s = 0; s < P.steps && active; ++s) {
-            bool finished = false, hit = false;
-            if (++budget > kRayStepCap) { err |= LUZ_DEV_TRAVERSAL_CAP; finished = true; }
-            else if (node >= 0) {
-                if (kStats) { if (in_blas) cnt.blas_nodes++; else cnt.tlas_nodes++; }
-                const float4* np = in_blas ? bn : ((uint32_t)node < staged ? smem : P.tlas_nodes);
-                np += (size_t)node * kNodeF4;
-                float4 n0 = np[0], n1 = np[1], n2 = np[2], n3 = np[3];
-                const V3 o = in_blas ? wt.o : wo;
-                int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-                float t0, t1;
-                bool h0 = c0 != kEmptyChild && slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, o, idir, tmin, tmax, t0);
-                bool h1 = c1 != kEmptyChild && slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, o, idir, tmin, tmax, t1);
-                if (h0 && h1) {
-                    int nearc = t1 < t0 ? c1 : c0, farc = t1 < t0 ? c0 : c1;
-                    if (sp < kSmemStack) s_stack[sp * 32] = (uint32_t)farc;
-                    else if (sp < kStackSize) lstack[sp - kSmemStack] = farc;
-                    else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
-                    ++sp;
-                    node = nearc;
-                    if (!finished) continue;
-                } else if (h0 || h1) {
-                    node = h0 ? c0 : c1;
-                    continue;
-                }
-            } else if (!in_blas) {
-                if (kStats) cnt.instances++;
-                const DevInstance* I = P.instances + (~node);
-                const float4* wp = reinterpret_cast<const float4*>(I->w2o);
-                uint4 meta = __ldg(reinterpret_cast<const uint4*>(&I->custom_index));
-                if ((meta.y & 0xFFu) != 0 && meta.w > 0) {
-                    float4 r0 = __ldg(wp), r1 = __ldg(wp + 1), r2 = __ldg(wp + 2);
-                    float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
-                    V3 od = xform_dir(m, wd);
-                    wt = wt_setup(xform_point(m, wo), od);
-                    idir = safe_inv(od);
-                    bn = I->nodes;
-                    bt = I->tris;
-                    if (sp < kSmemStack) s_stack[sp * 32] = (uint32_t)kStackMarker;
-                    else if (sp < kStackSize) lstack[sp - kSmemStack] = kStackMarker;
-                    else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
-                    ++sp;
-                    in_blas = true;
-                    node = 0;
-                    if (!finished) continue;
-                }
-            } else {
-                if (kStats) cnt.tris++;
-                const float4* tp = bt + (size_t)(~node) * kTriF4;
-                float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                float t, U, V, W, det;
-                if (wt_test(wt, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, V3{c.x, c.y, c.z}, t, U, V, W, det) &&
-                    t >= tmin && t <= tmax) {
-                    finished = true;
-                    hit = true;
-                }
-            }
-            // pop (at most one TLAS marker lies between two nodes)
-            while (!finished) {
-                if (sp == 0) { finished = true; break; }
-                --sp;
-                int v = sp < kSmemStack ? (int)s_stack[sp * 32] : lstack[sp - kSmemStack];
-                if (v == kStackMarker) {
-                    in_blas = false;
-                    idir = widir;
-                    continue;
-                }
-                node = v;
-                break;
-            }
-            if (finished) {
-                if (hit == record_hit) {
-                    uint32_t* w = out_word < P.shadow_slots * P.words ? P.shadow_bits + out_word
-                                                                      : P.ao_bits + (out_word - P.shadow_slots * P.words);
-                    atomicOr(w, out_bit);
-                }
-                active = false;
-            }
-        }
+        run_steps<kStats>(r, active, smem, staged, s_stack, lstack, C.steps, err, cnt);
     }
-    if (err) atomicOr(P.status, err);
-    if (kStats) {
-        atomicAdd(stats + 0, (unsigned long long)rays);
-        atomicAdd(stats + 1, (unsigned long long)cnt.tlas_nodes);
-        atomicAdd(stats + 2, (unsigned long long)cnt.blas_nodes);
-        atomicAdd(stats + 3, (unsigned long long)cnt.tris);
-        atomicAdd(stats + 4, (unsigned long long)cnt.instances);
-    }
+    if (err) atomicOr(C.status, err);
+    if (kStats) flush_stats(stats, rays, cnt);
 }
 
-// ---------------------------------------------------------------- host launchers
+// Many scenes in one launch: item g belongs to the scene s with
+// offsets[s] <= g < offsets[s+1]; each lane carries its scene's TLAS and outputs.
+template <bool kStats>
+__global__ void __launch_bounds__(256, 3) visibility_batch_kernel(const SceneVis* __restrict__ scenes, uint32_t n,
+                                                                  const unsigned long long* __restrict__ offsets,
+                                                                  VisCommon C, unsigned long long* stats) {
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t* s_stack = reinterpret_cast<uint32_t*>(smem) + warp * (kSmemStack * 32) + lane;
+    int lstack[kLocalStack];
+    const uint32_t full = 0xFFFFFFFFu, lt_mask = (1u << lane) - 1u;
+    const unsigned long long total = offsets[n];
+    uint32_t err = 0, rays = 0;
+    TraceCounters cnt{0, 0, 0, 0};
+    LaneRay r{};
+    bool active = false, exhausted = false;
+    for (;;) {
+        uint32_t idle = __ballot_sync(full, !active);
+        if (!exhausted && __popc(idle) >= (int)C.refill) {
+            int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(C.work_counter, (unsigned long long)__popc(idle));
+            base = __shfl_sync(full, base, leader);
+            if (base + __popc(idle) >= total) exhausted = true;
+            if (!active) {
+                unsigned long long item = base + __popc(idle & lt_mask);
+                if (item < total) {
+                    uint32_t lo = 0, hi = n - 1;
+                    while (lo < hi) {
+                        uint32_t mid = (lo + hi + 1) >> 1;
+                        if (offsets[mid] <= item) lo = mid; else hi = mid - 1;
+                    }
+                    const SceneVis& S = scenes[lo];
+                    uint32_t lit = *S.lit_count;
+                    unsigned long long local = item - offsets[lo];
+                    uint32_t slot = (uint32_t)(local / lit);
+                    uint32_t j = (uint32_t)(local - (unsigned long long)slot * lit);
+                    if (kStats) ++rays;
+                    active = setup_ray(r, S, C, slot, j);
+                }
+            }
+        }
+        if (exhausted && __ballot_sync(full, active) == 0) break;
+        run_steps<kStats>(r, active, nullptr, 0u, s_stack, lstack, C.steps, err, cnt);
+    }
+    if (err) atomicOr(C.status, err);
+    if (kStats) flush_stats(stats, rays, cnt);
+}
+
+// offsets[s] = rays of scenes 0..s-1 (lit pixels x samples), read after the
+// G-buffer passes have counted the lit pixels.
+__global__ void batch_offsets_kernel(const SceneVis* scenes, uint32_t n, unsigned long long* offsets) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned long long acc = 0;
+    for (uint32_t s = 0; s < n; ++s) {
+        offsets[s] = acc;
+        acc += (unsigned long long)(*scenes[s].lit_count) * (scenes[s].shadow_slots + scenes[s].ao_samples);
+    }
+    offsets[n] = acc;
+}
+
+// ---------------------------------------------------------------- host side
 // Defaults: the best shape of a sweep on the 1080p two-level scene (smem nodes
 // {0,256,512,1024} x refill {1,4,8,16} x steps {4,8,16,32} x CTAs/SM {2,3,4}).
 static const VisTuning g_tuning{256, 16, 32, 3, 1};
 
-luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int frame_index,
-                             unsigned long long* d_stats) {
-    uint32_t S = f->shadow_slots + f->ao_samples;
+const VisTuning& vis_tuning(const luz_ctx* ctx) { return ctx->vis_tuning.set ? ctx->vis_tuning : g_tuning; }
+
+SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index) {
+    SceneVis S;
+    S.tlas_nodes = t->nodes;
+    S.tlas_node_count = t->count ? t->node_count : 0;
+    S.instance_count = t->count;
+    S.instances = t->instances;
+    S.surf = f->surf;
+    S.lit_count = f->lit_count;
+    S.lights = f->d_lights;
+    S.slot_table = f->d_slot_table;
+    S.shadow_slots = f->shadow_slots;
+    S.ao_samples = f->ao_samples;
+    memcpy(S.cam, f->h_scene.cam_pos, 12);
+    S.ao_min = f->h_scene.ao_min;
+    S.ao_max = f->h_scene.ao_max;
+    S.sampler = f->h_scene.sampler;
+    S.frame = frame_index;
+    S.width = f->width;
+    S.words = f->words;
+    S.shadow_bits = f->shadow_bits;
+    S.ao_bits = f->ao_bits;
+    return S;
+}
+
+VisCommon make_vis_common(luz_ctx* ctx, unsigned long long* work_counter) {
+    const VisTuning& tu = vis_tuning(ctx);
+    VisCommon C;
+    C.blue_noise = ctx->d_blue_noise;
+    C.bn_size = ctx->blue_noise_size;
+    C.work_counter = work_counter;
+    C.status = ctx->d_status;
+    C.refill = tu.refill;
+    C.steps = tu.steps;
+    C.smem_nodes = tu.smem_nodes;
+    return C;
+}
+
+luz_status clear_visibility(luz_ctx* ctx, luz_frame* f) {
     cudaStream_t st = ctx->stream;
     if (f->shadow_slots)
         LUZ_CUDA(ctx, cudaMemsetAsync(f->shadow_bits, 0, (size_t)f->shadow_slots * f->words * 4, st));
     if (f->ao_samples)
         LUZ_CUDA(ctx, cudaMemsetAsync(f->ao_bits, 0, (size_t)f->ao_samples * f->words * 4, st));
-    if (S == 0) return LUZ_OK;
+    return LUZ_OK;
+}
+
+luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int frame_index,
+                             unsigned long long* d_stats) {
+    luz_status s = clear_visibility(ctx, f);
+    if (s != LUZ_OK) return s;
+    if (f->shadow_slots + f->ao_samples == 0) return LUZ_OK;
+    cudaStream_t st = ctx->stream;
     LUZ_CUDA(ctx, cudaMemsetAsync(f->work_counter, 0, 8, st));
-    const VisTuning& tu = ctx->vis_tuning.set ? ctx->vis_tuning : g_tuning;
-    VisParams P;
-    P.tlas_nodes = t->nodes;
-    P.tlas_node_count = t->count ? t->node_count : 0;
-    P.smem_nodes = tu.smem_nodes;
-    P.instances = t->instances;
-    P.instance_count = t->count;
-    P.surf = f->surf;
-    P.lit_count = f->lit_count;
-    P.lights = f->d_lights;
-    P.slot_table = f->d_slot_table;
-    P.shadow_slots = f->shadow_slots;
-    P.ao_samples = f->ao_samples;
-    memcpy(P.cam, f->h_scene.cam_pos, 12);
-    P.ao_min = f->h_scene.ao_min;
-    P.ao_max = f->h_scene.ao_max;
-    P.sampler = f->h_scene.sampler;
-    P.frame = frame_index;
-    P.blue_noise = ctx->d_blue_noise;
-    P.bn_size = ctx->blue_noise_size;
-    P.width = f->width;
-    P.words = f->words;
-    P.shadow_bits = f->shadow_bits;
-    // The AO planes follow the shadow planes in one index space (out_word); the
-    // kernel splits it back.
-    P.ao_bits = f->ao_bits;
-    P.work_counter = f->work_counter;
-    P.status = ctx->d_status;
-    P.refill = tu.refill;
-    P.steps = tu.steps;
-    uint32_t staged = std::min<uint32_t>(P.tlas_node_count, tu.smem_nodes);
+    SceneVis S = make_scene_vis(f, t, frame_index);
+    VisCommon C = make_vis_common(ctx, f->work_counter);
+    const VisTuning& tu = vis_tuning(ctx);
+    uint32_t staged = std::min<uint32_t>(S.tlas_node_count, tu.smem_nodes);
     size_t smem = (size_t)staged * 64 + (size_t)256 * kSmemStack * 4;
     static size_t attr_bytes = 0;
     if (smem > attr_bytes) {
@@ -287,11 +353,33 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     uint32_t grid = (uint32_t)ctx->sm_count * tu.ctas_per_sm;
     if (d_stats) {
         LUZ_CUDA(ctx, cudaMemsetAsync(d_stats, 0, 5 * sizeof(unsigned long long), st));
-        visibility_kernel<true><<<grid, 256, smem, st>>>(P, d_stats);
+        visibility_kernel<true><<<grid, 256, smem, st>>>(S, C, d_stats);
         LUZ_LAUNCHED(ctx, "visibility_kernel<stats>");
     } else {
-        visibility_kernel<false><<<grid, 256, smem, st>>>(P, nullptr);
+        visibility_kernel<false><<<grid, 256, smem, st>>>(S, C, nullptr);
         LUZ_LAUNCHED(ctx, "visibility_kernel");
+    }
+    return LUZ_OK;
+}
+
+luz_status launch_visibility_batch(luz_ctx* ctx, const SceneVis* d_scenes, uint32_t n,
+                                   unsigned long long* d_offsets, unsigned long long* work_counter,
+                                   unsigned long long* d_stats) {
+    cudaStream_t st = ctx->stream;
+    batch_offsets_kernel<<<1, 32, 0, st>>>(d_scenes, n, d_offsets);
+    LUZ_LAUNCHED(ctx, "batch_offsets_kernel");
+    LUZ_CUDA(ctx, cudaMemsetAsync(work_counter, 0, 8, st));
+    VisCommon C = make_vis_common(ctx, work_counter);
+    const VisTuning& tu = vis_tuning(ctx);
+    size_t smem = (size_t)256 * kSmemStack * 4;
+    uint32_t grid = (uint32_t)ctx->sm_count * tu.ctas_per_sm;
+    if (d_stats) {
+        LUZ_CUDA(ctx, cudaMemsetAsync(d_stats, 0, 5 * sizeof(unsigned long long), st));
+        visibility_batch_kernel<true><<<grid, 256, smem, st>>>(d_scenes, n, d_offsets, C, d_stats);
+        LUZ_LAUNCHED(ctx, "visibility_batch_kernel<stats>");
+    } else {
+        visibility_batch_kernel<false><<<grid, 256, smem, st>>>(d_scenes, n, d_offsets, C, nullptr);
+        LUZ_LAUNCHED(ctx, "visibility_batch_kernel");
     }
     return LUZ_OK;
 }
@@ -315,7 +403,7 @@ extern "C" luz_status luz_ctx_set_vis_tuning(luz_ctx* ctx, const luz_vis_tuning*
 extern "C" luz_status luz_ctx_get_vis_tuning(const luz_ctx* ctx, luz_vis_tuning* t) {
     using namespace luz;
     if (!ctx || !t) return LUZ_ERR_INVALID;
-    const VisTuning& tu = ctx->vis_tuning.set ? ctx->vis_tuning : g_tuning;
+    const VisTuning& tu = vis_tuning(ctx);
     *t = luz_vis_tuning{tu.smem_nodes, tu.refill, tu.steps, tu.ctas_per_sm};
     return LUZ_OK;
 }

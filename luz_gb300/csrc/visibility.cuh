@@ -1,0 +1,40 @@
+// visibility.cuh — inputs of the visibility kernels, shared with the batch driver.
+#pragma once
+#include "internal.cuh"
+
+namespace luz {
+
+// Per-scene inputs of the visibility pass (a device array in batch mode).
+struct SceneVis {
+    const float4* tlas_nodes;
+    uint32_t tlas_node_count;
+    uint32_t instance_count;
+    const DevInstance* instances;
+    const float4* surf;
+    const uint32_t* lit_count;
+    const luz_light* lights;
+    const uint32_t* slot_table;
+    uint32_t shadow_slots, ao_samples;
+    float cam[3];
+    float ao_min, ao_max;
+    int sampler, frame;
+    uint32_t width, words;
+    uint32_t* shadow_bits;
+    uint32_t* ao_bits;
+};
+
+struct VisCommon {
+    const uint8_t* blue_noise;
+    uint32_t bn_size;
+    unsigned long long* work_counter;
+    uint32_t* status;
+    uint32_t refill, steps, smem_nodes;
+};
+
+SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index);
+luz_status clear_visibility(luz_ctx* ctx, luz_frame* f);
+luz_status launch_visibility_batch(luz_ctx* ctx, const SceneVis* d_scenes, uint32_t n,
+                                   unsigned long long* d_offsets, unsigned long long* work_counter,
+                                   unsigned long long* d_stats);
+
+}  // namespace luz
