@@ -571,7 +571,7 @@ void gen_budget(luz_host_scene* s, const luz_gen_params& p, Rng& rng) {
     luz_gen_params q = p;
     q.meshes = nmesh;
     q.subdivisions = (uint32_t)level;
-    q.instances = std::max(8u, budget / per * 2);
+    q.instances = std::max(1u, (budget + per / 2) / per);   // instanced triangles ~ the budget
     gen_spheres(s, q, rng, q.instances, 8, 2);
 }
 
