@@ -461,6 +461,14 @@ __global__ void tlas_instance_kernel(const DevInstanceInput* in, uint32_t n, flo
     atomicMax(seg_bounds + 5, float_to_ordered(c.z));
 }
 
+__global__ void tlas_setup_kernel(uint32_t* bounds, SegDesc* seg, SegDesc value, uint32_t* zero) {
+    if (threadIdx.x < 6) bounds[threadIdx.x] = threadIdx.x < 3 ? 0xFFFFFFFFu : 0u;
+    if (threadIdx.x == 0) {
+        *seg = value;
+        *zero = 0;
+    }
+}
+
 __global__ void tlas_morton_kernel(const float4* inst_box, uint32_t n, const uint32_t* seg_bounds,
                                    unsigned long long* keys, uint32_t* vals) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -892,13 +900,11 @@ luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t) {
     sd.prim_count = n;
     sd.node_off = 0;
     sd.nodes = karras_nodes;
-    // bounds init + segment descriptor in one small upload via pinned staging
-    struct Small { uint32_t b[6]; uint32_t zero; } small;
-    for (int k = 0; k < 6; ++k) small.b[k] = k < 3 ? 0xFFFFFFFFu : 0u;
-    small.zero = 0;
-    LUZ_CUDA(ctx, cudaMemcpyAsync(bounds, small.b, 24, cudaMemcpyHostToDevice, st));
-    LUZ_CUDA(ctx, cudaMemcpyAsync(d_seg, &sd, sizeof(SegDesc), cudaMemcpyHostToDevice, st));
-    LUZ_CUDA(ctx, cudaMemsetAsync(d_zero, 0, 4, st));
+    // Bounds initialiser, segment descriptor and zero offset are written by a kernel from
+    // its parameters: a copy from host memory would, inside a CUDA graph, re-read a
+    // host address that no longer holds them.
+    tlas_setup_kernel<<<1, 32, 0, st>>>(bounds, d_seg, sd, d_zero);
+    LUZ_LAUNCHED(ctx, "tlas_setup_kernel");
     LUZ_CUDA(ctx, cudaMemsetAsync(node_parent, 0xFF, (size_t)m * 4, st));
     LUZ_CUDA(ctx, cudaMemsetAsync(leaf_parent, 0xFF, (size_t)n * 4, st));
     LUZ_CUDA(ctx, cudaMemsetAsync(flags, 0, (size_t)m * 4, st));
