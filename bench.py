@@ -443,7 +443,8 @@ def run_ours(args, rank, world, local):
         raise RuntimeError("device status word raised during timing")
 
     # roofline of the dominant kernel (visibility): algorithmic bytes per launch
-    vis_bytes = (stats["rays"] * (32 + 0.125) + (stats["tlas_nodes"] + stats["blas_nodes"]) * 64 +
+    # (a 4-wide node visit reads 7 of its 8 float4: 112 B)
+    vis_bytes = (stats["rays"] * (32 + 0.125) + (stats["tlas_nodes"] + stats["blas_nodes"]) * 112 +
                  stats["tris"] * 48 + stats["instances"] * 80)
     vis_s = stage_ms["visibility"] * 1e-3
     peak, peak_kind = measured_peaks()

@@ -195,8 +195,8 @@ luz_status luz_ctx_set_stream(luz_ctx* ctx, void* stream);
 luz_status luz_ctx_set_blue_noise(luz_ctx* ctx, const uint8_t* rgba8, uint32_t size);
 
 /* Launch shape of the persistent visibility kernel (no counterpart in the reference,
- * whose traversal is the driver's): TLAS nodes staged in shared memory per CTA
- * (0..2048), idle lanes that trigger a warp's refill (1..32), traversal steps between
+ * whose traversal is the driver's): 4-wide TLAS nodes (128 B each) staged in shared
+ * memory per CTA (0..1024), idle lanes that trigger a warp's refill (1..32), traversal steps between
  * refill checks (1..1024), CTAs per SM (1..16). All zero restores the defaults. */
 typedef struct luz_vis_tuning {
     uint32_t smem_nodes;

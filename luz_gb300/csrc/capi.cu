@@ -221,6 +221,8 @@ void luz_tlas_destroy(luz_tlas* t) {
     if (!t) return;
     cudaDeviceSynchronize();   // the handle may outlive its context: do not touch it
     if (t->nodes) cudaFree(t->nodes);
+    if (t->nodes4) cudaFree(t->nodes4);
+    if (t->levels) cudaFree(t->levels);
     if (t->instances) cudaFree(t->instances);
     if (t->shade) cudaFree(t->shade);
     if (t->d_input) cudaFree(t->d_input);

@@ -25,17 +25,24 @@ constexpr int32_t kEmptyChild = (int32_t)0x80000001;  // child slot with an inve
 constexpr int32_t kStackMarker = (int32_t)0x80000000; // two-level stack: back to the TLAS
 constexpr int kStackSize = 128;
 
-// One TLAS leaf, in sorted (leaf) order. 80 B, 16-B aligned for vector loads.
+// A 4-wide node (128 B = 8 x float4), the even-depth collapse of the binary tree:
+//   f0 lo.x[4], f1 hi.x[4], f2 lo.y[4], f3 hi.y[4], f4 lo.z[4], f5 hi.z[4],
+//   f6 child[4] (int bits: >= 0 a 4-wide node, < 0 a leaf ~index, kEmptyChild), f7 0.
+constexpr int kNode4F4 = 8;
+
+// One TLAS leaf, in sorted (leaf) order. 96 B, 16-B aligned for vector loads.
 struct __align__(16) DevInstance {
     float w2o[12];          // world -> object, 3x4 row-major
-    const float4* nodes;    // BLAS nodes
+    const float4* nodes;    // BLAS binary nodes
     const float4* tris;     // BLAS triangles
     uint32_t custom_index;  // instanceCustomIndex = modelRID
     uint32_t mask;
     uint32_t input_index;   // position in the caller's instance array
     uint32_t blas_prims;    // BLAS primitive count
+    const float4* nodes4;   // BLAS 4-wide nodes
+    const float4* pad;
 };
-static_assert(sizeof(DevInstance) == 80, "DevInstance layout");
+static_assert(sizeof(DevInstance) == 96, "DevInstance layout");
 
 // Per-instance data used by the G-buffer kernel, in the caller's instance order.
 struct DevShadeInstance {
@@ -56,6 +63,7 @@ struct DevInstanceInput {
     uint32_t mask;
     uint32_t blas_prims;
     uint32_t pad;
+    const float4* nodes4;
 };
 
 // ---------------------------------------------------------------- handles
@@ -97,6 +105,7 @@ struct luz_blas {
     luz_ctx* ctx = nullptr;
     luz::Arena* arena = nullptr;
     float4* nodes = nullptr;             // max(n-1,1) nodes
+    float4* nodes4 = nullptr;            // 4-wide collapse (at most max(n-1,1) nodes)
     float4* tris = nullptr;              // n triangles
     uint32_t* morton = nullptr;          // sorted 30-bit keys (n)
     uint32_t* order = nullptr;           // sorted primitive order (n)
@@ -111,6 +120,8 @@ struct luz_tlas {
     uint32_t max_instances = 0;
     uint32_t count = 0;
     float4* nodes = nullptr;             // BFS order, max(n-1,1) nodes
+    float4* nodes4 = nullptr;            // 4-wide collapse, breadth-first order
+    uint32_t* levels = nullptr;          // BFS level table (count, starts)
     luz::DevInstance* instances = nullptr;        // leaf order
     luz::DevShadeInstance* shade = nullptr;       // input order
     luz::DevInstanceInput* d_input = nullptr;

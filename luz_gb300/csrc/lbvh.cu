@@ -418,6 +418,198 @@ __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, 
     }
 }
 
+// ---------------------------------------------------------------- 4-wide collapse
+// Every binary node at even depth becomes a 4-wide node whose slots are its
+// grandchildren (or its children, where a child is a leaf). Numbering: the rank of
+// the node among its segment's even-depth nodes in binary-node order (root first).
+
+// flags[q] = 1 when internal node q lies at even depth in its segment's tree.
+__global__ void even_depth_kernel(const SegDesc* segs, const uint32_t* seg_node_off, int nseg, uint32_t total_nodes,
+                                  const uint32_t* node_parent, uint32_t* flags) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= total_nodes) return;
+    int s = find_seg(seg_node_off, nseg, q);
+    const uint32_t off = segs[s].node_off;
+    uint32_t d = 0, p = node_parent[q];
+    for (uint32_t guard = 0; p != 0xFFFFFFFFu && guard < 4096; ++guard) {
+        ++d;
+        p = node_parent[off + (p >> 1)];
+    }
+    flags[q] = (d & 1u) == 0u;
+}
+
+// Chunked exclusive scan of u32 (chunks of 1024 = 256 threads x 4).
+__global__ void __launch_bounds__(256) chunk_sum_kernel(const uint32_t* in, uint32_t n, uint32_t* sums) {
+    __shared__ uint32_t s_tmp[8];
+    uint32_t base = blockIdx.x * 1024 + threadIdx.x * 4, c = 0;
+    for (int k = 0; k < 4; ++k) c += base + k < n ? in[base + k] : 0u;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, o);
+    if ((threadIdx.x & 31) == 0) s_tmp[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < 8; ++w) t += s_tmp[w];
+        sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) chunk_scan_kernel(uint32_t* sums, uint32_t chunks) {
+    __shared__ uint32_t s_warp[32];
+    __shared__ uint32_t s_carry;
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < chunks; base += 1024) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < chunks ? sums[i] : 0u, x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        uint32_t pre = 0, all = 0;
+        for (int w = 0; w < 32; ++w) {
+            if (w < warp) pre += s_warp[w];
+            all += s_warp[w];
+        }
+        uint32_t carry = s_carry;
+        if (i < chunks) sums[i] = carry + pre + x - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry = carry + all;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) chunk_apply_kernel(const uint32_t* in, uint32_t n, const uint32_t* offs,
+                                                          uint32_t* out) {
+    __shared__ uint32_t s_tmp[8];
+    uint32_t base = blockIdx.x * 1024 + threadIdx.x * 4;
+    uint32_t v[4], c = 0;
+    for (int k = 0; k < 4; ++k) { v[k] = base + k < n ? in[base + k] : 0u; c += v[k]; }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_tmp[warp] = x;
+    __syncthreads();
+    uint32_t pre = 0;
+    for (int w = 0; w < warp; ++w) pre += s_tmp[w];
+    uint32_t run = offs[blockIdx.x] + pre + x - c;
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+}
+
+struct Slot4 {
+    float lx[4], hx[4], ly[4], hy[4], lz[4], hz[4];
+    int ch[4];
+    int k;
+};
+
+__device__ __forceinline__ void slot4_put(Slot4& s, const float4* n2, int side, int child) {
+    float4 a = n2[side], z = n2[2];
+    s.lx[s.k] = a.x; s.hx[s.k] = a.y; s.ly[s.k] = a.z; s.hy[s.k] = a.w;
+    s.lz[s.k] = side ? z.z : z.x;
+    s.hz[s.k] = side ? z.w : z.y;
+    s.ch[s.k] = child;
+    ++s.k;
+}
+
+__device__ __forceinline__ void slot4_store(Slot4& s, float4* out) {
+    const float inf = __int_as_float(0x7f800000);
+    for (; s.k < 4; ++s.k) {
+        s.lx[s.k] = s.ly[s.k] = s.lz[s.k] = inf;
+        s.hx[s.k] = s.hy[s.k] = s.hz[s.k] = -inf;
+        s.ch[s.k] = kEmptyChild;
+    }
+    out[0] = make_float4(s.lx[0], s.lx[1], s.lx[2], s.lx[3]);
+    out[1] = make_float4(s.hx[0], s.hx[1], s.hx[2], s.hx[3]);
+    out[2] = make_float4(s.ly[0], s.ly[1], s.ly[2], s.ly[3]);
+    out[3] = make_float4(s.hy[0], s.hy[1], s.hy[2], s.hy[3]);
+    out[4] = make_float4(s.lz[0], s.lz[1], s.lz[2], s.lz[3]);
+    out[5] = make_float4(s.hz[0], s.hz[1], s.hz[2], s.hz[3]);
+    out[6] = make_float4(__int_as_float(s.ch[0]), __int_as_float(s.ch[1]), __int_as_float(s.ch[2]),
+                         __int_as_float(s.ch[3]));
+    out[7] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// idx4[q]: exclusive prefix of the even-depth flags over all segments' nodes.
+__global__ void bvh4_emit_kernel(const SegDesc* segs, const uint32_t* seg_node_off, int nseg, uint32_t total_nodes,
+                                 const uint32_t* flags, const uint32_t* idx4) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= total_nodes || !flags[q]) return;
+    int s = find_seg(seg_node_off, nseg, q);
+    const SegDesc sd = segs[s];
+    if (!sd.nodes4) return;
+    const uint32_t base4 = idx4[sd.node_off];
+    const float4* n2 = sd.nodes + (size_t)(q - sd.node_off) * kNodeF4;
+    float4 n3 = n2[3];
+    int c[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
+    Slot4 s4;
+    s4.k = 0;
+    for (int side = 0; side < 2; ++side) {
+        if (c[side] < 0) {
+            slot4_put(s4, n2, side, c[side]);
+            continue;
+        }
+        const float4* m = sd.nodes + (size_t)c[side] * kNodeF4;
+        float4 m3 = m[3];
+        int g[2] = {__float_as_int(m3.x), __float_as_int(m3.y)};
+        for (int s2 = 0; s2 < 2; ++s2)
+            slot4_put(s4, m, s2, g[s2] < 0 ? g[s2] : (int)(idx4[sd.node_off + g[s2]] - base4));
+    }
+    slot4_store(s4, sd.nodes4 + (size_t)(idx4[q] - base4) * kNode4F4);
+}
+
+// TLAS: the binary tree is in breadth-first order with level table
+// levels = {L, start_0, ..., start_L}; the 4-wide nodes are the even levels, in order.
+__global__ void __launch_bounds__(1024) tlas_bvh4_kernel(const float4* nodes, uint32_t m, const uint32_t* levels,
+                                                         float4* nodes4) {
+    __shared__ uint32_t s_start[66], s_even[66];
+    __shared__ uint32_t s_levels;
+    if (threadIdx.x == 0) {
+        uint32_t L = min(levels[0], 64u);
+        s_levels = L;
+        uint32_t acc = 0;
+        for (uint32_t l = 0; l <= L; ++l) s_start[l] = levels[1 + l];
+        for (uint32_t l = 0; l < L; ++l) {
+            s_even[l] = acc;
+            if ((l & 1u) == 0) acc += s_start[l + 1] - s_start[l];
+        }
+    }
+    __syncthreads();
+    const uint32_t L = s_levels;
+    for (uint32_t b = threadIdx.x; b < m; b += blockDim.x) {
+        uint32_t l = 0;
+        while (l + 1 < L && s_start[l + 1] <= b) ++l;
+        if (l & 1u) continue;
+        const float4* n2 = nodes + (size_t)b * kNodeF4;
+        float4 n3 = n2[3];
+        int c[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
+        Slot4 s4;
+        s4.k = 0;
+        for (int side = 0; side < 2; ++side) {
+            if (c[side] < 0) {
+                slot4_put(s4, n2, side, c[side]);
+                continue;
+            }
+            const float4* mm = nodes + (size_t)c[side] * kNodeF4;
+            float4 m3 = mm[3];
+            int g[2] = {__float_as_int(m3.x), __float_as_int(m3.y)};
+            for (int s2 = 0; s2 < 2; ++s2) {
+                int ref = g[s2];
+                if (ref >= 0 && l + 2 < L) ref = (int)(s_even[l + 2] + ((uint32_t)ref - s_start[l + 2]));
+                slot4_put(s4, mm, s2, ref);
+            }
+        }
+        slot4_store(s4, nodes4 + (size_t)(s_even[l] + (b - s_start[l])) * kNode4F4);
+    }
+}
+
 // ---------------------------------------------------------------- TLAS
 __global__ void tlas_instance_kernel(const DevInstanceInput* in, uint32_t n, float4* inst_box,
                                      DevShadeInstance* shade, uint32_t* seg_bounds) {
@@ -493,6 +685,8 @@ __global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_
     DevInstance d;
     affine_inverse(ii.o2w, d.w2o);
     d.nodes = ii.nodes;
+    d.nodes4 = ii.nodes4;
+    d.pad = nullptr;
     d.tris = ii.tris;
     d.custom_index = ii.custom_index;
     d.mask = ii.mask;
@@ -507,15 +701,18 @@ __global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_
 // level keep their parents' order, left before right.
 __global__ void __launch_bounds__(1024)
 bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
-                    uint32_t* newidx) {
+                    uint32_t* newidx, uint32_t* levels) {
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_carry;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) { queue[0] = 0; newidx[0] = 0; s_carry = 0; }
     __syncthreads();
-    uint32_t head = 0, tail = 1;
+    uint32_t head = 0, tail = 1, level = 0;
     while (head < tail && tail <= m) {
         uint32_t level_end = tail;
+        // level table {L, start_0, ..., start_L} (depth is far below 64 for a TLAS)
+        if (tid == 0 && level < 64) levels[1 + level] = head;
+        ++level;
         for (uint32_t base = head; base < level_end; base += 1024) {
             uint32_t q = base + tid;
             int c0 = 0, c1 = 0;
@@ -559,6 +756,11 @@ bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
         __syncthreads();
         if (tid == 0) s_carry = 0;
         __syncthreads();
+    }
+    if (tid == 0) {
+        uint32_t L = level < 64 ? level : 64;
+        levels[0] = L;
+        levels[1 + L] = tail;
     }
     for (uint32_t old = tid; old < m; old += 1024) {
         const float4* s = src + (size_t)old * kNodeF4;
@@ -669,12 +871,13 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
     cudaStream_t st = ctx->stream;
     // Persistent arena: per BLAS nodes | tris | morton | order | vertices | indices.
     std::vector<size_t> off_nodes(count), off_tris(count), off_mort(count), off_ord(count),
-        off_vtx(count), off_idx(count);
+        off_vtx(count), off_idx(count), off_nodes4(count);
     size_t arena_bytes = 0;
     for (uint32_t s = 0; s < count; ++s) {
         uint32_t n = descs[s].index_count / 3;
         uint32_t m = std::max(n, 2u) - 1;
         off_nodes[s] = arena_bytes; arena_bytes += align256((size_t)m * 64);
+        off_nodes4[s] = arena_bytes; arena_bytes += align256((size_t)m * 128);
         off_tris[s] = arena_bytes; arena_bytes += align256((size_t)std::max(n, 1u) * 48);
         off_mort[s] = arena_bytes; arena_bytes += align256((size_t)std::max(n, 1u) * 4);
         off_ord[s] = arena_bytes; arena_bytes += align256((size_t)std::max(n, 1u) * 4);
@@ -717,6 +920,7 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
         sd.indices = (const uint32_t*)(ab + off_idx[s]);
         sd.nodes = (float4*)(ab + off_nodes[s]);
         sd.tris = (float4*)(ab + off_tris[s]);
+        sd.nodes4 = (float4*)(ab + off_nodes4[s]);
     }
     // Scratch: segs | prim_off | node_off | bounds | sort | leaf boxes | parents | flags |
     // sorted morton/order staging.
@@ -726,7 +930,8 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
                   align256(count * 24) + sort_scratch_bytes(std::max(N, 1u), passes) +
                   align256((size_t)std::max(N, 1u) * 32) + align256((size_t)M * 4) +
                   align256((size_t)std::max(N, 1u) * 4) + align256((size_t)M * 4) +
-                  2 * align256((size_t)std::max(N, 1u) * 4);
+                  2 * align256((size_t)std::max(N, 1u) * 4) + 2 * align256((size_t)M * 4) +
+                  align256((size_t)(M / 1024 + 1) * 4);
     luz_status stt = ensure_scratch(ctx, need);
     if (stt != LUZ_OK) { cudaFree(arena->base); delete arena; return stt; }
     char* p = (char*)ctx->d_scratch;
@@ -742,6 +947,9 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
     uint32_t* d_flags = (uint32_t*)p; p += align256((size_t)M * 4);
     uint32_t* d_mort = (uint32_t*)p; p += align256((size_t)std::max(N, 1u) * 4);
     uint32_t* d_ord = (uint32_t*)p; p += align256((size_t)std::max(N, 1u) * 4);
+    uint32_t* d_even = (uint32_t*)p; p += align256((size_t)M * 4);
+    uint32_t* d_idx4 = (uint32_t*)p; p += align256((size_t)M * 4);
+    uint32_t* d_sums = (uint32_t*)p; p += align256((size_t)(M / 1024 + 1) * 4);
 
     LUZ_CUDA(ctx, cudaMemcpyAsync(d_segs, segs.data(), count * sizeof(SegDesc), cudaMemcpyHostToDevice, st));
     LUZ_CUDA(ctx, cudaMemcpyAsync(d_prim_off, prim_off.data(), count * 4, cudaMemcpyHostToDevice, st));
@@ -778,6 +986,21 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
                                                    d_node_parent, d_leaf_parent, d_flags);
         LUZ_LAUNCHED(ctx, "refit_kernel");
     }
+    // 4-wide collapse of every segment's tree (the traversal structure of the
+    // shadow/AO rays; the binary tree stays the parity-checked structure).
+    {
+        uint32_t chunks = cdiv(M, 1024);
+        even_depth_kernel<<<cdiv(M, 256), 256, 0, st>>>(d_segs, d_node_off, count, M, d_node_parent, d_even);
+        LUZ_LAUNCHED(ctx, "even_depth_kernel");
+        chunk_sum_kernel<<<chunks, 256, 0, st>>>(d_even, M, d_sums);
+        LUZ_LAUNCHED(ctx, "chunk_sum_kernel");
+        chunk_scan_kernel<<<1, 1024, 0, st>>>(d_sums, chunks);
+        LUZ_LAUNCHED(ctx, "chunk_scan_kernel");
+        chunk_apply_kernel<<<chunks, 256, 0, st>>>(d_even, M, d_sums, d_idx4);
+        LUZ_LAUNCHED(ctx, "chunk_apply_kernel");
+        bvh4_emit_kernel<<<cdiv(M, 256), 256, 0, st>>>(d_segs, d_node_off, count, M, d_even, d_idx4);
+        LUZ_LAUNCHED(ctx, "bvh4_emit_kernel");
+    }
     for (uint32_t s = 0; s < count; ++s) {
         uint32_t n = segs[s].prim_count;
         if (n)
@@ -801,6 +1024,7 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
         b->arena = arena;
         arena->refs++;
         b->nodes = segs[s].nodes;
+        b->nodes4 = segs[s].nodes4;
         b->tris = segs[s].tris;
         b->morton = (uint32_t*)(ab + off_mort[s]);
         b->order = (uint32_t*)(ab + off_ord[s]);
@@ -828,6 +1052,8 @@ luz_status tlas_alloc(luz_ctx* ctx, luz_tlas* t) {
     uint32_t cap = std::max(t->max_instances, 1u);
     uint32_t m = std::max(cap, 2u) - 1;
     LUZ_CUDA(ctx, cudaMalloc(&t->nodes, (size_t)m * 64));
+    LUZ_CUDA(ctx, cudaMalloc(&t->nodes4, (size_t)m * 128));
+    LUZ_CUDA(ctx, cudaMalloc(&t->levels, 66 * 4));
     LUZ_CUDA(ctx, cudaMalloc(&t->instances, (size_t)cap * sizeof(DevInstance)));
     LUZ_CUDA(ctx, cudaMalloc(&t->shade, (size_t)cap * sizeof(DevShadeInstance)));
     LUZ_CUDA(ctx, cudaMalloc(&t->d_input, (size_t)cap * sizeof(DevInstanceInput)));
@@ -857,6 +1083,7 @@ luz_status pack_tlas_input(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, 
         d.mask = inst[i].mask;
         d.blas_prims = b->prims;
         d.pad = 0;
+        d.nodes4 = b->nodes4;
     }
     t->count = n;
     t->node_count = std::max(n, 2u) - 1;
@@ -926,8 +1153,10 @@ luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t) {
     refit_kernel<<<cdiv(n, 128), 128, 0, st>>>(d_seg, d_zero, 1, n, leaf_box, node_parent,
                                                leaf_parent, flags);
     LUZ_LAUNCHED(ctx, "refit_kernel");
-    bfs_relayout_kernel<<<1, 1024, 0, st>>>(karras_nodes, t->nodes, m, queue, newidx);
+    bfs_relayout_kernel<<<1, 1024, 0, st>>>(karras_nodes, t->nodes, m, queue, newidx, t->levels);
     LUZ_LAUNCHED(ctx, "bfs_relayout_kernel");
+    tlas_bvh4_kernel<<<1, 1024, 0, st>>>(t->nodes, m, t->levels, t->nodes4);
+    LUZ_LAUNCHED(ctx, "tlas_bvh4_kernel");
     return LUZ_OK;
 }
 

@@ -16,6 +16,7 @@ struct SegDesc {
     const uint32_t* indices;
     float4* nodes;         // output nodes of this segment
     float4* tris;          // output triangles of this segment
+    float4* nodes4;        // output 4-wide nodes (NULL: not built)
 };
 
 // Onesweep radix sort geometry.

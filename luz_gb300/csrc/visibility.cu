@@ -95,26 +95,37 @@ __device__ __forceinline__ void run_steps(LaneRay& r, bool& active, const float4
         bool finished = false, hit = false;
         if (++r.budget > kRayStepCap) { err |= LUZ_DEV_TRAVERSAL_CAP; finished = true; }
         else if (r.node >= 0) {
+            // 4-wide node: test the four child boxes, continue with the nearest hit
+            // child and push the other hits.
             if (kStats) { if (r.in_blas) cnt.blas_nodes++; else cnt.tlas_nodes++; }
             const float4* np = r.in_blas ? r.bn : ((uint32_t)r.node < staged ? smem_tlas : r.tlas);
-            np += (size_t)r.node * kNodeF4;
-            float4 n0 = np[0], n1 = np[1], n2 = np[2], n3 = np[3];
+            np += (size_t)r.node * kNode4F4;
+            const float4 lx = np[0], hx = np[1], ly = np[2], hy = np[3], lz = np[4], hz = np[5], cf = np[6];
             const V3 o = r.in_blas ? r.wt.o : r.wo;
-            int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-            float t0, t1;
-            bool h0 = c0 != kEmptyChild && slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, o, r.idir, r.tmin, r.tmax, t0);
-            bool h1 = c1 != kEmptyChild && slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, o, r.idir, r.tmin, r.tmax, t1);
-            if (h0 && h1) {
-                int nearc = t1 < t0 ? c1 : c0, farc = t1 < t0 ? c0 : c1;
-                if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)farc;
-                else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = farc;
-                else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
-                ++r.sp;
-                r.node = nearc;
+            const int ch[4] = {__float_as_int(cf.x), __float_as_int(cf.y), __float_as_int(cf.z),
+                               __float_as_int(cf.w)};
+            float tn[4];
+            bool h[4];
+            h[0] = ch[0] != kEmptyChild && slab(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, o, r.idir, r.tmin, r.tmax, tn[0]);
+            h[1] = ch[1] != kEmptyChild && slab(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, o, r.idir, r.tmin, r.tmax, tn[1]);
+            h[2] = ch[2] != kEmptyChild && slab(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, o, r.idir, r.tmin, r.tmax, tn[2]);
+            h[3] = ch[3] != kEmptyChild && slab(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, o, r.idir, r.tmin, r.tmax, tn[3]);
+            int best = -1;
+            float tb = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (h[k] && (best < 0 || tn[k] < tb)) { best = k; tb = tn[k]; }
+            if (best >= 0) {
+#pragma unroll
+                for (int k = 3; k >= 0; --k) {
+                    if (!h[k] || k == best) continue;
+                    if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)ch[k];
+                    else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = ch[k];
+                    else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
+                    ++r.sp;
+                }
+                r.node = ch[best];
                 if (!finished) continue;
-            } else if (h0 || h1) {
-                r.node = h0 ? c0 : c1;
-                continue;
             }
         } else if (!r.in_blas) {
             if (kStats) cnt.instances++;
@@ -127,7 +138,7 @@ __device__ __forceinline__ void run_steps(LaneRay& r, bool& active, const float4
                 V3 od = xform_dir(m, r.wd);
                 r.wt = wt_setup(xform_point(m, r.wo), od);
                 r.idir = safe_inv(od);
-                r.bn = I->nodes;
+                r.bn = I->nodes4;
                 r.bt = I->tris;
                 if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)kStackMarker;
                 else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = kStackMarker;
@@ -181,9 +192,9 @@ template <bool kStats>
 __global__ void __launch_bounds__(256, 3) visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
     extern __shared__ float4 smem[];
     const uint32_t staged = min(S.tlas_node_count, C.smem_nodes);
-    for (uint32_t i = threadIdx.x; i < staged * kNodeF4; i += blockDim.x) smem[i] = __ldg(S.tlas_nodes + i);
+    for (uint32_t i = threadIdx.x; i < staged * kNode4F4; i += blockDim.x) smem[i] = __ldg(S.tlas_nodes + i);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t* s_stack = reinterpret_cast<uint32_t*>(smem + staged * kNodeF4) + warp * (kSmemStack * 32) + lane;
+    uint32_t* s_stack = reinterpret_cast<uint32_t*>(smem + staged * kNode4F4) + warp * (kSmemStack * 32) + lane;
     int lstack[kLocalStack];
     __syncthreads();
     const uint32_t full = 0xFFFFFFFFu, lt_mask = (1u << lane) - 1u;
@@ -288,7 +299,9 @@ const VisTuning& vis_tuning(const luz_ctx* ctx) { return ctx->vis_tuning.set ? c
 
 SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index) {
     SceneVis S;
-    S.tlas_nodes = t->nodes;
+    // 4-wide nodes; node_count (the binary count) bounds the 4-wide count and the
+    // size of the nodes4 buffer, so staging that many stays inside it.
+    S.tlas_nodes = t->nodes4;
     S.tlas_node_count = t->count ? t->node_count : 0;
     S.instance_count = t->count;
     S.instances = t->instances;
@@ -343,7 +356,7 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     VisCommon C = make_vis_common(ctx, f->work_counter);
     const VisTuning& tu = vis_tuning(ctx);
     uint32_t staged = std::min<uint32_t>(S.tlas_node_count, tu.smem_nodes);
-    size_t smem = (size_t)staged * 64 + (size_t)256 * kSmemStack * 4;
+    size_t smem = (size_t)staged * kNode4F4 * 16 + (size_t)256 * kSmemStack * 4;
     static size_t attr_bytes = 0;
     if (smem > attr_bytes) {
         LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -393,7 +406,7 @@ extern "C" luz_status luz_ctx_set_vis_tuning(luz_ctx* ctx, const luz_vis_tuning*
         ctx->vis_tuning = VisTuning{0, 0, 0, 0, 0};
         return LUZ_OK;
     }
-    if (t->smem_nodes > 2048 || t->refill < 1 || t->refill > 32 || t->steps < 1 || t->steps > 1024 ||
+    if (t->smem_nodes > 1024 || t->refill < 1 || t->refill > 32 || t->steps < 1 || t->steps > 1024 ||
         t->ctas_per_sm < 1 || t->ctas_per_sm > 16)
         return set_error(ctx, LUZ_ERR_INVALID, "visibility tuning outside its documented ranges");
     ctx->vis_tuning = VisTuning{t->smem_nodes, t->refill, t->steps, t->ctas_per_sm, 1};
