@@ -4,7 +4,8 @@ Device translation units are compiled with FMA contraction off (-fmad=false) and
 IEEE division / square root, host code with -ffp-contract=off: rays generated on
 the device must be bit-identical to rays generated by a CPU following the same
 steps. Translation units compile in parallel; the result is linked against the
-static CUDA runtime so that loading the library needs no GPU.
+static CUDA runtime so that loading the library needs no GPU. LUZ_EXTRA_NVCC adds
+flags to every device translation unit (e.g. -DLUZ_VIS_MIN_BLOCKS=2).
 """
 from __future__ import annotations
 
@@ -59,7 +60,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", fmad, "-prec-div=true",
                "-prec-sqrt=true", "-ftz=false", "-Xptxas", "-warn-spills",
                "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", str(INCLUDE),
-               "-c", str(CSRC / tu), "-o", str(obj)]
+               "-c", str(CSRC / tu), "-o", str(obj)] + os.environ.get("LUZ_EXTRA_NVCC", "").split()
         jobs.append((tu, cmd))
         objs.append(obj)
     for tu in HOST_TUS:

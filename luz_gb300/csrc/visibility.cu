@@ -9,10 +9,14 @@
 // atomic and the idle lanes pick theirs by rank (popc of the lower lanes' ballot
 // bits), then generate their rays while the others keep traversing.
 //
-// Traversal: the TLAS top (breadth-first prefix) is staged in shared memory (single
-// scene); BLAS nodes and triangles come through 16-B vector loads; the stack is
-// warp-interleaved in shared memory (entry k of lane l at [k][l]) with a
-// local-memory tail for rare deep paths.
+// Traversal runs over 4-wide nodes (the even-depth collapse of the binary LBVH):
+// one step tests four child boxes, with the near and far planes picked per ray by
+// the direction's signs. Nodes and triangles come through 16-B vector loads (the
+// TLAS top can also be staged in shared memory); the stack is warp-interleaved in
+// shared memory (entry k of lane l at [k][l]) with a local-memory tail for rare deep
+// paths. Only the state a node step needs stays in registers; the rest of a ray
+// (world origin and direction, output bit, watertight shear) sits in shared memory,
+// which keeps the kernel at 64 registers and 4 CTAs per SM without spills.
 #include <algorithm>
 #include <cstring>
 
@@ -22,61 +26,116 @@
 
 namespace luz {
 
+// Minimum resident CTAs per SM the visibility kernels are compiled for (register cap).
+#ifndef LUZ_VIS_MIN_BLOCKS
+#define LUZ_VIS_MIN_BLOCKS 4
+#endif
+
+constexpr int kVisThreads = 256;
 constexpr int kSmemStack = 16;                      // shared-memory stack entries per lane
 constexpr int kLocalStack = kStackSize - kSmemStack;
 constexpr uint32_t kRayStepCap = 1u << 22;
 
+// Ray state that traversal touches only when it enters or leaves a BLAS, tests a
+// triangle or finishes lives in shared memory, one 32-bit field per row of
+// kVisThreads entries (conflict-free): world origin and direction, the output word
+// and bit, and the watertight shear of the current BLAS.
+enum ColdField : int {
+    kWoX, kWoY, kWoZ, kWdX, kWdY, kWdZ,
+    kOutLo, kOutHi, kOutBits,     // bit | record_hit << 5
+    kWtK, kWtSx, kWtSy, kWtSz,    // kx | ky << 2 | kz << 4; shear
+    kColdFields
+};
+constexpr size_t kColdBytes = (size_t)kColdFields * kVisThreads * 4;
+constexpr size_t kStackBytes = (size_t)kVisThreads * kSmemStack * 4;
+
+// Hot per-lane state (registers).
 struct LaneRay {
-    V3 wo, wd, widir, idir;
-    WtRay wt;
+    V3 o, idir;          // origin and inverse direction in the current space (world or BLAS object)
     float tmin, tmax;
     int node, sp;
-    bool in_blas, record_hit;
+    int nx, ny, nz;      // float4 row of the near plane per axis in a 4-wide node
+    bool in_blas;
     const float4* bn;
     const float4* bt;
-    const float4* tlas;
+    const float4* tlas;          // batched kernel: the lane's scene
     const DevInstance* insts;
-    uint32_t* out;
-    uint32_t out_bit, budget;
+    uint32_t budget;
 };
+
+struct Cold {
+    float* f;            // this lane's column: field k at f[k * kVisThreads]
+    __device__ __forceinline__ float& operator[](int k) const { return f[k * kVisThreads]; }
+    __device__ __forceinline__ V3 wo() const { return V3{(*this)[kWoX], (*this)[kWoY], (*this)[kWoZ]}; }
+    __device__ __forceinline__ V3 wd() const { return V3{(*this)[kWdX], (*this)[kWdY], (*this)[kWdZ]}; }
+};
+
+// Near-plane rows of a 4-wide node for a ray with inverse direction id: the lower
+// plane where the component is non-negative, else the upper one (the far plane is
+// the other row, index ^ 1). Rounding is monotonic, so (near - o) * id <= (far - o) * id
+// for every non-inverted box: the ordered test gives the same interval as the
+// min/max form of slab().
+__device__ __forceinline__ void near_planes(LaneRay& r) {
+    r.nx = r.idir.x < 0.0f ? 1 : 0;
+    r.ny = r.idir.y < 0.0f ? 3 : 2;
+    r.nz = r.idir.z < 0.0f ? 5 : 4;
+}
+
+__device__ __forceinline__ bool slab_ordered(float nx, float fx, float ny, float fy, float nz, float fz,
+                                             const LaneRay& r, float& tnear) {
+    const V3& o = r.o;
+    const V3& id = r.idir;
+    float tn = fmaxf(fmaxf((nx - o.x) * id.x, (ny - o.y) * id.y), fmaxf((nz - o.z) * id.z, r.tmin));
+    float tf = fminf(fminf((fx - o.x) * id.x, (fy - o.y) * id.y), fminf((fz - o.z) * id.z, r.tmax));
+    tnear = tn;
+    return tn - fabsf(tn) * kSlabEps <= tf + fabsf(tf) * kSlabEps;
+}
 
 // Generates the ray of item (slot, j) of scene S. Returns false when there is
 // nothing to trace; the miss (AO) has then already been recorded.
-__device__ __forceinline__ bool setup_ray(LaneRay& r, const SceneVis& S, const VisCommon& C, uint32_t slot,
-                                          uint32_t j) {
+__device__ __forceinline__ bool setup_ray(LaneRay& r, const Cold& c, const SceneVis& S, const VisCommon& C,
+                                          uint32_t slot, uint32_t j) {
     float4 s0 = __ldg(S.surf + 2 * (size_t)j), s1 = __ldg(S.surf + 2 * (size_t)j + 1);
     V3 p = V3{s0.x, s0.y, s0.z}, N = V3{s1.x, s1.y, s1.z};
     uint32_t pix = __float_as_uint(s0.w);
     uint32_t px = pix % S.width, py = pix / S.width;
     V3 cam = V3{S.cam[0], S.cam[1], S.cam[2]};
     float rx, ry;
+    V3 wo, wd;
+    uint32_t* out;
+    bool record_hit;
     if (slot < S.shadow_slots) {
         uint32_t e = __ldg(S.slot_table + slot);
         uint32_t li = e & 0xFFFFu, si = e >> 16;
         sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)si, S.frame, li + 1, &rx, &ry);
-        shadow_ray(S.lights[li], p, N, cam, rx, ry, r.wo, r.wd, r.tmax);
+        shadow_ray(S.lights[li], p, N, cam, rx, ry, wo, wd, r.tmax);
         r.tmin = 0.001f;
-        r.out = S.shadow_bits + (size_t)slot * S.words + (pix >> 5);
-        r.record_hit = true;
+        out = S.shadow_bits + (size_t)slot * S.words + (pix >> 5);
+        record_hit = true;
     } else {
         uint32_t a = slot - S.shadow_slots;
         sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)a, S.frame, 0u, &rx, &ry);
-        ao_ray(p, N, cam, rx, ry, r.wo, r.wd);
+        ao_ray(p, N, cam, rx, ry, wo, wd);
         r.tmin = S.ao_min;
         r.tmax = S.ao_max;
-        r.out = S.ao_bits + (size_t)a * S.words + (pix >> 5);
-        r.record_hit = false;
+        out = S.ao_bits + (size_t)a * S.words + (pix >> 5);
+        record_hit = false;
     }
-    r.out_bit = 1u << (pix & 31);
-    bool ok = S.instance_count > 0 && finite3(r.wo) && finite3(r.wd) && (r.tmin <= r.tmax) &&
-              !(r.wd.x == 0.0f && r.wd.y == 0.0f && r.wd.z == 0.0f);
+    bool ok = S.instance_count > 0 && finite3(wo) && finite3(wd) && (r.tmin <= r.tmax) &&
+              !(wd.x == 0.0f && wd.y == 0.0f && wd.z == 0.0f);
     if (!ok) {
-        if (!r.record_hit) atomicOr(r.out, r.out_bit);   // no ray: a miss
+        if (!record_hit) atomicOr(out, 1u << (pix & 31));   // no ray: a miss
         return false;
     }
-    r.widir = safe_inv(r.wd);
-    r.idir = r.widir;
-    r.wt.o = r.wo;
+    unsigned long long oa = reinterpret_cast<unsigned long long>(out);
+    c[kWoX] = wo.x; c[kWoY] = wo.y; c[kWoZ] = wo.z;
+    c[kWdX] = wd.x; c[kWdY] = wd.y; c[kWdZ] = wd.z;
+    c[kOutLo] = __uint_as_float((uint32_t)oa);
+    c[kOutHi] = __uint_as_float((uint32_t)(oa >> 32));
+    c[kOutBits] = __uint_as_float((pix & 31u) | (record_hit ? 32u : 0u));
+    r.o = wo;
+    r.idir = safe_inv(wd);
+    near_planes(r);
     r.node = 0;
     r.sp = 0;
     r.in_blas = false;
@@ -86,9 +145,22 @@ __device__ __forceinline__ bool setup_ray(LaneRay& r, const SceneVis& S, const V
     return true;
 }
 
+__device__ __forceinline__ void finish_ray(const Cold& c, bool& active, bool hit) {
+    uint32_t bits = __float_as_uint(c[kOutBits]);
+    if (hit == ((bits & 32u) != 0)) {
+        uint32_t* out = reinterpret_cast<uint32_t*>((unsigned long long)__float_as_uint(c[kOutLo]) |
+                                                    ((unsigned long long)__float_as_uint(c[kOutHi]) << 32));
+        atomicOr(out, 1u << (bits & 31u));
+    }
+    active = false;
+}
+
 // Up to `steps` traversal steps of one lane's ray; clears `active` when it ends.
+// tlas / insts: the scene's TLAS nodes and instances (kernel parameters in the
+// single-scene kernel, the lane's own scene in the batched one).
 template <bool kStats>
-__device__ __forceinline__ void run_steps(LaneRay& r, bool& active, const float4* smem_tlas, uint32_t staged,
+__device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& active, const float4* smem_tlas,
+                                          uint32_t staged, const float4* tlas, const DevInstance* insts,
                                           uint32_t* s_stack, int* lstack, uint32_t steps, uint32_t& err,
                                           TraceCounters& cnt) {
     for (uint32_t s = 0; s < steps && active; ++s) {
@@ -98,18 +170,18 @@ __device__ __forceinline__ void run_steps(LaneRay& r, bool& active, const float4
             // 4-wide node: test the four child boxes, continue with the nearest hit
             // child and push the other hits.
             if (kStats) { if (r.in_blas) cnt.blas_nodes++; else cnt.tlas_nodes++; }
-            const float4* np = r.in_blas ? r.bn : ((uint32_t)r.node < staged ? smem_tlas : r.tlas);
+            const float4* np = r.in_blas ? r.bn : ((uint32_t)r.node < staged ? smem_tlas : tlas);
             np += (size_t)r.node * kNode4F4;
-            const float4 lx = np[0], hx = np[1], ly = np[2], hy = np[3], lz = np[4], hz = np[5], cf = np[6];
-            const V3 o = r.in_blas ? r.wt.o : r.wo;
+            const float4 nx = np[r.nx], fx = np[r.nx ^ 1], ny = np[r.ny], fy = np[r.ny ^ 1], nz = np[r.nz],
+                         fz = np[r.nz ^ 1], cf = np[6];
             const int ch[4] = {__float_as_int(cf.x), __float_as_int(cf.y), __float_as_int(cf.z),
                                __float_as_int(cf.w)};
             float tn[4];
             bool h[4];
-            h[0] = ch[0] != kEmptyChild && slab(lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, o, r.idir, r.tmin, r.tmax, tn[0]);
-            h[1] = ch[1] != kEmptyChild && slab(lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, o, r.idir, r.tmin, r.tmax, tn[1]);
-            h[2] = ch[2] != kEmptyChild && slab(lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, o, r.idir, r.tmin, r.tmax, tn[2]);
-            h[3] = ch[3] != kEmptyChild && slab(lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, o, r.idir, r.tmin, r.tmax, tn[3]);
+            h[0] = ch[0] != kEmptyChild && slab_ordered(nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, r, tn[0]);
+            h[1] = ch[1] != kEmptyChild && slab_ordered(nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, r, tn[1]);
+            h[2] = ch[2] != kEmptyChild && slab_ordered(nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, r, tn[2]);
+            h[3] = ch[3] != kEmptyChild && slab_ordered(nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, r, tn[3]);
             int best = -1;
             float tb = 0.f;
 #pragma unroll
@@ -129,15 +201,21 @@ __device__ __forceinline__ void run_steps(LaneRay& r, bool& active, const float4
             }
         } else if (!r.in_blas) {
             if (kStats) cnt.instances++;
-            const DevInstance* I = r.insts + (~r.node);
+            const DevInstance* I = insts + (~r.node);
             const float4* wp = reinterpret_cast<const float4*>(I->w2o);
             uint4 meta = __ldg(reinterpret_cast<const uint4*>(&I->custom_index));
             if ((meta.y & 0xFFu) != 0 && meta.w > 0) {
                 float4 q0 = __ldg(wp), q1 = __ldg(wp + 1), q2 = __ldg(wp + 2);
                 float m[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
-                V3 od = xform_dir(m, r.wd);
-                r.wt = wt_setup(xform_point(m, r.wo), od);
+                V3 od = xform_dir(m, c.wd());
+                WtRay wt = wt_setup(xform_point(m, c.wo()), od);
+                c[kWtK] = __int_as_float(wt.kx | (wt.ky << 2) | (wt.kz << 4));
+                c[kWtSx] = wt.sx;
+                c[kWtSy] = wt.sy;
+                c[kWtSz] = wt.sz;
+                r.o = wt.o;
                 r.idir = safe_inv(od);
+                near_planes(r);
                 r.bn = I->nodes4;
                 r.bt = I->tris;
                 if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)kStackMarker;
@@ -151,9 +229,18 @@ __device__ __forceinline__ void run_steps(LaneRay& r, bool& active, const float4
         } else {
             if (kStats) cnt.tris++;
             const float4* tp = r.bt + (size_t)(~r.node) * kTriF4;
-            float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
+            WtRay wt;
+            int k = __float_as_int(c[kWtK]);
+            wt.o = r.o;
+            wt.kx = k & 3;
+            wt.ky = (k >> 2) & 3;
+            wt.kz = k >> 4;
+            wt.sx = c[kWtSx];
+            wt.sy = c[kWtSy];
+            wt.sz = c[kWtSz];
             float t, U, V, W, det;
-            if (wt_test(r.wt, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, V3{c.x, c.y, c.z}, t, U, V, W, det) &&
+            if (wt_test(wt, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, V3{cc.x, cc.y, cc.z}, t, U, V, W, det) &&
                 t >= r.tmin && t <= r.tmax) {
                 finished = true;
                 hit = true;
@@ -166,16 +253,15 @@ __device__ __forceinline__ void run_steps(LaneRay& r, bool& active, const float4
             int v = r.sp < kSmemStack ? (int)s_stack[r.sp * 32] : lstack[r.sp - kSmemStack];
             if (v == kStackMarker) {
                 r.in_blas = false;
-                r.idir = r.widir;
+                r.o = c.wo();
+                r.idir = safe_inv(c.wd());
+                near_planes(r);
                 continue;
             }
             r.node = v;
             break;
         }
-        if (finished) {
-            if (hit == r.record_hit) atomicOr(r.out, r.out_bit);
-            active = false;
-        }
+        if (finished) finish_ray(c, active, hit);
     }
 }
 
@@ -187,14 +273,18 @@ __device__ __forceinline__ void flush_stats(unsigned long long* stats, uint32_t 
     atomicAdd(stats + 4, (unsigned long long)cnt.instances);
 }
 
-// One scene, TLAS top staged in shared memory.
+// One scene, TLAS top staged in shared memory. Shared memory: staged TLAS nodes,
+// then the stacks, then the cold ray state.
 template <bool kStats>
-__global__ void __launch_bounds__(256, 3) visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
+__global__ void __launch_bounds__(kVisThreads, LUZ_VIS_MIN_BLOCKS)
+visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
     extern __shared__ float4 smem[];
     const uint32_t staged = min(S.tlas_node_count, C.smem_nodes);
     for (uint32_t i = threadIdx.x; i < staged * kNode4F4; i += blockDim.x) smem[i] = __ldg(S.tlas_nodes + i);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t* s_stack = reinterpret_cast<uint32_t*>(smem + staged * kNode4F4) + warp * (kSmemStack * 32) + lane;
+    uint32_t* stack_base = reinterpret_cast<uint32_t*>(smem + staged * kNode4F4);
+    uint32_t* s_stack = stack_base + warp * (kSmemStack * 32) + lane;
+    const Cold c{reinterpret_cast<float*>(stack_base + kVisThreads * kSmemStack) + threadIdx.x};
     int lstack[kLocalStack];
     __syncthreads();
     const uint32_t full = 0xFFFFFFFFu, lt_mask = (1u << lane) - 1u;
@@ -218,12 +308,13 @@ __global__ void __launch_bounds__(256, 3) visibility_kernel(SceneVis S, VisCommo
                     uint32_t slot = (uint32_t)(item / lit);
                     uint32_t j = (uint32_t)(item - (unsigned long long)slot * lit);
                     if (kStats) ++rays;
-                    active = setup_ray(r, S, C, slot, j);
+                    active = setup_ray(r, c, S, C, slot, j);
                 }
             }
         }
         if (exhausted && __ballot_sync(full, active) == 0) break;
-        run_steps<kStats>(r, active, smem, staged, s_stack, lstack, C.steps, err, cnt);
+        run_steps<kStats>(r, c, active, smem, staged, S.tlas_nodes, S.instances, s_stack, lstack, C.steps, err,
+                          cnt);
     }
     if (err) atomicOr(C.status, err);
     if (kStats) flush_stats(stats, rays, cnt);
@@ -232,12 +323,14 @@ __global__ void __launch_bounds__(256, 3) visibility_kernel(SceneVis S, VisCommo
 // Many scenes in one launch: item g belongs to the scene s with
 // offsets[s] <= g < offsets[s+1]; each lane carries its scene's TLAS and outputs.
 template <bool kStats>
-__global__ void __launch_bounds__(256, 3) visibility_batch_kernel(const SceneVis* __restrict__ scenes, uint32_t n,
-                                                                  const unsigned long long* __restrict__ offsets,
-                                                                  VisCommon C, unsigned long long* stats) {
+__global__ void __launch_bounds__(kVisThreads, LUZ_VIS_MIN_BLOCKS)
+visibility_batch_kernel(const SceneVis* __restrict__ scenes, uint32_t n, const unsigned long long* __restrict__ offsets,
+                        VisCommon C, unsigned long long* stats) {
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t* s_stack = reinterpret_cast<uint32_t*>(smem) + warp * (kSmemStack * 32) + lane;
+    uint32_t* stack_base = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* s_stack = stack_base + warp * (kSmemStack * 32) + lane;
+    const Cold c{reinterpret_cast<float*>(stack_base + kVisThreads * kSmemStack) + threadIdx.x};
     int lstack[kLocalStack];
     const uint32_t full = 0xFFFFFFFFu, lt_mask = (1u << lane) - 1u;
     const unsigned long long total = offsets[n];
@@ -267,12 +360,12 @@ __global__ void __launch_bounds__(256, 3) visibility_batch_kernel(const SceneVis
                     uint32_t slot = (uint32_t)(local / lit);
                     uint32_t j = (uint32_t)(local - (unsigned long long)slot * lit);
                     if (kStats) ++rays;
-                    active = setup_ray(r, S, C, slot, j);
+                    active = setup_ray(r, c, S, C, slot, j);
                 }
             }
         }
         if (exhausted && __ballot_sync(full, active) == 0) break;
-        run_steps<kStats>(r, active, nullptr, 0u, s_stack, lstack, C.steps, err, cnt);
+        run_steps<kStats>(r, c, active, nullptr, 0u, r.tlas, r.insts, s_stack, lstack, C.steps, err, cnt);
     }
     if (err) atomicOr(C.status, err);
     if (kStats) flush_stats(stats, rays, cnt);
@@ -292,8 +385,9 @@ __global__ void batch_offsets_kernel(const SceneVis* scenes, uint32_t n, unsigne
 
 // ---------------------------------------------------------------- host side
 // Defaults: the best shape of a sweep on the 1080p two-level scene (smem nodes
-// {0,256,512,1024} x refill {1,4,8,16} x steps {4,8,16,32} x CTAs/SM {2,3,4}).
-static const VisTuning g_tuning{256, 16, 32, 3, 1};
+// {0,128} x refill {2,4,8,16,24} x steps {8,16,32} x CTAs/SM {3,4}, kernel compiled
+// for 4 CTAs/SM). Staging the TLAS top in shared memory did not pay: L1 holds it.
+static const VisTuning g_tuning{0, 24, 16, 4, 1};
 
 const VisTuning& vis_tuning(const luz_ctx* ctx) { return ctx->vis_tuning.set ? ctx->vis_tuning : g_tuning; }
 
@@ -356,7 +450,7 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     VisCommon C = make_vis_common(ctx, f->work_counter);
     const VisTuning& tu = vis_tuning(ctx);
     uint32_t staged = std::min<uint32_t>(S.tlas_node_count, tu.smem_nodes);
-    size_t smem = (size_t)staged * kNode4F4 * 16 + (size_t)256 * kSmemStack * 4;
+    size_t smem = (size_t)staged * kNode4F4 * 16 + kStackBytes + kColdBytes;
     static size_t attr_bytes = 0;
     if (smem > attr_bytes) {
         LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -384,7 +478,7 @@ luz_status launch_visibility_batch(luz_ctx* ctx, const SceneVis* d_scenes, uint3
     LUZ_CUDA(ctx, cudaMemsetAsync(work_counter, 0, 8, st));
     VisCommon C = make_vis_common(ctx, work_counter);
     const VisTuning& tu = vis_tuning(ctx);
-    size_t smem = (size_t)256 * kSmemStack * 4;
+    size_t smem = kStackBytes + kColdBytes;
     uint32_t grid = (uint32_t)ctx->sm_count * tu.ctas_per_sm;
     if (d_stats) {
         LUZ_CUDA(ctx, cudaMemsetAsync(d_stats, 0, 5 * sizeof(unsigned long long), st));
