@@ -44,6 +44,7 @@ enum ColdField : int {
     kWoX, kWoY, kWoZ, kWdX, kWdY, kWdZ,
     kOutLo, kOutHi, kOutBits,     // bit | record_hit << 5
     kWtK, kWtSx, kWtSy, kWtSz,    // kx | ky << 2 | kz << 4; shear
+    kBtLo, kBtHi,                 // triangles of the current BLAS
     kColdFields
 };
 constexpr size_t kColdBytes = (size_t)kColdFields * kVisThreads * 4;
@@ -54,10 +55,9 @@ struct LaneRay {
     V3 o, idir;          // origin and inverse direction in the current space (world or BLAS object)
     float tmin, tmax;
     int node, sp;
-    int nx, ny, nz;      // float4 row of the near plane per axis in a 4-wide node
+    int signs;           // bit a set: the direction's component a is negative
     bool in_blas;
     const float4* bn;
-    const float4* bt;
     const float4* tlas;          // batched kernel: the lane's scene
     const DevInstance* insts;
     uint32_t budget;
@@ -76,9 +76,7 @@ struct Cold {
 // for every non-inverted box: the ordered test gives the same interval as the
 // min/max form of slab().
 __device__ __forceinline__ void near_planes(LaneRay& r) {
-    r.nx = r.idir.x < 0.0f ? 1 : 0;
-    r.ny = r.idir.y < 0.0f ? 3 : 2;
-    r.nz = r.idir.z < 0.0f ? 5 : 4;
+    r.signs = (r.idir.x < 0.0f ? 1 : 0) | (r.idir.y < 0.0f ? 2 : 0) | (r.idir.z < 0.0f ? 4 : 0);
 }
 
 __device__ __forceinline__ bool slab_ordered(float nx, float fx, float ny, float fy, float nz, float fz,
@@ -172,8 +170,9 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
             if (kStats) { if (r.in_blas) cnt.blas_nodes++; else cnt.tlas_nodes++; }
             const float4* np = r.in_blas ? r.bn : ((uint32_t)r.node < staged ? smem_tlas : tlas);
             np += (size_t)r.node * kNode4F4;
-            const float4 nx = np[r.nx], fx = np[r.nx ^ 1], ny = np[r.ny], fy = np[r.ny ^ 1], nz = np[r.nz],
-                         fz = np[r.nz ^ 1], cf = np[6];
+            const int sx = r.signs & 1, sy = (r.signs >> 1) & 1, sz = r.signs >> 2;
+            const float4 nx = np[sx], fx = np[sx ^ 1], ny = np[2 + sy], fy = np[3 - sy], nz = np[4 + sz],
+                         fz = np[5 - sz], cf = np[6];
             const int ch[4] = {__float_as_int(cf.x), __float_as_int(cf.y), __float_as_int(cf.z),
                                __float_as_int(cf.w)};
             float tn[4];
@@ -217,7 +216,9 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
                 r.idir = safe_inv(od);
                 near_planes(r);
                 r.bn = I->nodes4;
-                r.bt = I->tris;
+                const unsigned long long bt = reinterpret_cast<unsigned long long>(I->tris);
+                c[kBtLo] = __uint_as_float((uint32_t)bt);
+                c[kBtHi] = __uint_as_float((uint32_t)(bt >> 32));
                 if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)kStackMarker;
                 else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = kStackMarker;
                 else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
@@ -228,7 +229,9 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
             }
         } else {
             if (kStats) cnt.tris++;
-            const float4* tp = r.bt + (size_t)(~r.node) * kTriF4;
+            const float4* bt = reinterpret_cast<const float4*>((unsigned long long)__float_as_uint(c[kBtLo]) |
+                                                               ((unsigned long long)__float_as_uint(c[kBtHi]) << 32));
+            const float4* tp = bt + (size_t)(~r.node) * kTriF4;
             float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
             WtRay wt;
             int k = __float_as_int(c[kWtK]);
