@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-denoise", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-stress", action="store_true", help="skip the 4K 4096-instance stress scene")
     return ap.parse_args()
 
 
@@ -192,7 +193,7 @@ def run_reference(args, rank):
 
 
 # ---------------------------------------------------------------------------- denoised vs plain
-def denoised_vs_plain(g, ctx, stream, flush, K, W):
+def denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=16, curve_spp=(1, 2, 4, 8, 16, 32, 64, 128, 256)):
     """AO RMSE against 1024 samples (lit pixels, stratified samples) for the denoised
     single sample and the plain path; the smallest plain sample count with an RMSE at
     or below the denoised one; ms/frame of both frames (1 shadow ray per light each)."""
@@ -227,7 +228,7 @@ def denoised_vs_plain(g, ctx, stream, flush, K, W):
         fr.ao_resolve()
         return D.lit_rmse(fr.read(L.PLANE_AO), target, lit)
 
-    curve = {n: plain_rmse(n) for n in (1, 2, 4, 8, 16, 32, 64, 128, 256)}
+    curve = {n: plain_rmse(n) for n in curve_spp}
     setup(1, shadow_spp)
     fr.trace(tl, 7)
     den.denoise(fr)
@@ -290,8 +291,8 @@ def denoised_vs_plain(g, ctx, stream, flush, K, W):
     ms_ao_den = timed(ao_denoised)
     setup(n_star, 0)
     ms_ao_plain = timed(ao_plain)
-    setup(16, shadow_spp)   # back to the benchmark's sampling
-    sc.set_sampling(16, light_samples=1, sampler=L.SAMPLER_PARITY)
+    setup(restore_ao, shadow_spp)   # back to the benchmark's sampling
+    sc.set_sampling(restore_ao, light_samples=1, sampler=L.SAMPLER_PARITY)
     fr.upload(sc.block(), sc.lights(), sc.light_count, sc.models(), sc.instance_count)
     flops = 2.0 * (72 * 64 + 64 * 64 + 64 * 64 + 64 * 49) * fr.width * fr.height
     return {"rmse_vs_1024spp": {"denoised_1spp": r_den, "plain": {str(k): v for k, v in sorted(curve.items())}},
@@ -304,6 +305,66 @@ def denoised_vs_plain(g, ctx, stream, flush, K, W):
             "denoiser_tflops_bf16": flops / (ms_denoise_only * 1e-3) / 1e12,
             "shadow_rays_per_light": shadow_spp, "sampler": "stratified (8x8-block R2)",
             "weights": D.DEFAULT_WEIGHTS.name}
+
+
+# ---------------------------------------------------------------------------- stress scene
+def stress_config5(ctx, stream, flush, K, W):
+    """The stress scene: 4096 instances of the 64 displaced icospheres (335.5 M
+    instanced triangles) at 3840x2160, 145 lights (128 point + 16 spot + 1
+    directional, above the reference's 64-light block), 1 shadow ray per light and 64
+    AO rays per pixel on the plain path. Reports the BVH device bytes, the plain
+    frame (ms, Grays/s) and the denoised 1-spp frame against the plain frame at equal
+    AO RMSE."""
+    import torch
+
+    import luz_gb300 as L
+
+    scene = L.HostScene(5)
+    g = L.GPUScene(ctx, scene)
+    g.update_resources_gpu()
+    fr, tl = g.frame, g.tlas
+    mem = {"blas": {}, "tlas": tl.memory()}
+    for b in g.blas:
+        for k, v in b.memory().items():
+            mem["blas"][k] = mem["blas"].get(k, 0) + v
+    mem["total"] = mem["blas"]["total"] + mem["tlas"]["total"]
+
+    def frame(fi):
+        tl.build(g.instances, g.n_instances)
+        fr.gbuffer(tl)
+        fr.trace(tl, fi)
+        fr.light_pass(False)
+
+    for w in range(W):
+        frame(w)
+    torch.cuda.synchronize()
+    lit = fr.lit_count()
+    S = sum(g.lights[i].num_shadow_samples for i in range(scene.light_count)) + g.block.ao_num_samples
+    rays = scene.width * scene.height + lit * S
+    ts = []
+    for k in range(K):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        frame(W + k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    if ctx.device_status() != 0:
+        raise RuntimeError("device status word raised in the stress scene")
+    ms = statistics.mean(ts)
+    out = {"workload": "4096 instances x 64 displaced icospheres (335.5 M instanced tris), 3840x2160, "
+                       "145 lights, 1 shadow ray/light + 64 AO rays/px",
+           "lights": scene.light_count, "lit_pixels": lit, "rays_per_frame": rays, "ms_per_frame": ms,
+           "grays_per_s": rays / (ms * 1e-3) / 1e9, "bvh_device_bytes": mem,
+           "blas_build_ms": g.blas_build_ms}
+    out["denoised_vs_plain"] = denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=64,
+                                                 curve_spp=(1, 2, 4, 8, 16, 32, 64))
+    for b in g.blas:
+        b.close()
+    tl.close()
+    fr.close()
+    return out
 
 
 # ---------------------------------------------------------------------------- batched workload
@@ -510,6 +571,10 @@ def run_ours(args, rank, world, local):
         batched = batched_uneven(ctx, stream, flush, K, args.warmup)
         ctx.set_vis_tuning(**saved)
 
+    stress = None
+    if not args.no_stress:
+        stress = stress_config5(ctx, stream, flush, min(K, 5), args.warmup)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, _ = cpu_baseline(scene, args.cpu_rows)
@@ -524,7 +589,8 @@ def run_ours(args, rank, world, local):
                 "blas_build": {"ms": g.blas_build_ms, "triangles": g.blas_prims, "meshes": len(g.blas),
                                "note": "one batched device build, host->device vertex/index copies included"},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk, "denoised_vs_plain": denoised, "batched_uneven_64": batched}
+                "clocks": clk, "denoised_vs_plain": denoised, "batched_uneven_64": batched,
+                "stress_4k_4096_instances": stress}
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

@@ -255,6 +255,25 @@ luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint32_t vertex_
  * sorted primitive order (u32). Any pointer may be NULL. For parity tests. */
 luz_status luz_blas_download(luz_ctx* ctx, const luz_blas* blas, void* nodes, void* tris,
                              uint32_t* morton_sorted, uint32_t* order);
+/* Copies the 4-wide traversal nodes (128 B each: lo.x[4], hi.x[4], lo.y[4], hi.y[4],
+ * lo.z[4], hi.z[4], child[4] as int bits, 16 B zero) to host memory: the even-depth
+ * collapse of the binary tree, numbered by rank among the even-depth binary nodes in
+ * index order. The buffer holds max(n-1,1) entries; the first K are the nodes, K =
+ * the number of even-depth binary nodes. For parity tests. */
+luz_status luz_blas_download_wide(luz_ctx* ctx, const luz_blas* blas, void* nodes4);
+
+/* Device bytes held by a BLAS / TLAS, by part: binary nodes (closest-hit primary
+ * rays), 4-wide nodes (visibility), triangles / instance records, other (sort keys,
+ * order, shading copies of the vertex and index buffers, build scratch of a TLAS).
+ * The counterpart of the reference's vkGetAccelerationStructureBuildSizesKHR query
+ * (source/Graphics/VulkanWrapper.cpp:692-698, 809-812). */
+typedef struct luz_memory {
+    uint64_t nodes;
+    uint64_t wide_nodes;
+    uint64_t leaves;
+    uint64_t other;
+} luz_memory;
+luz_status luz_blas_memory(const luz_blas* blas, luz_memory* out);
 
 /* ------------------------------------------------------------------ TLAS
  * Replaces vkw::CreateTLAS(maxInstances) and vkw::CmdBuildTLAS(tlas, instances)
@@ -268,6 +287,10 @@ void luz_tlas_destroy(luz_tlas* tlas);
  * order (u32) to host memory. For parity tests. */
 luz_status luz_tlas_download(luz_ctx* ctx, const luz_tlas* tlas, void* nodes,
                              uint32_t* morton_sorted, uint32_t* order, uint32_t* node_count);
+/* The TLAS's 4-wide nodes (layout and numbering as luz_blas_download_wide; the
+ * buffer holds max(count,2)-1 entries). */
+luz_status luz_tlas_download_wide(luz_ctx* ctx, const luz_tlas* tlas, void* nodes4);
+luz_status luz_tlas_memory(const luz_tlas* tlas, luz_memory* out);
 
 /* ------------------------------------------------------------------ frame
  * A luz_frame owns the per-resolution images of DeferredRenderer::CreateImages

@@ -180,6 +180,20 @@ class Blas:
                self.ctx.handle, "blas download")
         return nodes, tris[:n], mort[:n], order[:n]
 
+    def download_wide(self) -> np.ndarray:
+        """The 4-wide traversal nodes, (max(n-1,1), 32) float32 (children as int bits
+        in columns 24..27); the leading even-depth-count rows are the nodes."""
+        m = max(self.prims, 2) - 1
+        nodes4 = np.zeros((m, 32), np.float32)
+        _check(lib.luz_blas_download_wide(self.ctx.handle, self._h, _abi.ptr(nodes4)), self.ctx.handle,
+               "blas download wide")
+        return nodes4
+
+    def memory(self) -> dict:
+        m = _abi.Memory()
+        _check(lib.luz_blas_memory(self._h, C.byref(m)), what="blas memory")
+        return m.as_dict()
+
     def close(self):
         if self._h:
             lib.luz_blas_destroy(self._h)
@@ -227,6 +241,19 @@ class Tlas:
         _check(lib.luz_tlas_download(self.ctx.handle, self._h, _abi.ptr(nodes), _abi.ptr(mort, _abi.c_u32_p),
                                      _abi.ptr(order, _abi.c_u32_p), C.byref(cnt)), self.ctx.handle, "tlas download")
         return nodes[:m], mort, order
+
+    def download_wide(self) -> np.ndarray:
+        cnt = C.c_uint32()
+        _check(lib.luz_tlas_download(self.ctx.handle, self._h, None, None, None, C.byref(cnt)))
+        nodes4 = np.zeros((max(cnt.value, 1), 32), np.float32)
+        _check(lib.luz_tlas_download_wide(self.ctx.handle, self._h, _abi.ptr(nodes4)), self.ctx.handle,
+               "tlas download wide")
+        return nodes4[:cnt.value]
+
+    def memory(self) -> dict:
+        m = _abi.Memory()
+        _check(lib.luz_tlas_memory(self._h, C.byref(m)), what="tlas memory")
+        return m.as_dict()
 
     def close(self):
         if self._h:

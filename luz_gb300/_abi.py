@@ -71,6 +71,15 @@ class Instance(C.Structure):
                 ("mask", C.c_uint32)]
 
 
+class Memory(C.Structure):
+    _fields_ = [("nodes", C.c_uint64), ("wide_nodes", C.c_uint64), ("leaves", C.c_uint64), ("other", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        d = {k: int(getattr(self, k)) for k, _ in self._fields_}
+        d["total"] = sum(d.values())
+        return d
+
+
 class BlasDesc(C.Structure):
     _fields_ = [("vertices", C.c_void_p), ("vertex_count", C.c_uint32), ("vertex_stride", C.c_uint32),
                 ("indices", C.c_void_p), ("index_count", C.c_uint32)]
@@ -128,11 +137,15 @@ SIGNATURES = [
     ("luz_blas_destroy", None, [P]),
     ("luz_blas_primitive_count", C.c_uint32, [P]),
     ("luz_blas_download", C.c_int32, [P, P, P, P, c_u32_p, c_u32_p]),
+    ("luz_blas_download_wide", C.c_int32, [P, P, P]),
+    ("luz_blas_memory", C.c_int32, [P, P]),
     ("luz_blas_build_noalloc", C.c_int32, [P, C.c_uint32, P, C.c_uint32, P, P, P, P, P]),
     ("luz_tlas_create", C.c_int32, [P, C.c_uint32, C.POINTER(P)]),
     ("luz_tlas_build", C.c_int32, [P, P, C.POINTER(Instance), C.c_uint32]),
     ("luz_tlas_destroy", None, [P]),
     ("luz_tlas_download", C.c_int32, [P, P, P, c_u32_p, c_u32_p, c_u32_p]),
+    ("luz_tlas_download_wide", C.c_int32, [P, P, P]),
+    ("luz_tlas_memory", C.c_int32, [P, P]),
     ("luz_frame_create", C.c_int32, [P, C.c_uint32, C.c_uint32, C.POINTER(P)]),
     ("luz_frame_destroy", None, [P]),
     ("luz_frame_upload", C.c_int32, [P, P, C.POINTER(Scene), C.POINTER(Light), C.c_uint32,

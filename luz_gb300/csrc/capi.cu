@@ -179,6 +179,21 @@ void luz_blas_destroy(luz_blas* b) {
 
 uint32_t luz_blas_primitive_count(const luz_blas* b) { return b ? b->prims : 0; }
 
+luz_status luz_blas_memory(const luz_blas* b, luz_memory* out) {
+    if (!b || !out) return LUZ_ERR_INVALID;
+    *out = b->memory;
+    return LUZ_OK;
+}
+
+luz_status luz_blas_download_wide(luz_ctx* ctx, const luz_blas* b, void* nodes4) {
+    if (!ctx || !b || !nodes4) return LUZ_ERR_INVALID;
+    if (!b->nodes4) return set_error(ctx, LUZ_ERR_INVALID, "BLAS has no 4-wide nodes");
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t m = std::max(b->prims, 2u) - 1;
+    LUZ_CUDA(ctx, cudaMemcpy(nodes4, b->nodes4, (size_t)m * 128, cudaMemcpyDeviceToHost));
+    return LUZ_OK;
+}
+
 luz_status luz_blas_download(luz_ctx* ctx, const luz_blas* b, void* nodes, void* tris,
                              uint32_t* morton_sorted, uint32_t* order) {
     if (!ctx || !b) return LUZ_ERR_INVALID;
@@ -243,6 +258,24 @@ luz_status luz_tlas_download(luz_ctx* ctx, const luz_tlas* t, void* nodes, uint3
     if (nodes && m) LUZ_CUDA(ctx, cudaMemcpy(nodes, t->nodes, (size_t)m * 64, cudaMemcpyDeviceToHost));
     if (morton_sorted && n) LUZ_CUDA(ctx, cudaMemcpy(morton_sorted, t->morton, (size_t)n * 4, cudaMemcpyDeviceToHost));
     if (order && n) LUZ_CUDA(ctx, cudaMemcpy(order, t->order, (size_t)n * 4, cudaMemcpyDeviceToHost));
+    return LUZ_OK;
+}
+
+luz_status luz_tlas_download_wide(luz_ctx* ctx, const luz_tlas* t, void* nodes4) {
+    if (!ctx || !t || !nodes4) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t n = t->count, m = n ? std::max(n, 2u) - 1 : 0;
+    if (m) LUZ_CUDA(ctx, cudaMemcpy(nodes4, t->nodes4, (size_t)m * 128, cudaMemcpyDeviceToHost));
+    return LUZ_OK;
+}
+
+luz_status luz_tlas_memory(const luz_tlas* t, luz_memory* out) {
+    if (!t || !out) return LUZ_ERR_INVALID;
+    uint64_t cap = std::max(t->max_instances, 1u), m = std::max<uint64_t>(cap, 2) - 1;
+    out->nodes = m * 64;
+    out->wide_nodes = m * 128;
+    out->leaves = cap * sizeof(DevInstance);
+    out->other = 66 * 4 + cap * (sizeof(DevShadeInstance) + sizeof(DevInstanceInput) + 8) + t->tmp_bytes;
     return LUZ_OK;
 }
 

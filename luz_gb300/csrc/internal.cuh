@@ -113,6 +113,7 @@ struct luz_blas {
     uint32_t* indices = nullptr;
     uint32_t prims = 0;
     uint32_t vertex_count = 0;
+    luz_memory memory{};                 // bytes of this BLAS's slices of the arena
 };
 
 struct luz_tlas {

@@ -869,7 +869,7 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
     if (total_prims >= (1ull << 30) - 1)
         return set_error(ctx, LUZ_ERR_LIMIT, "more than 2^30 triangles in one batch");
     cudaStream_t st = ctx->stream;
-    // Persistent arena: per BLAS nodes | tris | morton | order | vertices | indices.
+    // Persistent arena: per BLAS nodes | 4-wide nodes | tris | morton | order | vertices | indices.
     std::vector<size_t> off_nodes(count), off_tris(count), off_mort(count), off_ord(count),
         off_vtx(count), off_idx(count), off_nodes4(count);
     size_t arena_bytes = 0;
@@ -1025,6 +1025,10 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
         arena->refs++;
         b->nodes = segs[s].nodes;
         b->nodes4 = segs[s].nodes4;
+        b->memory.nodes = off_nodes4[s] - off_nodes[s];
+        b->memory.wide_nodes = off_tris[s] - off_nodes4[s];
+        b->memory.leaves = off_mort[s] - off_tris[s];
+        b->memory.other = (s + 1 < count ? off_nodes[s + 1] : arena_bytes) - off_mort[s];
         b->tris = segs[s].tris;
         b->morton = (uint32_t*)(ab + off_mort[s]);
         b->order = (uint32_t*)(ab + off_ord[s]);

@@ -212,3 +212,62 @@ class OracleFrame:
            _p(self.material), _p(self.emission), _p(self.depth), _p(self.shadow_bits), _p(self.ao_bits), _p(ao),
            self.W, self.H, _p(out), nthreads or threads(), y0, self.H if y1 is None else y1)
         return out.reshape(self.H, self.W, 4)
+
+
+K_EMPTY_CHILD = -2147483647   # 0x80000001: a child slot with an inverted box
+
+
+def _child_box(node: np.ndarray, side: int):
+    """Box of child `side` of a binary node (64 B: see the BVH layout of the library)."""
+    if side == 0:
+        return (node[0], node[2], node[8]), (node[1], node[3], node[9])
+    return (node[4], node[6], node[10]), (node[5], node[7], node[11])
+
+
+def collapse_wide(nodes: np.ndarray) -> np.ndarray:
+    """Even-depth 4-wide collapse of a binary BVH (rows of 16 float32, root at 0).
+
+    Every binary node at even depth becomes a 4-wide node; its slots are its
+    grandchildren, or its children where a child is a leaf (or an empty slot), in
+    left-to-right order, padded with inverted boxes and the empty-child id. Internal
+    slot ids are ranks among the even-depth nodes in index order. Rows of 32 float32:
+    lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] child[4] (int bits) 0[4].
+    """
+    m = len(nodes)
+    iv = nodes.view(np.int32)
+    depth = np.full(m, -1, np.int64)
+    depth[0] = 0
+    stack = [0]
+    while stack:
+        q = stack.pop()
+        for side in (0, 1):
+            c = int(iv[q, 12 + side])
+            if c >= 0:
+                depth[c] = depth[q] + 1
+                stack.append(c)
+    even = np.nonzero(depth % 2 == 0)[0]
+    rank = np.full(m, -1, np.int64)
+    rank[even] = np.arange(len(even))
+    out = np.zeros((len(even), 32), np.float32)
+    oi = out.view(np.int32)
+    for q in even:
+        slots = []
+        for side in (0, 1):
+            c = int(iv[q, 12 + side])
+            if c < 0:
+                slots.append((_child_box(nodes[q], side), c))
+                continue
+            for s2 in (0, 1):
+                g = int(iv[c, 12 + s2])
+                slots.append((_child_box(nodes[c], s2), g if g < 0 else int(rank[g])))
+        row = int(rank[q])
+        for k in range(4):
+            if k < len(slots):
+                (lo, hi), cid = slots[k]
+            else:
+                lo, hi, cid = (np.inf,) * 3, (-np.inf,) * 3, K_EMPTY_CHILD
+            for a in range(3):
+                out[row, 8 * a + k] = lo[a]
+                out[row, 8 * a + 4 + k] = hi[a]
+            oi[row, 24 + k] = cid
+    return out
