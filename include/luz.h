@@ -303,8 +303,22 @@ void luz_frame_destroy(luz_frame* frame);
 luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* frame, const luz_scene* scene,
                             const luz_light* lights, uint32_t light_count,
                             const luz_model* models, uint32_t model_count);
+/* Textures of the frame's ModelBlocks (RGBA8 UNORM, rows top to bottom, 4 B per
+ * texel): map fields >= 0 index this list. Replaces earlier textures. Mirrors the
+ * RGBA8_unorm images GPUScene creates per texture asset (GPUScene.cpp:56-106) with the
+ * reference's sampler: linear filtering, repeat addressing, one mip level
+ * (VulkanWrapper.cpp:500, 2429-2454). count 0 clears. */
+typedef struct luz_texture_desc {
+    const uint8_t* rgba8;     /* host memory, width * height * 4 bytes */
+    uint32_t width, height;
+} luz_texture_desc;
+luz_status luz_frame_set_textures(luz_ctx* ctx, luz_frame* frame, const luz_texture_desc* textures,
+                                  uint32_t count);
 /* Primary-ray G-buffer: the raster opaque pass (source/Shaders/opaque.vert:21-31,
- * opaque.frag:21-58; main.cpp:242-258) as closest-hit rays through pixel centres. */
+ * opaque.frag:21-58; main.cpp:242-258) as closest-hit rays through pixel centres.
+ * Texture maps are sampled at the hit's interpolated texcoord; a model with a colour
+ * map is alpha-tested per hit (opaque.frag's discard below 0.5), so the ray goes on
+ * to the surface behind. */
 luz_status luz_gbuffer_primary(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas);
 /* Shadow (light.frag:86-109,137-146) and AO (light.frag:111-135) any-hit rays of
  * every lit pixel; writes the visibility bit planes. */

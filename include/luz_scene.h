@@ -98,6 +98,35 @@ void luz_camera_matrices(const luz_camera* cam, float view[16], float proj[16]);
 /* Seeded RGBA8 substitute for the missing assets/blue_noise.png. */
 luz_status luz_blue_noise_generate(uint64_t seed, uint32_t size, uint8_t* rgba8);
 
+/* ------------------------------------------------------------------ scene files
+ * The reference's project files and importers: AssetManager::LoadProject /
+ * SaveProject (source/Resources/AssetManager.cpp:183-258, format of
+ * source/Resources/Serializer.hpp: a .luz JSON document plus a .luzbin binary
+ * store) and AssetIO::ImportSceneGLTF / ImportSceneOBJ
+ * (source/Resources/AssetIO.cpp:117-529). A loaded scene is packed as
+ * GPUScene::UpdateResources packs one (GPUScene.cpp:181-346): MeshNodes of a
+ * pre-order walk become instances with ModelBlocks, LightNodes LightBlocks; the
+ * project's main camera (or a default CameraNode) gets extent width x height.
+ * Textures (RGBA8) are numbered by first use and the ModelBlocks' map fields index
+ * them. Images in glTF / OBJ files must be PNG. On failure a message goes to err
+ * (err_len bytes, may be NULL). */
+luz_status luz_scene_load_project(const char* luz_path, const char* luzbin_path, uint32_t width, uint32_t height,
+                                  luz_host_scene** out, char* err, uint32_t err_len);
+/* A .gltf / .glb / .obj file added to an empty default scene (AssetManager::
+ * AddAssetsToScene, AssetManager.cpp:273-288). */
+luz_status luz_scene_import(const char* path, uint32_t width, uint32_t height, luz_host_scene** out, char* err,
+                            uint32_t err_len);
+/* Writes a scene as a .luz / .luzbin pair the reference's LoadProject reads (one
+ * MeshNode per instance, one LightNode per light, the camera as the main camera).
+ * Nodes also carry their exact matrix ("luzMatrix") and lights their exact direction
+ * ("luzDirection"), which luz_scene_load_project prefers, so scenes round-trip
+ * bit for bit through this library. */
+luz_status luz_scene_save_project(const luz_host_scene* s, const char* luz_path, const char* luzbin_path, char* err,
+                                  uint32_t err_len);
+uint32_t luz_scene_texture_count(const luz_host_scene* s);
+luz_status luz_scene_texture(const luz_host_scene* s, uint32_t i, const uint8_t** rgba8, uint32_t* width,
+                             uint32_t* height);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,6 +69,47 @@ class HostScene:
         _check(lib.luz_scene_generate(C.byref(p), C.byref(h)), what="scene generate")
         self._h = h
 
+    @classmethod
+    def _adopt(cls, h) -> "HostScene":
+        obj = cls.__new__(cls)
+        obj.params = None
+        obj._h = h
+        return obj
+
+    @classmethod
+    def load_project(cls, luz_path, luzbin_path, width: int = 1920, height: int = 1080) -> "HostScene":
+        """The initial scene of a .luz / .luzbin project (AssetManager::LoadProject)."""
+        h, err = C.c_void_p(), C.create_string_buffer(512)
+        st = lib.luz_scene_load_project(str(luz_path).encode(), str(luzbin_path).encode(), width, height,
+                                        C.byref(h), err, len(err))
+        if st != _abi.LUZ_OK:
+            raise LuzError(st, f"load project {luz_path}: {err.value.decode()}")
+        return cls._adopt(h)
+
+    @classmethod
+    def import_file(cls, path, width: int = 1920, height: int = 1080) -> "HostScene":
+        """A .gltf / .glb / .obj file in an empty default scene (AssetIO::Import)."""
+        h, err = C.c_void_p(), C.create_string_buffer(512)
+        st = lib.luz_scene_import(str(path).encode(), width, height, C.byref(h), err, len(err))
+        if st != _abi.LUZ_OK:
+            raise LuzError(st, f"import {path}: {err.value.decode()}")
+        return cls._adopt(h)
+
+    def save_project(self, luz_path, luzbin_path) -> None:
+        err = C.create_string_buffer(512)
+        st = lib.luz_scene_save_project(self._h, str(luz_path).encode(), str(luzbin_path).encode(), err, len(err))
+        if st != _abi.LUZ_OK:
+            raise LuzError(st, f"save project {luz_path}: {err.value.decode()}")
+
+    def textures(self) -> list[np.ndarray]:
+        """RGBA8 textures (h, w, 4) indexed by the ModelBlocks' map fields (copies)."""
+        out = []
+        for i in range(lib.luz_scene_texture_count(self._h)):
+            p, w, hh = _abi.c_u8_p(), C.c_uint32(), C.c_uint32()
+            _check(lib.luz_scene_texture(self._h, i, C.byref(p), C.byref(w), C.byref(hh)))
+            out.append(np.ctypeslib.as_array(p, shape=(hh.value, w.value, 4)).copy())
+        return out
+
     def __del__(self):
         if getattr(self, "_h", None):
             lib.luz_scene_destroy(self._h)
@@ -278,6 +319,17 @@ class Frame:
     def upload(self, scene: Scene, lights, light_count: int, models, model_count: int) -> None:
         _check(lib.luz_frame_upload(self.ctx.handle, self._h, C.byref(scene), lights, light_count, models,
                                     model_count), self.ctx.handle, "frame upload")
+
+    def set_textures(self, textures) -> None:
+        """RGBA8 arrays (h, w, 4) that the ModelBlocks' map fields index."""
+        tex = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        descs = (_abi.TextureDesc * max(len(tex), 1))()
+        for k, t in enumerate(tex):
+            descs[k].rgba8 = t.ctypes.data
+            descs[k].width = t.shape[1]
+            descs[k].height = t.shape[0]
+        _check(lib.luz_frame_set_textures(self.ctx.handle, self._h, descs, len(tex)), self.ctx.handle,
+               "set textures")
 
     def gbuffer(self, tlas: Tlas) -> None:
         _check(lib.luz_gbuffer_primary(self.ctx.handle, self._h, tlas.handle), self.ctx.handle, "gbuffer")
@@ -522,6 +574,9 @@ class GPUScene:
         self.blas_prims = sum(len(i) // 3 for _, i in meshes)
         self.tlas = ctx.tlas(max(scene.instance_count, 1))          # CreateTLAS
         self.frame = ctx.frame(scene.width, scene.height)           # DeferredRenderer::CreateImages
+        self.textures = scene.textures()                            # one RGBA8 image per texture asset
+        if self.textures:
+            self.frame.set_textures(self.textures)
         self.update_resources()
 
     def update_resources(self) -> None:

@@ -71,6 +71,10 @@ class Instance(C.Structure):
                 ("mask", C.c_uint32)]
 
 
+class TextureDesc(C.Structure):
+    _fields_ = [("rgba8", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
 class Memory(C.Structure):
     _fields_ = [("nodes", C.c_uint64), ("wide_nodes", C.c_uint64), ("leaves", C.c_uint64), ("other", C.c_uint64)]
 
@@ -138,6 +142,7 @@ SIGNATURES = [
     ("luz_blas_primitive_count", C.c_uint32, [P]),
     ("luz_blas_download", C.c_int32, [P, P, P, P, c_u32_p, c_u32_p]),
     ("luz_blas_download_wide", C.c_int32, [P, P, P]),
+    ("luz_frame_set_textures", C.c_int32, [P, P, P, C.c_uint32]),
     ("luz_blas_memory", C.c_int32, [P, P]),
     ("luz_blas_build_noalloc", C.c_int32, [P, C.c_uint32, P, C.c_uint32, P, P, P, P, P]),
     ("luz_tlas_create", C.c_int32, [P, C.c_uint32, C.POINTER(P)]),
@@ -198,6 +203,12 @@ SIGNATURES = [
     ("luz_scene_set_camera", C.c_int32, [P, C.POINTER(Camera)]),
     ("luz_scene_get_camera", C.c_int32, [P, C.POINTER(Camera)]),
     ("luz_scene_set_sampling", C.c_int32, [P, C.c_int32, C.c_float, C.c_float, C.c_int32, C.c_int32]),
+    ("luz_scene_load_project", C.c_int32, [C.c_char_p, C.c_char_p, C.c_uint32, C.c_uint32, C.POINTER(P),
+                                           C.c_char_p, C.c_uint32]),
+    ("luz_scene_import", C.c_int32, [C.c_char_p, C.c_uint32, C.c_uint32, C.POINTER(P), C.c_char_p, C.c_uint32]),
+    ("luz_scene_save_project", C.c_int32, [P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint32]),
+    ("luz_scene_texture_count", C.c_uint32, [P]),
+    ("luz_scene_texture", C.c_int32, [P, C.c_uint32, C.POINTER(c_u8_p), c_u32_p, c_u32_p]),
     ("luz_compose_transform", None, [c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     ("luz_camera_matrices", None, [C.POINTER(Camera), c_float_p, c_float_p]),
     ("luz_blue_noise_generate", C.c_int32, [C.c_uint64, C.c_uint32, c_u8_p]),

@@ -25,7 +25,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_TUS = ["lbvh.cu", "trace.cu", "visibility.cu", "lightpass.cu", "capi.cu", "blas_noalloc.cu",
             "denoise.cu", "batch.cu"]
 FMA_TUS = {"denoise.cu"}
-HOST_TUS = ["scene.cpp"]
+HOST_TUS = ["scene.cpp", "ingest.cpp"]
 
 
 def _nvcc() -> str:

@@ -54,7 +54,8 @@ static void free_frame_buffers(luz_frame* f) {
                     f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->surf,
                     f->features, f->lin_depth,
                     f->block_counts, f->lit_count, f->d_scene, f->d_lights, f->d_models,
-                    f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter};
+                    f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter, f->d_textures,
+                    f->d_texels};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -373,8 +374,14 @@ luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, 
     if (!f->d_slot_table) LUZ_CUDA(ctx, cudaMalloc(&f->d_slot_table, (size_t)LUZ_MAX_SHADOW_SLOTS * 4));
     f->h_slot_table = slot_table;
     std::vector<uint8_t> skip(std::max(model_count, 1u), 0);
-    for (uint32_t m = 0; m < model_count; ++m)
-        skip[m] = (models[m].color_map < 0 && models[m].color[3] < 0.5f) ? 1 : 0;
+    int32_t max_map = -1;
+    for (uint32_t m = 0; m < model_count; ++m) {
+        const luz_model& md = models[m];
+        skip[m] = md.color_map >= 0 ? 2 : (md.color[3] < 0.5f ? 1 : 0);
+        for (int32_t t : {md.ao_map, md.color_map, md.normal_map, md.emission_map, md.metallic_roughness_map})
+            max_map = std::max(max_map, t);
+    }
+    f->max_map_index = max_map;
     f->h_scene = *scene;
     f->light_count = light_count;
     f->model_count = model_count;
@@ -394,6 +401,36 @@ luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, 
     // Pageable sources: the copies above are staged before returning; the vectors
     // may go out of scope once the stream has consumed them.
     LUZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return LUZ_OK;
+}
+
+luz_status luz_frame_set_textures(luz_ctx* ctx, luz_frame* f, const luz_texture_desc* tex, uint32_t count) {
+    if (!ctx || !f || (count && !tex)) return LUZ_ERR_INVALID;
+    size_t total = 0;
+    std::vector<size_t> off(count);
+    for (uint32_t k = 0; k < count; ++k) {
+        if (!tex[k].rgba8 || tex[k].width == 0 || tex[k].height == 0 || tex[k].width > 65536 || tex[k].height > 65536)
+            return set_error(ctx, LUZ_ERR_INVALID, "texture " + std::to_string(k) + ": empty or larger than 65536");
+        off[k] = total;
+        total += ((size_t)tex[k].width * tex[k].height * 4 + 255) & ~(size_t)255;
+    }
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (f->d_textures) { cudaFree(f->d_textures); f->d_textures = nullptr; }
+    if (f->d_texels) { cudaFree(f->d_texels); f->d_texels = nullptr; }
+    f->texture_count = 0;
+    if (!count) return LUZ_OK;
+    LUZ_CUDA(ctx, cudaMalloc(&f->d_texels, total));
+    LUZ_CUDA(ctx, cudaMalloc(&f->d_textures, (size_t)count * sizeof(DevTexture)));
+    std::vector<DevTexture> table(count);
+    for (uint32_t k = 0; k < count; ++k) {
+        table[k].texels = (const uint32_t*)((char*)f->d_texels + off[k]);
+        table[k].width = tex[k].width;
+        table[k].height = tex[k].height;
+        LUZ_CUDA(ctx, cudaMemcpy((char*)f->d_texels + off[k], tex[k].rgba8, (size_t)tex[k].width * tex[k].height * 4,
+                                 cudaMemcpyHostToDevice));
+    }
+    LUZ_CUDA(ctx, cudaMemcpy(f->d_textures, table.data(), (size_t)count * sizeof(DevTexture), cudaMemcpyHostToDevice));
+    f->texture_count = count;
     return LUZ_OK;
 }
 

@@ -44,6 +44,12 @@ struct __align__(16) DevInstance {
 };
 static_assert(sizeof(DevInstance) == 96, "DevInstance layout");
 
+// A frame texture: RGBA8 texels (one u32 each, rows top to bottom).
+struct DevTexture {
+    const uint32_t* texels;
+    uint32_t width, height;
+};
+
 // Per-instance data used by the G-buffer kernel, in the caller's instance order.
 struct DevShadeInstance {
     float normal_mat[9];    // transpose(inverse(model 3x3)), row-major
@@ -171,7 +177,11 @@ struct luz_frame {
     uint32_t* d_slot_table = nullptr;  // per shadow slot: light | sample << 16
     std::vector<uint32_t> h_slot_table;
     uint32_t* d_light_slot = nullptr;  // per light: first shadow slot
-    uint8_t* d_model_skip = nullptr;   // per model: 1 = discarded by the alpha test
+    uint8_t* d_model_skip = nullptr;   // per model: 1 = discarded by the alpha test, 2 = tested per hit
+    int32_t max_map_index = -1;        // largest texture index of the uploaded ModelBlocks
+    luz::DevTexture* d_textures = nullptr;
+    void* d_texels = nullptr;
+    uint32_t texture_count = 0;
     unsigned long long* work_counter = nullptr;
 };
 

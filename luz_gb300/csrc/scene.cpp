@@ -12,8 +12,11 @@
 
 #include "../../include/luz_scene.h"
 #include "pathmath.cuh"
+#include "scene_internal.hpp"
 
 namespace {
+
+using luz::host::Mesh;
 
 // ---------------------------------------------------------------- PRNG
 // SplitMix64 (S. Vigna): integer-only, identical on every platform.
@@ -211,10 +214,6 @@ void camera_matrices(const luz_camera& cam, luz_camera& updated, M4& view, M4& p
 }
 
 // ---------------------------------------------------------------- meshes
-struct Mesh {
-    std::vector<luz_vertex> v;
-    std::vector<uint32_t> i;
-};
 
 luz_vertex vert(float px, float py, float pz, float nx, float ny, float nz) {
     luz_vertex v;
@@ -336,18 +335,6 @@ Mesh displace(const Mesh& base, Rng& rng, float amplitude) {
 
 }  // namespace
 
-struct luz_host_scene {
-    std::vector<Mesh> meshes;
-    std::vector<uint32_t> instance_mesh;
-    std::vector<luz_model> models;
-    std::vector<luz_light> lights;
-    luz_scene block{};
-    luz_camera camera{};
-    uint32_t width = 0, height = 0;
-    int32_t light_samples = 1;
-    M4 prev_view_proj = identity();
-};
-
 namespace {
 
 luz_model default_model() {   // GPUScene.cpp:19-30
@@ -425,7 +412,7 @@ void update_block(luz_host_scene* s) {
     s->camera = upd;
     luz_scene& b = s->block;
     M4 vp = mul(proj, view);
-    memcpy(b.prev_view_proj, s->prev_view_proj.data(), 64);
+    memcpy(b.prev_view_proj, s->prev_view_proj, 64);
     memcpy(b.proj, proj.data(), 64);
     memcpy(b.view, view.data(), 64);
     memcpy(b.view_proj, vp.data(), 64);
@@ -438,7 +425,7 @@ void update_block(luz_host_scene* s) {
     b.cam_pos[1] = s->camera.eye[1];
     b.cam_pos[2] = s->camera.eye[2];
     b.num_lights = (int32_t)s->lights.size();
-    s->prev_view_proj = vp;
+    memcpy(s->prev_view_proj, vp.data(), 64);
 }
 
 luz_camera look_camera(F3 eye, F3 center, float fovy, uint32_t w, uint32_t h, float zn, float zf) {
@@ -577,6 +564,23 @@ void gen_budget(luz_host_scene* s, const luz_gen_params& p, Rng& rng) {
 
 }  // namespace
 
+namespace luz {
+namespace host {
+luz_model default_model() { return ::default_model(); }
+void refresh_block(luz_host_scene* s) {
+    update_block(s);
+    update_block(s);   // prevViewProj = viewProj for a static camera
+}
+void compose_transform(const float pos[3], const float rot_deg[3], const float scl[3], const float parent[16],
+                       float out[16]) {
+    M4 par = identity();
+    if (parent) memcpy(par.data(), parent, 64);
+    M4 r = compose(pos, rot_deg, scl, par);
+    memcpy(out, r.data(), 64);
+}
+}  // namespace host
+}  // namespace luz
+
 extern "C" {
 
 luz_status luz_scene_default_params(int32_t config, luz_gen_params* out) {
@@ -637,7 +641,20 @@ luz_status luz_scene_generate(const luz_gen_params* p, luz_host_scene** out) {
     return LUZ_OK;
 }
 
+
 void luz_scene_destroy(luz_host_scene* s) { delete s; }
+
+uint32_t luz_scene_texture_count(const luz_host_scene* s) { return s ? (uint32_t)s->textures.size() : 0; }
+
+luz_status luz_scene_texture(const luz_host_scene* s, uint32_t i, const uint8_t** rgba8, uint32_t* width,
+                             uint32_t* height) {
+    if (!s || i >= s->textures.size()) return LUZ_ERR_INVALID;
+    const luz::host::Texture& t = s->textures[i];
+    if (rgba8) *rgba8 = t.rgba.data();
+    if (width) *width = t.width;
+    if (height) *height = t.height;
+    return LUZ_OK;
+}
 
 uint32_t luz_scene_mesh_count(const luz_host_scene* s) { return s ? (uint32_t)s->meshes.size() : 0; }
 

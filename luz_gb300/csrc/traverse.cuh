@@ -115,13 +115,21 @@ struct TraceCounters {
     uint32_t tlas_nodes, blas_nodes, tris, instances;
 };
 
+// Accepts every closest-hit candidate.
+struct AcceptAll {
+    __device__ __forceinline__ bool operator()(uint32_t, uint32_t, uint32_t, float, float, float) const { return true; }
+};
+
 // kClosest = false: any-hit, returns at the first accepted triangle.
-// skip: closest-hit skips instances whose custom index is flagged in `skip`.
-template <bool kClosest, bool kStats = false>
+// skip: closest-hit skips instances whose custom index is flagged 1 in `skip`; for a
+// flag of 2 every candidate hit is offered to `accept(instance input, custom index,
+// primitive, b0, b1, b2)` first, and a rejected hit leaves the ray going (an
+// alpha test).
+template <bool kClosest, bool kStats = false, typename Accept = AcceptAll>
 __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float tmin, float tmax,
                                           uint32_t ray_mask, const uint8_t* __restrict__ skip,
                                           uint32_t skip_count, ClosestHit* hit, uint32_t& err,
-                                          TraceCounters* cnt = nullptr) {
+                                          TraceCounters* cnt = nullptr, const Accept& accept = Accept()) {
     if (T.count == 0) return false;
     if (!finite3(wo) || !finite3(wd) || !(tmin <= tmax)) return false;
     if (wd.x == 0.0f && wd.y == 0.0f && wd.z == 0.0f) return false;
@@ -135,6 +143,7 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
     const float4* __restrict__ nodes = T.nodes;
     const float4* __restrict__ tris = nullptr;
     uint32_t inst_input = 0, inst_custom = 0;
+    bool inst_tested = false;
     bool found = false;
     unsigned long long best_key = ~0ull;
     for (uint32_t iter = 0;; ++iter) {
@@ -173,7 +182,11 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
             uint4 meta = __ldg(reinterpret_cast<const uint4*>(&I->custom_index));
             // meta = (custom_index, mask, input_index, blas_prims)
             bool take = (meta.y & ray_mask) != 0 && meta.w > 0;
-            if (kClosest && take && skip && meta.x < skip_count) take = skip[meta.x] == 0;
+            bool tested = false;
+            if (kClosest && take && skip && meta.x < skip_count) {
+                take = skip[meta.x] != 1;
+                tested = skip[meta.x] == 2;
+            }
             if (take) {
                 float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
                 V3 oo = xform_point(m, wo);
@@ -188,6 +201,7 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
                 tris = ptris;
                 inst_input = meta.z;
                 inst_custom = meta.x;
+                inst_tested = tested;
                 node = 0;
                 pop = false;
             }
@@ -201,7 +215,8 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
                 if (!kClosest) return true;
                 uint32_t prim = (uint32_t)__float_as_int(a.w);
                 unsigned long long key = ((unsigned long long)inst_input << 32) | prim;
-                if (!found || t < tmax || key < best_key) {
+                if ((!found || t < tmax || key < best_key) &&
+                    (!inst_tested || accept(inst_input, inst_custom, prim, U / det, V / det, W / det))) {
                     found = true;
                     tmax = t;
                     best_key = key;

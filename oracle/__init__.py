@@ -42,7 +42,7 @@ def load() -> C.CDLL:
             "oracle_tlas_get": (None, [P, P, P, P, P]),
             "oracle_tlas_destroy": (None, [P]),
             "oracle_gbuffer": (C.c_int, [P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P, P, P, P, C.c_int,
-                                         C.c_uint32, C.c_uint32]),
+                                         C.c_uint32, C.c_uint32, P, P, C.c_uint32]),
             "oracle_visibility": (C.c_uint64, [P, P, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, C.c_uint32,
                                                C.c_uint32, C.c_int, P, C.c_uint32, P, P, C.c_int, C.c_int]),
             "oracle_light_pass": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32, P,
@@ -188,11 +188,15 @@ class OracleFrame:
         self.shadow_bits = np.zeros((max(ns, 1), self.words), np.uint32)
         self.ao_bits = np.zeros((max(self.ao_samples, 1), self.words), np.uint32)
 
-    def gbuffer(self, nthreads=None, y0: int = 0, y1: int | None = None):
+    def gbuffer(self, nthreads=None, y0: int = 0, y1: int | None = None, textures=()):
+        """textures: RGBA8 arrays (h, w, 4) indexed by the ModelBlocks' map fields."""
+        tex = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        ptrs = (C.c_void_p * max(len(tex), 1))(*[t.ctypes.data for t in tex])
+        dims = np.array([[t.shape[1], t.shape[0]] for t in tex] or [[0, 0]], np.uint32)
         load().oracle_gbuffer(self.tlas.handle, scene_bytes(self.scene), C.cast(self.models, C.c_void_p), self.nm,
                               self.W, self.H, _p(self.albedo), _p(self.normal), _p(self.material),
                               _p(self.emission), _p(self.depth), _p(self.primary_hit), nthreads or threads(),
-                              y0, self.H if y1 is None else y1)
+                              y0, self.H if y1 is None else y1, C.cast(ptrs, C.c_void_p), _p(dims), len(tex))
 
     def visibility(self, frame: int, bn: np.ndarray, y0: int = 0, y1: int | None = None, brute: bool = False,
                    nthreads=None) -> int:

@@ -472,10 +472,16 @@ struct Hit {
     float b0, b1, b2;
 };
 
+// Per-hit alpha test of the primary rays (opaque.frag:29-34 discard).
+struct AlphaTest {
+    virtual bool accept(uint32_t input, uint32_t custom, uint32_t prim, float b0, float b1, float b2) const = 0;
+    virtual ~AlphaTest() {}
+};
+
 // Object-space closest/any hit inside one BLAS. Returns true if any accepted hit.
 template <bool kClosest>
 static bool trace_blas(const Blas& b, v3 o, v3 d, float tmin, float& tmax, uint32_t input, uint32_t custom,
-                       bool& found, Hit* hit, uint64_t& best_key) {
+                       bool& found, Hit* hit, uint64_t& best_key, const AlphaTest* alpha = nullptr) {
     if (b.prims == 0) return false;
     v3 id = safe_inv(d);
     WtRay wt = wt_setup(o, d);
@@ -500,7 +506,8 @@ static bool trace_blas(const Blas& b, v3 o, v3 d, float tmin, float& tmax, uint3
             uint32_t prim;
             memcpy(&prim, &tr[3], 4);
             uint64_t key = ((uint64_t)input << 32) | prim;
-            if (!found || t < tmax || key < best_key) {
+            if ((!found || t < tmax || key < best_key) &&
+                (!alpha || alpha->accept(input, custom, prim, U / det, V / det, W / det))) {
                 found = true;
                 any = true;
                 tmax = t;
@@ -519,8 +526,10 @@ static bool ray_ok(v3 o, v3 d, float tmin, float tmax) {
     return true;
 }
 
+// skip[custom]: 1 = instance never hit by closest-hit rays, 2 = every hit alpha-tested.
 template <bool kClosest>
-static bool trace(const Tlas& T, v3 o, v3 d, float tmin, float tmax, const uint8_t* skip, uint32_t skip_n, Hit* hit) {
+static bool trace(const Tlas& T, v3 o, v3 d, float tmin, float tmax, const uint8_t* skip, uint32_t skip_n, Hit* hit,
+                  const AlphaTest* alpha = nullptr) {
     if (T.inst.empty() || !ray_ok(o, d, tmin, tmax)) return false;
     v3 id = safe_inv(d);
     int32_t stack[256];
@@ -538,9 +547,11 @@ static bool trace(const Tlas& T, v3 o, v3 d, float tmin, float tmax, const uint8
             if (!slab(get_slot(node, c), o, id, tmin, tmax, tn)) continue;
             if (ch >= 0) { stack[sp++] = ch; continue; }
             const Instance& I = T.inst[~ch];
-            if (kClosest && skip && I.custom < skip_n && skip[I.custom]) continue;
+            const bool tested = kClosest && skip && I.custom < skip_n && skip[I.custom] == 2;
+            if (kClosest && skip && I.custom < skip_n && skip[I.custom] == 1) continue;
             v3 oo = xpoint(I.w2o, o), od = xdir(I.w2o, d);
-            bool h = trace_blas<kClosest>(*I.blas, oo, od, tmin, tmax, I.input, I.custom, found, hit, best_key);
+            bool h = trace_blas<kClosest>(*I.blas, oo, od, tmin, tmax, I.input, I.custom, found, hit, best_key,
+                                          tested ? alpha : nullptr);
             if (h && !kClosest) return true;
         }
     }
@@ -851,13 +862,82 @@ void oracle_tlas_get(const oracle_tlas* ot, float* nodes, uint32_t* morton, uint
 
 void oracle_tlas_destroy(oracle_tlas* t) { delete t; }
 
+// ---------------------------------------------------------------- textures
+// One RGBA8 UNORM level sampled bilinearly with repeat addressing (the reference's
+// sampler, VulkanWrapper.cpp:2429-2454): u*width - 0.5 to texel space, weights from
+// the fractional part, texels as c / 255.
+struct Tex {
+    const uint32_t* texels;
+    uint32_t w, h;
+};
+static uint32_t tex_wrap(float f, uint32_t n) {
+    float m = std::fmod(f, (float)n);
+    if (m < 0.0f) m += (float)n;
+    uint32_t i = (uint32_t)m;
+    return i < n ? i : 0u;
+}
+static void tex_texel(const Tex& t, uint32_t x, uint32_t y, float c[4]) {
+    uint32_t v = t.texels[(size_t)y * t.w + x];
+    for (int k = 0; k < 4; ++k) c[k] = (float)((v >> (8 * k)) & 255u) / 255.0f;
+}
+static void tex_sample(const Tex& t, float u, float v, float out[4]) {
+    float x = u * (float)t.w - 0.5f, y = v * (float)t.h - 0.5f;
+    if (!std::isfinite(x)) x = 0.0f;
+    if (!std::isfinite(y)) y = 0.0f;
+    float fx = std::floor(x), fy = std::floor(y);
+    float ax = x - fx, ay = y - fy;
+    uint32_t x0 = tex_wrap(fx, t.w), y0 = tex_wrap(fy, t.h);
+    uint32_t x1 = x0 + 1 == t.w ? 0u : x0 + 1, y1 = y0 + 1 == t.h ? 0u : y0 + 1;
+    float c00[4], c10[4], c01[4], c11[4];
+    tex_texel(t, x0, y0, c00);
+    tex_texel(t, x1, y0, c10);
+    tex_texel(t, x0, y1, c01);
+    tex_texel(t, x1, y1, c11);
+    float bx = 1.0f - ax, by = 1.0f - ay;
+    for (int k = 0; k < 4; ++k) out[k] = (c00[k] * bx + c10[k] * ax) * by + (c01[k] * bx + c11[k] * ax) * ay;
+}
+
+static void hit_uv(const Blas& b, uint32_t prim, float b0, float b1, float b2, float& u, float& v) {
+    const luz_vertex& v0 = b.vertices[b.indices[3 * prim]];
+    const luz_vertex& v1 = b.vertices[b.indices[3 * prim + 1]];
+    const luz_vertex& v2 = b.vertices[b.indices[3 * prim + 2]];
+    u = (v0.texcoord[0] * b0 + v1.texcoord[0] * b1) + v2.texcoord[0] * b2;
+    v = (v0.texcoord[1] * b0 + v1.texcoord[1] * b1) + v2.texcoord[1] * b2;
+}
+
+struct ColourAlpha : AlphaTest {
+    const Tlas* T;
+    const luz_model* models;
+    uint32_t nmodels;
+    const std::vector<Tex>* tex;
+    bool accept(uint32_t input, uint32_t custom, uint32_t prim, float b0, float b1, float b2) const override {
+        if (custom >= nmodels) return true;
+        const luz_model& m = models[custom];
+        if (m.color_map < 0 || (uint32_t)m.color_map >= tex->size()) return !(m.color[3] < 0.5f);
+        float u, v, c[4];
+        hit_uv(*T->by_input[input].blas, prim, b0, b1, b2, u, v);
+        tex_sample((*tex)[(size_t)m.color_map], u, v, c);
+        return !(m.color[3] * c[3] < 0.5f);
+    }
+};
+
 // Primary-ray G-buffer (opaque.vert:21-31 + opaque.frag:21-58 at the closest hit).
+// textures: ntex pointers to RGBA8 texel arrays, dims: width, height per texture.
 int oracle_gbuffer(const oracle_tlas* ot, const luz_scene* S, const luz_model* models, uint32_t nmodels, uint32_t W,
                    uint32_t H, uint32_t* albedo, float* normal, uint32_t* material, uint32_t* emission, float* depth,
-                   uint32_t* primary_hit, int threads, uint32_t y0, uint32_t y1) {
+                   uint32_t* primary_hit, int threads, uint32_t y0, uint32_t y1, const uint32_t* const* textures,
+                   const uint32_t* dims, uint32_t ntex) {
     const Tlas& T = ot->t;
+    std::vector<Tex> tex(ntex);
+    for (uint32_t k = 0; k < ntex; ++k) tex[k] = Tex{textures[k], dims[2 * k], dims[2 * k + 1]};
     std::vector<uint8_t> skip(std::max(nmodels, 1u), 0);
-    for (uint32_t m = 0; m < nmodels; ++m) skip[m] = (models[m].color_map < 0 && models[m].color[3] < 0.5f) ? 1 : 0;
+    for (uint32_t m = 0; m < nmodels; ++m)
+        skip[m] = models[m].color_map >= 0 ? 2 : (models[m].color[3] < 0.5f ? 1 : 0);
+    ColourAlpha alpha;
+    alpha.T = &T;
+    alpha.models = models;
+    alpha.nmodels = nmodels;
+    alpha.tex = &tex;
     // Normal matrices transpose(inverse(model)) = transpose of the w2o 3x3, per input instance.
     y1 = std::min(y1, H);
     const uint32_t p0 = std::min(y0, y1) * W;
@@ -868,7 +948,8 @@ int oracle_gbuffer(const oracle_tlas* ot, const luz_scene* S, const luz_model* m
             v3 target = DepthToWorld(*S, pixel_uv(x, W), pixel_uv(y, H), 1.0f);
             v3 dir = normalize(target - cam);
             Hit h{};
-            bool hit = trace<true>(T, cam, dir, 0.0f, std::numeric_limits<float>::infinity(), skip.data(), nmodels, &h);
+            bool hit = trace<true>(T, cam, dir, 0.0f, std::numeric_limits<float>::infinity(), skip.data(), nmodels, &h,
+                                   &alpha);
             if (!hit) {
                 albedo[pix] = 0; material[pix] = 0; emission[pix] = 0; depth[pix] = 1.0f;
                 for (int k = 0; k < 4; ++k) normal[4 * pix + k] = 0.0f;
@@ -878,30 +959,75 @@ int oracle_gbuffer(const oracle_tlas* ot, const luz_scene* S, const luz_model* m
             v3 p = cam + dir * h.t;
             float pw[4] = {p.x, p.y, p.z, 1.0f}, clip[4];
             mat4_vec4(S->view_proj, pw, clip);
-            float color[4] = {1, 1, 1, 1}, em[3] = {0, 0, 0}, metallic = 0.0f, roughness = 0.5f;
+            float color[4] = {1, 1, 1, 1}, em[4] = {0, 0, 0, 1}, metallic = 0.0f, roughness = 0.5f, occl = 1.0f;
+            int32_t cmap = -1, mrmap = -1, aomap = -1, nmap = -1, emap = -1;
             if (h.custom < nmodels) {
                 const luz_model& m = models[h.custom];
                 for (int k = 0; k < 4; ++k) color[k] = m.color[k];
                 for (int k = 0; k < 3; ++k) em[k] = m.emission[k];
                 metallic = m.metallic;
                 roughness = m.roughness;
+                auto ok = [&](int32_t i) { return i >= 0 && (uint32_t)i < ntex ? i : -1; };
+                cmap = ok(m.color_map);
+                mrmap = ok(m.metallic_roughness_map);
+                aomap = ok(m.ao_map);
+                nmap = ok(m.normal_map);
+                emap = ok(m.emission_map);
             }
             const Instance& I = T.by_input[h.input];
             const Blas& bl = *I.blas;
-            v3 nv[3];
+            const float* w = I.w2o;
+            // transpose(inverse(modelMat)) * vec4(x, 0): rows of the transposed inverse
+            auto tim = [&](const float* n) {
+                return v3{w[0] * n[0] + w[4] * n[1] + w[8] * n[2], w[1] * n[0] + w[5] * n[1] + w[9] * n[2],
+                          w[2] * n[0] + w[6] * n[1] + w[10] * n[2]};
+            };
+            v3 nv[3], tv[3], bv[3];
             for (int k = 0; k < 3; ++k) {
-                const float* n = bl.vertices[bl.indices[3 * h.prim + k]].normal;
-                const float* w = I.w2o;
-                // transpose(inverse(modelMat)) * vec4(n, 0): rows of the transposed inverse.
-                v3 t = {w[0] * n[0] + w[4] * n[1] + w[8] * n[2], w[1] * n[0] + w[5] * n[1] + w[9] * n[2],
-                        w[2] * n[0] + w[6] * n[1] + w[10] * n[2]};
-                nv[k] = normalize(t);
+                const luz_vertex& vx = bl.vertices[bl.indices[3 * h.prim + k]];
+                nv[k] = normalize(tim(vx.normal));
+                if (nmap >= 0) {   // opaque.vert:27-30
+                    v3 tg = normalize(tim(vx.tangent));
+                    tv[k] = normalize(tg - nv[k] * dot(tg, nv[k]));
+                    bv[k] = cross(nv[k], tv[k]) * vx.tangent[3];
+                }
             }
-            v3 N = normalize((nv[0] * h.b0 + nv[1] * h.b1) + nv[2] * h.b2);
+            v3 Ni = (nv[0] * h.b0 + nv[1] * h.b1) + nv[2] * h.b2;
+            v3 N = normalize(Ni);
+            float u = 0.0f, v = 0.0f, c[4];
+            if (cmap >= 0 || mrmap >= 0 || aomap >= 0 || nmap >= 0 || emap >= 0) hit_uv(bl, h.prim, h.b0, h.b1, h.b2, u, v);
+            if (cmap >= 0) {
+                tex_sample(tex[cmap], u, v, c);
+                for (int k = 0; k < 4; ++k) color[k] *= c[k];
+            }
+            if (mrmap >= 0) {
+                tex_sample(tex[mrmap], u, v, c);
+                roughness *= c[1];
+                metallic *= c[2];
+            }
+            if (aomap >= 0) {
+                tex_sample(tex[aomap], u, v, c);
+                occl = c[0];
+            }
+            if (emap >= 0) {
+                tex_sample(tex[emap], u, v, c);
+                for (int k = 0; k < 4; ++k) em[k] *= c[k];
+            }
+            if (nmap >= 0) {   // opaque.frag:45-50
+                tex_sample(tex[nmap], u, v, c);
+                v3 ti = (tv[0] * h.b0 + tv[1] * h.b1) + tv[2] * h.b2;
+                v3 bi = (bv[0] * h.b0 + bv[1] * h.b1) + bv[2] * h.b2;
+                bool flat_t = ti.x == 0.0f && ti.y == 0.0f && ti.z == 0.0f;
+                bool white = c[0] == 1.0f && c[1] == 1.0f && c[2] == 1.0f;
+                if (!flat_t && !white) {
+                    v3 ns = normalize(v3{c[0] * 2.0f - 1.0f, c[1] * 2.0f - 1.0f, c[2] * 2.0f - 1.0f});
+                    N = normalize((ti * ns.x + bi * ns.y) + Ni * ns.z);
+                }
+            }
             albedo[pix] = pack8(color[0], color[1], color[2], color[3]);
             normal[4 * pix] = N.x; normal[4 * pix + 1] = N.y; normal[4 * pix + 2] = N.z; normal[4 * pix + 3] = 1.0f;
-            material[pix] = pack8(roughness, metallic, 1.0f, 1.0f);
-            emission[pix] = pack8(em[0], em[1], em[2], 1.0f);
+            material[pix] = pack8(roughness, metallic, occl, 1.0f);
+            emission[pix] = pack8(em[0], em[1], em[2], em[3]);
             depth[pix] = clip[2] / clip[3];
             primary_hit[2 * pix] = h.custom;
             primary_hit[2 * pix + 1] = h.prim;

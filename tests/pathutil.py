@@ -15,10 +15,12 @@ def oracle_scene(scene: L.HostScene):
     return ob, tl
 
 
-def oracle_frame(scene: L.HostScene, tlas: "O.OracleTlas", frame: int = 0, bn=None, brute=False):
-    b, lights, models = scene.block(), scene.lights(), scene.models()
+def oracle_frame(scene: L.HostScene, tlas: "O.OracleTlas", frame: int = 0, bn=None, brute=False, models=None,
+                 textures=None):
+    b, lights = scene.block(), scene.lights()
+    models = scene.models() if models is None else models
     f = O.OracleFrame(tlas, b, lights, scene.light_count, models, scene.instance_count, scene.width, scene.height)
-    f.gbuffer()
+    f.gbuffer(textures=scene.textures() if textures is None else textures)
     f.visibility(frame, L.blue_noise() if bn is None else bn, brute=brute)
     return f
 
