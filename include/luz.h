@@ -177,7 +177,9 @@ enum {
     LUZ_PLANE_PRIMARY_HIT = 10, /* u32x2 per pixel: (instance custom index, prim id), ~0 = miss */
     LUZ_PLANE_FEATURES = 11,    /* 8 x bf16 per pixel: denoiser input channels           */
     LUZ_PLANE_LIN_DEPTH = 12,   /* F32 distance to the camera, 0 for background          */
-    LUZ_PLANE_COUNT = 13
+    LUZ_PLANE_TAA = 13,         /* RGBA32F temporal anti-aliasing output (= next history)  */
+    LUZ_PLANE_COMPOSE = 14,     /* BGRA8 UNORM composed, tone-mapped output (bytes B,G,R,A) */
+    LUZ_PLANE_COUNT = 15
 };
 
 /* ------------------------------------------------------------------ context */
@@ -341,6 +343,37 @@ luz_status luz_light_pass(luz_ctx* ctx, luz_frame* frame, int32_t use_denoised_a
 luz_status luz_render_frame(luz_ctx* ctx, luz_frame* frame, luz_tlas* tlas,
                             const luz_instance* instances, uint32_t instance_count,
                             int32_t frame_index);
+/* Temporal anti-aliasing of the light image (taa.comp, dispatched by
+ * DeferredRenderer::TAAPass, DeferredRenderer.cpp:425-445): reprojects last frame's
+ * output by the depth-derived motion (SceneBlock prevViewProj / jitter / prevJitter
+ * of the uploaded scene), clips it to the 3x3 neighbourhood and blends with
+ * anti-flicker weights. reconstruct != 0: Mitchell-weighted 3x3 source (the scene's
+ * taaReconstruct). Writes LUZ_PLANE_TAA, which is also the next call's history (the
+ * reference's SwapLightHistory, main.cpp:310). The history starts at zero. */
+luz_status luz_taa(luz_ctx* ctx, luz_frame* frame, int32_t reconstruct);
+luz_status luz_taa_reset(luz_ctx* ctx, luz_frame* frame);
+/* Compose pass (present.frag, DeferredRenderer::ComposePass, DeferredRenderer.cpp:347-369)
+ * into LUZ_PLANE_COMPOSE, the reference's BGRA8 compose image, headless: image_type 0
+ * = ACES tone-mapped light (source 0: LUZ_PLANE_LIGHT, 1: LUZ_PLANE_TAA), 1 albedo,
+ * 2 normal, 3 material, 4 emission, 5 linearised depth, 6 all six in a 3x2 grid. The
+ * debug-line overlay is empty. */
+luz_status luz_compose(luz_ctx* ctx, luz_frame* frame, int32_t source, int32_t image_type);
+/* Luminance histogram of the light (source 0) or TAA (1) image and its average
+ * (histogram.comp, histogramAverage.comp with DeferredRenderer.cpp:447-466's constants:
+ * 256 bins of log2 luminance over [-10, 2]). The bins are exact counts; the
+ * reference's shader zeroes the global bins from every workgroup, which races, and
+ * stores the weighted bin sum where its average belongs — here the weighted sum, the
+ * weighted log average, the average luminance and the luminance adapted from the
+ * previous call over delta_time are all returned. */
+typedef struct luz_histogram {
+    uint32_t bins[256];
+    float weighted_sum;
+    float log_average;
+    float average_luminance;
+    float adapted_luminance;
+} luz_histogram;
+luz_status luz_luminance_histogram(luz_ctx* ctx, luz_frame* frame, int32_t source, float delta_time,
+                                   luz_histogram* out);
 /* Size in bytes of one plane of this frame (LUZ_PLANE_*). */
 size_t luz_frame_plane_bytes(const luz_frame* frame, int32_t plane);
 /* Device→host copy of a plane. */

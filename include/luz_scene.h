@@ -89,6 +89,12 @@ luz_status luz_scene_get_camera(const luz_host_scene* s, luz_camera* cam);
 luz_status luz_scene_set_sampling(luz_host_scene* s, int32_t ao_samples, float ao_min, float ao_max,
                                   int32_t light_samples, int32_t sampler);
 
+/* Advances one frame as GPUScene::UpdateResources does (GPUScene.cpp:223-233):
+ * prevViewProj / prevJitter take the current values, the camera steps its jitter
+ * (CameraNode::NextJitter: Halton(2,3) over 16 frames, scaled to +-1 pixel; zero
+ * when use_jitter is 0) and the SceneBlock matrices are recomputed. */
+luz_status luz_scene_next_frame(luz_host_scene* s, int32_t use_jitter);
+
 /* Node::ComposeTransform (AssetManager.cpp:38-43): parent * T * R(quat(radians(rot))) * S.
  * parent may be NULL (identity). Column-major 4x4 out. */
 void luz_compose_transform(const float pos[3], const float rot_deg[3], const float scale[3],

@@ -20,7 +20,8 @@ import numpy as np
 from . import _abi
 from ._abi import (BLUE_NOISE_SIZE, LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_SPOT, PLANE_ALBEDO, PLANE_AO,
                    PLANE_AO_BITS, PLANE_AO_DENOISED, PLANE_DEPTH, PLANE_DTYPES, PLANE_EMISSION, PLANE_LIGHT,
-                   PLANE_MATERIAL, PLANE_NORMAL, PLANE_PRIMARY_HIT, PLANE_SHADOW_BITS, SAMPLER_PARITY,
+                   PLANE_MATERIAL, PLANE_NORMAL, PLANE_PRIMARY_HIT, PLANE_SHADOW_BITS, PLANE_TAA, PLANE_COMPOSE,
+                   PLANE_FEATURES, PLANE_LIN_DEPTH, SAMPLER_PARITY,
                    SAMPLER_STRATIFIED, SHADOW_RAYTRACING, BlasDesc, Camera, GenParams, Instance, Light, Model,
                    Scene, Vertex)
 
@@ -182,6 +183,10 @@ class HostScene:
         _check(lib.luz_scene_set_sampling(self._h, ao_samples, b.ao_min if ao_min is None else ao_min,
                                           b.ao_max if ao_max is None else ao_max, light_samples,
                                           b.sampler if sampler is None else sampler))
+
+    def next_frame(self, jitter: bool = True) -> None:
+        """One frame on: prev matrices / jitter <- current, next jitter (GPUScene::UpdateResources)."""
+        _check(lib.luz_scene_next_frame(self._h, int(jitter)), what="next frame")
 
     def camera(self) -> Camera:
         c = Camera()
@@ -354,6 +359,29 @@ class Frame:
 
     def light_pass(self, use_denoised_ao: bool = False) -> None:
         _check(lib.luz_light_pass(self.ctx.handle, self._h, int(use_denoised_ao)), self.ctx.handle, "light pass")
+
+    def taa(self, reconstruct: bool = True) -> None:
+        """Temporal anti-aliasing of the light image into PLANE_TAA (the next history)."""
+        _check(lib.luz_taa(self.ctx.handle, self._h, int(reconstruct)), self.ctx.handle, "taa")
+
+    def compose(self, source_taa: bool = False, image_type: int = 0) -> None:
+        """present.frag into PLANE_COMPOSE (BGRA8): 0 tone-mapped light, 1-5 G-buffer views, 6 grid."""
+        _check(lib.luz_compose(self.ctx.handle, self._h, int(source_taa), image_type), self.ctx.handle, "compose")
+
+    def composed_rgba(self) -> np.ndarray:
+        """PLANE_COMPOSE as an (H, W, 4) RGBA8 array."""
+        bgra = self.read(PLANE_COMPOSE).view(np.uint8).reshape(self.height, self.width, 4)
+        return bgra[..., [2, 1, 0, 3]].copy()
+
+    def luminance_histogram(self, source_taa: bool = False, delta_time: float = 1.0 / 60.0) -> dict:
+        h = _abi.Histogram()
+        _check(lib.luz_luminance_histogram(self.ctx.handle, self._h, int(source_taa), delta_time, C.byref(h)),
+               self.ctx.handle, "luminance histogram")
+        return {"bins": np.array(h.bins, np.uint32), "weighted_sum": h.weighted_sum, "log_average": h.log_average,
+                "average_luminance": h.average_luminance, "adapted_luminance": h.adapted_luminance}
+
+    def taa_reset(self) -> None:
+        _check(lib.luz_taa_reset(self.ctx.handle, self._h), self.ctx.handle, "taa reset")
 
     def device_ptr(self, plane: int) -> int:
         return lib.luz_frame_plane_device_ptr(self._h, plane) or 0

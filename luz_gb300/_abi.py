@@ -28,10 +28,12 @@ BLUE_NOISE_SIZE = 128
 
 PLANE_ALBEDO, PLANE_NORMAL, PLANE_MATERIAL, PLANE_EMISSION, PLANE_DEPTH, PLANE_LIGHT = range(6)
 PLANE_SHADOW_BITS, PLANE_AO_BITS, PLANE_AO, PLANE_AO_DENOISED, PLANE_PRIMARY_HIT = range(6, 11)
+PLANE_TAA, PLANE_COMPOSE = 13, 14
 PLANE_DTYPES = {PLANE_ALBEDO: (np.uint32, 1), PLANE_NORMAL: (np.float32, 4), PLANE_MATERIAL: (np.uint32, 1),
                 PLANE_EMISSION: (np.uint32, 1), PLANE_DEPTH: (np.float32, 1), PLANE_LIGHT: (np.float32, 4),
                 PLANE_SHADOW_BITS: (np.uint32, 1), PLANE_AO_BITS: (np.uint32, 1), PLANE_AO: (np.float32, 1),
-                PLANE_AO_DENOISED: (np.float32, 1), PLANE_PRIMARY_HIT: (np.uint32, 2)}
+                PLANE_AO_DENOISED: (np.float32, 1), PLANE_PRIMARY_HIT: (np.uint32, 2),
+                PLANE_TAA: (np.float32, 4), PLANE_COMPOSE: (np.uint32, 1)}
 
 
 class Vertex(C.Structure):
@@ -69,6 +71,11 @@ class Scene(C.Structure):
 class Instance(C.Structure):
     _fields_ = [("blas", C.c_void_p), ("transform", (C.c_float * 4) * 3), ("custom_index", C.c_uint32),
                 ("mask", C.c_uint32)]
+
+
+class Histogram(C.Structure):
+    _fields_ = [("bins", C.c_uint32 * 256), ("weighted_sum", C.c_float), ("log_average", C.c_float),
+                ("average_luminance", C.c_float), ("adapted_luminance", C.c_float)]
 
 
 class TextureDesc(C.Structure):
@@ -143,6 +150,10 @@ SIGNATURES = [
     ("luz_blas_download", C.c_int32, [P, P, P, P, c_u32_p, c_u32_p]),
     ("luz_blas_download_wide", C.c_int32, [P, P, P]),
     ("luz_frame_set_textures", C.c_int32, [P, P, P, C.c_uint32]),
+    ("luz_taa", C.c_int32, [P, P, C.c_int32]),
+    ("luz_compose", C.c_int32, [P, P, C.c_int32, C.c_int32]),
+    ("luz_luminance_histogram", C.c_int32, [P, P, C.c_int32, C.c_float, P]),
+    ("luz_taa_reset", C.c_int32, [P, P]),
     ("luz_blas_memory", C.c_int32, [P, P]),
     ("luz_blas_build_noalloc", C.c_int32, [P, C.c_uint32, P, C.c_uint32, P, P, P, P, P]),
     ("luz_tlas_create", C.c_int32, [P, C.c_uint32, C.POINTER(P)]),
@@ -208,6 +219,7 @@ SIGNATURES = [
     ("luz_scene_import", C.c_int32, [C.c_char_p, C.c_uint32, C.c_uint32, C.POINTER(P), C.c_char_p, C.c_uint32]),
     ("luz_scene_save_project", C.c_int32, [P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint32]),
     ("luz_scene_texture_count", C.c_uint32, [P]),
+    ("luz_scene_next_frame", C.c_int32, [P, C.c_int32]),
     ("luz_scene_texture", C.c_int32, [P, C.c_uint32, C.POINTER(c_u8_p), c_u32_p, c_u32_p]),
     ("luz_compose_transform", None, [c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     ("luz_camera_matrices", None, [C.POINTER(Camera), c_float_p, c_float_p]),

@@ -52,7 +52,7 @@ luz_status ensure_scratch(luz_ctx* ctx, size_t bytes) {
 static void free_frame_buffers(luz_frame* f) {
     void* ptrs[] = {f->albedo, f->normal, f->material, f->emission, f->depth, f->light,
                     f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->surf,
-                    f->features, f->lin_depth,
+                    f->features, f->lin_depth, f->taa, f->taa_next, f->compose, f->hist, f->hist_state,
                     f->block_counts, f->lit_count, f->d_scene, f->d_lights, f->d_models,
                     f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter, f->d_textures,
                     f->d_texels};
@@ -306,6 +306,11 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     A((void**)&f->ao_denoised, P * 4);
     A((void**)&f->features, P * 16);
     A((void**)&f->lin_depth, P * 4);
+    A((void**)&f->taa, P * 16);
+    A((void**)&f->taa_next, P * 16);
+    A((void**)&f->compose, P * 4);
+    A((void**)&f->hist, (256 + 260) * 4);
+    A((void**)&f->hist_state, 16);
     A((void**)&f->surf, P * 32);
     A((void**)&f->block_counts, (size_t)chunks * 4);
     A((void**)&f->lit_count, 4);
@@ -317,6 +322,9 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
         return cuda_error(ctx, e, "cudaMalloc(frame)");
     }
     cudaMemset(f->ao_denoised, 0, P * 4);
+    cudaMemset(f->taa, 0, P * 16);
+    cudaMemset(f->compose, 0, P * 4);
+    cudaMemset(f->hist_state, 0, 16);
     *out = f;
     return LUZ_OK;
 }
@@ -489,8 +497,9 @@ size_t luz_frame_plane_bytes(const luz_frame* f, int32_t plane) {
     size_t P = f->pixels;
     switch (plane) {
         case LUZ_PLANE_ALBEDO: case LUZ_PLANE_MATERIAL: case LUZ_PLANE_EMISSION: case LUZ_PLANE_DEPTH:
-        case LUZ_PLANE_AO: case LUZ_PLANE_AO_DENOISED: case LUZ_PLANE_LIN_DEPTH: return P * 4;
-        case LUZ_PLANE_NORMAL: case LUZ_PLANE_LIGHT: case LUZ_PLANE_FEATURES: return P * 16;
+        case LUZ_PLANE_AO: case LUZ_PLANE_AO_DENOISED: case LUZ_PLANE_LIN_DEPTH:
+        case LUZ_PLANE_COMPOSE: return P * 4;
+        case LUZ_PLANE_NORMAL: case LUZ_PLANE_LIGHT: case LUZ_PLANE_FEATURES: case LUZ_PLANE_TAA: return P * 16;
         case LUZ_PLANE_PRIMARY_HIT: return P * 8;
         case LUZ_PLANE_SHADOW_BITS: return (size_t)f->shadow_slots * f->words * 4;
         case LUZ_PLANE_AO_BITS: return (size_t)f->ao_samples * f->words * 4;
@@ -514,6 +523,8 @@ void* luz_frame_plane_device_ptr(luz_frame* f, int32_t plane) {
         case LUZ_PLANE_PRIMARY_HIT: return f->primary_hit;
         case LUZ_PLANE_FEATURES: return f->features;
         case LUZ_PLANE_LIN_DEPTH: return f->lin_depth;
+        case LUZ_PLANE_TAA: return f->taa;
+        case LUZ_PLANE_COMPOSE: return f->compose;
         default: return nullptr;
     }
 }

@@ -160,6 +160,11 @@ struct luz_frame {
     float* ao_denoised = nullptr;
     void* features = nullptr;       // 8 x bf16 per pixel (denoiser input)
     float* lin_depth = nullptr;
+    float4* taa = nullptr;          // TAA output = next frame's history
+    float4* taa_next = nullptr;
+    uint32_t* compose = nullptr;    // BGRA8 tone-mapped output
+    uint32_t* hist = nullptr;       // 256 bins | luz_histogram
+    float* hist_state = nullptr;    // adapted luminance across frames
     uint32_t shadow_planes_cap = 0, ao_planes_cap = 0;
     uint32_t shadow_slots = 0, ao_samples = 0;
     // compacted lit pixels

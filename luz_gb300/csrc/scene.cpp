@@ -419,6 +419,8 @@ void update_block(luz_host_scene* s) {
     M4 ip = inverse(proj), iv = inverse(view);
     memcpy(b.inverse_proj, ip.data(), 64);
     memcpy(b.inverse_view, iv.data(), 64);
+    b.prev_jitter[0] = b.jitter[0];
+    b.prev_jitter[1] = b.jitter[1];
     b.jitter[0] = s->camera.jitter[0];
     b.jitter[1] = s->camera.jitter[1];
     b.cam_pos[0] = s->camera.eye[0];
@@ -698,6 +700,32 @@ luz_status luz_scene_set_camera(luz_host_scene* s, const luz_camera* cam) {
 luz_status luz_scene_get_camera(const luz_host_scene* s, luz_camera* cam) {
     if (!s || !cam) return LUZ_ERR_INVALID;
     *cam = s->camera;
+    return LUZ_OK;
+}
+
+// Util.hpp Halton(i, b), single precision.
+static float halton(uint32_t i, uint32_t b) {
+    float f = 1.0f, r = 0.0f;
+    while (i > 0) {
+        f /= (float)b;
+        r = r + f * (float)(i % b);
+        i = (uint32_t)std::floor((float)i / (float)b);
+    }
+    return r;
+}
+
+luz_status luz_scene_next_frame(luz_host_scene* s, int32_t use_jitter) {
+    if (!s) return LUZ_ERR_INVALID;
+    luz_camera& c = s->camera;
+    if (use_jitter) {   // CameraNode::NextJitter (AssetManager.cpp:383-392)
+        s->jitter_index = (s->jitter_index + 1) % 16;
+        float jx = halton(s->jitter_index + 1, 2), jy = halton(s->jitter_index + 1, 3);
+        c.jitter[0] = (2.0f * jx - 1.0f) / c.extent[0];
+        c.jitter[1] = (2.0f * jy - 1.0f) / c.extent[1];
+    } else {
+        c.jitter[0] = c.jitter[1] = 0.0f;
+    }
+    update_block(s);
     return LUZ_OK;
 }
 

@@ -39,5 +39,6 @@ struct luz_host_scene {
     luz_camera camera{};
     uint32_t width = 0, height = 0;
     int32_t light_samples = 1;
+    uint32_t jitter_index = 0;   // CameraNode::jitterIndex
     float prev_view_proj[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
 };

@@ -53,6 +53,9 @@ def load() -> C.CDLL:
             "oracle_generate_rays": (C.c_uint64, [P, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, C.c_int, P,
                                                   C.c_uint32, P, C.c_uint64]),
             "oracle_sincos": (None, [P, P, P, C.c_uint32]),
+            "oracle_taa": (None, [P, P, P, P, C.c_uint32, C.c_uint32, C.c_int, P, C.c_int]),
+            "oracle_compose": (None, [P, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_int, P]),
+            "oracle_histogram": (None, [P, C.c_uint32, C.c_float, P, P]),
             "oracle_disk_sample": (None, [C.c_float, C.c_float, C.c_float, P, P]),
             "oracle_hemisphere_sample": (None, [C.c_float, C.c_float, P]),
             "oracle_ggx_terms": (None, [P, P, P, C.c_float, P, P, P, P]),
@@ -275,3 +278,36 @@ def collapse_wide(nodes: np.ndarray) -> np.ndarray:
                 out[row, 8 * a + 4 + k] = hi[a]
             oi[row, 24 + k] = cid
     return out
+
+
+def taa(scene, light: np.ndarray, history: np.ndarray, depth: np.ndarray, reconstruct: bool = True,
+        nthreads=None) -> np.ndarray:
+    """One TAA pass (taa.comp) over (H, W, 4) float32 images and an (H, W) depth."""
+    H, W = depth.shape
+    light = np.ascontiguousarray(light, np.float32)
+    history = np.ascontiguousarray(history, np.float32)
+    depth = np.ascontiguousarray(depth, np.float32)
+    out = np.zeros((H, W, 4), np.float32)
+    load().oracle_taa(scene_bytes(scene), _p(light), _p(history), _p(depth), W, H, int(bool(reconstruct)), _p(out),
+                      nthreads or threads())
+    return out
+
+
+def compose(light, albedo, normal, material, emission, depth, image_type: int = 0) -> np.ndarray:
+    """present.frag over (H, W) images -> BGRA8 words (H, W) uint32."""
+    H, W = depth.shape
+    arrs = [np.ascontiguousarray(a) for a in (light, albedo, normal, material, emission, depth)]
+    out = np.zeros((H, W), np.uint32)
+    load().oracle_compose(*[_p(a) for a in arrs], W, H, image_type, _p(out))
+    return out
+
+
+def histogram(img, delta_time: float = 1.0 / 60.0, state=None):
+    """Luminance histogram + averages of an (..., 4) float32 image; state: [adapted]."""
+    img = np.ascontiguousarray(img, np.float32).reshape(-1, 4)
+    st = np.zeros(1, np.float32) if state is None else state
+    out = np.zeros(260, np.uint32)
+    load().oracle_histogram(_p(img), img.shape[0], delta_time, _p(st), _p(out))
+    f = out[256:].view(np.float32)
+    return {"bins": out[:256].copy(), "weighted_sum": float(f[0]), "log_average": float(f[1]),
+            "average_luminance": float(f[2]), "adapted_luminance": float(f[3])}, st

@@ -1036,6 +1036,253 @@ int oracle_gbuffer(const oracle_tlas* ot, const luz_scene* S, const luz_model* m
     return LUZ_OK;
 }
 
+// ---------------------------------------------------------------- TAA (taa.comp)
+// The reference's sampler (linear, repeat, one level) on float images.
+struct Bil {
+    uint32_t x0, x1, y0, y1;
+    float ax, ay, bx, by;
+};
+static Bil bil(float u, float v, uint32_t w, uint32_t h) {
+    float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+    if (!std::isfinite(x)) x = 0.0f;
+    if (!std::isfinite(y)) y = 0.0f;
+    float fx = std::floor(x), fy = std::floor(y);
+    Bil b;
+    b.ax = x - fx;
+    b.ay = y - fy;
+    b.bx = 1.0f - b.ax;
+    b.by = 1.0f - b.ay;
+    b.x0 = tex_wrap(fx, w);
+    b.y0 = tex_wrap(fy, h);
+    b.x1 = b.x0 + 1 == w ? 0u : b.x0 + 1;
+    b.y1 = b.y0 + 1 == h ? 0u : b.y0 + 1;
+    return b;
+}
+static float bl(float c00, float c10, float c01, float c11, const Bil& b) {
+    return (c00 * b.bx + c10 * b.ax) * b.by + (c01 * b.bx + c11 * b.ax) * b.ay;
+}
+struct f4 {
+    float v[4];
+};
+static f4 samp4(const float* img, uint32_t w, uint32_t h, float u, float v) {
+    Bil b = bil(u, v, w, h);
+    const float* c00 = img + 4 * ((size_t)b.y0 * w + b.x0);
+    const float* c10 = img + 4 * ((size_t)b.y0 * w + b.x1);
+    const float* c01 = img + 4 * ((size_t)b.y1 * w + b.x0);
+    const float* c11 = img + 4 * ((size_t)b.y1 * w + b.x1);
+    f4 r;
+    for (int k = 0; k < 4; ++k) r.v[k] = bl(c00[k], c10[k], c01[k], c11[k], b);
+    return r;
+}
+static float samp1(const float* img, uint32_t w, uint32_t h, float u, float v) {
+    Bil b = bil(u, v, w, h);
+    return bl(img[(size_t)b.y0 * w + b.x0], img[(size_t)b.y0 * w + b.x1], img[(size_t)b.y1 * w + b.x0],
+              img[(size_t)b.y1 * w + b.x1], b);
+}
+static float gmin(float x, float y) { return y < x ? y : x; }   // GLSL min / max
+static float gmax(float x, float y) { return x < y ? y : x; }
+static f4 op(const f4& a, const f4& b, int o) {
+    f4 r;
+    for (int k = 0; k < 4; ++k)
+        r.v[k] = o == 0 ? gmin(a.v[k], b.v[k]) : o == 1 ? gmax(a.v[k], b.v[k]) : o == 2 ? a.v[k] + b.v[k] : a.v[k] - b.v[k];
+    return r;
+}
+static f4 scale(const f4& a, float s) { f4 r; for (int k = 0; k < 4; ++k) r.v[k] = a.v[k] * s; return r; }
+static f4 divide(const f4& a, float s) { f4 r; for (int k = 0; k < 4; ++k) r.v[k] = a.v[k] / s; return r; }
+static bool anynan(const f4& a) { return std::isnan(a.v[0]) || std::isnan(a.v[1]) || std::isnan(a.v[2]) || std::isnan(a.v[3]); }
+static float MitchellFilter(float x) {   // utils.glsl
+    const float B = 1.0f / 3.0f, C = 1.0f / 3.0f;
+    float x2 = x * x;
+    float x3 = x2 * x;
+    return (6.0f - 2.0f * B) * x3 - (6.0f - 2.0f * B - 3.0f * C) * x2 + 1.0f;
+}
+
+// One TAA pass over rgba images (4 floats per pixel): taa.comp main (taa.comp:288-307).
+void oracle_taa(const luz_scene* S, const float* input, const float* history, const float* depth, uint32_t W,
+                uint32_t H, int reconstruct, float* out, int threads) {
+    parallel_for(W * H, threads, [&](uint32_t b0, uint32_t e0) {
+        for (uint32_t pix = b0; pix < e0; ++pix) {
+            uint32_t x = pix % W, y = pix / W;
+            const float su = ((float)x + 0.5f) / (float)W, sv = ((float)y + 0.5f) / (float)H;
+            // find_closest_3x3
+            const float ddx = std::fabs(1.0f / (float)W), ddy = std::fabs(1.0f / (float)H);
+            float bx = 0, by = 0, bz = 0;
+            bool first = true;
+            for (int dy = -1; dy <= 1; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    float u = dx < 0 ? su - ddx : (dx > 0 ? su + ddx : su);
+                    float v = dy < 0 ? sv - ddy : (dy > 0 ? sv + ddy : sv);
+                    float z = samp1(depth, W, H, u, v);
+                    if (first || bz > z) { bx = (float)dx; by = (float)dy; bz = z; first = false; }
+                }
+            float cu = su + ddx * bx, cv = sv + ddy * by;
+            // get_motion_vector
+            float d = samp1(depth, W, H, cu, cv);
+            v3 wp = DepthToWorld(*S, cu, cv, d);
+            float p4[4] = {wp.x, wp.y, wp.z, 1.0f}, prev[4], cur[4];
+            mat4_vec4(S->prev_view_proj, p4, prev);
+            mat4_vec4(S->view_proj, p4, cur);
+            float mx = ((cur[0] / cur[3] - S->jitter[0]) - (prev[0] / prev[3] - S->prev_jitter[0])) * 0.5f;
+            float my = ((cur[1] / cur[3] - S->jitter[1]) - (prev[1] / prev[3] - S->prev_jitter[1])) * 0.5f;
+            const float hu = su - mx, hv = sv - my;
+            f4 hist = samp4(history, W, H, hu, hv);
+            // get_neighbor_3x3
+            const float du = 1.0f / (float)W, dv = 1.0f / (float)H;
+            f4 c[9];
+            for (int k = 0; k < 9; ++k) {
+                int dx = k % 3 - 1, dy = k / 3 - 1;
+                float u = dx < 0 ? su - du : (dx > 0 ? su + du : su);
+                float v = dy < 0 ? sv - dv : (dy > 0 ? sv + dv : sv);
+                c[k] = samp4(input, W, H, u, v);
+            }
+            f4 cmin = c[8], cmax = c[8];
+            for (int k = 7; k >= 0; --k) { cmin = op(c[k], cmin, 0); cmax = op(c[k], cmax, 1); }
+            f4 cavg = c[0];
+            for (int k = 1; k < 9; ++k) cavg = op(cavg, c[k], 2);
+            cavg = divide(cavg, 9.0f);
+            f4 cmin5 = op(c[1], op(c[3], op(c[4], op(c[5], c[7], 0), 0), 0), 0);
+            f4 cmax5 = op(c[1], op(c[3], op(c[4], op(c[5], c[7], 1), 1), 1), 1);
+            f4 cavg5 = divide(op(op(op(op(c[1], c[3], 2), c[4], 2), c[5], 2), c[7], 2), 5.0f);
+            cmin = scale(op(cmin, cmin5, 2), 0.5f);
+            cmax = scale(op(cmax, cmax5, 2), 0.5f);
+            cavg = scale(op(cavg, cavg5, 2), 0.5f);
+            f4 src = {{0, 0, 0, 0}};
+            if (reconstruct == 1) {
+                float wsum = 0.0f;
+                for (int k = 0; k < 9; ++k) {
+                    float dx = (float)(k % 3 - 1), dy = (float)(k / 3 - 1);
+                    float wgt = MitchellFilter(std::sqrt(dx * dx + dy * dy));
+                    src = op(src, scale(c[k], wgt), 2);
+                    wsum += wgt;
+                }
+                src = divide(src, wsum);
+            }
+            if (reconstruct == 0 || anynan(src)) src = samp4(input, W, H, su, sv);
+            f4 res;
+            if (hu > 1.0f || hv > 1.0f || hu < 0.0f || hv < 0.0f) {
+                res = src;
+            } else {
+                f4 p = op(op(cavg, cmin, 1), cmax, 0);   // clamp(cavg, cmin, cmax)
+                f4 r = op(hist, p, 3);
+                const float eps = 0.00000001f;
+                float rmax[3], rmin[3];
+                for (int k = 0; k < 3; ++k) { rmax[k] = cmax.v[k] - p.v[k]; rmin[k] = cmin.v[k] - p.v[k]; }
+                for (int k = 0; k < 3; ++k) if (r.v[k] > rmax[k] + eps) r = scale(r, rmax[k] / r.v[k]);
+                for (int k = 0; k < 3; ++k) if (r.v[k] < rmin[k] - eps) r = scale(r, rmin[k] / r.v[k]);
+                hist = op(p, r, 2);
+                float sw = 0.05f, hw = 1.0f - sw;
+                float rs = 1.0f / (gmax(gmax(src.v[0], src.v[1]), src.v[2]) + 1.0f);
+                float rh = 1.0f / (gmax(gmax(hist.v[0], hist.v[1]), hist.v[2]) + 1.0f);
+                float ls = (src.v[0] * rs) * 0.2127f + (src.v[1] * rs) * 0.7152f + (src.v[2] * rs) * 0.0722f;
+                float lh = (hist.v[0] * rh) * 0.2127f + (hist.v[1] * rh) * 0.7152f + (hist.v[2] * rh) * 0.0722f;
+                sw *= 1.0f / (1.0f + ls);
+                hw *= 1.0f / (1.0f + lh);
+                res = divide(op(scale(src, sw), scale(hist, hw), 2), gmax(sw + hw, 0.0000001f));
+                if (anynan(res)) res = src;
+            }
+            for (int k = 0; k < 4; ++k) out[4 * (size_t)pix + k] = res.v[k];
+        }
+    });
+}
+
+// ---------------------------------------------------------------- compose (present.frag)
+static f4 samp_rgba8(const uint32_t* img, uint32_t w, uint32_t h, float u, float v) {
+    Bil b = bil(u, v, w, h);
+    uint32_t t[4] = {img[(size_t)b.y0 * w + b.x0], img[(size_t)b.y0 * w + b.x1], img[(size_t)b.y1 * w + b.x0],
+                     img[(size_t)b.y1 * w + b.x1]};
+    f4 r;
+    for (int k = 0; k < 4; ++k) {
+        float c[4];
+        for (int q = 0; q < 4; ++q) c[q] = (float)((t[q] >> (8 * k)) & 255u) / 255.0f;
+        r.v[k] = bl(c[0], c[1], c[2], c[3], b);
+    }
+    return r;
+}
+static float aces(float x) {
+    const float a = 2.51f, b = 0.03f, c = 2.43f, d = 0.59f, e = 0.14f;
+    x = (x * (a * x + b)) / (x * (c * x + d) + e);
+    return std::pow(x, 1.0f / 2.2f);
+}
+static uint32_t unorm8c(float x) {
+    x = gmin(gmax(x, 0.0f), 1.0f);
+    return (uint32_t)(x * 255.0f + 0.5f);
+}
+
+// present.frag main over every pixel into BGRA8 words.
+void oracle_compose(const float* light, const uint32_t* albedo, const float* normal, const uint32_t* material,
+                    const uint32_t* emission, const float* depth, uint32_t W, uint32_t H, int image_type,
+                    uint32_t* out) {
+    for (uint32_t y = 0; y < H; ++y)
+        for (uint32_t x = 0; x < W; ++x) {
+            float tu = ((float)x + 0.5f) / (float)W, tv = ((float)y + 0.5f) / (float)H;
+            int type = image_type;
+            float fu = tu, fv = tv;
+            if (type == 6) {
+                fu = tu * 3.0f;
+                fv = tv * 2.0f;
+                if (tv < 0.5f) {
+                    if (tu < 1.0f / 3.0f) type = 0;
+                    else if (tu < 2.0f / 3.0f) { type = 1; fu -= 1.0f; }
+                    else { type = 2; fu -= 2.0f; }
+                } else {
+                    fv -= 1.0f;
+                    if (tu < 1.0f / 3.0f) type = 3;
+                    else if (tu < 2.0f / 3.0f) { type = 4; fu -= 1.0f; }
+                    else { type = 5; fu -= 2.0f; }
+                }
+                fu = 1.0f / 6.0f + fu * 2.0f / 3.0f;
+            }
+            f4 v;
+            switch (type) {
+                case 1: v = samp_rgba8(albedo, W, H, fu, fv); break;
+                case 2: v = samp4(normal, W, H, fu, fv); break;
+                case 3: v = samp_rgba8(material, W, H, fu, fv); break;
+                case 4: v = samp_rgba8(emission, W, H, fu, fv); break;
+                case 5: v = f4{{samp1(depth, W, H, fu, fv), 0.0f, 0.0f, 1.0f}}; break;
+                default: v = samp4(light, W, H, fu, fv); break;
+            }
+            if (type == 0) {
+                v = f4{{aces(v.v[0]), aces(v.v[1]), aces(v.v[2]), 1.0f}};
+            } else if (type == 2) {
+                for (int k = 0; k < 4; ++k) v.v[k] = (v.v[k] + 1.0f) / 2.0f;
+            } else if (type == 5) {
+                const float nearp = 0.01f, farp = 5.0f;
+                float l = (2.0f * nearp) / (farp + nearp - v.v[0] * (farp - nearp));
+                v = f4{{l, l, l, l}};
+            }
+            out[(size_t)y * W + x] = unorm8c(v.v[2]) | (unorm8c(v.v[1]) << 8) | (unorm8c(v.v[0]) << 16) | (255u << 24);
+        }
+}
+
+// histogram.comp + histogramAverage.comp (DeferredRenderer.cpp:447-466 constants).
+// out: 256 bins then 4 floats (weighted sum, log average, average, adapted).
+void oracle_histogram(const float* img, uint32_t n, float delta_time, float* state, uint32_t* out) {
+    const float min_log = -10.0f, one_over_log = 1.0f / 12.0f;
+    std::vector<uint32_t> bins(256, 0);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* c = img + 4 * (size_t)i;
+        float lum = c[0] * 0.2127f + c[1] * 0.7152f + c[2] * 0.0722f;
+        uint32_t bin = 0;
+        if (!(lum < 0.000001f)) {
+            float t = (std::log2(lum) - min_log) * one_over_log;
+            t = gmin(gmax(t, 0.0f), 1.0f);
+            bin = (uint32_t)(t * 254.0f + 1.0f);
+        }
+        bins[bin]++;
+    }
+    float sh[256];
+    for (int i = 0; i < 256; ++i) sh[i] = (float)bins[i] * (float)i;
+    for (int k = 128; k > 0; k >>= 1)
+        for (int i = 0; i < k; ++i) sh[i] += sh[i + k];
+    float wla = (sh[0] / gmax((float)n - (float)bins[0], 1.0f)) - 1.0f;
+    float avg = std::exp2(((wla / 254.0f) * one_over_log) + min_log);
+    float adapted = state[0] + (avg - state[0]) * (1.0f - std::exp(-delta_time * 1.1f));
+    state[0] = adapted;
+    for (int i = 0; i < 256; ++i) out[i] = bins[i];
+    float f[4] = {sh[0], wla, avg, adapted};
+    memcpy(out + 256, f, 16);
+}
+
 // Shadow + AO visibility bits for the pixel rows [y0, y1). brute != 0 uses the
 // all-triangles oracle instead of the BVH. Returns the number of rays traced.
 uint64_t oracle_visibility(const oracle_tlas* ot, const luz_scene* S, const luz_light* lights, uint32_t nl,
