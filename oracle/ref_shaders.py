@@ -26,6 +26,10 @@ from pathlib import Path
 LIGHT_FUNCS = ["DistributionGGX", "GeometrySchlickGGX", "GeometrySmith", "FresnelSchlick", "DiskSample",
                "HemisphereSample", "BlueNoiseSample", "TraceShadowRay", "TraceAORays", "EvaluateShadow", "main"]
 UTIL_FUNCS = ["DepthToWorld"]
+TAA_UTIL_FUNCS = ["DepthToWorld", "MitchellFilter", "rcp", "Luminance"]
+TAA_FUNCS = ["get_uv", "get_motion_vector", "get_neighbor_3x3", "find_closest_3x3", "clip_aabb", "anti_flicker",
+             "main"]
+COMPOSE_FUNCS = ["LinearizeDepth", "Tonemap", "TonemapACES", "TonemapExposure", "main"]
 
 
 def extract(src: str, name: str) -> str:
@@ -42,6 +46,16 @@ def extract(src: str, name: str) -> str:
             if depth == 0:
                 return src[m.start():j + 1]
     raise SystemExit(f"unbalanced braces in {name}")
+
+
+def params(s: str) -> str:
+    """GLSL `out T x` / `inout T x` parameters become C++ references."""
+    return re.sub(r"\b(?:inout|out)\s+(\w+)\s+(\w+)", r"\1& \2", s)
+
+
+def divide_by_w(s: str) -> str:
+    """`v.xyz /= v.w;` (a swizzle assignment) -> `v = vec4(vec3(v) / v.w, v.w);`."""
+    return re.sub(r"(\w+)\.xyz\s*/=\s*(\w+)\.w\s*;", r"\1 = vec4(vec3(\1) / \2.w, \1.w);", s)
 
 
 def float_literals(s: str) -> str:
@@ -80,6 +94,83 @@ def swizzles(s: str) -> str:
         ctor = "vec3" if m.group(1) in ("xyz", "rgb") else "vec2"
         out = out[:i] + f"{ctor}({operand})" + out[m.end():]
 
+
+TAA_HEAD = """// Generated by oracle/ref_shaders.py from the reference's taa.comp and utils.glsl.
+#include <cstddef>
+#include "ref_shim.hpp"
+#include "luz.h"
+static SceneBlock t_scene;
+static sampler2D t_textures[4];
+static image2D t_images[1];
+static PostProcessingConstants t_ctx;
+static uvec3 gl_GlobalInvocationID;
+#define scene t_scene
+#define textures t_textures
+#define images t_images
+#define ctx t_ctx
+"""
+
+TAA_WRAPPER = r"""
+#undef scene
+#undef textures
+#undef images
+#undef ctx
+extern "C" void ref_taa(const luz_scene* S, const float* input, const float* history, const float* depth, int W,
+                        int H, int reconstruct, float* out) {
+    memset(&t_scene, 0, sizeof(t_scene));
+    memcpy((char*)&t_scene + sizeof(LightBlock) * LUZ_MAX_LIGHTS, S, sizeof(luz_scene));
+    t_textures[0] = {input, W, H, 1, 1};
+    t_textures[1] = {history, W, H, 1, 1};
+    t_textures[2] = {depth, W, H, 2, 1};
+    t_images[0] = {out, W, H};
+    memset(&t_ctx, 0, sizeof(t_ctx));
+    t_ctx.lightInputRID = 0; t_ctx.lightHistoryRID = 1; t_ctx.depthRID = 2; t_ctx.lightOutputRID = 0;
+    t_ctx.size = vec2((float)W, (float)H);
+    t_ctx.reconstruct = reconstruct;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            gl_GlobalInvocationID = uvec3(x, y, 0);
+            taa_main();
+        }
+}
+"""
+
+COMPOSE_HEAD = """// Generated by oracle/ref_shaders.py from the reference's present.frag.
+#include <cstddef>
+#include "ref_shim.hpp"
+#include "luz.h"
+static sampler2D c_textures[8];
+static ComposeConstants c_ctx;
+static vec2 fragTexCoord;
+static vec4 outColor;
+#define textures c_textures
+#define ctx c_ctx
+"""
+
+COMPOSE_WRAPPER = r"""
+#undef textures
+#undef ctx
+extern "C" void ref_compose(const float* light, const uint32_t* albedo, const float* normal, const uint32_t* material,
+                            const uint32_t* emission, const float* depth, int W, int H, int image_type, float* out) {
+    c_textures[0] = {light, W, H, 1, 1};
+    c_textures[1] = {albedo, W, H, 0, 1};
+    c_textures[2] = {normal, W, H, 1, 1};
+    c_textures[3] = {material, W, H, 0, 1};
+    c_textures[4] = {emission, W, H, 0, 1};
+    c_textures[5] = {depth, W, H, 2, 1};
+    c_textures[6] = {nullptr, 1, 1, 0, 1};   // the debug-line overlay: empty
+    memset(&c_ctx, 0, sizeof(c_ctx));
+    c_ctx.lightRID = 0; c_ctx.albedoRID = 1; c_ctx.normalRID = 2; c_ctx.materialRID = 3; c_ctx.emissionRID = 4;
+    c_ctx.depthRID = 5; c_ctx.debugRID = 6; c_ctx.imageType = image_type;
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            fragTexCoord = vec2((x + 0.5f) / (float)W, (y + 0.5f) / (float)H);
+            compose_main();
+            float* o = out + 4 * ((size_t)y * W + x);
+            o[0] = outColor.x; o[1] = outColor.y; o[2] = outColor.z; o[3] = outColor.w;
+        }
+}
+"""
 
 WRAPPER = r"""
 #undef scene
@@ -165,6 +256,21 @@ def main():
         "",
     ])
     (out / "ref_shaders.cpp").write_text(head + body + "\n" + WRAPPER)
+
+    # taa.comp (+ utils.glsl helpers) and present.frag
+    taa = (ref / "taa.comp").read_text()
+    tbody = "\n\n".join([extract(utils, f) for f in TAA_UTIL_FUNCS] + [extract(taa, f) for f in TAA_FUNCS])
+    tbody = tbody.replace("void main()", "void taa_main()")
+    tbody = tbody.replace("greaterThanEqual(pixelPos, ctx.size)", "greaterThanEqual(vec2(pixelPos), ctx.size)")
+    tbody = swizzles(float_literals(divide_by_w(params(tbody))))
+    (out / "ref_taa.cpp").write_text(TAA_HEAD + "namespace {\n" + tbody + "\n}  // namespace\n" + TAA_WRAPPER)
+    present = (ref / "present.frag").read_text()
+    cbody = "\n\n".join(extract(present, f) for f in COMPOSE_FUNCS)
+    cbody = cbody.replace("void main()", "void compose_main()")
+    cbody = cbody.replace("LinearizeDepth(value.r).xxxx", "vec4(LinearizeDepth(value.r))")
+    cbody = swizzles(float_literals(cbody))
+    (out / "ref_compose.cpp").write_text(COMPOSE_HEAD + "namespace {\n" + cbody + "\n}  // namespace\n" +
+                                         COMPOSE_WRAPPER)
 
 
 if __name__ == "__main__":

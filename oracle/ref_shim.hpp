@@ -31,10 +31,13 @@ using namespace glm;
 
 namespace refshim {
 
-// texture kinds: 0 = RGBA8 UNORM, 1 = RGBA32F, 2 = R32F
+// texture kinds: 0 = RGBA8 UNORM, 1 = RGBA32F, 2 = R32F. filter 0: the texel under the
+// coordinate (full-screen passes read texel centres); 1: the reference's sampler,
+// bilinear with repeat addressing (VulkanWrapper.cpp:2429-2454), in the oracle's
+// arithmetic — the one part of the post-processing passes this shim defines itself.
 struct sampler2D {
     const void* data = nullptr;
-    int w = 1, h = 1, kind = 0;
+    int w = 1, h = 1, kind = 0, filter = 0;
 };
 struct samplerCube {};
 
@@ -79,8 +82,36 @@ using refshim::rayQueryEXT;
 using refshim::sampler2D;
 using refshim::samplerCube;
 
+inline int wrap_texel(float f, int n) {
+    float m = std::fmod(f, (float)n);
+    if (m < 0.0f) m += (float)n;
+    int i = (int)m;
+    return i < n ? i : 0;
+}
 inline vec4 texture(const sampler2D& s, vec2 uv) {
-    return refshim::fetch(s, (int)std::floor(uv.x * s.w), (int)std::floor(uv.y * s.h));
+    if (s.filter == 0) return refshim::fetch(s, (int)std::floor(uv.x * s.w), (int)std::floor(uv.y * s.h));
+    float x = uv.x * (float)s.w - 0.5f, y = uv.y * (float)s.h - 0.5f;
+    if (!std::isfinite(x)) x = 0.0f;
+    if (!std::isfinite(y)) y = 0.0f;
+    float fx = std::floor(x), fy = std::floor(y);
+    float ax = x - fx, ay = y - fy, bx = 1.0f - ax, by = 1.0f - ay;
+    int x0 = wrap_texel(fx, s.w), y0 = wrap_texel(fy, s.h);
+    int x1 = x0 + 1 == s.w ? 0 : x0 + 1, y1 = y0 + 1 == s.h ? 0 : y0 + 1;
+    vec4 c00 = refshim::fetch(s, x0, y0), c10 = refshim::fetch(s, x1, y0);
+    vec4 c01 = refshim::fetch(s, x0, y1), c11 = refshim::fetch(s, x1, y1);
+    vec4 r;
+    for (int k = 0; k < 4; ++k) r[k] = (c00[k] * bx + c10[k] * ax) * by + (c01[k] * bx + c11[k] * ax) * ay;
+    return r;
+}
+// Storage image of the compute passes (RGBA32F).
+struct image2D {
+    float* data = nullptr;
+    int w = 1, h = 1;
+};
+inline void imageStore(image2D& im, ivec2 p, vec4 v) {
+    if (!im.data || p.x < 0 || p.y < 0 || p.x >= im.w || p.y >= im.h) return;
+    float* o = im.data + 4 * ((size_t)p.y * im.w + p.x);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
 }
 inline vec4 texture(const samplerCube&, vec3) { return vec4(0.0f); }
 inline ivec2 textureSize(const sampler2D& s, int) { return ivec2(s.w, s.h); }

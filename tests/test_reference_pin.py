@@ -68,3 +68,62 @@ def test_reference_light_pass_matches_oracle():
     # a handful of pixels may see a grazing ray flip between hit and miss
     assert close.mean() > 0.995, close.mean()
     assert np.median(rel[..., :3]) < 1e-6
+
+
+# ---------------------------------------------------------------- post-processing passes
+# taa.comp and present.frag from the reference tree, compiled the same way; their
+# texture() reads go through the shim's bilinear, repeat-addressed sampler (the one
+# piece defined here rather than taken from the reference). glm evaluates mat4 * vec4
+# as (c0 x + c1 y) + (c2 z + c3 w), the oracle as ((c0 x + c1 y) + c2 z) + c3 w, so the
+# reprojected history differs in the last bits once the camera moves.
+
+def _post_fns():
+    REF.ref_taa.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_int, C.c_int, C.c_void_p]
+    REF.ref_compose.argtypes = [C.c_void_p] * 6 + [C.c_int, C.c_int, C.c_int, C.c_void_p]
+    return REF.ref_taa, REF.ref_compose
+
+
+def test_taa_matches_reference_shader():
+    ref_taa, _ = _post_fns()
+    W, H = 96, 72
+    s = L.HostScene(1, width=W, height=H)
+    _, tl = oracle_scene(s)
+    hist = np.zeros((H, W, 4), np.float32)
+    for k in range(3):
+        if k == 1:   # camera motion: real reprojection
+            cam = s.camera()
+            cam.eye[0] += 0.4
+            s.set_camera(cam)
+        s.next_frame(True)
+        f = oracle_frame(s, tl)
+        light = f.light_pass().reshape(H, W, 4)
+        depth = f.depth.reshape(H, W)
+        b = s.block()
+        for rec in (True, False):
+            ours = O.taa(b, light, hist, depth, rec)
+            ref = np.zeros_like(ours)
+            ref_taa(C.cast(C.pointer(b), C.c_void_p), O._p(light), O._p(hist), O._p(depth), W, H, int(rec), O._p(ref))
+            rel = np.abs(ours - ref) / np.maximum(np.abs(ref), 1e-3)
+            # the history lookup moves with the motion vector's last bits: 5e-4 relative
+            assert rel.max() <= 5e-4, (k, rec, rel.max())
+            if k == 0:
+                assert np.array_equal(ours.view(np.uint32), ref.view(np.uint32))
+        hist = O.taa(b, light, hist, depth, True)
+
+
+def test_compose_matches_reference_shader():
+    _, ref_compose = _post_fns()
+    W, H = 96, 72
+    s = L.HostScene(1, width=W, height=H)
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    planes = [np.ascontiguousarray(p) for p in (f.light_pass().reshape(H, W, 4), f.albedo.reshape(H, W),
+                                                 f.normal.reshape(H, W, 4), f.material.reshape(H, W),
+                                                 f.emission.reshape(H, W), f.depth.reshape(H, W))]
+    for t in range(7):
+        ours = O.compose(*planes, image_type=t)
+        ref = np.zeros((H, W, 4), np.float32)
+        ref_compose(*[O._p(p) for p in planes], W, H, t, O._p(ref))
+        q = (np.clip(np.nan_to_num(ref, nan=0.0), 0, 1) * 255 + 0.5).astype(np.uint32)
+        words = q[..., 2] | (q[..., 1] << 8) | (q[..., 0] << 16) | (255 << 24)
+        assert np.array_equal(words, ours), t
