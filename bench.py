@@ -308,6 +308,38 @@ def denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=16, curve_spp=(1, 
             "weights": D.DEFAULT_WEIGHTS.name}
 
 
+# ---------------------------------------------------------------------------- post passes
+def post_passes(g, stream, flush, K, W):
+    """TAA (taa.comp), compose / ACES (present.frag) and the luminance histogram on the
+    1080p frame: ms per pass and the HBM byte rate of its algorithmic traffic (TAA 52
+    B/px: light 16 + history 16 + depth 4 + output 16; compose 20 B/px; histogram 16 B/px)."""
+    import torch
+
+    fr = g.frame
+    px = fr.width * fr.height
+    peak, _ = measured_peaks()
+    passes = {"taa": (lambda: fr.taa(True), 52), "compose": (lambda: fr.compose(True, 0), 20),
+              "histogram": (lambda: fr.luminance_histogram(True), 16)}
+    out = {}
+    for name, (fn, bpp) in passes.items():
+        for _ in range(W):
+            fn()
+        ts = []
+        for _ in range(K):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        ms = statistics.mean(ts)
+        gbs = bpp * px / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "bytes_per_px": bpp, "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak}
+    out["note"] = "histogram includes its 1 KB read-back (a host sync); TAA/compose are device-only"
+    return out
+
+
 # ---------------------------------------------------------------------------- stress scene
 def stress_config5(ctx, stream, flush, K, W):
     """The stress scene: 4096 instances of the 64 displaced icospheres (335.5 M
@@ -575,6 +607,8 @@ def run_ours(args, rank, world, local):
         batched = batched_uneven(ctx, stream, flush, K, args.warmup)
         ctx.set_vis_tuning(**saved)
 
+    post = post_passes(g, stream, flush, K, args.warmup)
+
     stress = None
     if not args.no_stress:
         stress = stress_config5(ctx, stream, flush, min(K, 5), args.warmup)
@@ -594,7 +628,7 @@ def run_ours(args, rank, world, local):
                                "note": "one batched device build, host->device vertex/index copies included"},
                 "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk, "denoised_vs_plain": denoised, "batched_uneven_64": batched,
-                "stress_4k_4096_instances": stress}
+                "stress_4k_4096_instances": stress, "post_passes_1080p": post}
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
