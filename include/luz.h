@@ -41,7 +41,8 @@ enum {
     LUZ_DEV_TRAVERSAL_CAP = 1u << 2,
     LUZ_DEV_KARRAS_RANGE = 1u << 3,
     LUZ_DEV_BATCH_QUEUE = 1u << 4,
-    LUZ_DEV_BAD_INDEX = 1u << 5
+    LUZ_DEV_BAD_INDEX = 1u << 5,
+    LUZ_DEV_RASTER_OVERFLOW = 1u << 6
 };
 
 /* ------------------------------------------------------------------ limits */
@@ -316,6 +317,28 @@ typedef struct luz_texture_desc {
 } luz_texture_desc;
 luz_status luz_frame_set_textures(luz_ctx* ctx, luz_frame* frame, const luz_texture_desc* textures,
                                   uint32_t count);
+/* Shadow maps (scene shadow type LUZ_SHADOW_MAP; light.frag:147-165). Per light the
+ * LightBlock tail that the reference fills in GPUScene::UpdateResources
+ * (GPUScene.cpp:266-303): point lights have six cube faces (+x, -x, +y, -y, +z, -z)
+ * storing distance / z_far, other lights one orthographic map fitted to the camera
+ * frustum storing NDC depth. luz_scene_shadow_lights (luz_scene.h) computes them. */
+typedef struct luz_shadow_light {
+    float view_proj[6][16];   /* column-major; only [0] for non-point lights */
+    float z_far;              /* LightNode::shadowMapFar */
+    uint32_t faces;           /* 6 point, 1 other, 0 = no map (shadowMap == -1) */
+    float position[3];
+    uint32_t pad;
+} luz_shadow_light;
+/* Rasterises every instance of the TLAS into each light's shadow map
+ * (DeferredRenderer::ShadowMapPass, DeferredRenderer.cpp:268-292, with the shadowMap
+ * vertex/geometry/fragment shaders): resolution^2 texels per face, depth test LESS from
+ * a clear of 1.0, front faces culled, counter-clockwise front. The light pass then
+ * reads them when the uploaded scene's shadow_type is LUZ_SHADOW_MAP. */
+luz_status luz_frame_render_shadow_maps(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas,
+                                        const luz_shadow_light* lights, uint32_t light_count,
+                                        uint32_t resolution);
+/* Copies light `light`'s shadow map (faces * resolution^2 floats) to host memory. */
+luz_status luz_frame_read_shadow_map(luz_ctx* ctx, luz_frame* frame, uint32_t light, float* dst, size_t bytes);
 /* Primary-ray G-buffer: the raster opaque pass (source/Shaders/opaque.vert:21-31,
  * opaque.frag:21-58; main.cpp:242-258) as closest-hit rays through pixel centres.
  * Texture maps are sampled at the hit's interpolated texcoord; a model with a colour

@@ -89,6 +89,16 @@ luz_status luz_scene_get_camera(const luz_host_scene* s, luz_camera* cam);
 luz_status luz_scene_set_sampling(luz_host_scene* s, int32_t ao_samples, float ao_min, float ao_max,
                                   int32_t light_samples, int32_t sampler);
 
+/* Shadow-map matrices of every light (GPUScene.cpp:266-303): point lights six
+ * 90-degree perspective cube faces (near 0, far = shadowMapFar), others an
+ * orthographic box fitted to the camera frustum cut at farDistance / shadowMapRange,
+ * including the reference's start of the fit's min/max at a world-space corner.
+ * out holds luz_scene_light_count entries. */
+luz_status luz_scene_shadow_lights(const luz_host_scene* s, luz_shadow_light* out);
+/* SceneAsset::shadowType (LUZ_SHADOW_*); lights trace lightSamples shadow rays only
+ * under LUZ_SHADOW_RAYTRACING (GPUScene.cpp:248). */
+luz_status luz_scene_set_shadow_type(luz_host_scene* s, int32_t shadow_type);
+
 /* Advances one frame as GPUScene::UpdateResources does (GPUScene.cpp:223-233):
  * prevViewProj / prevJitter take the current values, the camera steps its jitter
  * (CameraNode::NextJitter: Halton(2,3) over 16 frames, scaled to +-1 pixel; zero

@@ -184,6 +184,16 @@ class HostScene:
                                           b.ao_max if ao_max is None else ao_max, light_samples,
                                           b.sampler if sampler is None else sampler))
 
+    def shadow_lights(self) -> C.Array:
+        """luz_shadow_light per light: the shadow-map matrices GPUScene computes."""
+        n = self.light_count
+        arr = (_abi.ShadowLight * max(n, 1))()
+        _check(lib.luz_scene_shadow_lights(self._h, arr), what="shadow lights")
+        return arr if n else (_abi.ShadowLight * 0)()
+
+    def set_shadow_type(self, shadow_type: int) -> None:
+        _check(lib.luz_scene_set_shadow_type(self._h, shadow_type), what="shadow type")
+
     def next_frame(self, jitter: bool = True) -> None:
         """One frame on: prev matrices / jitter <- current, next jitter (GPUScene::UpdateResources)."""
         _check(lib.luz_scene_next_frame(self._h, int(jitter)), what="next frame")
@@ -335,6 +345,19 @@ class Frame:
             descs[k].height = t.shape[0]
         _check(lib.luz_frame_set_textures(self.ctx.handle, self._h, descs, len(tex)), self.ctx.handle,
                "set textures")
+
+    def render_shadow_maps(self, tlas: Tlas, lights, resolution: int = 1024) -> None:
+        self._shadow_faces = [int(l.faces) for l in lights]
+        self._shadow_res = resolution
+        _check(lib.luz_frame_render_shadow_maps(self.ctx.handle, self._h, tlas.handle, C.cast(lights, C.c_void_p),
+                                                len(lights), resolution), self.ctx.handle, "shadow maps")
+
+    def read_shadow_map(self, light: int) -> np.ndarray:
+        f, r = self._shadow_faces[light], self._shadow_res
+        out = np.zeros((f, r, r), np.float32)
+        _check(lib.luz_frame_read_shadow_map(self.ctx.handle, self._h, light, _abi.ptr(out), out.nbytes),
+               self.ctx.handle, "read shadow map")
+        return out
 
     def gbuffer(self, tlas: Tlas) -> None:
         _check(lib.luz_gbuffer_primary(self.ctx.handle, self._h, tlas.handle), self.ctx.handle, "gbuffer")

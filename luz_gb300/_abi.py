@@ -78,6 +78,11 @@ class Histogram(C.Structure):
                 ("average_luminance", C.c_float), ("adapted_luminance", C.c_float)]
 
 
+class ShadowLight(C.Structure):
+    _fields_ = [("view_proj", (C.c_float * 16) * 6), ("z_far", C.c_float), ("faces", C.c_uint32),
+                ("position", C.c_float * 3), ("pad", C.c_uint32)]
+
+
 class TextureDesc(C.Structure):
     _fields_ = [("rgba8", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32)]
 
@@ -220,6 +225,10 @@ SIGNATURES = [
     ("luz_scene_save_project", C.c_int32, [P, C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint32]),
     ("luz_scene_texture_count", C.c_uint32, [P]),
     ("luz_scene_next_frame", C.c_int32, [P, C.c_int32]),
+    ("luz_scene_shadow_lights", C.c_int32, [P, P]),
+    ("luz_scene_set_shadow_type", C.c_int32, [P, C.c_int32]),
+    ("luz_frame_render_shadow_maps", C.c_int32, [P, P, P, P, C.c_uint32, C.c_uint32]),
+    ("luz_frame_read_shadow_map", C.c_int32, [P, P, C.c_uint32, P, C.c_size_t]),
     ("luz_scene_texture", C.c_int32, [P, C.c_uint32, C.POINTER(c_u8_p), c_u32_p, c_u32_p]),
     ("luz_compose_transform", None, [c_float_p, c_float_p, c_float_p, c_float_p, c_float_p]),
     ("luz_camera_matrices", None, [C.POINTER(Camera), c_float_p, c_float_p]),

@@ -23,7 +23,7 @@ LIB = PKG / "libluz_gb300.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 CUDA_TUS = ["lbvh.cu", "trace.cu", "visibility.cu", "lightpass.cu", "capi.cu", "blas_noalloc.cu",
-            "denoise.cu", "batch.cu", "post.cu"]
+            "denoise.cu", "batch.cu", "post.cu", "shadowmap.cu"]
 FMA_TUS = {"denoise.cu"}
 HOST_TUS = ["scene.cpp", "ingest.cpp"]
 

@@ -55,7 +55,7 @@ static void free_frame_buffers(luz_frame* f) {
                     f->features, f->lin_depth, f->taa, f->taa_next, f->compose, f->hist, f->hist_state,
                     f->block_counts, f->lit_count, f->d_scene, f->d_lights, f->d_models,
                     f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter, f->d_textures,
-                    f->d_texels};
+                    f->d_texels, f->d_shadow_lights, f->d_shadow_maps};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -340,8 +340,6 @@ luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, 
                             uint32_t light_count, const luz_model* models, uint32_t model_count) {
     if (!ctx || !f || !scene || (light_count && !lights) || (model_count && !models))
         return LUZ_ERR_INVALID;
-    if (scene->shadow_type == LUZ_SHADOW_MAP)
-        return set_error(ctx, LUZ_ERR_INVALID, "shadow maps are not part of the ray-traced path");
     if (scene->ao_num_samples < 0 || scene->ao_num_samples > LUZ_MAX_AO_SAMPLES)
         return set_error(ctx, LUZ_ERR_LIMIT, "ao_num_samples outside [0, LUZ_MAX_AO_SAMPLES]");
     if (light_count > 65535) return set_error(ctx, LUZ_ERR_LIMIT, "more than 65535 lights");

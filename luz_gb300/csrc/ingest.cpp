@@ -1316,6 +1316,8 @@ luz_host_scene* to_host_scene(const Project& p, const SceneAsset& sc, uint32_t w
         l.radius = n.radius;
         l.shadow_map = -1;
         s->lights.push_back(l);
+        s->shadow_range.push_back(n.shadow_map_range);
+        s->shadow_far.push_back(n.shadow_map_far);
     }
     luz_scene& b = s->block;
     memset(&b, 0, sizeof(b));
@@ -1478,6 +1480,8 @@ Project from_host_scene(const luz_host_scene* s) {
         n.outer_angle = l.outer_angle * r2d;
         n.has_direction = true;
         memcpy(n.direction, l.direction, 12);
+        if (k < s->shadow_range.size()) n.shadow_map_range = s->shadow_range[k];
+        if (k < s->shadow_far.size()) n.shadow_map_far = s->shadow_far[k];
         // a rotation that takes (0,-1,0) to the direction, for readers of the plain format:
         // pitch about x, then yaw about y
         float dl = std::sqrt(l.direction[0] * l.direction[0] + l.direction[1] * l.direction[1] +

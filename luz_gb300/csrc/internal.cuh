@@ -50,6 +50,16 @@ struct DevTexture {
     uint32_t width, height;
 };
 
+// A light's shadow map as the light pass reads it.
+struct DevShadowLight {
+    const float* map;        // faces * res * res depths
+    float view_proj0[16];
+    float position[3];
+    float z_far;
+    uint32_t faces;          // 0 = no map, 1 = 2D, 6 = cube (+x, -x, +y, -y, +z, -z)
+    uint32_t res;
+};
+
 // Per-instance data used by the G-buffer kernel, in the caller's instance order.
 struct DevShadeInstance {
     float normal_mat[9];    // transpose(inverse(model 3x3)), row-major
@@ -164,6 +174,12 @@ struct luz_frame {
     float4* taa_next = nullptr;
     uint32_t* compose = nullptr;    // BGRA8 tone-mapped output
     uint32_t* hist = nullptr;       // 256 bins | luz_histogram
+    luz::DevShadowLight* d_shadow_lights = nullptr;
+    float* d_shadow_maps = nullptr;
+    size_t shadow_maps_bytes = 0;
+    uint32_t shadow_light_count = 0, shadow_res = 0;
+    std::vector<size_t> h_shadow_offset;     // per light: first float of its map
+    std::vector<uint32_t> h_shadow_faces;
     float* hist_state = nullptr;    // adapted luminance across frames
     uint32_t shadow_planes_cap = 0, ao_planes_cap = 0;
     uint32_t shadow_slots = 0, ao_samples = 0;

@@ -4,6 +4,7 @@
 #include <cstring>
 
 #include "internal.cuh"
+#include "shadowmap.cuh"
 
 namespace luz {
 
@@ -31,6 +32,8 @@ struct LightParams {
     uint32_t words;
     uint32_t ao_samples;
     int shadow_type;
+    const DevShadowLight* shadow_lights;   // LUZ_SHADOW_MAP: per light, shadow_count of them
+    uint32_t shadow_count;
     float inverse_proj[16], inverse_view[16];
     float cam[3];
     float ambient[3];
@@ -109,6 +112,8 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     V3 V = normalize(cam - p);
     V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + albedo * metallic;
     V3 Lo = V3{0.0f, 0.0f, 0.0f};
+    // EvaluateShadow's origin (light.frag:138-139), used by the 2D shadow maps
+    const V3 shadow_origin = p + N * fmax_(length(p - cam) * 0.01f, 0.05f);
     for (uint32_t i = 0; i < P.light_count; ++i) {
         const luz_light& lt = s_lights[i];
         V3 lpos = V3{lt.position[0], lt.position[1], lt.position[2]};
@@ -139,6 +144,8 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
                 for (int s = 0; s < ns; ++s) hits += bit_at(P.shadow_bits, first + s, P.words, pix);
                 shadow = (float)hits / (float)ns;
             }
+        } else if (P.shadow_type == LUZ_SHADOW_MAP && i < P.shadow_count && P.shadow_lights[i].faces) {
+            shadow = shadow_map_factor(P.shadow_lights[i], p, shadow_origin);   // light.frag:147-164
         }
         V3 color = V3{lt.color[0], lt.color[1], lt.color[2]};
         V3 radiance = ((color * lt.intensity) * attenuation) * (1.0f - shadow);
@@ -199,6 +206,8 @@ luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
     P.words = f->words;
     P.ao_samples = f->ao_samples;
     P.shadow_type = f->h_scene.shadow_type;
+    P.shadow_lights = f->d_shadow_lights;
+    P.shadow_count = f->shadow_light_count;
     memcpy(P.inverse_proj, f->h_scene.inverse_proj, 64);
     memcpy(P.inverse_view, f->h_scene.inverse_view, 64);
     memcpy(P.cam, f->h_scene.cam_pos, 12);

@@ -703,6 +703,88 @@ luz_status luz_scene_get_camera(const luz_host_scene* s, luz_camera* cam) {
     return LUZ_OK;
 }
 
+luz_status luz_scene_set_shadow_type(luz_host_scene* s, int32_t shadow_type) {
+    if (!s || shadow_type < LUZ_SHADOW_DISABLED || shadow_type > LUZ_SHADOW_MAP) return LUZ_ERR_INVALID;
+    s->block.shadow_type = shadow_type;
+    for (auto& l : s->lights) l.num_shadow_samples = shadow_type == LUZ_SHADOW_RAYTRACING ? s->light_samples : 0;
+    return LUZ_OK;
+}
+
+luz_status luz_scene_shadow_lights(const luz_host_scene* s, luz_shadow_light* out) {
+    if (!s || (!out && !s->lights.empty())) return LUZ_ERR_INVALID;
+    const float d2r = 0.01745329251994329576923690768489f;
+    const luz_camera& cam = s->camera;
+    M4 view;
+    memcpy(view.data(), s->block.view, 64);
+    for (size_t k = 0; k < s->lights.size(); ++k) {
+        const luz_light& l = s->lights[k];
+        luz_shadow_light& o = out[k];
+        memset(&o, 0, sizeof(o));
+        float range = k < s->shadow_range.size() ? s->shadow_range[k] : 3.0f;
+        float zfar = k < s->shadow_far.size() ? s->shadow_far[k] : 2000.0f;
+        o.z_far = zfar;
+        memcpy(o.position, l.position, 12);
+        F3 pos = {l.position[0], l.position[1], l.position[2]};
+        if (l.type == LUZ_LIGHT_POINT) {
+            o.faces = 6;
+            M4 proj = perspective_zo(90.0f * d2r, 1.0f, 0.0f, zfar);
+            const F3 dirs[6] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+            const F3 ups[6] = {{0, -1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}, {0, -1, 0}, {0, -1, 0}};
+            for (int f = 0; f < 6; ++f) {
+                M4 vp = mul(proj, look_at(pos, {pos.x + dirs[f].x, pos.y + dirs[f].y, pos.z + dirs[f].z}, ups[f]));
+                memcpy(o.view_proj[f], vp.data(), 64);
+            }
+        } else {
+            o.faces = 1;
+            // camera->GetProj(near, far / range): no jitter, y flipped
+            M4 cp;
+            if (cam.camera_type == 0) {
+                cp = perspective_zo(cam.horizontal_fov * d2r, cam.extent[0] / cam.extent[1], cam.near_distance,
+                                    cam.far_distance / range);
+            } else {
+                float sx = cam.zoom, sy = cam.extent[1] / cam.extent[0] * cam.zoom;
+                cp = ortho_zo(-sx, sx, -sy, sy, cam.ortho_near_distance, cam.ortho_far_distance);
+            }
+            cp[5] *= -1.0f;
+            M4 inv = inverse(mul(cp, view));
+            float corners[8][4];
+            int c = 0;
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    for (int kk = 0; kk < 2; ++kk, ++c) {
+                        float pt[4] = {2.0f * i - 1.0f, 2.0f * j - 1.0f, 2.0f * kk - 1.0f, 1.0f};
+                        float r[4];
+                        for (int q = 0; q < 4; ++q)
+                            r[q] = inv[q] * pt[0] + inv[4 + q] * pt[1] + inv[8 + q] * pt[2] + inv[12 + q] * pt[3];
+                        for (int q = 0; q < 4; ++q) corners[c][q] = r[q] / r[3];
+                    }
+            F3 center = {0.0f, 0.0f, 0.0f};
+            for (int q = 0; q < 8; ++q) center = {center.x + corners[q][0], center.y + corners[q][1], center.z + corners[q][2]};
+            center = {center.x / 8.0f, center.y / 8.0f, center.z / 8.0f};
+            F3 front = {l.direction[0], l.direction[1], l.direction[2]};
+            M4 lv = look_at({center.x + front.x, center.y + front.y, center.z + front.z}, center, {0.0f, 1.0f, 0.0f});
+            // the reference starts min / max at the world-space corner 0 (GPUScene.cpp:292-293)
+            float mn[3] = {corners[0][0], corners[0][1], corners[0][2]}, mx[3] = {mn[0], mn[1], mn[2]};
+            for (int q = 0; q < 8; ++q) {
+                float v[3];
+                for (int a = 0; a < 3; ++a)
+                    v[a] = lv[a] * corners[q][0] + lv[4 + a] * corners[q][1] + lv[8 + a] * corners[q][2] +
+                           lv[12 + a] * corners[q][3];
+                for (int a = 0; a < 3; ++a) {
+                    mn[a] = mn[a] < v[a] ? mn[a] : v[a];
+                    mx[a] = v[a] < mx[a] ? mx[a] : v[a];
+                }
+            }
+            mn[2] = mn[2] < 0 ? mn[2] * range : mn[2] / range;
+            mx[2] = mx[2] < 0 ? mx[2] / range : mx[2] * range;
+            M4 proj = ortho_zo(mn[0], mx[0], mn[1], mx[1], mx[2], mn[2]);
+            M4 vp = mul(proj, lv);
+            memcpy(o.view_proj[0], vp.data(), 64);
+        }
+    }
+    return LUZ_OK;
+}
+
 // Util.hpp Halton(i, b), single precision.
 static float halton(uint32_t i, uint32_t b) {
     float f = 1.0f, r = 0.0f;

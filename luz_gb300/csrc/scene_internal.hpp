@@ -40,5 +40,6 @@ struct luz_host_scene {
     uint32_t width = 0, height = 0;
     int32_t light_samples = 1;
     uint32_t jitter_index = 0;   // CameraNode::jitterIndex
+    std::vector<float> shadow_range, shadow_far;   // per light; defaults 3 and 2000 when missing
     float prev_view_proj[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
 };

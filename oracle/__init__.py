@@ -55,6 +55,8 @@ def load() -> C.CDLL:
             "oracle_sincos": (None, [P, P, P, C.c_uint32]),
             "oracle_taa": (None, [P, P, P, P, C.c_uint32, C.c_uint32, C.c_int, P, C.c_int]),
             "oracle_compose": (None, [P, P, P, P, P, P, C.c_uint32, C.c_uint32, C.c_int, P]),
+            "oracle_render_shadow_maps": (None, [P, P, C.c_uint32, C.c_uint32, P, C.c_int]),
+            "oracle_clear_shadow_maps": (None, []),
             "oracle_histogram": (None, [P, C.c_uint32, C.c_float, P, P]),
             "oracle_disk_sample": (None, [C.c_float, C.c_float, C.c_float, P, P]),
             "oracle_hemisphere_sample": (None, [C.c_float, C.c_float, P]),
@@ -311,3 +313,27 @@ def histogram(img, delta_time: float = 1.0 / 60.0, state=None):
     f = out[256:].view(np.float32)
     return {"bins": out[:256].copy(), "weighted_sum": float(f[0]), "log_average": float(f[1]),
             "average_luminance": float(f[2]), "adapted_luminance": float(f[3])}, st
+
+
+def render_shadow_maps(tlas, lights, res: int, nthreads=None):
+    """Shadow maps of every light (a ctypes array of luz_shadow_light); returns a list of
+    (faces, res, res) float32 arrays and registers them for OracleFrame.light_pass."""
+    n = len(lights)
+    total = sum(int(l.faces) for l in lights) * res * res
+    buf = np.zeros(max(total, 1), np.float32)
+    load().oracle_render_shadow_maps(tlas.handle, C.cast(lights, C.c_void_p), n, res, _p(buf), nthreads or threads())
+    out, off = [], 0
+    for l in lights:
+        k = int(l.faces) * res * res
+        out.append(buf[off:off + k].reshape(int(l.faces), res, res))
+        off += k
+    _keep_maps[:] = [buf]
+    return out
+
+
+_keep_maps = []
+
+
+def clear_shadow_maps():
+    load().oracle_clear_shadow_maps()
+    _keep_maps.clear()

@@ -655,6 +655,122 @@ template <typename T> static vec3<T> FresnelSchlick(T cosTheta, vec3<T> F0) {
     return F0 + (vec3<T>{T(1), T(1), T(1)} - F0) * p5;
 }
 
+// ---------------------------------------------------------------- shadow maps
+// The shadow-map pass (shadowMap.vert/.geom/.frag) as a depth rasteriser and the
+// lookups of EvaluateShadow's map branch (light.frag:147-165), restated with the same
+// single-precision steps as the device: clip to w >= 1e-5 for cube faces, pixel-centre
+// edge functions with a top-left rule, front faces (counter-clockwise) culled, depth
+// LESS from 1.0; bilinear lookups (repeat for 2D maps, clamp per cube face).
+struct OShadow {
+    const float* map = nullptr;
+    float vp0[16];
+    float pos[3];
+    float zfar = 1.0f;
+    uint32_t faces = 0, res = 0;
+};
+static std::vector<OShadow> g_shadow;
+
+static uint32_t sm_wrap(float f, uint32_t n) {
+    float m = std::fmod(f, (float)n);
+    if (m < 0.0f) m += (float)n;
+    uint32_t i = (uint32_t)m;
+    return i < n ? i : 0u;
+}
+static uint32_t sm_clamp(float f, uint32_t n) {
+    if (!(f > 0.0f)) return 0u;
+    if (f >= (float)(n - 1)) return n - 1;
+    return (uint32_t)f;
+}
+static float sm_sample(const float* face, uint32_t res, float u, float v, bool repeat) {
+    float x = u * (float)res - 0.5f, y = v * (float)res - 0.5f;
+    if (!std::isfinite(x)) x = 0.0f;
+    if (!std::isfinite(y)) y = 0.0f;
+    float fx = std::floor(x), fy = std::floor(y);
+    float ax = x - fx, ay = y - fy, bx = 1.0f - ax, by = 1.0f - ay;
+    uint32_t x0, x1, y0, y1;
+    if (repeat) {
+        x0 = sm_wrap(fx, res); y0 = sm_wrap(fy, res);
+        x1 = x0 + 1 == res ? 0u : x0 + 1; y1 = y0 + 1 == res ? 0u : y0 + 1;
+    } else {
+        x0 = sm_clamp(fx, res); y0 = sm_clamp(fy, res); x1 = sm_clamp(fx + 1.0f, res); y1 = sm_clamp(fy + 1.0f, res);
+    }
+    float c00 = face[(size_t)y0 * res + x0], c10 = face[(size_t)y0 * res + x1];
+    float c01 = face[(size_t)y1 * res + x0], c11 = face[(size_t)y1 * res + x1];
+    return (c00 * bx + c10 * ax) * by + (c01 * bx + c11 * ax) * ay;
+}
+static float shadow_map_factor(const OShadow& S, v3 frag, v3 origin) {
+    if (S.faces == 6) {
+        v3 d = frag - v3{S.pos[0], S.pos[1], S.pos[2]};
+        float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z), ma, sc, tc;
+        uint32_t face;
+        if (ax >= ay && ax >= az) { face = d.x >= 0.0f ? 0u : 1u; ma = ax; sc = d.x >= 0.0f ? -d.z : d.z; tc = -d.y; }
+        else if (ay >= az) { face = d.y >= 0.0f ? 2u : 3u; ma = ay; sc = d.x; tc = d.y >= 0.0f ? d.z : -d.z; }
+        else { face = d.z >= 0.0f ? 4u : 5u; ma = az; sc = d.z >= 0.0f ? d.x : -d.x; tc = -d.y; }
+        float s_, t_;
+        if (ma == 0.0f) { face = 0; s_ = t_ = 0.5f; }
+        else { s_ = 0.5f * (sc / ma + 1.0f); t_ = 0.5f * (tc / ma + 1.0f); }
+        float depth = sm_sample(S.map + (size_t)face * S.res * S.res, S.res, s_, t_, false);
+        return length(d) - 0.05f >= depth * S.zfar ? 1.0f : 0.0f;
+    }
+    float p4[4] = {origin.x, origin.y, origin.z, 1.0f}, fl[4];
+    mat4_vec4(S.vp0, p4, fl);
+    float depth = sm_sample(S.map, S.res, fl[0] * 0.5f + 0.5f, fl[1] * 0.5f + 0.5f, true);
+    return fl[2] >= depth ? 1.0f : 0.0f;
+}
+
+struct RV {
+    float x, y, z, iw, wx, wy, wz;
+};
+static float r_edge(const RV& a, const RV& b, float px, float py) {
+    return (b.x - a.x) * (py - a.y) - (b.y - a.y) * (px - a.x);
+}
+static bool r_top_left(const RV& a, const RV& b) {
+    float dy = b.y - a.y, dx = b.x - a.x;
+    return dy > 0.0f || (dy == 0.0f && dx < 0.0f);
+}
+static void r_tri(const RV* v, uint32_t faces, uint32_t res, const float light[3], float inv_zfar, uint32_t* face_map) {
+    float sarea = (v[0].x * v[1].y - v[1].x * v[0].y) + (v[1].x * v[2].y - v[2].x * v[1].y) + (v[2].x * v[0].y - v[0].x * v[2].y);
+    float a = -0.5f * sarea;
+    if (!(a < 0.0f)) return;
+    float area2 = (v[1].x - v[0].x) * (v[2].y - v[0].y) - (v[1].y - v[0].y) * (v[2].x - v[0].x);
+    if (!(area2 > 0.0f)) return;
+    float mnx = std::fmin(std::fmin(v[0].x, v[1].x), v[2].x), mxx = std::fmax(std::fmax(v[0].x, v[1].x), v[2].x);
+    float mny = std::fmin(std::fmin(v[0].y, v[1].y), v[2].y), mxy = std::fmax(std::fmax(v[0].y, v[1].y), v[2].y);
+    float lx = std::fmax(std::floor(mnx - 0.5f), 0.0f), ly = std::fmax(std::floor(mny - 0.5f), 0.0f);
+    float hx = std::fmin(std::ceil(mxx - 0.5f), (float)res - 1.0f), hy = std::fmin(std::ceil(mxy - 0.5f), (float)res - 1.0f);
+    if (!(lx <= hx && ly <= hy)) return;
+    for (uint32_t py = (uint32_t)ly; py <= (uint32_t)hy; ++py)
+        for (uint32_t px = (uint32_t)lx; px <= (uint32_t)hx; ++px) {
+            float sx = (float)px + 0.5f, sy = (float)py + 0.5f;
+            float e0 = r_edge(v[1], v[2], sx, sy), e1 = r_edge(v[2], v[0], sx, sy), e2 = r_edge(v[0], v[1], sx, sy);
+            bool in0 = e0 > 0.0f || (e0 == 0.0f && r_top_left(v[1], v[2]));
+            bool in1 = e1 > 0.0f || (e1 == 0.0f && r_top_left(v[2], v[0]));
+            bool in2 = e2 > 0.0f || (e2 == 0.0f && r_top_left(v[0], v[1]));
+            if (!(in0 && in1 && in2)) continue;
+            float b0 = e0 / area2, b1 = e1 / area2, b2 = e2 / area2, depth;
+            if (faces == 6) {
+                float w0 = b0 * v[0].iw, w1 = b1 * v[1].iw, w2 = b2 * v[2].iw;
+                float iw = (w0 + w1) + w2;
+                float fx = ((w0 * v[0].wx + w1 * v[1].wx) + w2 * v[2].wx) / iw;
+                float fy = ((w0 * v[0].wy + w1 * v[1].wy) + w2 * v[2].wy) / iw;
+                float fz = ((w0 * v[0].wz + w1 * v[1].wz) + w2 * v[2].wz) / iw;
+                float dx = light[0] - fx, dy = light[1] - fy, dz = light[2] - fz;
+                depth = std::sqrt(dx * dx + dy * dy + dz * dz) * inv_zfar;
+            } else {
+                depth = (b0 * v[0].z + b1 * v[1].z) + b2 * v[2].z;
+            }
+            if (!(depth >= 0.0f && depth < 1.0f)) continue;
+            uint32_t bits;
+            memcpy(&bits, &depth, 4);
+            uint32_t& m = face_map[(size_t)py * res + px];
+            if (bits < m) m = bits;
+        }
+}
+static RV r_screen(const float c[4], const float w[3], uint32_t res) {
+    float iw = 1.0f / c[3];
+    return RV{(c[0] * iw * 0.5f + 0.5f) * (float)res, (c[1] * iw * 0.5f + 0.5f) * (float)res, c[2] * iw, iw, w[0], w[1], w[2]};
+}
+
 struct Planes {
     const uint32_t* albedo;
     const float* normal;
@@ -727,6 +843,12 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
                     hits += (P.shadow_bits[(size_t)(first_slot[i] + s) * words + (pix >> 5)] >> (pix & 31)) & 1u;
                 shadow = (T)hits / (T)ns;                                                    // light.frag:108
             }
+        } else if (S.shadow_type == LUZ_SHADOW_MAP && i < g_shadow.size() && g_shadow[i].faces) {   // 147-164
+            v3 fp = {(float)fragPos.x, (float)fragPos.y, (float)fragPos.z};
+            v3 nf = {(float)N.x, (float)N.y, (float)N.z};
+            v3 camf = {S.cam_pos[0], S.cam_pos[1], S.cam_pos[2]};
+            v3 origin = fp + nf * fmax_(length(fp - camf) * 0.01f, 0.05f);
+            shadow = (T)shadow_map_factor(g_shadow[i], fp, origin);
         }
         vec3<T> color = {(T)lt.color[0], (T)lt.color[1], (T)lt.color[2]};
         vec3<T> radiance = ((color * (T)lt.intensity) * attenuation) * (T(1) - shadow);    // light.frag:210
@@ -1282,6 +1404,84 @@ void oracle_histogram(const float* img, uint32_t n, float delta_time, float* sta
     float f[4] = {sh[0], wla, avg, adapted};
     memcpy(out + 256, f, 16);
 }
+
+// Shadow maps of every light into out (per light faces * res * res floats, lights in
+// order) and registered for the light pass (oracle_clear_shadow_maps drops them).
+void oracle_render_shadow_maps(const oracle_tlas* ot, const luz_shadow_light* lights, uint32_t count, uint32_t res,
+                               float* out, int threads) {
+    const Tlas& T = ot->t;
+    g_shadow.assign(count, OShadow{});
+    size_t off = 0;
+    for (uint32_t l = 0; l < count; ++l) {
+        const luz_shadow_light& L = lights[l];
+        OShadow& o = g_shadow[l];
+        o.map = out + off;
+        memcpy(o.vp0, L.view_proj[0], 64);
+        memcpy(o.pos, L.position, 12);
+        o.zfar = L.z_far;
+        o.faces = L.faces;
+        o.res = res;
+        const size_t face_px = (size_t)res * res;
+        std::vector<uint32_t> bits((size_t)L.faces * face_px, 0x3F800000u);
+        const float inv_zfar = 1.0f / L.z_far;
+        // faces in parallel (each face's map is its own)
+        parallel_for(L.faces, std::min<int>(threads, (int)L.faces), [&](uint32_t f0, uint32_t f1) {
+            for (uint32_t face = f0; face < f1; ++face)
+                for (const Instance& I : T.by_input) {
+                    const Blas& b = *I.blas;
+                    for (uint32_t t = 0; t < b.prims; ++t) {
+                        float clip[3][4], world[3][3];
+                        for (int k = 0; k < 3; ++k) {
+                            const float* p = b.vertices[b.indices[3 * t + k]].position;
+                            const float* m = I.o2w;
+                            for (int r = 0; r < 3; ++r)
+                                world[k][r] = m[r * 4 + 0] * p[0] + m[r * 4 + 1] * p[1] + m[r * 4 + 2] * p[2] + m[r * 4 + 3];
+                            float w4[4] = {world[k][0], world[k][1], world[k][2], 1.0f};
+                            mat4_vec4(L.view_proj[face], w4, clip[k]);
+                        }
+                        uint32_t* fm = bits.data() + face * face_px;
+                        if (L.faces != 6) {
+                            RV v[3] = {r_screen(clip[0], world[0], res), r_screen(clip[1], world[1], res),
+                                       r_screen(clip[2], world[2], res)};
+                            r_tri(v, L.faces, res, L.position, inv_zfar, fm);
+                            continue;
+                        }
+                        const float kNearW = 1e-5f;
+                        float pc[4][4], pw[4][3];
+                        int n = 0;
+                        for (int k = 0; k < 3; ++k) {
+                            const int j = (k + 1) % 3;
+                            const bool ink = clip[k][3] >= kNearW, inj = clip[j][3] >= kNearW;
+                            if (ink) {
+                                for (int q = 0; q < 4; ++q) pc[n][q] = clip[k][q];
+                                for (int q = 0; q < 3; ++q) pw[n][q] = world[k][q];
+                                ++n;
+                            }
+                            if (ink != inj) {
+                                float tt = (kNearW - clip[k][3]) / (clip[j][3] - clip[k][3]);
+                                for (int q = 0; q < 4; ++q) pc[n][q] = clip[k][q] + (clip[j][q] - clip[k][q]) * tt;
+                                for (int q = 0; q < 3; ++q) pw[n][q] = world[k][q] + (world[j][q] - world[k][q]) * tt;
+                                ++n;
+                            }
+                        }
+                        if (n < 3) continue;
+                        RV sv[4];
+                        for (int k = 0; k < n; ++k) sv[k] = r_screen(pc[k], pw[k], res);
+                        RV t0[3] = {sv[0], sv[1], sv[2]};
+                        r_tri(t0, 6, res, L.position, inv_zfar, fm);
+                        if (n == 4) {
+                            RV t1[3] = {sv[0], sv[2], sv[3]};
+                            r_tri(t1, 6, res, L.position, inv_zfar, fm);
+                        }
+                    }
+                }
+        });
+        memcpy(out + off, bits.data(), bits.size() * 4);
+        off += bits.size();
+    }
+}
+
+void oracle_clear_shadow_maps() { g_shadow.clear(); }
 
 // Shadow + AO visibility bits for the pixel rows [y0, y1). brute != 0 uses the
 // all-triangles oracle instead of the BVH. Returns the number of rays traced.
