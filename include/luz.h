@@ -255,7 +255,10 @@ luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint32_t vertex_
                                   uint32_t* d_order, void* stream);
 /* Copies the built BLAS to host memory: nodes (64 B each, count = max(n-1,1)),
  * triangles (48 B each, sorted leaf order), the sorted Morton keys (u32) and the
- * sorted primitive order (u32). Any pointer may be NULL. For parity tests. */
+ * sorted primitive order (u32). Any pointer may be NULL. For parity tests. The root
+ * node's third child word (float 14) holds the bounding sphere's squared radius about
+ * the root box centre (the largest squared distance of a triangle vertex from it, as
+ * float bits); the TLAS build clips each instance box with the transformed sphere. */
 luz_status luz_blas_download(luz_ctx* ctx, const luz_blas* blas, void* nodes, void* tris,
                              uint32_t* morton_sorted, uint32_t* order);
 /* Copies the 4-wide traversal nodes (128 B each: lo.x[4], hi.x[4], lo.y[4], hi.y[4],
@@ -308,7 +311,7 @@ luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* frame, const luz_scene* sce
                             const luz_model* models, uint32_t model_count);
 /* Textures of the frame's ModelBlocks (RGBA8 UNORM, rows top to bottom, 4 B per
  * texel): map fields >= 0 index this list. Replaces earlier textures. Mirrors the
- * RGBA8_unorm images GPUScene creates per texture asset (GPUScene.cpp:56-106) with the
+ * RGBA8_unorm images GPUScene::AddTexture creates (GPUScene.cpp:140-156) with the
  * reference's sampler: linear filtering, repeat addressing, one mip level
  * (VulkanWrapper.cpp:500, 2429-2454). count 0 clears. */
 typedef struct luz_texture_desc {

@@ -196,6 +196,8 @@ extern "C" luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint3
         NOALLOC_LAUNCHED();
         refit_kernel<<<cdiv(n, 256), 256, 0, st>>>(d_seg, zero, 1, n, leaf_box, node_parent, leaf_parent, flags);
         NOALLOC_LAUNCHED();
+        blas_radius_kernel<<<cdiv(n, 256), 256, 0, st>>>(d_seg, zero, 1, n);
+        NOALLOC_LAUNCHED();
     }
     // Synchronous, like the reference's per-mesh build (GPUScene.cpp:132-137): read
     // this build's status word into host memory.

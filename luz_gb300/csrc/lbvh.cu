@@ -418,6 +418,50 @@ __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, 
     }
 }
 
+// ---------------------------------------------------------------- bounding sphere
+// Centre of a BLAS's root box (the union of the root node's two slots).
+__device__ __forceinline__ V3 root_centre(float4 n0, float4 n1, float4 n2) {
+    V3 lo = V3{fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z)};
+    V3 hi = V3{fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w)};
+    return V3{(lo.x + hi.x) * 0.5f + 0.0f, (lo.y + hi.y) * 0.5f + 0.0f, (lo.z + hi.z) * 0.5f + 0.0f};
+}
+
+// Bounding sphere of every BLAS about its root box centre: the largest squared
+// distance of a triangle vertex from the centre, kept as float bits in the root
+// node's spare word n3.z (zero after karras_kernel; positive floats order like their
+// bits, so atomicMax on the bits is a float max). Runs after the refit. The TLAS
+// build intersects each instance's transformed root box with the transformed sphere.
+__global__ void blas_radius_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
+                                   uint32_t total) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    bool in = g < total;
+    int s = in ? find_seg(seg_prim_off, nseg, g) : -1;
+    uint32_t r2 = 0u;
+    float4* root = nullptr;
+    if (in) {
+        const SegDesc sd = segs[s];
+        root = sd.nodes;
+        V3 c = root_centre(__ldcg(root + 0), __ldcg(root + 1), __ldcg(root + 2));
+        const float4* t = sd.tris + (size_t)(g - sd.prim_off) * kTriF4;
+        for (int k = 0; k < 3; ++k) {
+            float4 v = t[k];
+            float dx = v.x - c.x, dy = v.y - c.y, dz = v.z - c.z;
+            float d2 = dx * dx + dy * dy + dz * dz;
+            r2 = max(r2, __float_as_uint(d2));
+        }
+    }
+    const uint32_t full = 0xFFFFFFFFu;
+    int s0 = __shfl_sync(full, s, 0);
+    bool uniform = __all_sync(full, s == s0 || s < 0);
+    if (uniform) {
+        uint32_t r = __reduce_max_sync(full, r2);
+        float4* root0 = (float4*)__shfl_sync(full, (unsigned long long)root, 0);
+        if ((threadIdx.x & 31) == 0 && s0 >= 0) atomicMax((uint32_t*)&root0[3].z, r);
+    } else if (s >= 0) {
+        atomicMax((uint32_t*)&root[3].z, r2);
+    }
+}
+
 // ---------------------------------------------------------------- 4-wide collapse
 // Every binary node at even depth becomes a 4-wide node whose slots are its
 // grandchildren (or its children, where a child is a leaf). Numbering: the rank of
@@ -636,6 +680,20 @@ __global__ void tlas_instance_kernel(const DevInstanceInput* in, uint32_t n, flo
             V3 w = xform_point(ii.o2w, p);
             wlo = V3{fmin_(wlo.x, w.x), fmin_(wlo.y, w.y), fmin_(wlo.z, w.z)};
             whi = V3{fmax_(whi.x, w.x), fmax_(whi.y, w.y), fmax_(whi.z, w.z)};
+        }
+        // Clip with the axis box of the transformed bounding sphere: an ellipsoid
+        // c' + M u (|u| <= r) reaches r * |row_a(M)| from its centre along world axis a.
+        uint32_t r2 = __float_as_uint(ii.nodes[3].z);
+        if (r2 < 0x7F800000u) {
+            V3 c = root_centre(n0, n1, n2);
+            V3 cw = xform_point(ii.o2w, c);
+            float r = sqrtf(__uint_as_float(r2));
+            const float* m = ii.o2w;
+            float ex = r * sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+            float ey = r * sqrtf(m[4] * m[4] + m[5] * m[5] + m[6] * m[6]);
+            float ez = r * sqrtf(m[8] * m[8] + m[9] * m[9] + m[10] * m[10]);
+            wlo = V3{fmax_(wlo.x, cw.x - ex), fmax_(wlo.y, cw.y - ey), fmax_(wlo.z, cw.z - ez)};
+            whi = V3{fmin_(whi.x, cw.x + ex), fmin_(whi.y, cw.y + ey), fmin_(whi.z, cw.z + ez)};
         }
         float px = box_pad(wlo.x, whi.x), py = box_pad(wlo.y, whi.y), pz = box_pad(wlo.z, whi.z);
         wlo = V3{wlo.x - px, wlo.y - py, wlo.z - pz};
@@ -985,6 +1043,8 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
         refit_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, d_leaf_box,
                                                    d_node_parent, d_leaf_parent, d_flags);
         LUZ_LAUNCHED(ctx, "refit_kernel");
+        blas_radius_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N);
+        LUZ_LAUNCHED(ctx, "blas_radius_kernel");
     }
     // 4-wide collapse of every segment's tree (the traversal structure of the
     // shadow/AO rays; the binary tree stays the parity-checked structure).

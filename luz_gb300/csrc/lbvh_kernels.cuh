@@ -56,5 +56,7 @@ __global__ void blas_emit_kernel(const SegDesc* segs, const uint32_t* seg_prim_o
 __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                              uint32_t total, const float4* leaf_box, const uint32_t* node_parent,
                              const uint32_t* leaf_parent, uint32_t* flags);
+__global__ void blas_radius_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
+                                   uint32_t total);
 
 }  // namespace luz

@@ -248,6 +248,12 @@ static Box get_slot(const float* node, int slot) {
     if (slot == 0) return {{node[0], node[2], node[8]}, {node[1], node[3], node[9]}};
     return {{node[4], node[6], node[10]}, {node[5], node[7], node[11]}};
 }
+// Centre of a BLAS root box (the union of the root node's two slots), as
+// lbvh.cu root_centre.
+static v3 root_centre(const float* root) {
+    Box rb = unite(get_slot(root, 0), get_slot(root, 1));
+    return {(rb.lo.x + rb.hi.x) * 0.5f + 0.0f, (rb.lo.y + rb.hi.y) * 0.5f + 0.0f, (rb.lo.z + rb.hi.z) * 0.5f + 0.0f};
+}
 
 // Karras delta: common prefix length of keys i and j, index-extended for equal keys.
 static int kdelta(const std::vector<uint32_t>& k, int n, int i, int j) {
@@ -918,6 +924,22 @@ int oracle_blas_build(const void* vertices, uint32_t nv, uint32_t stride, const 
         int32_t pi = (int32_t)p;
         memcpy(&t[3], &pi, 4);
     }
+    if (b.prims) {
+        // Bounding sphere about the root box centre: the largest squared vertex
+        // distance, as float bits in the root's spare word (lbvh.cu blas_radius_kernel).
+        float* root = b.tree.nodes.data();
+        v3 c = root_centre(root);
+        uint32_t r2 = 0;
+        for (size_t k = 0; k < (size_t)b.prims * 3; ++k) {
+            const float* v = &b.tris[4 * k];
+            float dx = v[0] - c.x, dy = v[1] - c.y, dz = v[2] - c.z;
+            float d2 = dx * dx + dy * dy + dz * dz;
+            uint32_t u;
+            memcpy(&u, &d2, 4);
+            r2 = std::max(r2, u);
+        }
+        memcpy(&root[14], &r2, 4);
+    }
     *out = ob;
     return LUZ_OK;
 }
@@ -958,6 +980,22 @@ int oracle_tlas_build(const oracle_blas* const* blas, const float* transforms, c
                 v3 w = xpoint(I.o2w, p);
                 wb.lo = {fmin_(wb.lo.x, w.x), fmin_(wb.lo.y, w.y), fmin_(wb.lo.z, w.z)};
                 wb.hi = {fmax_(wb.hi.x, w.x), fmax_(wb.hi.y, w.y), fmax_(wb.hi.z, w.z)};
+            }
+            // Clip with the axis box of the transformed bounding sphere (lbvh.cu
+            // tlas_instance_kernel): extent r * |row_a(M)| along world axis a.
+            uint32_t r2;
+            memcpy(&r2, &root[14], 4);
+            if (r2 < 0x7F800000u) {
+                v3 cw = xpoint(I.o2w, root_centre(root));
+                float r2f;
+                memcpy(&r2f, &r2, 4);
+                float r = std::sqrt(r2f);
+                const float* m = I.o2w;
+                float ex = r * std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+                float ey = r * std::sqrt(m[4] * m[4] + m[5] * m[5] + m[6] * m[6]);
+                float ez = r * std::sqrt(m[8] * m[8] + m[9] * m[9] + m[10] * m[10]);
+                wb.lo = {fmax_(wb.lo.x, cw.x - ex), fmax_(wb.lo.y, cw.y - ey), fmax_(wb.lo.z, cw.z - ez)};
+                wb.hi = {fmin_(wb.hi.x, cw.x + ex), fmin_(wb.hi.y, cw.y + ey), fmin_(wb.hi.z, cw.z + ez)};
             }
             float px = inst_pad(wb.lo.x, wb.hi.x), py = inst_pad(wb.lo.y, wb.hi.y), pz = inst_pad(wb.lo.z, wb.hi.z);
             wb = {{wb.lo.x - px, wb.lo.y - py, wb.lo.z - pz}, {wb.hi.x + px, wb.hi.y + py, wb.hi.z + pz}};
