@@ -180,6 +180,7 @@ luz_status luz_batch_autotune(luz_ctx* ctx, luz_batch* b, uint32_t reps, luz_vis
     LUZ_CUDA(ctx, cudaEventCreate(&e0));
     LUZ_CUDA(ctx, cudaEventCreate(&e1));
     const uint32_t refills[] = {8, 16, 32}, steps[] = {16, 32, 64}, ctas[] = {2, 3, 4};
+    const uint32_t base_smem = vis_tuning(ctx).smem_nodes;
     VisTuning best{0, 0, 0, 0, 0};
     float best_t = 3.0e38f;
     for (uint32_t rf : refills)
@@ -206,8 +207,8 @@ luz_status luz_batch_autotune(luz_ctx* ctx, luz_batch* b, uint32_t reps, luz_vis
             }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    // the single-scene TLAS staging size keeps its default
-    best.smem_nodes = 256;
+    // the single-scene TLAS staging size keeps its current value
+    best.smem_nodes = base_smem;
     ctx->vis_tuning = best;
     if (chosen) *chosen = luz_vis_tuning{best.smem_nodes, best.refill, best.steps, best.ctas_per_sm};
     if (best_ms) *best_ms = best_t;

@@ -342,6 +342,9 @@ luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, 
         return LUZ_ERR_INVALID;
     if (scene->ao_num_samples < 0 || scene->ao_num_samples > LUZ_MAX_AO_SAMPLES)
         return set_error(ctx, LUZ_ERR_LIMIT, "ao_num_samples outside [0, LUZ_MAX_AO_SAMPLES]");
+    // aoMin is the AO rays' tMin (light.frag:125-126); a ray query's tMin must not be
+    // negative (the editor clamps it to [0, 10], Editor.cpp:329).
+    if (scene->ao_min < 0.0f) return set_error(ctx, LUZ_ERR_INVALID, "ao_min is negative (a ray query's tMin)");
     if (light_count > 65535) return set_error(ctx, LUZ_ERR_LIMIT, "more than 65535 lights");
     // Shadow slots: Σ numShadowSamples (GPUScene.cpp:248), one bit plane each.
     std::vector<uint32_t> slot_table, light_slot(std::max(light_count, 1u));

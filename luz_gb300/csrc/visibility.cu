@@ -57,7 +57,7 @@ struct LaneRay {
     int node, sp;
     int signs;           // bit a set: the direction's component a is negative
     bool in_blas;
-    const float4* bn;
+    const float4* nb;    // 4-wide nodes of the current space (the TLAS, or the entered BLAS)
     const float4* tlas;          // batched kernel: the lane's scene
     const DevInstance* insts;
     uint32_t budget;
@@ -79,6 +79,12 @@ __device__ __forceinline__ void near_planes(LaneRay& r) {
     r.signs = (r.idir.x < 0.0f ? 1 : 0) | (r.idir.y < 0.0f ? 2 : 0) | (r.idir.z < 0.0f ? 4 : 0);
 }
 
+// Entry distances are >= tmin >= 0 (luz_frame_upload rejects a negative aoMin, as
+// a ray query's tMin must not be negative), so scaling the entry down by 2^-16
+// relative widens the interval by at least the 2^-18 margin of each side in
+// traverse.cuh's slab(): still conservative, one multiply instead of two
+// multiply-adds. An inverted (empty) slot gives tn = +inf, tf = -inf and fails.
+constexpr float kSlabShrink = 1.0f - 0x1p-16f;
 __device__ __forceinline__ bool slab_ordered(float nx, float fx, float ny, float fy, float nz, float fz,
                                              const LaneRay& r, float& tnear) {
     const V3& o = r.o;
@@ -86,7 +92,7 @@ __device__ __forceinline__ bool slab_ordered(float nx, float fx, float ny, float
     float tn = fmaxf(fmaxf((nx - o.x) * id.x, (ny - o.y) * id.y), fmaxf((nz - o.z) * id.z, r.tmin));
     float tf = fminf(fminf((fx - o.x) * id.x, (fy - o.y) * id.y), fminf((fz - o.z) * id.z, r.tmax));
     tnear = tn;
-    return tn - fabsf(tn) * kSlabEps <= tf + fabsf(tf) * kSlabEps;
+    return tn * kSlabShrink <= tf;
 }
 
 // Generates the ray of item (slot, j) of scene S. Returns false when there is
@@ -139,6 +145,7 @@ __device__ __forceinline__ bool setup_ray(LaneRay& r, const Cold& c, const Scene
     r.in_blas = false;
     r.budget = 0;
     r.tlas = S.tlas_nodes;
+    r.nb = S.tlas_nodes;
     r.insts = S.instances;
     return true;
 }
@@ -153,39 +160,56 @@ __device__ __forceinline__ void finish_ray(const Cold& c, bool& active, bool hit
     active = false;
 }
 
+// 4-wide node loads: read-only global memory (__ldg) unless the TLAS top may come
+// from shared memory (kStaged), where the pointer is generic.
+template <bool kStaged>
+__device__ __forceinline__ float4 node_load(const float4* p) {
+    if (kStaged) return *p;
+    return __ldg(p);
+}
+
 // Up to `steps` traversal steps of one lane's ray; clears `active` when it ends.
 // tlas / insts: the scene's TLAS nodes and instances (kernel parameters in the
-// single-scene kernel, the lane's own scene in the batched one).
-template <bool kStats>
+// single-scene kernel, the lane's own scene in the batched one). The step cap of a
+// ray is charged `steps` per call, so a ray ends after at most kRayStepCap + steps.
+template <bool kStats, bool kStaged>
 __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& active, const float4* smem_tlas,
                                           uint32_t staged, const float4* tlas, const DevInstance* insts,
                                           uint32_t* s_stack, int* lstack, uint32_t steps, uint32_t& err,
                                           TraceCounters& cnt) {
+    if (active && (r.budget += steps) > kRayStepCap) {
+        err |= LUZ_DEV_TRAVERSAL_CAP;
+        finish_ray(c, active, false);
+    }
     for (uint32_t s = 0; s < steps && active; ++s) {
         bool finished = false, hit = false;
-        if (++r.budget > kRayStepCap) { err |= LUZ_DEV_TRAVERSAL_CAP; finished = true; }
-        else if (r.node >= 0) {
+        if (r.node >= 0) {
             // 4-wide node: test the four child boxes, continue with the nearest hit
-            // child and push the other hits.
+            // child and push the other hits. Empty slots hold inverted boxes, which
+            // no ray overlaps.
             if (kStats) { if (r.in_blas) cnt.blas_nodes++; else cnt.tlas_nodes++; }
-            const float4* np = r.in_blas ? r.bn : ((uint32_t)r.node < staged ? smem_tlas : tlas);
+            const float4* np = kStaged ? (r.in_blas ? r.nb : ((uint32_t)r.node < staged ? smem_tlas : tlas)) : r.nb;
             np += (size_t)r.node * kNode4F4;
             const int sx = r.signs & 1, sy = (r.signs >> 1) & 1, sz = r.signs >> 2;
-            const float4 nx = np[sx], fx = np[sx ^ 1], ny = np[2 + sy], fy = np[3 - sy], nz = np[4 + sz],
-                         fz = np[5 - sz], cf = np[6];
+            const float4 nx = node_load<kStaged>(np + sx), fx = node_load<kStaged>(np + (sx ^ 1)),
+                         ny = node_load<kStaged>(np + 2 + sy), fy = node_load<kStaged>(np + 3 - sy),
+                         nz = node_load<kStaged>(np + 4 + sz), fz = node_load<kStaged>(np + 5 - sz),
+                         cf = node_load<kStaged>(np + 6);
             const int ch[4] = {__float_as_int(cf.x), __float_as_int(cf.y), __float_as_int(cf.z),
                                __float_as_int(cf.w)};
             float tn[4];
             bool h[4];
-            h[0] = ch[0] != kEmptyChild && slab_ordered(nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, r, tn[0]);
-            h[1] = ch[1] != kEmptyChild && slab_ordered(nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, r, tn[1]);
-            h[2] = ch[2] != kEmptyChild && slab_ordered(nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, r, tn[2]);
-            h[3] = ch[3] != kEmptyChild && slab_ordered(nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, r, tn[3]);
-            int best = -1;
+            h[0] = slab_ordered(nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, r, tn[0]);
+            h[1] = slab_ordered(nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, r, tn[1]);
+            h[2] = slab_ordered(nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, r, tn[2]);
+            h[3] = slab_ordered(nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, r, tn[3]);
+            // Nearest hit child by constant-index selects (a dynamic ch[best] would
+            // put ch[] in local memory).
+            int best = -1, bc = 0;
             float tb = 0.f;
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if (h[k] && (best < 0 || tn[k] < tb)) { best = k; tb = tn[k]; }
+                if (h[k] && (best < 0 || tn[k] < tb)) { best = k; tb = tn[k]; bc = ch[k]; }
             if (best >= 0) {
 #pragma unroll
                 for (int k = 3; k >= 0; --k) {
@@ -195,7 +219,7 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
                     else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
                     ++r.sp;
                 }
-                r.node = ch[best];
+                r.node = bc;
                 if (!finished) continue;
             }
         } else if (!r.in_blas) {
@@ -215,7 +239,7 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
                 r.o = wt.o;
                 r.idir = safe_inv(od);
                 near_planes(r);
-                r.bn = I->nodes4;
+                r.nb = I->nodes4;
                 const unsigned long long bt = reinterpret_cast<unsigned long long>(I->tris);
                 c[kBtLo] = __uint_as_float((uint32_t)bt);
                 c[kBtHi] = __uint_as_float((uint32_t)(bt >> 32));
@@ -256,6 +280,7 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
             int v = r.sp < kSmemStack ? (int)s_stack[r.sp * 32] : lstack[r.sp - kSmemStack];
             if (v == kStackMarker) {
                 r.in_blas = false;
+                r.nb = tlas;
                 r.o = c.wo();
                 r.idir = safe_inv(c.wd());
                 near_planes(r);
@@ -278,7 +303,7 @@ __device__ __forceinline__ void flush_stats(unsigned long long* stats, uint32_t 
 
 // One scene, TLAS top staged in shared memory. Shared memory: staged TLAS nodes,
 // then the stacks, then the cold ray state.
-template <bool kStats>
+template <bool kStats, bool kStaged>
 __global__ void __launch_bounds__(kVisThreads, LUZ_VIS_MIN_BLOCKS)
 visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
     extern __shared__ float4 smem[];
@@ -316,8 +341,8 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
             }
         }
         if (exhausted && __ballot_sync(full, active) == 0) break;
-        run_steps<kStats>(r, c, active, smem, staged, S.tlas_nodes, S.instances, s_stack, lstack, C.steps, err,
-                          cnt);
+        run_steps<kStats, kStaged>(r, c, active, smem, staged, S.tlas_nodes, S.instances, s_stack, lstack, C.steps, err,
+                                   cnt);
     }
     if (err) atomicOr(C.status, err);
     if (kStats) flush_stats(stats, rays, cnt);
@@ -368,7 +393,7 @@ visibility_batch_kernel(const SceneVis* __restrict__ scenes, uint32_t n, const u
             }
         }
         if (exhausted && __ballot_sync(full, active) == 0) break;
-        run_steps<kStats>(r, c, active, nullptr, 0u, r.tlas, r.insts, s_stack, lstack, C.steps, err, cnt);
+        run_steps<kStats, false>(r, c, active, nullptr, 0u, r.tlas, r.insts, s_stack, lstack, C.steps, err, cnt);
     }
     if (err) atomicOr(C.status, err);
     if (kStats) flush_stats(stats, rays, cnt);
@@ -456,17 +481,21 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     size_t smem = (size_t)staged * kNode4F4 * 16 + kStackBytes + kColdBytes;
     static size_t attr_bytes = 0;
     if (smem > attr_bytes) {
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_bytes = smem;
     }
     uint32_t grid = (uint32_t)ctx->sm_count * tu.ctas_per_sm;
     if (d_stats) {
         LUZ_CUDA(ctx, cudaMemsetAsync(d_stats, 0, 5 * sizeof(unsigned long long), st));
-        visibility_kernel<true><<<grid, 256, smem, st>>>(S, C, d_stats);
+        if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, d_stats);
+        else visibility_kernel<true, false><<<grid, 256, smem, st>>>(S, C, d_stats);
         LUZ_LAUNCHED(ctx, "visibility_kernel<stats>");
     } else {
-        visibility_kernel<false><<<grid, 256, smem, st>>>(S, C, nullptr);
+        if (staged) visibility_kernel<false, true><<<grid, 256, smem, st>>>(S, C, nullptr);
+        else visibility_kernel<false, false><<<grid, 256, smem, st>>>(S, C, nullptr);
         LUZ_LAUNCHED(ctx, "visibility_kernel");
     }
     return LUZ_OK;

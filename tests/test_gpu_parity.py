@@ -132,3 +132,12 @@ def test_deterministic_rebuild(ctx):
     ctx.synchronize()
     assert np.array_equal(a, g1.frame.read(L.PLANE_AO_BITS))
     assert np.array_equal(n1.view(np.uint32), g1.tlas.download()[0].view(np.uint32))
+
+
+def test_negative_ao_min_is_rejected(ctx):
+    # aoMin is the AO rays' tMin; a ray query's tMin must not be negative.
+    s = _cfg1(32, 32)
+    s.set_sampling(4, ao_min=-0.5)
+    g = L.GPUScene(ctx, s)
+    with pytest.raises(L.LuzError, match="ao_min is negative"):
+        g.update_resources_gpu()
