@@ -211,13 +211,22 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
             for (int k = 0; k < 4; ++k)
                 if (h[k] && (best < 0 || tn[k] < tb)) { best = k; tb = tn[k]; bc = ch[k]; }
             if (best >= 0) {
+                // The other hits go on the stack, farthest index first; when they all
+                // fit in the shared-memory part the pushes are predicated stores.
+                const int n = (int)h[0] + (int)h[1] + (int)h[2] + (int)h[3] - 1;
+                if (r.sp + n <= kSmemStack) {
 #pragma unroll
-                for (int k = 3; k >= 0; --k) {
-                    if (!h[k] || k == best) continue;
-                    if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)ch[k];
-                    else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = ch[k];
-                    else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
-                    ++r.sp;
+                    for (int k = 3; k >= 0; --k)
+                        if (h[k] && k != best) { s_stack[r.sp * 32] = (uint32_t)ch[k]; ++r.sp; }
+                } else {
+#pragma unroll
+                    for (int k = 3; k >= 0; --k) {
+                        if (!h[k] || k == best) continue;
+                        if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)ch[k];
+                        else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = ch[k];
+                        else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
+                        ++r.sp;
+                    }
                 }
                 r.node = bc;
                 if (!finished) continue;
