@@ -9,7 +9,7 @@
 
 namespace luz {
 
-constexpr int kSmemTlasNodes = 1024;   // 64 KB of TLAS top levels per CTA
+constexpr int kSmemTlasNodes = 256;    // 32 KB of 4-wide TLAS top levels per CTA
 
 __device__ __forceinline__ uint32_t unorm8(float x) {
     return (uint32_t)(clamp01(x) * 255.0f + 0.5f);
@@ -37,7 +37,7 @@ __device__ __forceinline__ uint32_t block_excl(uint32_t v, uint32_t* s_tmp /*8*/
 __device__ __forceinline__ void stage_tlas(const float4* __restrict__ g, uint32_t node_count,
                                            float4* s, uint32_t& staged) {
     staged = min(node_count, (uint32_t)kSmemTlasNodes);
-    for (uint32_t i = threadIdx.x; i < staged * kNodeF4; i += blockDim.x) s[i] = __ldg(g + i);
+    for (uint32_t i = threadIdx.x; i < staged * kNode4F4; i += blockDim.x) s[i] = __ldg(g + i);
     __syncthreads();
 }
 
@@ -333,7 +333,9 @@ __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, co
 // ---------------------------------------------------------------- host launchers
 luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
     GbufParams G;
-    G.tlas_nodes = t->nodes;
+    // 4-wide nodes; node_count (the binary count) bounds the 4-wide count and the
+    // nodes4 buffer, so staging that many stays inside it.
+    G.tlas_nodes = t->nodes4;
     G.tlas_node_count = t->count ? t->node_count : 0;
     G.instances = t->instances;
     G.instance_count = t->count;
@@ -362,10 +364,10 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
     static bool attr_set = false;
     if (!attr_set) {
         LUZ_CUDA(ctx, cudaFuncSetAttribute(gbuffer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           kSmemTlasNodes * 64));
+                                           kSmemTlasNodes * 128));
         attr_set = true;
     }
-    size_t smem = (size_t)std::min<uint32_t>(G.tlas_node_count, kSmemTlasNodes) * 64;
+    size_t smem = (size_t)std::min<uint32_t>(G.tlas_node_count, kSmemTlasNodes) * 128;
     gbuffer_kernel<<<tiles, 256, smem, ctx->stream>>>(G);
     LUZ_LAUNCHED(ctx, "gbuffer_kernel");
     // compaction of lit pixels

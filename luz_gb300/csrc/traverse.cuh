@@ -11,13 +11,15 @@
 //   (instance input index, primitive), so both results are independent of the
 //   traversal order.
 // * Box tests are conservative: leaf boxes are padded and the slab interval is
-//   widened by a relative 2^-18, so no box that holds an accepted hit is culled.
+//   widened by a relative 2^-16, so no box that holds an accepted hit is culled.
+// * Traversal runs over the 4-wide nodes (the even-depth collapse of the binary
+//   LBVH): the nearest hit child is visited next, the other hits are pushed
+//   farthest first.
 #pragma once
 #include "internal.cuh"
 
 namespace luz {
 
-constexpr float kSlabEps = 0x1p-18f;
 constexpr uint32_t kTraversalCap = 1u << 24;
 
 __device__ __forceinline__ float comp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
@@ -83,20 +85,26 @@ __device__ __forceinline__ V3 safe_inv(V3 d) {
     return V3{1.0f / x, 1.0f / y, 1.0f / z};
 }
 
-__device__ __forceinline__ bool slab(float lx, float hx, float ly, float hy, float lz, float hz,
-                                     V3 o, V3 id, float tmin, float tmax, float& tnear) {
-    float tx0 = (lx - o.x) * id.x, tx1 = (hx - o.x) * id.x;
-    float ty0 = (ly - o.y) * id.y, ty1 = (hy - o.y) * id.y;
-    float tz0 = (lz - o.z) * id.z, tz1 = (hz - o.z) * id.z;
-    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+// Conservative slab test of one box with near / far planes already picked by the
+// ray's direction signs (rounding is monotonic, so near <= far for every
+// non-inverted box). Entry distances are >= tmin >= 0, so scaling the entry down by
+// 2^-16 relative widens the interval past the rounding of the plane distances; an
+// inverted (empty) slot gives tn = +inf, tf = -inf and fails.
+constexpr float kSlabShrink = 1.0f - 0x1p-16f;
+__device__ __forceinline__ bool slab_ordered(float nx, float fx, float ny, float fy, float nz, float fz, V3 o,
+                                             V3 id, float tmin, float tmax, float& tnear) {
+    float tn = fmaxf(fmaxf((nx - o.x) * id.x, (ny - o.y) * id.y), fmaxf((nz - o.z) * id.z, tmin));
+    float tf = fminf(fminf((fx - o.x) * id.x, (fy - o.y) * id.y), fminf((fz - o.z) * id.z, tmax));
     tnear = tn;
-    return tn - fabsf(tn) * kSlabEps <= tf + fabsf(tf) * kSlabEps;
+    return tn * kSlabShrink <= tf;
+}
+__device__ __forceinline__ int dir_signs(V3 idir) {
+    return (idir.x < 0.0f ? 1 : 0) | (idir.y < 0.0f ? 2 : 0) | (idir.z < 0.0f ? 4 : 0);
 }
 
 struct TlasView {
-    const float4* __restrict__ nodes;    // global, BFS order
-    const float4* smem_nodes;            // first `smem_count` nodes staged in shared memory
+    const float4* __restrict__ nodes;    // global 4-wide nodes
+    const float4* smem_nodes;            // first `smem_count` 4-wide nodes staged in shared memory
     uint32_t smem_count;
     const DevInstance* __restrict__ instances;
     uint32_t count;
@@ -135,6 +143,8 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
     if (wd.x == 0.0f && wd.y == 0.0f && wd.z == 0.0f) return false;
     const V3 widir = safe_inv(wd);
     V3 o = wo, idir = widir;
+    int signs = dir_signs(idir);
+    const float tmin_box = fmaxf(tmin, 0.0f);   // the entry shrink wants tn >= 0; callers pass tmin >= 0
     WtRay wt{};
     int stack[kStackSize];
     int sp = 0;
@@ -151,33 +161,47 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
         bool pop = true;
         if (node >= 0) {
             if (kStats) { if (in_blas) cnt->blas_nodes++; else cnt->tlas_nodes++; }
-            float4 n0, n1, n2, n3;
-            if (!in_blas && (uint32_t)node < T.smem_count) {
-                const float4* s = T.smem_nodes + (size_t)node * kNodeF4;
-                n0 = s[0]; n1 = s[1]; n2 = s[2]; n3 = s[3];
-            } else {
-                const float4* g = nodes + (size_t)node * kNodeF4;
-                n0 = __ldg(g); n1 = __ldg(g + 1); n2 = __ldg(g + 2); n3 = __ldg(g + 3);
+            const float4* np = (!in_blas && (uint32_t)node < T.smem_count) ? T.smem_nodes + (size_t)node * kNode4F4
+                                                                            : nodes + (size_t)node * kNode4F4;
+            const int sx = signs & 1, sy = (signs >> 1) & 1, sz = signs >> 2;
+            const float4 nx = np[sx], fx = np[sx ^ 1], ny = np[2 + sy], fy = np[3 - sy], nz = np[4 + sz],
+                         fz = np[5 - sz], cf = np[6];
+            int ch[4] = {__float_as_int(cf.x), __float_as_int(cf.y), __float_as_int(cf.z), __float_as_int(cf.w)};
+            float tn[4];
+            bool h[4];
+            h[0] = slab_ordered(nx.x, fx.x, ny.x, fy.x, nz.x, fz.x, o, idir, tmin_box, tmax, tn[0]);
+            h[1] = slab_ordered(nx.y, fx.y, ny.y, fy.y, nz.y, fz.y, o, idir, tmin_box, tmax, tn[1]);
+            h[2] = slab_ordered(nx.z, fx.z, ny.z, fy.z, nz.z, fz.z, o, idir, tmin_box, tmax, tn[2]);
+            h[3] = slab_ordered(nx.w, fx.w, ny.w, fy.w, nz.w, fz.w, o, idir, tmin_box, tmax, tn[3]);
+            // Misses sort last; a network of five compare-exchanges orders the hits by
+            // entry distance (constant indices keep everything in registers).
+            const float inf = __int_as_float(0x7f800000);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) if (!h[k]) tn[k] = inf;
+#define LUZ_CX(a, b)                                                              \
+            if (tn[b] < tn[a]) {                                                  \
+                float tt = tn[a]; tn[a] = tn[b]; tn[b] = tt;                      \
+                int tc = ch[a]; ch[a] = ch[b]; ch[b] = tc;                        \
+                bool th = h[a]; h[a] = h[b]; h[b] = th;                           \
             }
-            int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-            float t0, t1;
-            bool h0 = c0 != kEmptyChild && slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, o, idir, tmin, tmax, t0);
-            bool h1 = c1 != kEmptyChild && slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, o, idir, tmin, tmax, t1);
-            if (h0 && h1) {
-                int nearc = c0, farc = c1;
-                if (t1 < t0) { nearc = c1; farc = c0; }
-                if (sp >= kStackSize) { err |= LUZ_DEV_STACK_OVERFLOW; return false; }
-                stack[sp++] = farc;
-                node = nearc;
+            LUZ_CX(0, 1) LUZ_CX(2, 3) LUZ_CX(0, 2) LUZ_CX(1, 3) LUZ_CX(1, 2)
+#undef LUZ_CX
+            if (h[0]) {
+#pragma unroll
+                for (int k = 3; k >= 1; --k) {
+                    if (!h[k]) continue;
+                    if (sp >= kStackSize) { err |= LUZ_DEV_STACK_OVERFLOW; return false; }
+                    stack[sp++] = ch[k];
+                }
+                node = ch[0];
                 pop = false;
-            } else if (h0) { node = c0; pop = false; }
-            else if (h1) { node = c1; pop = false; }
+            }
         } else if (!in_blas) {
             if (kStats) cnt->instances++;
             const DevInstance* I = T.instances + (~node);
             const float4* wp = reinterpret_cast<const float4*>(I->w2o);
             float4 r0 = __ldg(wp), r1 = __ldg(wp + 1), r2 = __ldg(wp + 2);
-            const float4* pnodes = I->nodes;
+            const float4* pnodes = I->nodes4;
             const float4* ptris = I->tris;
             uint4 meta = __ldg(reinterpret_cast<const uint4*>(&I->custom_index));
             // meta = (custom_index, mask, input_index, blas_prims)
@@ -195,6 +219,7 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
                 stack[sp++] = kStackMarker;
                 o = oo;
                 idir = safe_inv(od);
+                signs = dir_signs(idir);
                 wt = wt_setup(oo, od);
                 in_blas = true;
                 nodes = pnodes;
@@ -239,6 +264,7 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
                     nodes = T.nodes;
                     o = wo;
                     idir = widir;
+                    signs = dir_signs(idir);
                     continue;
                 }
                 break;

@@ -45,6 +45,7 @@ enum ColdField : int {
     kOutLo, kOutHi, kOutBits,     // bit | record_hit << 5
     kWtK, kWtSx, kWtSy, kWtSz,    // kx | ky << 2 | kz << 4; shear
     kBtLo, kBtHi,                 // triangles of the current BLAS
+    kOoX, kOoY, kOoZ,             // origin in the current BLAS's object space
     kColdFields
 };
 constexpr size_t kColdBytes = (size_t)kColdFields * kVisThreads * 4;
@@ -52,7 +53,7 @@ constexpr size_t kStackBytes = (size_t)kVisThreads * kSmemStack * 4;
 
 // Hot per-lane state (registers).
 struct LaneRay {
-    V3 o, idir;          // origin and inverse direction in the current space (world or BLAS object)
+    V3 on, of, idir;     // origin offsets (set_origin) and inverse direction in the current space
     float tmin, tmax;
     int node, sp;
     int signs;           // bit a set: the direction's component a is negative
@@ -68,29 +69,36 @@ struct Cold {
     __device__ __forceinline__ float& operator[](int k) const { return f[k * kVisThreads]; }
     __device__ __forceinline__ V3 wo() const { return V3{(*this)[kWoX], (*this)[kWoY], (*this)[kWoZ]}; }
     __device__ __forceinline__ V3 wd() const { return V3{(*this)[kWdX], (*this)[kWdY], (*this)[kWdZ]}; }
+    __device__ __forceinline__ V3 oo() const { return V3{(*this)[kOoX], (*this)[kOoY], (*this)[kOoZ]}; }
 };
 
 // Near-plane rows of a 4-wide node for a ray with inverse direction id: the lower
 // plane where the component is non-negative, else the upper one (the far plane is
-// the other row, index ^ 1). Rounding is monotonic, so (near - o) * id <= (far - o) * id
-// for every non-inverted box: the ordered test gives the same interval as the
-// min/max form of slab().
-__device__ __forceinline__ void near_planes(LaneRay& r) {
-    r.signs = (r.idir.x < 0.0f ? 1 : 0) | (r.idir.y < 0.0f ? 2 : 0) | (r.idir.z < 0.0f ? 4 : 0);
-}
+// the other row, index ^ 1); see slab_ordered in traverse.cuh.
+__device__ __forceinline__ void near_planes(LaneRay& r) { r.signs = dir_signs(r.idir); }
 
-// Entry distances are >= tmin >= 0 (luz_frame_upload rejects a negative aoMin, as
-// a ray query's tMin must not be negative), so scaling the entry down by 2^-16
-// relative widens the interval by at least the 2^-18 margin of each side in
-// traverse.cuh's slab(): still conservative, one multiply instead of two
-// multiply-adds. An inverted (empty) slot gives tn = +inf, tf = -inf and fails.
-constexpr float kSlabShrink = 1.0f - 0x1p-16f;
+// The slab test of traverse.cuh (ordered planes, entry shrink kSlabShrink) on the
+// lane's ray, which needs tmin >= 0: shadow rays start at 0.001 and
+// luz_frame_upload rejects a negative aoMin (a ray query's tMin must not be
+// negative). Plane distances as one FMA each, t = p * idir - o * idir. The product o * idir
+// is rounded once per ray, so each axis carries the bound E = |o * idir| * 2^-21 of
+// that rounding (and of its own), folded into two per-ray offsets: near planes use
+// on = o * idir + E (a lower bound of the distance), far planes of = o * idir - E
+// (an upper bound). The remaining errors are relative (the rounding of idir and of
+// the FMA) and lie inside the entry shrink. Overflowed offsets only widen the box.
+__device__ __forceinline__ void set_origin(LaneRay& r, V3 o) {
+    V3 oid = V3{o.x * r.idir.x, o.y * r.idir.y, o.z * r.idir.z};
+    V3 e = V3{fabsf(oid.x) * 0x1p-21f, fabsf(oid.y) * 0x1p-21f, fabsf(oid.z) * 0x1p-21f};
+    r.on = V3{oid.x + e.x, oid.y + e.y, oid.z + e.z};
+    r.of = V3{oid.x - e.x, oid.y - e.y, oid.z - e.z};
+}
 __device__ __forceinline__ bool slab_ordered(float nx, float fx, float ny, float fy, float nz, float fz,
                                              const LaneRay& r, float& tnear) {
-    const V3& o = r.o;
     const V3& id = r.idir;
-    float tn = fmaxf(fmaxf((nx - o.x) * id.x, (ny - o.y) * id.y), fmaxf((nz - o.z) * id.z, r.tmin));
-    float tf = fminf(fminf((fx - o.x) * id.x, (fy - o.y) * id.y), fminf((fz - o.z) * id.z, r.tmax));
+    float tn = fmaxf(fmaxf(__fmaf_rn(nx, id.x, -r.on.x), __fmaf_rn(ny, id.y, -r.on.y)),
+                     fmaxf(__fmaf_rn(nz, id.z, -r.on.z), r.tmin));
+    float tf = fminf(fminf(__fmaf_rn(fx, id.x, -r.of.x), __fmaf_rn(fy, id.y, -r.of.y)),
+                     fminf(__fmaf_rn(fz, id.z, -r.of.z), r.tmax));
     tnear = tn;
     return tn * kSlabShrink <= tf;
 }
@@ -137,8 +145,8 @@ __device__ __forceinline__ bool setup_ray(LaneRay& r, const Cold& c, const Scene
     c[kOutLo] = __uint_as_float((uint32_t)oa);
     c[kOutHi] = __uint_as_float((uint32_t)(oa >> 32));
     c[kOutBits] = __uint_as_float((pix & 31u) | (record_hit ? 32u : 0u));
-    r.o = wo;
     r.idir = safe_inv(wd);
+    set_origin(r, wo);
     near_planes(r);
     r.node = 0;
     r.sp = 0;
@@ -245,8 +253,11 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
                 c[kWtSx] = wt.sx;
                 c[kWtSy] = wt.sy;
                 c[kWtSz] = wt.sz;
-                r.o = wt.o;
+                c[kOoX] = wt.o.x;
+                c[kOoY] = wt.o.y;
+                c[kOoZ] = wt.o.z;
                 r.idir = safe_inv(od);
+                set_origin(r, wt.o);
                 near_planes(r);
                 r.nb = I->nodes4;
                 const unsigned long long bt = reinterpret_cast<unsigned long long>(I->tris);
@@ -268,7 +279,7 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
             float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
             WtRay wt;
             int k = __float_as_int(c[kWtK]);
-            wt.o = r.o;
+            wt.o = c.oo();
             wt.kx = k & 3;
             wt.ky = (k >> 2) & 3;
             wt.kz = k >> 4;
@@ -290,8 +301,8 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
             if (v == kStackMarker) {
                 r.in_blas = false;
                 r.nb = tlas;
-                r.o = c.wo();
                 r.idir = safe_inv(c.wd());
+                set_origin(r, c.wo());
                 near_planes(r);
                 continue;
             }
