@@ -30,6 +30,11 @@ constexpr int kStackSize = 128;
 //   f6 child[4] (int bits: >= 0 a 4-wide node, < 0 a leaf ~index, kEmptyChild), f7 0.
 constexpr int kNode4F4 = 8;
 
+// Items (rays) per visibility chunk: the ray generation pass writes one chunk of
+// 32-B ray records (4 GiB at most; a 1080p frame with 57 rays per pixel fits one
+// chunk even when every pixel is lit), the traversal kernel consumes it.
+constexpr uint32_t kRayChunk = 1u << 27;
+
 // One TLAS leaf, in sorted (leaf) order. 96 B, 16-B aligned for vector loads.
 struct __align__(16) DevInstance {
     float w2o[12];          // world -> object, 3x4 row-major
@@ -204,6 +209,11 @@ struct luz_frame {
     void* d_texels = nullptr;
     uint32_t texture_count = 0;
     unsigned long long* work_counter = nullptr;
+    // generated shadow / AO rays of one chunk (structure of arrays, rays_cap each):
+    // (origin, tMax) and (direction, pixel); tMax = -inf marks an item with no ray
+    float4* rays_a = nullptr;
+    float4* rays_b = nullptr;
+    uint32_t rays_cap = 0;
 };
 
 // ---------------------------------------------------------------- error plumbing

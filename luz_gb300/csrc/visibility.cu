@@ -103,48 +103,54 @@ __device__ __forceinline__ bool slab_ordered(float nx, float fx, float ny, float
     return tn * kSlabShrink <= tf;
 }
 
-// Generates the ray of item (slot, j) of scene S. Returns false when there is
-// nothing to trace; the miss (AO) has then already been recorded.
-__device__ __forceinline__ bool setup_ray(LaneRay& r, const Cold& c, const SceneVis& S, const VisCommon& C,
-                                          uint32_t slot, uint32_t j) {
+// The ray of item (slot, j) of scene S (light.frag:86-135): world origin and
+// direction, t range, output word and whether a hit (shadow) or a miss (AO) is
+// recorded. Returns false when there is nothing to trace; the miss (AO) has then
+// already been recorded.
+__device__ __forceinline__ bool gen_ray(const SceneVis& S, const VisCommon& C, uint32_t slot, uint32_t j, V3& wo,
+                                        V3& wd, float& tmin, float& tmax, uint32_t*& out, bool& record_hit,
+                                        uint32_t& pix) {
     float4 s0 = __ldg(S.surf + 2 * (size_t)j), s1 = __ldg(S.surf + 2 * (size_t)j + 1);
     V3 p = V3{s0.x, s0.y, s0.z}, N = V3{s1.x, s1.y, s1.z};
-    uint32_t pix = __float_as_uint(s0.w);
+    pix = __float_as_uint(s0.w);
     uint32_t px = pix % S.width, py = pix / S.width;
     V3 cam = V3{S.cam[0], S.cam[1], S.cam[2]};
     float rx, ry;
-    V3 wo, wd;
-    uint32_t* out;
-    bool record_hit;
     if (slot < S.shadow_slots) {
         uint32_t e = __ldg(S.slot_table + slot);
         uint32_t li = e & 0xFFFFu, si = e >> 16;
         sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)si, S.frame, li + 1, &rx, &ry);
-        shadow_ray(S.lights[li], p, N, cam, rx, ry, wo, wd, r.tmax);
-        r.tmin = 0.001f;
+        shadow_ray(S.lights[li], p, N, cam, rx, ry, wo, wd, tmax);
+        tmin = 0.001f;
         out = S.shadow_bits + (size_t)slot * S.words + (pix >> 5);
         record_hit = true;
     } else {
         uint32_t a = slot - S.shadow_slots;
         sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)a, S.frame, 0u, &rx, &ry);
         ao_ray(p, N, cam, rx, ry, wo, wd);
-        r.tmin = S.ao_min;
-        r.tmax = S.ao_max;
+        tmin = S.ao_min;
+        tmax = S.ao_max;
         out = S.ao_bits + (size_t)a * S.words + (pix >> 5);
         record_hit = false;
     }
-    bool ok = S.instance_count > 0 && finite3(wo) && finite3(wd) && (r.tmin <= r.tmax) &&
+    bool ok = S.instance_count > 0 && finite3(wo) && finite3(wd) && (tmin <= tmax) &&
               !(wd.x == 0.0f && wd.y == 0.0f && wd.z == 0.0f);
-    if (!ok) {
-        if (!record_hit) atomicOr(out, 1u << (pix & 31));   // no ray: a miss
-        return false;
-    }
+    if (!ok && !record_hit) atomicOr(out, 1u << (pix & 31));   // no ray: a miss
+    return ok;
+}
+
+// Starts a lane on a generated ray: cold state in shared memory, hot state in
+// registers, traversal at the TLAS root.
+__device__ __forceinline__ void start_ray(LaneRay& r, const Cold& c, const SceneVis& S, V3 wo, V3 wd, float tmin,
+                                          float tmax, const uint32_t* out, bool record_hit, uint32_t pix) {
     unsigned long long oa = reinterpret_cast<unsigned long long>(out);
     c[kWoX] = wo.x; c[kWoY] = wo.y; c[kWoZ] = wo.z;
     c[kWdX] = wd.x; c[kWdY] = wd.y; c[kWdZ] = wd.z;
     c[kOutLo] = __uint_as_float((uint32_t)oa);
     c[kOutHi] = __uint_as_float((uint32_t)(oa >> 32));
     c[kOutBits] = __uint_as_float((pix & 31u) | (record_hit ? 32u : 0u));
+    r.tmin = tmin;
+    r.tmax = tmax;
     r.idir = safe_inv(wd);
     set_origin(r, wo);
     near_planes(r);
@@ -155,6 +161,18 @@ __device__ __forceinline__ bool setup_ray(LaneRay& r, const Cold& c, const Scene
     r.tlas = S.tlas_nodes;
     r.nb = S.tlas_nodes;
     r.insts = S.instances;
+}
+
+// Generates and starts the ray of item (slot, j) (the batched kernel).
+__device__ __forceinline__ bool setup_ray(LaneRay& r, const Cold& c, const SceneVis& S, const VisCommon& C,
+                                          uint32_t slot, uint32_t j) {
+    V3 wo, wd;
+    float tmin, tmax;
+    uint32_t* out;
+    bool record_hit;
+    uint32_t pix;
+    if (!gen_ray(S, C, slot, j, wo, wd, tmin, tmax, out, record_hit, pix)) return false;
+    start_ray(r, c, S, wo, wd, tmin, tmax, out, record_hit, pix);
     return true;
 }
 
@@ -321,11 +339,49 @@ __device__ __forceinline__ void flush_stats(unsigned long long* stats, uint32_t 
     atomicAdd(stats + 4, (unsigned long long)cnt.instances);
 }
 
-// One scene, TLAS top staged in shared memory. Shared memory: staged TLAS nodes,
-// then the stacks, then the cold ray state.
+// Ray generation pass of one chunk: items [k0, k0 + chunk) of the frame's
+// (slot, lit pixel) list, slot-major, one record per item in structure-of-arrays
+// form: rays_a = (origin, tMax), rays_b = (direction, pixel). An item with no ray
+// gets tMax = -inf (its AO miss is recorded here). Separated from traversal so the
+// long arithmetic of light.frag's sampling runs on full warps, not on the few idle
+// lanes of a traversing warp. Also resets the traversal's work counter.
+__global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, unsigned long long k0,
+                                                     unsigned long long chunk, float4* __restrict__ rays_a,
+                                                     float4* __restrict__ rays_b) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *C.work_counter = 0ull;
+    const uint32_t lit = *S.lit_count;
+    const unsigned long long total = (unsigned long long)lit * (S.shadow_slots + S.ao_samples);
+    if (k0 >= total) return;
+    const unsigned long long end = min(total, k0 + chunk);
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const float ninf = __int_as_float(0xff800000);
+    for (unsigned long long item = k0 + blockIdx.x * blockDim.x + threadIdx.x; item < end; item += stride) {
+        uint32_t slot, j;
+        if (total <= 0xFFFFFFFFull) {
+            slot = (uint32_t)item / lit;
+            j = (uint32_t)item - slot * lit;
+        } else {
+            slot = (uint32_t)(item / lit);
+            j = (uint32_t)(item - (unsigned long long)slot * lit);
+        }
+        V3 wo, wd;
+        float tmin, tmax;
+        uint32_t* out;
+        bool record_hit;
+        uint32_t pix;
+        bool ok = gen_ray(S, C, slot, j, wo, wd, tmin, tmax, out, record_hit, pix);
+        rays_a[item - k0] = make_float4(wo.x, wo.y, wo.z, ok ? tmax : ninf);
+        rays_b[item - k0] = make_float4(wd.x, wd.y, wd.z, __uint_as_float(pix));
+    }
+}
+
+// Traversal of one chunk of generated rays (one scene; the TLAS top may be staged
+// in shared memory). Shared memory: staged TLAS nodes, then the stacks, then the
+// cold ray state.
 template <bool kStats, bool kStaged>
 __global__ void __launch_bounds__(kVisThreads, LUZ_VIS_MIN_BLOCKS)
-visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
+visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long long chunk,
+                  const float4* __restrict__ rays_a, const float4* __restrict__ rays_b, unsigned long long* stats) {
     extern __shared__ float4 smem[];
     const uint32_t staged = min(S.tlas_node_count, C.smem_nodes);
     for (uint32_t i = threadIdx.x; i < staged * kNode4F4; i += blockDim.x) smem[i] = __ldg(S.tlas_nodes + i);
@@ -338,6 +394,7 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
     const uint32_t full = 0xFFFFFFFFu, lt_mask = (1u << lane) - 1u;
     const uint32_t lit = *S.lit_count;
     const unsigned long long total = (unsigned long long)lit * (S.shadow_slots + S.ao_samples);
+    const unsigned long long n = total > k0 ? min(chunk, total - k0) : 0ull;   // items of this chunk
     uint32_t err = 0, rays = 0;
     TraceCounters cnt{0, 0, 0, 0};
     LaneRay r{};
@@ -349,14 +406,34 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long* stats) {
             unsigned long long base = 0;
             if (lane == leader) base = atomicAdd(C.work_counter, (unsigned long long)__popc(idle));
             base = __shfl_sync(full, base, leader);
-            if (base + __popc(idle) >= total) exhausted = true;
+            if (base + __popc(idle) >= n) exhausted = true;
+            // Slot of the warp's first item, by one division in the leader; the
+            // lanes step from it (their items follow in rank order).
+            uint32_t slot0 = 0, j0 = 0;
+            if (lane == leader && base < n) {
+                const unsigned long long g = k0 + base;
+                slot0 = (uint32_t)(g / lit);
+                j0 = (uint32_t)(g - (unsigned long long)slot0 * lit);
+            }
+            slot0 = __shfl_sync(full, slot0, leader);
+            j0 = __shfl_sync(full, j0, leader);
             if (!active) {
-                unsigned long long item = base + __popc(idle & lt_mask);
-                if (item < total) {
-                    uint32_t slot = (uint32_t)(item / lit);
-                    uint32_t j = (uint32_t)(item - (unsigned long long)slot * lit);
+                const uint32_t rank = __popc(idle & lt_mask);
+                const unsigned long long local = base + rank;
+                if (local < n) {
+                    uint32_t slot = slot0, j = j0 + rank;
+                    while (j >= lit) { j -= lit; ++slot; }
+                    const float4 a = __ldg(rays_a + local), b = __ldg(rays_b + local);
                     if (kStats) ++rays;
-                    active = setup_ray(r, c, S, C, slot, j);
+                    const bool record_hit = slot < S.shadow_slots;
+                    const float tmin = record_hit ? 0.001f : S.ao_min;
+                    if (tmin <= a.w) {
+                        const uint32_t pix = __float_as_uint(b.w);
+                        uint32_t* out = record_hit ? S.shadow_bits + (size_t)slot * S.words + (pix >> 5)
+                                                   : S.ao_bits + (size_t)(slot - S.shadow_slots) * S.words + (pix >> 5);
+                        start_ray(r, c, S, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, tmin, a.w, out, record_hit, pix);
+                        active = true;
+                    }
                 }
             }
         }
@@ -493,7 +570,6 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     if (s != LUZ_OK) return s;
     if (f->shadow_slots + f->ao_samples == 0) return LUZ_OK;
     cudaStream_t st = ctx->stream;
-    LUZ_CUDA(ctx, cudaMemsetAsync(f->work_counter, 0, 8, st));
     SceneVis S = make_scene_vis(f, t, frame_index);
     VisCommon C = make_vis_common(ctx, f->work_counter);
     const VisTuning& tu = vis_tuning(ctx);
@@ -508,15 +584,34 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         attr_bytes = smem;
     }
     uint32_t grid = (uint32_t)ctx->sm_count * tu.ctas_per_sm;
-    if (d_stats) {
-        LUZ_CUDA(ctx, cudaMemsetAsync(d_stats, 0, 5 * sizeof(unsigned long long), st));
-        if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, d_stats);
-        else visibility_kernel<true, false><<<grid, 256, smem, st>>>(S, C, d_stats);
-        LUZ_LAUNCHED(ctx, "visibility_kernel<stats>");
-    } else {
-        if (staged) visibility_kernel<false, true><<<grid, 256, smem, st>>>(S, C, nullptr);
-        else visibility_kernel<false, false><<<grid, 256, smem, st>>>(S, C, nullptr);
-        LUZ_LAUNCHED(ctx, "visibility_kernel");
+    if (d_stats) LUZ_CUDA(ctx, cudaMemsetAsync(d_stats, 0, 5 * sizeof(unsigned long long), st));
+    // Chunks of at most rays_cap items over the largest possible ray count (every
+    // pixel lit); a chunk past the frame's actual count returns at once on the device.
+    const unsigned long long max_items = (unsigned long long)f->pixels * (f->shadow_slots + f->ao_samples);
+    const uint32_t need = (uint32_t)std::min<unsigned long long>(max_items, kRayChunk);
+    if (need > f->rays_cap) {   // first trace of this frame shape: allocate the ray records
+        LUZ_CUDA(ctx, cudaStreamSynchronize(st));
+        cudaFree(f->rays_a);
+        cudaFree(f->rays_b);
+        f->rays_a = f->rays_b = nullptr;
+        f->rays_cap = 0;
+        LUZ_CUDA(ctx, cudaMalloc(&f->rays_a, (size_t)need * sizeof(float4)));
+        LUZ_CUDA(ctx, cudaMalloc(&f->rays_b, (size_t)need * sizeof(float4)));
+        f->rays_cap = need;
+    }
+    const unsigned long long chunk = std::min<unsigned long long>(max_items, f->rays_cap);
+    for (unsigned long long k0 = 0; k0 < max_items; k0 += chunk) {
+        raygen_kernel<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b);
+        LUZ_LAUNCHED(ctx, "raygen_kernel");
+        if (d_stats) {
+            if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, d_stats);
+            else visibility_kernel<true, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, d_stats);
+            LUZ_LAUNCHED(ctx, "visibility_kernel<stats>");
+        } else {
+            if (staged) visibility_kernel<false, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, nullptr);
+            else visibility_kernel<false, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, nullptr);
+            LUZ_LAUNCHED(ctx, "visibility_kernel");
+        }
     }
     return LUZ_OK;
 }
