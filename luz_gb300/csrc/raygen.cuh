@@ -5,14 +5,23 @@
 
 namespace luz {
 
-// EvaluateShadow (light.frag:137-146) + TraceShadowRay (light.frag:86-109) for one
-// sample: origin, direction and tMax of the shadow ray; tMin is 0.001.
-__device__ __forceinline__ void shadow_ray(const luz_light& lt, V3 p, V3 N, V3 cam, float rx,
-                                           float ry, V3& O, V3& dir, float& tmax) {
+// The light vector L of light.frag main (light.frag:194-198), which both the shadow
+// ray and the light pass's max(dot(N, L), 0) use.
+__device__ __forceinline__ V3 light_vector(const luz_light& lt, V3 p) {
     V3 lpos = V3{lt.position[0], lt.position[1], lt.position[2]};
     V3 ldir = V3{lt.direction[0], lt.direction[1], lt.direction[2]};
     V3 L = normalize(lpos - p);
     if (lt.type == LUZ_LIGHT_DIRECTIONAL) L = normalize(-ldir);
+    return L;
+}
+
+// EvaluateShadow (light.frag:137-146) + TraceShadowRay (light.frag:86-109) for one
+// sample, given L = light_vector(lt, p): origin, direction and tMax of the shadow
+// ray; tMin is 0.001.
+__device__ __forceinline__ void shadow_ray(const luz_light& lt, V3 p, V3 N, V3 cam, float rx,
+                                           float ry, V3 L, V3& O, V3& dir, float& tmax) {
+    V3 lpos = V3{lt.position[0], lt.position[1], lt.position[2]};
+    V3 ldir = V3{lt.direction[0], lt.direction[1], lt.direction[2]};
     float bias = fmax_(length(p - cam) * 0.01f, 0.05f);
     O = p + N * bias;
     float dist = length(lpos - p);

@@ -119,11 +119,17 @@ __device__ __forceinline__ bool gen_ray(const SceneVis& S, const VisCommon& C, u
     if (slot < S.shadow_slots) {
         uint32_t e = __ldg(S.slot_table + slot);
         uint32_t li = e & 0xFFFFu, si = e >> 16;
-        sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)si, S.frame, li + 1, &rx, &ry);
-        shadow_ray(S.lights[li], p, N, cam, rx, ry, wo, wd, tmax);
-        tmin = 0.001f;
         out = S.shadow_bits + (size_t)slot * S.words + (pix >> 5);
         record_hit = true;
+        const V3 L = light_vector(S.lights[li], p);
+        // The light pass multiplies this light's shadowed radiance by
+        // max(dot(N, L), 0) with the same N and L (light.frag:209-226): at 0 (or NaN)
+        // the shadow factor cannot change the pixel, so the ray is not traced and
+        // its bit stays 0.
+        if (!(dot(N, L) > 0.0f)) return false;
+        sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)si, S.frame, li + 1, &rx, &ry);
+        shadow_ray(S.lights[li], p, N, cam, rx, ry, L, wo, wd, tmax);
+        tmin = 0.001f;
     } else {
         uint32_t a = slot - S.shadow_slots;
         sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)a, S.frame, 0u, &rx, &ry);
@@ -424,10 +430,10 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
                     uint32_t slot = slot0, j = j0 + rank;
                     while (j >= lit) { j -= lit; ++slot; }
                     const float4 a = __ldg(rays_a + local), b = __ldg(rays_b + local);
-                    if (kStats) ++rays;
                     const bool record_hit = slot < S.shadow_slots;
                     const float tmin = record_hit ? 0.001f : S.ao_min;
                     if (tmin <= a.w) {
+                        if (kStats) ++rays;
                         const uint32_t pix = __float_as_uint(b.w);
                         uint32_t* out = record_hit ? S.shadow_bits + (size_t)slot * S.words + (pix >> 5)
                                                    : S.ao_bits + (size_t)(slot - S.shadow_slots) * S.words + (pix >> 5);
@@ -484,8 +490,8 @@ visibility_batch_kernel(const SceneVis* __restrict__ scenes, uint32_t n, const u
                     unsigned long long local = item - offsets[lo];
                     uint32_t slot = (uint32_t)(local / lit);
                     uint32_t j = (uint32_t)(local - (unsigned long long)slot * lit);
-                    if (kStats) ++rays;
                     active = setup_ray(r, c, S, C, slot, j);
+                    if (kStats && active) ++rays;
                 }
             }
         }

@@ -44,7 +44,8 @@ def load() -> C.CDLL:
             "oracle_gbuffer": (C.c_int, [P, P, P, C.c_uint32, C.c_uint32, C.c_uint32, P, P, P, P, P, P, C.c_int,
                                          C.c_uint32, C.c_uint32, P, P, C.c_uint32]),
             "oracle_visibility": (C.c_uint64, [P, P, P, C.c_uint32, P, P, C.c_uint32, C.c_uint32, C.c_uint32,
-                                               C.c_uint32, C.c_int, P, C.c_uint32, P, P, C.c_int, C.c_int]),
+                                               C.c_uint32, C.c_int, P, C.c_uint32, P, P, C.c_int, C.c_int,
+                                               C.c_int]),
             "oracle_light_pass": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32, P,
                                             C.c_int, C.c_uint32, C.c_uint32]),
             "oracle_light_pass_f64": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32,
@@ -204,13 +205,16 @@ class OracleFrame:
                               y0, self.H if y1 is None else y1, C.cast(ptrs, C.c_void_p), _p(dims), len(tex))
 
     def visibility(self, frame: int, bn: np.ndarray, y0: int = 0, y1: int | None = None, brute: bool = False,
-                   nthreads=None) -> int:
+                   nthreads=None, cull: bool = True) -> int:
+        """Shadow/AO bit planes. cull: leave out the shadow rays whose light has a zero
+        max(dot(N, L), 0) weight in the light pass, as the device does; False traces
+        every ray of light.frag. Returns the rays traced."""
         bn = np.ascontiguousarray(bn, np.uint8)
         y1 = self.H if y1 is None else y1
         return load().oracle_visibility(self.tlas.handle, scene_bytes(self.scene), C.cast(self.lights, C.c_void_p),
                                         self.nl, _p(self.normal), _p(self.depth), self.W, self.H, y0, y1, frame,
                                         _p(bn), bn.shape[0], _p(self.shadow_bits), _p(self.ao_bits),
-                                        nthreads or threads(), int(brute))
+                                        nthreads or threads(), int(brute), int(cull))
 
     def light_pass(self, ao_override=None, f64=False, nthreads=None, y0: int = 0, y1: int | None = None) -> np.ndarray:
         P_ = self.W * self.H

@@ -1522,11 +1522,14 @@ void oracle_render_shadow_maps(const oracle_tlas* ot, const luz_shadow_light* li
 void oracle_clear_shadow_maps() { g_shadow.clear(); }
 
 // Shadow + AO visibility bits for the pixel rows [y0, y1). brute != 0 uses the
-// all-triangles oracle instead of the BVH. Returns the number of rays traced.
+// all-triangles oracle instead of the BVH. cull != 0 leaves out (bit 0) the shadow
+// rays of a light whose max(dot(N, L), 0) weight in the light pass is 0, as the
+// device's ray generation does; cull = 0 traces every ray light.frag traces.
+// Returns the number of rays traced.
 uint64_t oracle_visibility(const oracle_tlas* ot, const luz_scene* S, const luz_light* lights, uint32_t nl,
                            const float* normal, const float* depth, uint32_t W, uint32_t H, uint32_t y0, uint32_t y1,
                            int frame, const uint8_t* bn, uint32_t bn_size, uint32_t* shadow_bits, uint32_t* ao_bits,
-                           int threads, int brute) {
+                           int threads, int brute, int cull) {
     const Tlas& T = ot->t;
     uint32_t words = (W * H + 31) / 32;
     Sampler smp{S->sampler, bn, bn_size, frame};
@@ -1549,6 +1552,13 @@ uint64_t oracle_visibility(const oracle_tlas* ot, const luz_scene* S, const luz_
                 v3 p = DepthToWorld(*S, pixel_uv(x, W), pixel_uv(y, H), depth[pix]);
                 uint32_t bit = 1u << (pix & 31);
                 for (uint32_t l = 0; l < nl; ++l) {
+                    if (cull && first[l + 1] > first[l]) {
+                        v3 lpos = {lights[l].position[0], lights[l].position[1], lights[l].position[2]};
+                        v3 ldir = {lights[l].direction[0], lights[l].direction[1], lights[l].direction[2]};
+                        v3 Ln = normalize(lpos - p);                                  // light.frag:194-195
+                        if (lights[l].type == LUZ_LIGHT_DIRECTIONAL) Ln = normalize(-ldir);
+                        if (!(dot(N, Ln) > 0.0f)) continue;                           // weight max(N.L, 0) = 0
+                    }
                     for (uint32_t s = 0; s < first[l + 1] - first[l]; ++s) {
                         float rx, ry;
                         smp.rg(x, y, (int)s, l + 1, &rx, &ry);

@@ -30,6 +30,30 @@ def test_bvh_anyhit_equals_bruteforce_spheres():
     assert np.array_equal(a.ao_bits, b.ao_bits)
 
 
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_culled_shadow_rays_leave_the_image_unchanged(cfg):
+    # Shadow rays of lights with max(dot(N, L), 0) = 0 are not traced (bit 0): the
+    # light pass weights them by that 0, so its output equals tracing every ray.
+    kw = dict(width=96, height=96) if cfg == 1 else dict(width=80, height=48, meshes=3, instances=60,
+                                                            subdivisions=3)
+    s = L.HostScene(cfg, **kw)
+    _, tl = oracle_scene(s)
+    b, lights, models = s.block(), s.lights(), s.models()
+    frames = []
+    for cull in (True, False):
+        f = O.OracleFrame(tl, b, lights, s.light_count, models, s.instance_count, s.width, s.height)
+        f.gbuffer()
+        n = f.visibility(0, L.blue_noise(), cull=cull)
+        frames.append((f, n, f.light_pass()))
+    (fc, nc, oc), (fa, na, oa) = frames
+    assert nc < na                                          # some rays were left out
+    assert np.array_equal(fc.ao_bits, fa.ao_bits)
+    assert not (fc.shadow_bits & ~fa.shadow_bits).any()     # culling only clears bits
+    assert (fc.shadow_bits != fa.shadow_bits).any()         # and some culled rays were occluded
+    same = (oc.view(np.uint32) == oa.view(np.uint32)) | (np.isnan(oc) & np.isnan(oa))
+    assert same.all()
+
+
 def test_random_rays_bvh_vs_bruteforce():
     s = L.HostScene(1, width=16, height=16)
     _, tl = oracle_scene(s)
