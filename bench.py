@@ -630,10 +630,10 @@ def run_ours(args, rank, world, local):
                                parallelism=f"replicas{world}" if world > 1 else "single"),
                 "rays_per_frame": rays_per_frame, "rays_traversed_per_frame": scene.width * scene.height + stats["rays"],
                 "rays_note": "rays_per_frame (the unit of value) counts the rays light.frag traces: primary "
-                             "+ lit pixels x (41 shadow + 16 AO). A shadow ray whose light has "
-                             "max(dot(N, L), 0) = 0 at the pixel is resolved at generation without "
-                             "traversal (the light pass weights it by 0, so the image is unchanged); "
-                             "rays_traversed_per_frame are the rays actually traced.",
+                             "+ lit pixels x (41 shadow + 16 AO). A shadow ray whose light's term in "
+                             "the light pass cannot depend on it (weight max(dot(N, L), 0) = 0 or zero "
+                             "unshadowed radiance) is resolved at generation without traversal, the "
+                             "image is unchanged; rays_traversed_per_frame are the rays actually traced.",
                 "lit_pixels": lit, "stage_ms": stage_ms,
                 "blas_build": {"ms": g.blas_build_ms, "triangles": g.blas_prims, "meshes": len(g.blas),
                                "note": "one batched device build, host->device vertex/index copies included"},

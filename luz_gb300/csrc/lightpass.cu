@@ -4,6 +4,7 @@
 #include <cstring>
 
 #include "internal.cuh"
+#include "raygen.cuh"
 #include "shadowmap.cuh"
 
 namespace luz {
@@ -116,22 +117,8 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     const V3 shadow_origin = p + N * fmax_(length(p - cam) * 0.01f, 0.05f);
     for (uint32_t i = 0; i < P.light_count; ++i) {
         const luz_light& lt = s_lights[i];
-        V3 lpos = V3{lt.position[0], lt.position[1], lt.position[2]};
-        V3 ldir = V3{lt.direction[0], lt.direction[1], lt.direction[2]};
-        V3 L = normalize(lpos - p);
-        float attenuation = 1.0f;
-        if (lt.type == LUZ_LIGHT_DIRECTIONAL) {
-            L = normalize(-ldir);
-        } else if (lt.type == LUZ_LIGHT_SPOT) {
-            float dist = length(lpos - p);
-            attenuation = 1.0f / (dist * dist);
-            float theta = dot(L, normalize(-ldir));
-            float epsilon = lt.inner_angle - lt.outer_angle;
-            attenuation *= clamp01((theta - lt.outer_angle) / epsilon);
-        } else if (lt.type == LUZ_LIGHT_POINT) {
-            float dist = length(lpos - p);
-            attenuation = 1.0f / (dist * dist);
-        }
+        const V3 L = light_vector(lt, p);                    // light.frag:194-198
+        const float attenuation = light_attenuation(lt, p, L);   // light.frag:199-208
         // EvaluateShadow (light.frag:137-169): ray-traced factor = hits / samples.
         float shadow = 1.0f;
         if (P.shadow_type == LUZ_SHADOW_RAYTRACING) {

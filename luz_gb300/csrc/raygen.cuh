@@ -15,6 +15,39 @@ __device__ __forceinline__ V3 light_vector(const luz_light& lt, V3 p) {
     return L;
 }
 
+// Attenuation of light.frag main (light.frag:196-208) given L = light_vector(lt, p):
+// 1 for directional lights, 1/d^2 for point lights, times the cone term for spots.
+__device__ __forceinline__ float light_attenuation(const luz_light& lt, V3 p, V3 L) {
+    V3 lpos = V3{lt.position[0], lt.position[1], lt.position[2]};
+    V3 ldir = V3{lt.direction[0], lt.direction[1], lt.direction[2]};
+    float attenuation = 1.0f;
+    if (lt.type == LUZ_LIGHT_SPOT) {
+        float dist = length(lpos - p);
+        attenuation = 1.0f / (dist * dist);
+        float theta = dot(L, normalize(-ldir));
+        float epsilon = lt.inner_angle - lt.outer_angle;
+        attenuation *= clamp01((theta - lt.outer_angle) / epsilon);
+    } else if (lt.type == LUZ_LIGHT_POINT) {
+        float dist = length(lpos - p);
+        attenuation = 1.0f / (dist * dist);
+    }
+    return attenuation;
+}
+
+// True when the light pass's contribution of this light cannot depend on its shadow
+// factor s: it adds ((kD * albedo / pi + spec) * radiance) * max(dot(N, L), 0) with
+// radiance = ((color * intensity) * attenuation) * (1 - s) (light.frag:209-226). If
+// the weight max(dot(N, L), 0) is 0 (dot <= 0 or NaN), or every channel of
+// (color * intensity) * attenuation is +-0 (radiance +-0 for every s in [0, 1]), the
+// sum takes the same value for every s (a +-0 term leaves Lo unchanged, a non-finite
+// factor gives NaN either way).
+__device__ __forceinline__ bool shadow_has_no_effect(const luz_light& lt, V3 p, V3 N, V3 L) {
+    if (!(dot(N, L) > 0.0f)) return true;
+    const float a = light_attenuation(lt, p, L);
+    const V3 c = (V3{lt.color[0], lt.color[1], lt.color[2]} * lt.intensity) * a;
+    return c.x == 0.0f && c.y == 0.0f && c.z == 0.0f;
+}
+
 // EvaluateShadow (light.frag:137-146) + TraceShadowRay (light.frag:86-109) for one
 // sample, given L = light_vector(lt, p): origin, direction and tMax of the shadow
 // ray; tMin is 0.001.

@@ -122,11 +122,10 @@ __device__ __forceinline__ bool gen_ray(const SceneVis& S, const VisCommon& C, u
         out = S.shadow_bits + (size_t)slot * S.words + (pix >> 5);
         record_hit = true;
         const V3 L = light_vector(S.lights[li], p);
-        // The light pass multiplies this light's shadowed radiance by
-        // max(dot(N, L), 0) with the same N and L (light.frag:209-226): at 0 (or NaN)
-        // the shadow factor cannot change the pixel, so the ray is not traced and
-        // its bit stays 0.
-        if (!(dot(N, L) > 0.0f)) return false;
+        // When the light pass's term of this light cannot depend on its shadow factor
+        // (zero weight max(dot(N, L), 0) or zero unshadowed radiance, computed as the
+        // light pass computes them), the ray is not traced and its bit stays 0.
+        if (shadow_has_no_effect(S.lights[li], p, N, L)) return false;
         sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)si, S.frame, li + 1, &rx, &ry);
         shadow_ray(S.lights[li], p, N, cam, rx, ry, L, wo, wd, tmax);
         tmin = 0.001f;

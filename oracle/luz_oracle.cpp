@@ -788,6 +788,43 @@ struct Planes {
     const float* ao_override;
 };
 
+// light.frag:194-198: the light vector L.
+template <typename T>
+static vec3<T> light_vector(const luz_light& lt, vec3<T> p) {
+    vec3<T> lpos = {(T)lt.position[0], (T)lt.position[1], (T)lt.position[2]};
+    vec3<T> ldir = {(T)lt.direction[0], (T)lt.direction[1], (T)lt.direction[2]};
+    vec3<T> L = normalize(lpos - p);
+    if (lt.type == LUZ_LIGHT_DIRECTIONAL) L = normalize(-ldir);
+    return L;
+}
+// light.frag:199-208: 1 (directional), 1/d^2 (point), 1/d^2 times the cone term (spot).
+template <typename T>
+static T light_attenuation(const luz_light& lt, vec3<T> p, vec3<T> L) {
+    vec3<T> lpos = {(T)lt.position[0], (T)lt.position[1], (T)lt.position[2]};
+    vec3<T> ldir = {(T)lt.direction[0], (T)lt.direction[1], (T)lt.direction[2]};
+    T attenuation = T(1);
+    if (lt.type == LUZ_LIGHT_SPOT) {
+        T dist = length(lpos - p);
+        attenuation = T(1) / (dist * dist);
+        T theta = dot(L, normalize(-ldir));
+        T epsilon = (T)lt.inner_angle - (T)lt.outer_angle;
+        attenuation *= tclamp01((theta - (T)lt.outer_angle) / epsilon);
+    } else if (lt.type == LUZ_LIGHT_POINT) {
+        T dist = length(lpos - p);
+        attenuation = T(1) / (dist * dist);
+    }
+    return attenuation;
+}
+// The light pass's term of this light cannot depend on its shadow factor: zero
+// weight max(dot(N, L), 0) or zero unshadowed radiance in every channel
+// (light.frag:209-226; the device's shadow_has_no_effect).
+static bool shadow_has_no_effect(const luz_light& lt, v3 p, v3 N, v3 L) {
+    if (!(dot(N, L) > 0.0f)) return true;
+    const float a = light_attenuation<float>(lt, p, L);
+    const v3 c = (v3{lt.color[0], lt.color[1], lt.color[2]} * lt.intensity) * a;
+    return c.x == 0.0f && c.y == 0.0f && c.z == 0.0f;
+}
+
 template <typename T>
 static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl, const std::vector<uint32_t>& first_slot,
                         const Planes& P, uint32_t W, uint32_t H, uint32_t words, uint32_t ao_n, uint32_t pix,
@@ -823,22 +860,8 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
     vec3<T> Lo = {T(0), T(0), T(0)};
     for (uint32_t i = 0; i < nl; ++i) {                                                    // light.frag:192
         const luz_light& lt = lights[i];
-        vec3<T> lpos = {(T)lt.position[0], (T)lt.position[1], (T)lt.position[2]};
-        vec3<T> ldir = {(T)lt.direction[0], (T)lt.direction[1], (T)lt.direction[2]};
-        vec3<T> L = normalize(lpos - fragPos);
-        T attenuation = T(1);
-        if (lt.type == LUZ_LIGHT_DIRECTIONAL) {
-            L = normalize(-ldir);
-        } else if (lt.type == LUZ_LIGHT_SPOT) {
-            T dist = length(lpos - fragPos);
-            attenuation = T(1) / (dist * dist);
-            T theta = dot(L, normalize(-ldir));
-            T epsilon = (T)lt.inner_angle - (T)lt.outer_angle;
-            attenuation *= tclamp01((theta - (T)lt.outer_angle) / epsilon);
-        } else if (lt.type == LUZ_LIGHT_POINT) {
-            T dist = length(lpos - fragPos);
-            attenuation = T(1) / (dist * dist);
-        }
+        vec3<T> L = light_vector<T>(lt, fragPos);                                           // light.frag:194-198
+        T attenuation = light_attenuation<T>(lt, fragPos, L);                                // light.frag:199-208
         T shadow = T(1);                                                                     // light.frag:166-167
         if (S.shadow_type == LUZ_SHADOW_RAYTRACING) {
             int ns = lt.num_shadow_samples;
@@ -1523,8 +1546,9 @@ void oracle_clear_shadow_maps() { g_shadow.clear(); }
 
 // Shadow + AO visibility bits for the pixel rows [y0, y1). brute != 0 uses the
 // all-triangles oracle instead of the BVH. cull != 0 leaves out (bit 0) the shadow
-// rays of a light whose max(dot(N, L), 0) weight in the light pass is 0, as the
-// device's ray generation does; cull = 0 traces every ray light.frag traces.
+// rays of a light whose term in the light pass cannot depend on its shadow factor
+// (shadow_has_no_effect), as the device's ray generation does; cull = 0 traces every
+// ray light.frag traces.
 // Returns the number of rays traced.
 uint64_t oracle_visibility(const oracle_tlas* ot, const luz_scene* S, const luz_light* lights, uint32_t nl,
                            const float* normal, const float* depth, uint32_t W, uint32_t H, uint32_t y0, uint32_t y1,
@@ -1552,13 +1576,9 @@ uint64_t oracle_visibility(const oracle_tlas* ot, const luz_scene* S, const luz_
                 v3 p = DepthToWorld(*S, pixel_uv(x, W), pixel_uv(y, H), depth[pix]);
                 uint32_t bit = 1u << (pix & 31);
                 for (uint32_t l = 0; l < nl; ++l) {
-                    if (cull && first[l + 1] > first[l]) {
-                        v3 lpos = {lights[l].position[0], lights[l].position[1], lights[l].position[2]};
-                        v3 ldir = {lights[l].direction[0], lights[l].direction[1], lights[l].direction[2]};
-                        v3 Ln = normalize(lpos - p);                                  // light.frag:194-195
-                        if (lights[l].type == LUZ_LIGHT_DIRECTIONAL) Ln = normalize(-ldir);
-                        if (!(dot(N, Ln) > 0.0f)) continue;                           // weight max(N.L, 0) = 0
-                    }
+                    if (cull && first[l + 1] > first[l] &&
+                        shadow_has_no_effect(lights[l], p, N, light_vector<float>(lights[l], p)))
+                        continue;
                     for (uint32_t s = 0; s < first[l + 1] - first[l]; ++s) {
                         float rx, ry;
                         smp.rg(x, y, (int)s, l + 1, &rx, &ry);
