@@ -431,7 +431,12 @@ def batched_uneven(ctx, stream, flush, K, W, count=64, seed=4004):
     b.render(0)
     st = b.stats(0)
     pixels = sum(sc.width * sc.height for sc in scenes)
-    rays = st["rays"] + pixels
+    # light.frag's rays (the unit of grays_per_s, as for the single frame) and the
+    # rays actually traversed
+    rays = pixels + sum(f.lit_count() * (sum(sc.lights()[i].num_shadow_samples for i in range(sc.light_count)) +
+                                         sc.block().ao_num_samples)
+                        for f, sc in zip(b.frames, scenes))
+    traversed = st["rays"] + pixels
     b.capture(0)
     for _ in range(W):
         b.replay()
@@ -449,7 +454,8 @@ def batched_uneven(ctx, stream, flush, K, W, count=64, seed=4004):
         raise RuntimeError("device status word raised in the batched workload")
     ms = statistics.mean(ts)
     out = {"scenes": count, "pixels": pixels, "instanced_triangles": b.triangles,
-           "blas_meshes": len(b.blas), "rays_per_replay": rays, "ms_per_replay": ms,
+           "blas_meshes": len(b.blas), "rays_per_replay": rays, "rays_traversed_per_replay": traversed,
+           "ms_per_replay": ms,
            "grays_per_s": rays / (ms * 1e-3) / 1e9, "graph": "one CUDA graph per batch frame",
            "autotuned_shape": tun, "autotune_best_visibility_ms": tune_ms,
            "host_generation_s": t_gen, "blas_build_and_setup_s": t_build}
