@@ -392,6 +392,7 @@ luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, 
     }
     f->max_map_index = max_map;
     f->h_scene = *scene;
+    f->surf_valid = false;   // the lit list's positions come from this scene's matrices
     f->light_count = light_count;
     f->model_count = model_count;
     f->shadow_slots = shadow_slots;
@@ -549,6 +550,7 @@ luz_status luz_frame_write(luz_ctx* ctx, luz_frame* f, int32_t plane, const void
     if (need == 0) return LUZ_OK;
     LUZ_CUDA(ctx, cudaMemcpyAsync(dst, src, need, cudaMemcpyHostToDevice, ctx->stream));
     LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (plane == LUZ_PLANE_NORMAL || plane == LUZ_PLANE_DEPTH) f->surf_valid = false;
     return LUZ_OK;
 }
 

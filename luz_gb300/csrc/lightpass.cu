@@ -1,6 +1,8 @@
 // lightpass.cu — the deferred light pass: light.frag main (light.frag:171-235) over
-// the G-buffer planes and the visibility bit planes, one thread per pixel, with
-// coalesced 128-bit loads of the RGBA32F normal and stores of the RGBA32F output.
+// the G-buffer planes and the visibility bit planes. Thread t shades the t-th lit
+// pixel of the compacted list the G-buffer pass wrote (world position and normal;
+// every lane of a warp runs the same light loop) and writes the background colour
+// of pixel t if that pixel is unlit.
 #include <cstring>
 
 #include "internal.cuh"
@@ -18,11 +20,12 @@ luz_status upload_srgb_lut(luz_ctx* ctx, const float* lut) {
 }
 
 struct LightParams {
+    const float4* surf;          // compacted lit pixels: (fragPos, pixel), (N, 0)
+    const uint32_t* lit_count;
     const uint32_t* albedo;
     const float4* normal;
     const uint32_t* material;
     const uint32_t* emission;
-    const float* depth;
     const uint32_t* shadow_bits;
     const uint32_t* ao_bits;
     const float* ao_denoised;
@@ -35,7 +38,6 @@ struct LightParams {
     int shadow_type;
     const DevShadowLight* shadow_lights;   // LUZ_SHADOW_MAP: per light, shadow_count of them
     uint32_t shadow_count;
-    float inverse_proj[16], inverse_view[16];
     float cam[3];
     float ambient[3];
     float ambient_intensity;
@@ -87,18 +89,26 @@ __device__ __forceinline__ uint32_t bit_at(const uint32_t* __restrict__ planes, 
 
 __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     extern __shared__ luz_light s_lights[];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lit = *P.lit_count;
+    const V3 amb = V3{P.ambient[0], P.ambient[1], P.ambient[2]};
+    // background (light.frag:178-181) of pixel t
+    if (t < P.width * P.height) {
+        float4 nb = P.normal[t];
+        if (length(V3{nb.x, nb.y, nb.z}) == 0.0f) {
+            V3 c = amb * P.ambient_intensity;
+            P.out[t] = make_float4(c.x, c.y, c.z, 1.0f);
+        }
+    }
+    if (blockIdx.x * blockDim.x >= lit) return;   // no lit pixel in this block
     for (uint32_t i = threadIdx.x; i < P.light_count; i += blockDim.x) s_lights[i] = P.lights[i];
     __syncthreads();
-    uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= P.width * P.height) return;
-    float4 nn = P.normal[pix];
-    V3 N = V3{nn.x, nn.y, nn.z};
-    V3 amb = V3{P.ambient[0], P.ambient[1], P.ambient[2]};
-    if (length(N) == 0.0f) {
-        V3 c = amb * P.ambient_intensity;
-        P.out[pix] = make_float4(c.x, c.y, c.z, 1.0f);
-        return;
-    }
+    if (t >= lit) return;
+    // lit pixel t: fragPos is the G-buffer pass's DepthToWorld of this pixel
+    // (light.frag:186), N its normal
+    const float4 s0 = __ldg(P.surf + 2 * (size_t)t), s1 = __ldg(P.surf + 2 * (size_t)t + 1);
+    const uint32_t pix = __float_as_uint(s0.w);
+    const V3 N = V3{s1.x, s1.y, s1.z};
     uint32_t a8 = P.albedo[pix], m8 = P.material[pix], e8 = P.emission[pix];
     V3 albedo = V3{c_srgb_lut[a8 & 0xFF], c_srgb_lut[(a8 >> 8) & 0xFF], c_srgb_lut[(a8 >> 16) & 0xFF]};
     float roughness = unorm8_to_float(m8 & 0xFF);
@@ -106,9 +116,7 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     float occlusion = unorm8_to_float((m8 >> 16) & 0xFF);
     V3 emission = V3{unorm8_to_float(e8 & 0xFF), unorm8_to_float((e8 >> 8) & 0xFF),
                      unorm8_to_float((e8 >> 16) & 0xFF)};
-    uint32_t x = pix % P.width, y = pix / P.width;
-    V3 p = depth_to_world(P.inverse_proj, P.inverse_view, pixel_uv(x, P.width), pixel_uv(y, P.height),
-                          P.depth[pix]);
+    const V3 p = V3{s0.x, s0.y, s0.z};
     V3 cam = V3{P.cam[0], P.cam[1], P.cam[2]};
     V3 V = normalize(cam - p);
     V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + albedo * metallic;
@@ -176,13 +184,18 @@ __global__ void __launch_bounds__(256) ao_resolve_kernel(const float4* normal, c
     ao[pix] = (float)misses / (float)samples;
 }
 
+luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f);
+
 luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
+    luz_status st = ensure_lit_list(ctx, f);
+    if (st != LUZ_OK) return st;
     LightParams P;
+    P.surf = f->surf;
+    P.lit_count = f->lit_count;
     P.albedo = f->albedo;
     P.normal = f->normal;
     P.material = f->material;
     P.emission = f->emission;
-    P.depth = f->depth;
     P.shadow_bits = f->shadow_bits;
     P.ao_bits = f->ao_bits;
     P.ao_denoised = f->ao_denoised;
@@ -195,8 +208,6 @@ luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
     P.shadow_type = f->h_scene.shadow_type;
     P.shadow_lights = f->d_shadow_lights;
     P.shadow_count = f->shadow_light_count;
-    memcpy(P.inverse_proj, f->h_scene.inverse_proj, 64);
-    memcpy(P.inverse_view, f->h_scene.inverse_view, 64);
     memcpy(P.cam, f->h_scene.cam_pos, 12);
     memcpy(P.ambient, f->h_scene.ambient_light_color, 12);
     P.ambient_intensity = f->h_scene.ambient_light_intensity;

@@ -331,6 +331,8 @@ __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, co
 }
 
 // ---------------------------------------------------------------- host launchers
+luz_status launch_lit_compaction(luz_ctx* ctx, luz_frame* f);
+
 luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
     GbufParams G;
     // 4-wide nodes; node_count (the binary count) bounds the 4-wide count and the
@@ -370,7 +372,12 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
     size_t smem = (size_t)std::min<uint32_t>(G.tlas_node_count, kSmemTlasNodes) * 128;
     gbuffer_kernel<<<tiles, 256, smem, ctx->stream>>>(G);
     LUZ_LAUNCHED(ctx, "gbuffer_kernel");
-    // compaction of lit pixels
+    return launch_lit_compaction(ctx, f);
+}
+
+// Compaction of the lit pixels (length(N) != 0) of the normal plane into the
+// (fragPos, pixel), (N, 0) list that ray generation and the light pass read.
+luz_status launch_lit_compaction(luz_ctx* ctx, luz_frame* f) {
     uint32_t chunks = (f->pixels + kChunk - 1) / kChunk;
     lit_count_kernel<<<chunks, 256, 0, ctx->stream>>>(f->normal, f->pixels, f->block_counts);
     LUZ_LAUNCHED(ctx, "lit_count_kernel");
@@ -382,7 +389,14 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
                                                       (const float*)((const char*)f->d_scene + offsetof(luz_scene, inverse_view)),
                                                       f->surf);
     LUZ_LAUNCHED(ctx, "lit_write_kernel");
+    f->surf_valid = true;
     return LUZ_OK;
+}
+
+// Rebuilds the lit-pixel list when the planes or scene constants it came from were
+// replaced since the last G-buffer pass (luz_frame_write, luz_frame_upload).
+luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f) {
+    return f->surf_valid ? LUZ_OK : launch_lit_compaction(ctx, f);
 }
 
 }  // namespace luz

@@ -569,10 +569,13 @@ luz_status clear_visibility(luz_ctx* ctx, luz_frame* f) {
     return LUZ_OK;
 }
 
+luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f);
+
 luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int frame_index,
                              unsigned long long* d_stats) {
     luz_status s = clear_visibility(ctx, f);
     if (s != LUZ_OK) return s;
+    if ((s = ensure_lit_list(ctx, f)) != LUZ_OK) return s;
     if (f->shadow_slots + f->ao_samples == 0) return LUZ_OK;
     cudaStream_t st = ctx->stream;
     SceneVis S = make_scene_vis(f, t, frame_index);
