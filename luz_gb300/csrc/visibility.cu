@@ -347,7 +347,7 @@ __device__ __forceinline__ void flush_stats(unsigned long long* stats, uint32_t 
 // Ray generation pass of one chunk: items [k0, k0 + chunk) of the frame's
 // (slot, lit pixel) list, slot-major, one record per item in structure-of-arrays
 // form: rays_a = (origin, tMax), rays_b = (direction, pixel). An item with no ray
-// gets tMax = -inf (its AO miss is recorded here). Separated from traversal so the
+// gets tMax = -inf (its AO miss is recorded here) and no rays_b entry. Separated from traversal so the
 // long arithmetic of light.frag's sampling runs on full warps, not on the few idle
 // lanes of a traversing warp. Also resets the traversal's work counter.
 __global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, unsigned long long k0,
@@ -376,7 +376,7 @@ __global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, un
         uint32_t pix;
         bool ok = gen_ray(S, C, slot, j, wo, wd, tmin, tmax, out, record_hit, pix);
         rays_a[item - k0] = make_float4(wo.x, wo.y, wo.z, ok ? tmax : ninf);
-        rays_b[item - k0] = make_float4(wd.x, wd.y, wd.z, __uint_as_float(pix));
+        if (ok) rays_b[item - k0] = make_float4(wd.x, wd.y, wd.z, __uint_as_float(pix));   // read only for rays
     }
 }
 
@@ -428,10 +428,11 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
                 if (local < n) {
                     uint32_t slot = slot0, j = j0 + rank;
                     while (j >= lit) { j -= lit; ++slot; }
-                    const float4 a = __ldg(rays_a + local), b = __ldg(rays_b + local);
+                    const float4 a = __ldg(rays_a + local);
                     const bool record_hit = slot < S.shadow_slots;
                     const float tmin = record_hit ? 0.001f : S.ao_min;
                     if (tmin <= a.w) {
+                        const float4 b = __ldg(rays_b + local);
                         if (kStats) ++rays;
                         const uint32_t pix = __float_as_uint(b.w);
                         uint32_t* out = record_hit ? S.shadow_bits + (size_t)slot * S.words + (pix >> 5)
