@@ -16,6 +16,7 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
                              unsigned long long* d_stats);
 luz_status frame_lit_count(luz_ctx* ctx, luz_frame* f, uint32_t* count);
 luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised);
+uint32_t lit_chunks(uint32_t width, uint32_t height);
 luz_status launch_ao_resolve(luz_ctx* ctx, luz_frame* f);
 luz_status upload_srgb_lut(luz_ctx* ctx, const float* lut);
 
@@ -292,7 +293,7 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     f->pixels = width * height;
     f->words = (f->pixels + 31) / 32;
     size_t P = f->pixels;
-    uint32_t chunks = (f->pixels + 1023) / 1024;
+    uint32_t chunks = lit_chunks(width, height);
     cudaError_t e = cudaSuccess;
     auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, std::max(bytes, (size_t)16)); };
     A((void**)&f->albedo, P * 4);

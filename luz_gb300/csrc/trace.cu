@@ -246,22 +246,34 @@ __global__ void __launch_bounds__(256) gbuffer_kernel(GbufParams G) {
 }
 
 // ---------------------------------------------------------------- lit-pixel compaction
-// A pixel is lit when length(N) != 0 (light.frag:178). Chunks of 1024 pixels;
-// the compacted order is the pixel order.
+// A pixel is lit when length(N) != 0 (light.frag:178). The list follows a tiled
+// order of the image — kLitTile x kLitTile pixel tiles in row order, pixels in row
+// order inside a tile — so the 32 rays a warp takes at once (32 neighbouring items of
+// one light) start from a compact patch of pixels rather than a 32-pixel row.
+// Chunks of 1024 positions of that order.
 constexpr int kChunk = 1024;
+constexpr uint32_t kLitTile = 4;   // measured at 1080p: 4x4 3.85 ms, 8x8 3.88, 16x16 3.94, rows 4.24
 
-__device__ __forceinline__ bool pixel_lit(const float4* normal, uint32_t pix, uint32_t n) {
-    if (pix >= n) return false;
+// Pixel at position o of the tiled order, or ~0u past the image.
+__device__ __forceinline__ uint32_t tiled_pixel(uint32_t o, uint32_t width, uint32_t height) {
+    const uint32_t tiles_x = (width + kLitTile - 1) / kLitTile;
+    const uint32_t tile = o / (kLitTile * kLitTile), w = o % (kLitTile * kLitTile);
+    const uint32_t x = (tile % tiles_x) * kLitTile + w % kLitTile, y = (tile / tiles_x) * kLitTile + w / kLitTile;
+    return (x < width && y < height) ? y * width + x : ~0u;
+}
+
+__device__ __forceinline__ bool pixel_lit(const float4* normal, uint32_t pix) {
+    if (pix == ~0u) return false;
     float4 v = normal[pix];
     return !(length(V3{v.x, v.y, v.z}) == 0.0f);
 }
 
-__global__ void __launch_bounds__(256) lit_count_kernel(const float4* normal, uint32_t n,
+__global__ void __launch_bounds__(256) lit_count_kernel(const float4* normal, uint32_t width, uint32_t height,
                                                         uint32_t* chunk_counts) {
     __shared__ uint32_t s_tmp[8];
     uint32_t base = blockIdx.x * kChunk + threadIdx.x * 4;
     uint32_t c = 0;
-    for (int k = 0; k < 4; ++k) c += pixel_lit(normal, base + k, n);
+    for (int k = 0; k < 4; ++k) c += pixel_lit(normal, tiled_pixel(base + k, width, height));
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, o);
     if ((threadIdx.x & 31) == 0) s_tmp[threadIdx.x >> 5] = c;
     __syncthreads();
@@ -312,15 +324,19 @@ __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, co
     __shared__ float s_ip[16], s_iv[16];
     if (threadIdx.x < 16) { s_ip[threadIdx.x] = inverse_proj[threadIdx.x]; s_iv[threadIdx.x] = inverse_view[threadIdx.x]; }
     __syncthreads();
-    uint32_t n = width * height;
     uint32_t base = blockIdx.x * kChunk + threadIdx.x * 4;
     bool lit[4];
+    uint32_t px[4];
     uint32_t c = 0;
-    for (int k = 0; k < 4; ++k) { lit[k] = pixel_lit(normal, base + k, n); c += lit[k]; }
+    for (int k = 0; k < 4; ++k) {
+        px[k] = tiled_pixel(base + k, width, height);
+        lit[k] = pixel_lit(normal, px[k]);
+        c += lit[k];
+    }
     uint32_t pos = chunk_offsets[blockIdx.x] + block_excl(c, s_tmp);
     for (int k = 0; k < 4; ++k) {
         if (!lit[k]) continue;
-        uint32_t pix = base + k;
+        uint32_t pix = px[k];
         uint32_t x = pix % width, y = pix / width;
         V3 p = depth_to_world(s_ip, s_iv, pixel_uv(x, width), pixel_uv(y, height), depth[pix]);
         float4 nn = normal[pix];
@@ -377,9 +393,15 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
 
 // Compaction of the lit pixels (length(N) != 0) of the normal plane into the
 // (fragPos, pixel), (N, 0) list that ray generation and the light pass read.
+uint32_t lit_chunks(uint32_t width, uint32_t height) {
+    const uint64_t positions = (uint64_t)((width + kLitTile - 1) / kLitTile) * ((height + kLitTile - 1) / kLitTile) *
+                               kLitTile * kLitTile;
+    return (uint32_t)((positions + kChunk - 1) / kChunk);
+}
+
 luz_status launch_lit_compaction(luz_ctx* ctx, luz_frame* f) {
-    uint32_t chunks = (f->pixels + kChunk - 1) / kChunk;
-    lit_count_kernel<<<chunks, 256, 0, ctx->stream>>>(f->normal, f->pixels, f->block_counts);
+    uint32_t chunks = lit_chunks(f->width, f->height);
+    lit_count_kernel<<<chunks, 256, 0, ctx->stream>>>(f->normal, f->width, f->height, f->block_counts);
     LUZ_LAUNCHED(ctx, "lit_count_kernel");
     lit_scan_kernel<<<1, 1024, 0, ctx->stream>>>(f->block_counts, chunks, f->lit_count);
     LUZ_LAUNCHED(ctx, "lit_scan_kernel");
