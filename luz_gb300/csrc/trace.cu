@@ -9,7 +9,11 @@
 
 namespace luz {
 
-constexpr int kSmemTlasNodes = 256;    // 32 KB of 4-wide TLAS top levels per CTA
+// 8x8 pixels per CTA of 64 threads, 16 CTAs per SM (64 registers): measured at
+// 1080p 0.65 ms against 0.75 ms for 16x16-pixel CTAs with the TLAS top staged in
+// shared memory (L1 holds it as well, and the CTAs retire at a finer grain).
+constexpr uint32_t kGbTile = 8;
+constexpr int kGbMinBlocks = 16;
 
 __device__ __forceinline__ uint32_t unorm8(float x) {
     return (uint32_t)(clamp01(x) * 255.0f + 0.5f);
@@ -34,12 +38,6 @@ __device__ __forceinline__ uint32_t block_excl(uint32_t v, uint32_t* s_tmp /*8*/
     return pre + x - v;
 }
 
-__device__ __forceinline__ void stage_tlas(const float4* __restrict__ g, uint32_t node_count,
-                                           float4* s, uint32_t& staged) {
-    staged = min(node_count, (uint32_t)kSmemTlasNodes);
-    for (uint32_t i = threadIdx.x; i < staged * kNode4F4; i += blockDim.x) s[i] = __ldg(g + i);
-    __syncthreads();
-}
 
 // ---------------------------------------------------------------- textures
 // Bilinear sample with repeat addressing of one RGBA8 UNORM level (the reference's
@@ -127,17 +125,14 @@ struct AlphaTest {
 };
 
 // opaque.vert:21-31 + opaque.frag:21-58 evaluated at the closest hit of the
-// pixel-centre ray. 16x16 pixel tiles per CTA.
-__global__ void __launch_bounds__(256) gbuffer_kernel(GbufParams G) {
-    extern __shared__ float4 s_nodes[];
-    uint32_t staged;
-    stage_tlas(G.tlas_nodes, G.tlas_node_count, s_nodes, staged);
-    uint32_t tiles_x = (G.width + 15) / 16;
+// pixel-centre ray. kGbTile x kGbTile pixel tiles per CTA.
+__global__ void __launch_bounds__(kGbTile * kGbTile, kGbMinBlocks) gbuffer_kernel(GbufParams G) {
+    uint32_t tiles_x = (G.width + kGbTile - 1) / kGbTile;
     uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    uint32_t x = tx * 16 + (threadIdx.x & 15), y = ty * 16 + (threadIdx.x >> 4);
+    uint32_t x = tx * kGbTile + (threadIdx.x % kGbTile), y = ty * kGbTile + (threadIdx.x / kGbTile);
     if (x >= G.width || y >= G.height) return;
     uint32_t pix = y * G.width + x;
-    TlasView T{G.tlas_nodes, s_nodes, staged, G.instances, G.instance_count};
+    TlasView T{G.tlas_nodes, G.instances, G.instance_count};
     float u = pixel_uv(x, G.width), v = pixel_uv(y, G.height);
     V3 cam = V3{G.cam[0], G.cam[1], G.cam[2]};
     V3 target = depth_to_world(G.inverse_proj, G.inverse_view, u, v, 1.0f);
@@ -378,15 +373,8 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
     G.texture_count = f->texture_count;
     if (f->max_map_index >= (int32_t)f->texture_count)
         return set_error(ctx, LUZ_ERR_INVALID, "a ModelBlock map index is beyond the frame's textures");
-    uint32_t tiles = ((f->width + 15) / 16) * ((f->height + 15) / 16);
-    static bool attr_set = false;
-    if (!attr_set) {
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(gbuffer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           kSmemTlasNodes * 128));
-        attr_set = true;
-    }
-    size_t smem = (size_t)std::min<uint32_t>(G.tlas_node_count, kSmemTlasNodes) * 128;
-    gbuffer_kernel<<<tiles, 256, smem, ctx->stream>>>(G);
+    uint32_t tiles = ((f->width + kGbTile - 1) / kGbTile) * ((f->height + kGbTile - 1) / kGbTile);
+    gbuffer_kernel<<<tiles, kGbTile * kGbTile, 0, ctx->stream>>>(G);
     LUZ_LAUNCHED(ctx, "gbuffer_kernel");
     return launch_lit_compaction(ctx, f);
 }

@@ -104,8 +104,6 @@ __device__ __forceinline__ int dir_signs(V3 idir) {
 
 struct TlasView {
     const float4* __restrict__ nodes;    // global 4-wide nodes
-    const float4* smem_nodes;            // first `smem_count` 4-wide nodes staged in shared memory
-    uint32_t smem_count;
     const DevInstance* __restrict__ instances;
     uint32_t count;
 };
@@ -161,11 +159,10 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
         bool pop = true;
         if (node >= 0) {
             if (kStats) { if (in_blas) cnt->blas_nodes++; else cnt->tlas_nodes++; }
-            const float4* np = (!in_blas && (uint32_t)node < T.smem_count) ? T.smem_nodes + (size_t)node * kNode4F4
-                                                                            : nodes + (size_t)node * kNode4F4;
+            const float4* np = nodes + (size_t)node * kNode4F4;
             const int sx = signs & 1, sy = (signs >> 1) & 1, sz = signs >> 2;
-            const float4 nx = np[sx], fx = np[sx ^ 1], ny = np[2 + sy], fy = np[3 - sy], nz = np[4 + sz],
-                         fz = np[5 - sz], cf = np[6];
+            const float4 nx = __ldg(np + sx), fx = __ldg(np + (sx ^ 1)), ny = __ldg(np + 2 + sy),
+                         fy = __ldg(np + 3 - sy), nz = __ldg(np + 4 + sz), fz = __ldg(np + 5 - sz), cf = __ldg(np + 6);
             int ch[4] = {__float_as_int(cf.x), __float_as_int(cf.y), __float_as_int(cf.z), __float_as_int(cf.w)};
             float tn[4];
             bool h[4];
