@@ -42,10 +42,11 @@ LUZ_HD V3 cross(V3 a, V3 b) {
     return V3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
 }
 LUZ_HD float length(V3 a) { return sqrtf(dot(a, a)); }
-// normalize(v) = v / length(v), componentwise IEEE division.
+// normalize(v) = v * (1 / length(v)): one IEEE division, as glm's
+// x * inversesqrt(dot(x, x)) form (the reciprocal here correctly rounded).
 LUZ_HD V3 normalize(V3 a) {
-    float l = length(a);
-    return V3{a.x / l, a.y / l, a.z / l};
+    float inv = 1.0f / length(a);
+    return V3{a.x * inv, a.y * inv, a.z * inv};
 }
 // min/max by comparison (not fminf/fmaxf): identical results for signed zeros and
 // NaN on every compiler, which the byte-exact BVH comparison relies on.

@@ -55,9 +55,9 @@ template <typename T> static inline vec3<T> cross(vec3<T> a, vec3<T> b) {
     return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
 }
 template <typename T> static inline T length(vec3<T> a) { return std::sqrt(dot(a, a)); }
-template <typename T> static inline vec3<T> normalize(vec3<T> a) {
-    T l = length(a);
-    return {a.x / l, a.y / l, a.z / l};
+template <typename T> static inline vec3<T> normalize(vec3<T> a) {   // pathmath.cuh normalize
+    T inv = T(1) / length(a);
+    return {a.x * inv, a.y * inv, a.z * inv};
 }
 template <typename T> static inline T tmax_(T a, T b) { return a > b ? a : b; }
 template <typename T> static inline T tmin_(T a, T b) { return a < b ? a : b; }
