@@ -304,14 +304,9 @@ __device__ __forceinline__ void write_inverted_slot(float4* node, int slot) {
 
 // seg_node_off: first internal node of each segment (global); sorted keys per segment
 // start at seg_prim_off. node_parent / leaf_parent: (local parent << 1) | side.
-__global__ void karras_kernel(const SegDesc* segs, const uint32_t* seg_node_off, int nseg,
-                              uint32_t total_nodes, const unsigned long long* keys,
-                              uint32_t* node_parent, uint32_t* leaf_parent, uint32_t* dev_status) {
-    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= total_nodes) return;
-    int s = find_seg(seg_node_off, nseg, q);
-    const SegDesc sd = segs[s];
-    int i = (int)(q - sd.node_off);
+// Internal node i of segment sd.
+__device__ __forceinline__ void karras_node(const SegDesc& sd, int i, const unsigned long long* keys,
+                                            uint32_t* node_parent, uint32_t* leaf_parent, uint32_t* dev_status) {
     int n = (int)sd.prim_count;
     float4* node = sd.nodes + (size_t)i * kNodeF4;
     if (n <= 1) {
@@ -353,6 +348,16 @@ __global__ void karras_kernel(const SegDesc* segs, const uint32_t* seg_node_off,
     node[3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
 }
 
+__global__ void karras_kernel(const SegDesc* segs, const uint32_t* seg_node_off, int nseg,
+                              uint32_t total_nodes, const unsigned long long* keys,
+                              uint32_t* node_parent, uint32_t* leaf_parent, uint32_t* dev_status) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= total_nodes) return;
+    int s = find_seg(seg_node_off, nseg, q);
+    const SegDesc sd = segs[s];
+    karras_node(sd, (int)(q - sd.node_off), keys, node_parent, leaf_parent, dev_status);
+}
+
 // ---------------------------------------------------------------- leaves + refit
 // BLAS: gather triangles into leaf order; padded leaf boxes; sorted morton/order.
 __global__ void blas_emit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
@@ -390,13 +395,13 @@ __device__ __forceinline__ void write_slot(float4* node, int slot, float4 lo, fl
     }
 }
 
-__global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
-                             uint32_t total, const float4* leaf_box, const uint32_t* node_parent,
-                             const uint32_t* leaf_parent, uint32_t* flags) {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= total) return;
-    int s = find_seg(seg_prim_off, nseg, g);
-    const SegDesc sd = segs[s];
+// Leaf g (global index) of segment sd: writes its box into its parent and climbs
+// while it is the second child to arrive. kBlock: every leaf of the tree is handled
+// by one CTA, so block-scope fences order the node writes.
+template <bool kBlock>
+__device__ __forceinline__ void refit_leaf(const SegDesc& sd, uint32_t g, const float4* leaf_box,
+                                           const uint32_t* node_parent, const uint32_t* leaf_parent,
+                                           uint32_t* flags) {
     float4 lo = leaf_box[2 * g], hi = leaf_box[2 * g + 1];
     uint32_t p = leaf_parent[g];
     const uint32_t node_count = sd.prim_count > 1 ? sd.prim_count - 1 : 1;
@@ -406,16 +411,25 @@ __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, 
         if (p == 0xFFFFFFFFu || local >= node_count) return;
         float4* node = sd.nodes + (size_t)local * kNodeF4;
         write_slot(node, p & 1, lo, hi);
-        __threadfence();
+        if (kBlock) __threadfence_block(); else __threadfence();
         uint32_t old = atomicAdd(flags + sd.node_off + local, 1u);
         if (old == 0) return;
-        __threadfence();
+        if (kBlock) __threadfence_block(); else __threadfence();
         float4 n0 = __ldcg(node + 0), n1 = __ldcg(node + 1), n2 = __ldcg(node + 2);
         lo = make_float4(fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z), 0.f);
         hi = make_float4(fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w), 0.f);
         p = node_parent[sd.node_off + local];
         if (p == 0xFFFFFFFFu) return;
     }
+}
+
+__global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
+                             uint32_t total, const float4* leaf_box, const uint32_t* node_parent,
+                             const uint32_t* leaf_parent, uint32_t* flags) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int s = find_seg(seg_prim_off, nseg, g);
+    refit_leaf<false>(segs[s], g, leaf_box, node_parent, leaf_parent, flags);
 }
 
 // ---------------------------------------------------------------- bounding sphere
@@ -611,8 +625,8 @@ __global__ void bvh4_emit_kernel(const SegDesc* segs, const uint32_t* seg_node_o
 
 // TLAS: the binary tree is in breadth-first order with level table
 // levels = {L, start_0, ..., start_L}; the 4-wide nodes are the even levels, in order.
-__global__ void __launch_bounds__(1024) tlas_bvh4_kernel(const float4* nodes, uint32_t m, const uint32_t* levels,
-                                                         float4* nodes4) {
+__device__ __forceinline__ void tlas_bvh4_block(const float4* nodes, uint32_t m, const uint32_t* levels,
+                                                float4* nodes4) {
     __shared__ uint32_t s_start[66], s_even[66];
     __shared__ uint32_t s_levels;
     if (threadIdx.x == 0) {
@@ -654,11 +668,16 @@ __global__ void __launch_bounds__(1024) tlas_bvh4_kernel(const float4* nodes, ui
     }
 }
 
+__global__ void __launch_bounds__(1024) tlas_bvh4_kernel(const float4* nodes, uint32_t m, const uint32_t* levels,
+                                                         float4* nodes4) {
+    tlas_bvh4_block(nodes, m, levels, nodes4);
+}
+
 // ---------------------------------------------------------------- TLAS
-__global__ void tlas_instance_kernel(const DevInstanceInput* in, uint32_t n, float4* inst_box,
-                                     DevShadeInstance* shade, uint32_t* seg_bounds) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// Instance i: shading record, padded world box; returns false when the box centre
+// is not finite (no contribution to the Morton bounds).
+__device__ __forceinline__ bool tlas_instance_one(const DevInstanceInput* in, uint32_t i, float4* inst_box,
+                                                  DevShadeInstance* shade, V3& c) {
     const DevInstanceInput ii = in[i];
     float w2o[12];
     affine_inverse(ii.o2w, w2o);
@@ -701,8 +720,16 @@ __global__ void tlas_instance_kernel(const DevInstanceInput* in, uint32_t n, flo
     }
     inst_box[2 * i] = make_float4(wlo.x, wlo.y, wlo.z, 0.f);
     inst_box[2 * i + 1] = make_float4(whi.x, whi.y, whi.z, 0.f);
-    V3 c = V3{(wlo.x + whi.x) * 0.5f + 0.0f, (wlo.y + whi.y) * 0.5f + 0.0f, (wlo.z + whi.z) * 0.5f + 0.0f};
-    if (!finite3(c)) return;
+    c = V3{(wlo.x + whi.x) * 0.5f + 0.0f, (wlo.y + whi.y) * 0.5f + 0.0f, (wlo.z + whi.z) * 0.5f + 0.0f};
+    return finite3(c);
+}
+
+__global__ void tlas_instance_kernel(const DevInstanceInput* in, uint32_t n, float4* inst_box,
+                                     DevShadeInstance* shade, uint32_t* seg_bounds) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V3 c;
+    if (!tlas_instance_one(in, i, inst_box, shade, c)) return;
     atomicMin(seg_bounds + 0, float_to_ordered(c.x));
     atomicMin(seg_bounds + 1, float_to_ordered(c.y));
     atomicMin(seg_bounds + 2, float_to_ordered(c.z));
@@ -730,14 +757,11 @@ __global__ void tlas_morton_kernel(const float4* inst_box, uint32_t n, const uin
     vals[i] = i;
 }
 
-__global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_box, uint32_t n,
-                                 const unsigned long long* keys, const uint32_t* vals,
-                                 DevInstance* inst_out, float4* leaf_box, uint32_t* morton_out,
-                                 uint32_t* order_out) {
-    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    uint32_t i = vals[j];
-    morton_out[j] = (uint32_t)keys[j] & 0x3FFFFFFFu;
+// Leaf j of the sorted order: instance record, leaf box, sorted Morton key and order.
+__device__ __forceinline__ void tlas_emit_one(const DevInstanceInput* in, const float4* inst_box, uint32_t j,
+                                              unsigned long long key, uint32_t i, DevInstance* inst_out,
+                                              float4* leaf_box, uint32_t* morton_out, uint32_t* order_out) {
+    morton_out[j] = (uint32_t)key & 0x3FFFFFFFu;
     order_out[j] = i;
     const DevInstanceInput ii = in[i];
     DevInstance d;
@@ -755,11 +779,20 @@ __global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_
     leaf_box[2 * j + 1] = inst_box[2 * i + 1];
 }
 
+__global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_box, uint32_t n,
+                                 const unsigned long long* keys, const uint32_t* vals,
+                                 DevInstance* inst_out, float4* leaf_box, uint32_t* morton_out,
+                                 uint32_t* order_out) {
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    tlas_emit_one(in, inst_box, j, keys[j], vals[j], inst_out, leaf_box, morton_out, order_out);
+}
+
+
 // Breadth-first relayout of one tree (single block of 1024 threads). Children of a
 // level keep their parents' order, left before right.
-__global__ void __launch_bounds__(1024)
-bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
-                    uint32_t* newidx, uint32_t* levels) {
+__device__ __forceinline__ void bfs_relayout_block(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
+                                                   uint32_t* newidx, uint32_t* levels) {
     __shared__ uint32_t s_warp[32];
     __shared__ uint32_t s_carry;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -832,6 +865,93 @@ bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
         d[2] = s[2];
         d[3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
     }
+}
+
+__global__ void __launch_bounds__(1024)
+bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
+                    uint32_t* newidx, uint32_t* levels) {
+    bfs_relayout_block(src, dst, m, queue, newidx, levels);
+}
+
+// The whole TLAS build in one CTA of 1024 threads for up to kFusedTlasMax instances
+// (the per-frame rebuild of GPUScene::UpdateResourcesGPU is otherwise a chain of ten
+// small launches): instance boxes and Morton bounds, Morton keys sorted with their
+// index in shared memory (bitonic network; the (key, index) order is the stable
+// order the radix sort gives), Karras hierarchy, leaves, refit, breadth-first
+// relayout and 4-wide collapse, separated by block barriers. Same results as the
+// multi-kernel path, bit for bit.
+constexpr uint32_t kFusedTlasMax = 4096;
+__global__ void __launch_bounds__(1024)
+tlas_fused_kernel(const DevInstanceInput* __restrict__ in, uint32_t n, float4* inst_box, DevShadeInstance* shade,
+                  unsigned long long* keys, uint32_t* vals, float4* karras_nodes, uint32_t* node_parent,
+                  uint32_t* leaf_parent, uint32_t* flags, DevInstance* inst_out, float4* leaf_box,
+                  uint32_t* morton_out, uint32_t* order_out, float4* nodes_out, uint32_t* queue, uint32_t* newidx,
+                  uint32_t* levels, float4* nodes4, uint32_t* dev_status) {
+    __shared__ unsigned long long s_keys[kFusedTlasMax];
+    __shared__ uint32_t s_bounds[6];
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t m = max(n, 2u) - 1;
+    if (tid < 6) s_bounds[tid] = tid < 3 ? 0xFFFFFFFFu : 0u;
+    for (uint32_t q = tid; q < m; q += nt) { node_parent[q] = 0xFFFFFFFFu; flags[q] = 0u; }
+    for (uint32_t g = tid; g < n; g += nt) leaf_parent[g] = 0xFFFFFFFFu;
+    __syncthreads();
+    for (uint32_t i = tid; i < n; i += nt) {
+        V3 c;
+        if (!tlas_instance_one(in, i, inst_box, shade, c)) continue;
+        atomicMin(s_bounds + 0, float_to_ordered(c.x));
+        atomicMin(s_bounds + 1, float_to_ordered(c.y));
+        atomicMin(s_bounds + 2, float_to_ordered(c.z));
+        atomicMax(s_bounds + 3, float_to_ordered(c.x));
+        atomicMax(s_bounds + 4, float_to_ordered(c.y));
+        atomicMax(s_bounds + 5, float_to_ordered(c.z));
+    }
+    __syncthreads();
+    uint32_t P = 1;
+    while (P < n) P <<= 1;
+    {
+        V3 cmin, ext;
+        decode_bounds(s_bounds, cmin, ext);
+        for (uint32_t i = tid; i < P; i += nt) {
+            if (i < n) {
+                const float4 l = inst_box[2 * i], h = inst_box[2 * i + 1];
+                const unsigned long long key = morton30(V3{l.x, l.y, l.z}, V3{h.x, h.y, h.z}, cmin, ext);
+                s_keys[i] = (key << 32) | i;
+            } else {
+                s_keys[i] = ~0ull;
+            }
+        }
+    }
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = tid; i < P; i += nt) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = s_keys[i], b = s_keys[ixj];
+                    if ((a > b) == ((i & k) == 0)) { s_keys[i] = b; s_keys[ixj] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t j = tid; j < n; j += nt) {
+        keys[j] = s_keys[j] >> 32;
+        vals[j] = (uint32_t)s_keys[j];
+    }
+    __syncthreads();
+    SegDesc sd{};
+    sd.prim_count = n;
+    sd.nodes = karras_nodes;
+    for (uint32_t q = tid; q < m; q += nt) karras_node(sd, (int)q, keys, node_parent, leaf_parent, dev_status);
+    __syncthreads();
+    for (uint32_t j = tid; j < n; j += nt)
+        tlas_emit_one(in, inst_box, j, keys[j], vals[j], inst_out, leaf_box, morton_out, order_out);
+    __syncthreads();
+    for (uint32_t g = tid; g < n; g += nt) refit_leaf<true>(sd, g, leaf_box, node_parent, leaf_parent, flags);
+    __syncthreads();
+    bfs_relayout_block(karras_nodes, nodes_out, m, queue, newidx, levels);
+    __syncthreads();
+    tlas_bvh4_block(nodes_out, m, levels, nodes4);
 }
 
 // ---------------------------------------------------------------- host drivers
@@ -1186,6 +1306,13 @@ luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t) {
     SegDesc* d_seg = (SegDesc*)p; p += align256(sizeof(SegDesc));
     uint32_t* d_zero = (uint32_t*)p; p += align256(4);
 
+    if (n <= kFusedTlasMax) {
+        tlas_fused_kernel<<<1, 1024, 0, st>>>(t->d_input, n, inst_box, t->shade, sb.keys[0], sb.vals[0], karras_nodes,
+                                              node_parent, leaf_parent, flags, t->instances, leaf_box, t->morton,
+                                              t->order, t->nodes, queue, newidx, t->levels, t->nodes4, ctx->d_status);
+        LUZ_LAUNCHED(ctx, "tlas_fused_kernel");
+        return LUZ_OK;
+    }
     SegDesc sd{};
     sd.prim_off = 0;
     sd.prim_count = n;
