@@ -53,8 +53,10 @@ def test_blas_batch_icospheres_bit_exact(ctx):
         assert np.array_equal(gt.view(np.uint32), ot.view(np.uint32))
 
 
-def test_tlas_bit_exact(ctx):
-    s = L.HostScene(2, width=64, height=36, meshes=4, instances=300, subdivisions=3)
+@pytest.mark.parametrize("instances", [1, 2, 300, 4096, 5000])
+def test_tlas_bit_exact(ctx, instances):
+    # up to 4096 instances: the single-CTA build; above: the multi-kernel build
+    s = L.HostScene(2, width=64, height=36, meshes=4, instances=instances, subdivisions=3 if instances <= 300 else 1)
     g = L.GPUScene(ctx, s)
     g.update_resources_gpu()
     gn, gm, go = g.tlas.download()
