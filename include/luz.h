@@ -145,7 +145,10 @@ typedef struct luz_frame luz_frame;
 /* VkAccelerationStructureInstanceKHR as filled by vkw::CmdBuildTLAS
  * (source/Graphics/VulkanWrapper.cpp:1111-1126): 3x4 row-major object-to-world
  * transform (rows = the first three rows of modelMat), custom index = modelRID,
- * mask 0xFF, triangle facing cull disabled (every traversal here is two-sided). */
+ * mask 0xFF, triangle facing cull disabled (every traversal here is two-sided). Rays
+ * use cull mask 0xFF (light.frag:100,126), so an instance whose mask has none of
+ * the low eight bits set is invisible to the G-buffer, shadow and AO rays (shadow
+ * maps, a raster pass in the reference, draw every instance). */
 typedef struct luz_instance {
     const luz_blas* blas;
     float transform[3][4];

@@ -460,7 +460,10 @@ luz_status luz_trace_visibility_stats(luz_ctx* ctx, luz_frame* f, const luz_tlas
     if (!ctx || !f || !t || !out) return LUZ_ERR_INVALID;
     unsigned long long* d = nullptr;
     LUZ_CUDA(ctx, cudaMalloc(&d, 5 * sizeof(unsigned long long)));
-    luz_status s = launch_visibility(ctx, f, t, frame_index, d);
+    luz_status s = LUZ_OK;
+    cudaError_t z = cudaMemsetAsync(d, 0, 5 * sizeof(unsigned long long), ctx->stream);   // zero when nothing is traced
+    if (z != cudaSuccess) s = cuda_error(ctx, z, "stats clear");
+    if (s == LUZ_OK) s = launch_visibility(ctx, f, t, frame_index, d);
     if (s == LUZ_OK) {
         cudaError_t e = cudaMemcpyAsync(out, d, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);

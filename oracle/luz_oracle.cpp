@@ -553,6 +553,9 @@ static bool trace(const Tlas& T, v3 o, v3 d, float tmin, float tmax, const uint8
             if (!slab(get_slot(node, c), o, id, tmin, tmax, tn)) continue;
             if (ch >= 0) { stack[sp++] = ch; continue; }
             const Instance& I = T.inst[~ch];
+            // the rays' cull mask is 0xFF (light.frag:100,126): an instance whose mask
+            // shares no bit with it is invisible
+            if ((I.mask & 0xFFu) == 0) continue;
             const bool tested = kClosest && skip && I.custom < skip_n && skip[I.custom] == 2;
             if (kClosest && skip && I.custom < skip_n && skip[I.custom] == 1) continue;
             v3 oo = xpoint(I.w2o, o), od = xdir(I.w2o, d);
@@ -568,6 +571,7 @@ static bool trace(const Tlas& T, v3 o, v3 d, float tmin, float tmax, const uint8
 static bool trace_bruteforce(const Tlas& T, v3 o, v3 d, float tmin, float tmax) {
     if (!ray_ok(o, d, tmin, tmax)) return false;
     for (const Instance& I : T.by_input) {
+        if ((I.mask & 0xFFu) == 0) continue;   // invisible to the 0xFF cull mask
         const Blas& b = *I.blas;
         v3 oo = xpoint(I.w2o, o), od = xdir(I.w2o, d);
         WtRay wt = wt_setup(oo, od);
