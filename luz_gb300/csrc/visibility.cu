@@ -39,13 +39,17 @@ constexpr uint32_t kRayStepCap = 1u << 22;
 // Ray state that traversal touches only when it enters or leaves a BLAS, tests a
 // triangle or finishes lives in shared memory, one 32-bit field per row of
 // kVisThreads entries (conflict-free): world origin and direction, the output word
-// and bit, and the watertight shear of the current BLAS.
+// and bit, the watertight shear and origin of the current BLAS, and the world-space
+// box-test state restored when the ray leaves a BLAS.
 enum ColdField : int {
     kWoX, kWoY, kWoZ, kWdX, kWdY, kWdZ,
     kOutLo, kOutHi, kOutBits,     // bit | record_hit << 5
     kWtK, kWtSx, kWtSy, kWtSz,    // kx | ky << 2 | kz << 4; shear
     kBtLo, kBtHi,                 // triangles of the current BLAS
     kOoX, kOoY, kOoZ,             // origin in the current BLAS's object space
+    kWiX, kWiY, kWiZ,             // world inverse direction and origin offsets, restored on
+    kWnX, kWnY, kWnZ,             // the way out of a BLAS
+    kWfX, kWfY, kWfZ,
     kColdFields
 };
 constexpr size_t kColdBytes = (size_t)kColdFields * kVisThreads * 4;
@@ -159,6 +163,9 @@ __device__ __forceinline__ void start_ray(LaneRay& r, const Cold& c, const Scene
     r.idir = safe_inv(wd);
     set_origin(r, wo);
     near_planes(r);
+    c[kWiX] = r.idir.x; c[kWiY] = r.idir.y; c[kWiZ] = r.idir.z;
+    c[kWnX] = r.on.x; c[kWnY] = r.on.y; c[kWnZ] = r.on.z;
+    c[kWfX] = r.of.x; c[kWfY] = r.of.y; c[kWfZ] = r.of.z;
     r.node = 0;
     r.sp = 0;
     r.in_blas = false;
@@ -324,8 +331,9 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
             if (v == kStackMarker) {
                 r.in_blas = false;
                 r.nb = tlas;
-                r.idir = safe_inv(c.wd());
-                set_origin(r, c.wo());
+                r.idir = V3{c[kWiX], c[kWiY], c[kWiZ]};
+                r.on = V3{c[kWnX], c[kWnY], c[kWnZ]};
+                r.of = V3{c[kWfX], c[kWfY], c[kWfZ]};
                 near_planes(r);
                 continue;
             }
