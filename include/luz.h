@@ -304,7 +304,8 @@ luz_status luz_tlas_memory(const luz_tlas* tlas, luz_memory* out);
 /* ------------------------------------------------------------------ frame
  * A luz_frame owns the per-resolution images of DeferredRenderer::CreateImages
  * (source/Graphics/DeferredRenderer.cpp:175-248) plus the visibility planes and the
- * device copies of SceneBlock/ModelBlock/lights (GPUScene.cpp:348-353). */
+ * device copies of SceneBlock/ModelBlock/lights (GPUScene.cpp:348-353). At most
+ * 65535 pixels wide or high and 2^27 pixels in all (LUZ_ERR_LIMIT beyond). */
 luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_frame** out);
 void luz_frame_destroy(luz_frame* frame);
 /* Host→device copy of the scene constants, lights and model blocks; mirrors the two

@@ -286,6 +286,8 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     if (!ctx || !out || width == 0 || height == 0) return LUZ_ERR_INVALID;
     if ((uint64_t)width * height > (1ull << 27))
         return set_error(ctx, LUZ_ERR_LIMIT, "frame larger than 2^27 pixels");
+    if (width > 65535 || height > 65535)   // lit-pixel records carry x | y << 16
+        return set_error(ctx, LUZ_ERR_LIMIT, "frame wider or taller than 65535 pixels");
     luz_frame* f = new luz_frame();
     f->ctx = ctx;
     f->width = width;

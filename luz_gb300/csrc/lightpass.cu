@@ -20,7 +20,7 @@ luz_status upload_srgb_lut(luz_ctx* ctx, const float* lut) {
 }
 
 struct LightParams {
-    const float4* surf;          // compacted lit pixels: (fragPos, pixel), (N, 0)
+    const float4* surf;          // compacted lit pixels: (fragPos, pixel), (N, x | y << 16)
     const uint32_t* lit_count;
     const uint32_t* albedo;
     const float4* normal;

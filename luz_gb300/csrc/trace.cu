@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, co
         V3 p = depth_to_world(s_ip, s_iv, pixel_uv(x, width), pixel_uv(y, height), depth[pix]);
         float4 nn = normal[pix];
         surf[2 * (size_t)pos] = make_float4(p.x, p.y, p.z, __uint_as_float(pix));
-        surf[2 * (size_t)pos + 1] = make_float4(nn.x, nn.y, nn.z, 0.f);
+        surf[2 * (size_t)pos + 1] = make_float4(nn.x, nn.y, nn.z, __uint_as_float(x | (y << 16)));
         ++pos;
     }
 }
@@ -380,7 +380,7 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
 }
 
 // Compaction of the lit pixels (length(N) != 0) of the normal plane into the
-// (fragPos, pixel), (N, 0) list that ray generation and the light pass read.
+// (fragPos, pixel), (N, x | y << 16) list that ray generation and the light pass read.
 uint32_t lit_chunks(uint32_t width, uint32_t height) {
     const uint64_t positions = (uint64_t)((width + kLitTile - 1) / kLitTile) * ((height + kLitTile - 1) / kLitTile) *
                                kLitTile * kLitTile;

@@ -117,7 +117,8 @@ __device__ __forceinline__ bool gen_ray(const SceneVis& S, const VisCommon& C, u
     float4 s0 = __ldg(S.surf + 2 * (size_t)j), s1 = __ldg(S.surf + 2 * (size_t)j + 1);
     V3 p = V3{s0.x, s0.y, s0.z}, N = V3{s1.x, s1.y, s1.z};
     pix = __float_as_uint(s0.w);
-    uint32_t px = pix % S.width, py = pix / S.width;
+    const uint32_t pxy = __float_as_uint(s1.w);   // x | y << 16 of the lit pixel
+    const uint32_t px = pxy & 0xFFFFu, py = pxy >> 16;
     V3 cam = V3{S.cam[0], S.cam[1], S.cam[2]};
     float rx, ry;
     if (slot < S.shadow_slots) {
