@@ -52,6 +52,20 @@ LUZ_HD V3 normalize(V3 a) {
 // NaN on every compiler, which the byte-exact BVH comparison relies on.
 LUZ_HD float fmin_(float a, float b) { return a < b ? a : b; }
 LUZ_HD float fmax_(float a, float b) { return a > b ? a : b; }
+
+// Repeat addressing (the reference's sampler, VulkanWrapper.cpp:2429-2454) of an
+// integer-valued float texel coordinate f (a floor result) into [0, n): the same
+// value as fmodf(f, n) (+ n when negative), without the division for |f| < n, which
+// covers every coordinate of a texture coordinate in [-1, 2).
+LUZ_HD uint32_t repeat_index(float f, uint32_t n) {
+    const float nf = (float)n;
+    if (f >= 0.0f && f < nf) return (uint32_t)f;
+    if (f < 0.0f && f >= -nf) return (uint32_t)(f + nf);   // exact: integers below 2^24
+    float m = fmodf(f, nf);
+    if (m < 0.0f) m += nf;
+    uint32_t i = (uint32_t)m;
+    return i < n ? i : 0u;
+}
 LUZ_HD float clamp01(float x) { return fmin_(fmax_(x, 0.0f), 1.0f); }
 LUZ_HD float fract_(float x) { return x - floorf(x); }
 LUZ_HD bool finite3(V3 a) { return isfinite(a.x) && isfinite(a.y) && isfinite(a.z); }

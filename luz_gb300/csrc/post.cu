@@ -29,12 +29,7 @@ __device__ __forceinline__ float4 div4(float4 a, float s) { return make_float4(a
 __device__ __forceinline__ bool anynan4(float4 a) { return isnan(a.x) || isnan(a.y) || isnan(a.z) || isnan(a.w); }
 
 // ---------------------------------------------------------------- sampling
-__device__ __forceinline__ uint32_t wrap_texel(float f, uint32_t n) {
-    float m = fmodf(f, (float)n);
-    if (m < 0.0f) m += (float)n;
-    uint32_t i = (uint32_t)m;
-    return i < n ? i : 0u;
-}
+__device__ __forceinline__ uint32_t wrap_texel(float f, uint32_t n) { return repeat_index(f, n); }
 
 struct Bilinear {
     uint32_t x0, x1, y0, y1;

@@ -6,12 +6,7 @@
 
 namespace luz {
 
-__device__ __forceinline__ uint32_t sm_wrap(float f, uint32_t n) {
-    float m = fmodf(f, (float)n);
-    if (m < 0.0f) m += (float)n;
-    uint32_t i = (uint32_t)m;
-    return i < n ? i : 0u;
-}
+__device__ __forceinline__ uint32_t sm_wrap(float f, uint32_t n) { return repeat_index(f, n); }
 
 __device__ __forceinline__ uint32_t sm_clamp(float f, uint32_t n) {
     if (!(f > 0.0f)) return 0u;

@@ -43,12 +43,7 @@ __device__ __forceinline__ uint32_t block_excl(uint32_t v, uint32_t* s_tmp /*8*/
 // Bilinear sample with repeat addressing of one RGBA8 UNORM level (the reference's
 // sampler, VulkanWrapper.cpp:2429-2454): texel centres at (i + 0.5) / size, weights
 // from the fractional part, texels as c / 255.
-__device__ __forceinline__ uint32_t tex_wrap(float f, uint32_t n) {
-    float m = fmodf(f, (float)n);   // exact
-    if (m < 0.0f) m += (float)n;
-    uint32_t i = (uint32_t)m;
-    return i < n ? i : 0u;
-}
+__device__ __forceinline__ uint32_t tex_wrap(float f, uint32_t n) { return repeat_index(f, n); }
 
 __device__ __forceinline__ float4 tex_texel(const DevTexture& t, uint32_t x, uint32_t y) {
     uint32_t c = __ldg(t.texels + (size_t)y * t.width + x);
