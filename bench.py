@@ -18,8 +18,9 @@ L2). e2e: the same frame through the C ABI from pinned host buffers — scene,
 light and model blocks and the instance array copied host->device, the RGBA32F
 light image read back — timed on the host around the synchronised call.
 
---impl reference runs the reference path's CPU restatement (the oracle) on all
-host cores over a bounded row sample of the same frame.
+--impl reference runs the reference path's CPU restatement (the oracle, tracing
+every ray light.frag traces) on all host cores over the same frame (each step one
+whole frame; --cpu-rows bounds it to a band of rows).
 """
 from __future__ import annotations
 
@@ -53,7 +54,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-rows", type=int, default=24, help="rows of the CPU baseline sample")
+    ap.add_argument("--cpu-rows", type=int, default=1080,
+                    help="rows of the CPU baseline sample (default: the whole 1080-row frame)")
     ap.add_argument("--width", type=int, default=1920, help="smaller sizes only for profiling captures")
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--no-cpu", action="store_true")
@@ -140,7 +142,8 @@ class Clocks:
 
 # ---------------------------------------------------------------------------- CPU baseline
 def cpu_baseline(scene, rows: int, repeats: int = 1):
-    """Oracle frame over a bounded band of rows at the image centre, all host cores."""
+    """Oracle frame (by default all of it; else a band of rows at the image centre) on
+    all host cores, `repeats` times; the BLAS build is not timed."""
     import numpy as np
 
     import luz_gb300 as L
@@ -182,7 +185,8 @@ def cpu_baseline(scene, rows: int, repeats: int = 1):
     lit1 = int((np.linalg.norm(f.normal[y0 * W:(y0 + 2) * W, :3], axis=1) > 0).sum())
     single = (2 * W + lit1 * S) / dt1 / 1e9
     return {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "single_thread_value": single,
-            "sample": f"rows {y0}-{y1} of 1920x1080 ({(y1 - y0) * W} px, {rays_list[0]} rays per sample): "
+            "sample": f"rows {y0}-{y1} of 1920x1080 ({(y1 - y0) * W} px, {rays_list[0]} rays per sample, "
+                      f"{len(times)} samples): "
                       f"TLAS build + G-buffer + shadow/AO any-hit + light pass; BLAS build untimed; "
                       f"single_thread_value: rows {y0}-{y0 + 2} on one core, TLAS build untimed"}, times
 
@@ -638,7 +642,7 @@ def run_ours(args, rank, world, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu, _ = cpu_baseline(scene, args.cpu_rows)
+        cpu, _ = cpu_baseline(scene, args.cpu_rows, repeats=3)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
