@@ -312,14 +312,15 @@ def denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=16, curve_spp=(1, 
     setup(restore_ao, shadow_spp)   # back to the benchmark's sampling
     sc.set_sampling(restore_ao, light_samples=1, sampler=L.SAMPLER_PARITY)
     fr.upload(sc.block(), sc.lights(), sc.light_count, sc.models(), sc.instance_count)
-    flops = 2.0 * (72 * 64 + 64 * 64 + 64 * 64 + 64 * 49) * fr.width * fr.height
+    lit = fr.lit_count()   # the frame path filters the lit pixels only
+    flops = 2.0 * (72 * 64 + 64 * 64 + 64 * 64 + 64 * 49) * lit
     return {"rmse_vs_1024spp": {"denoised_1spp": r_den, "plain": {str(k): v for k, v in sorted(curve.items())}},
             "equal_rmse_spp": n_star,
             "ms_per_frame_denoised": ms_den, "ms_per_frame_plain_equal_rmse": ms_plain,
             "frame_speedup": ms_plain / ms_den,
             "ao_only": {"ms_denoised_1spp": ms_ao_den, "ms_plain_equal_rmse": ms_ao_plain,
                         "speedup": ms_ao_plain / ms_ao_den},
-            "denoiser_ms": ms_denoise_only,
+            "denoiser_ms": ms_denoise_only, "denoised_pixels": lit,
             "denoiser_tflops_bf16": flops / (ms_denoise_only * 1e-3) / 1e12,
             "shadow_rays_per_light": shadow_spp, "sampler": "stratified (8x8-block R2)",
             "weights": D.DEFAULT_WEIGHTS.name}

@@ -42,7 +42,8 @@ enum {
     LUZ_DEV_KARRAS_RANGE = 1u << 3,
     LUZ_DEV_BATCH_QUEUE = 1u << 4,
     LUZ_DEV_BAD_INDEX = 1u << 5,
-    LUZ_DEV_RASTER_OVERFLOW = 1u << 6
+    LUZ_DEV_RASTER_OVERFLOW = 1u << 6,
+    LUZ_DEV_MMA_WAIT = 1u << 7          /* a tensor-core product did not complete in time */
 };
 
 /* ------------------------------------------------------------------ limits */

@@ -39,7 +39,6 @@ constexpr int pW4 = pW3 + 64 * sW;
 constexpr int pW2T = pW4 + 56 * sW;     // transposed copies for the backward pass: [in][out]
 constexpr int pW3T = pW2T + 64 * sW;
 constexpr int pW4T = pW3T + 64 * sW;
-constexpr int pFwdEnd = pW2T;           // what inference needs
 constexpr int pEnd = pW4T + 64 * sW;
 constexpr int kBias = 64 + 64 + 64 + 56;   // b1 | b2 | b3 | b4 (padded)
 constexpr int kTile = 128;                 // pixels per CTA tile (8 warps x 16)
@@ -75,6 +74,7 @@ struct FeatParams {
     uint4* feat;       // 8 x bf16 per pixel
     float* lin_depth;  // distance to the camera (0 = background)
     float* ao;         // noisy AO value
+    float* denoised;   // if set: 0 written here for background pixels (the denoiser skips them)
 };
 
 __constant__ float c_lin_lut[256];   // pow(i/255, 2.2)
@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
         F.feat[pix] = make_uint4(0, 0, 0, 0);
         F.lin_depth[pix] = 0.0f;
         F.ao[pix] = 0.0f;
+        if (F.denoised) F.denoised[pix] = 0.0f;
         return;
     }
     uint32_t w = pix >> 5, bit = 1u << (pix & 31);
@@ -125,6 +126,12 @@ struct ImageGeom {
     uint32_t images;
 };
 
+// Depth of a neighbour relative to the centre, (d_q - d_p) / d_p clamped to [-1, 1],
+// from the centre's reciprocal.
+__device__ __forceinline__ float relative_depth(float dq, float dc, float inv_dc) {
+    return fminf(fmaxf((dq - dc) * inv_dc, -1.0f), 1.0f);
+}
+
 // Gathers the 16 x 80 feature tile of a warp into `stage` ([16][sW1] bf16) for the
 // pixels base..base+15 (global index over images). Invalid pixels get zeros.
 __device__ __forceinline__ void gather_tile(const uint4* __restrict__ feat, const float* __restrict__ ld,
@@ -147,7 +154,7 @@ __device__ __forceinline__ void gather_tile(const uint4* __restrict__ feat, cons
                 uint32_t q = img * G.pixels + (uint32_t)qy * G.width + (uint32_t)qx;
                 v = feat[q];
                 float dq = ld[q];
-                float rel = dq > 0.0f ? fminf(fmaxf((dq - dc) / dc, -1.0f), 1.0f) : 0.0f;
+                float rel = dq > 0.0f ? relative_depth(dq, dc, 1.0f / dc) : 0.0f;
                 // channel 5 (upper half of v.z) carries the relative depth
                 v.z = (v.z & 0xFFFFu) | (pack2(0.0f, rel) & 0xFFFF0000u);
             }
@@ -268,52 +275,275 @@ struct InferParams {
     const float* ao;
     ImageGeom G;
     float* out;
+    // optional pixel list (one image): entry i's x | y << 16 in surf[2 * i + 1].w, the
+    // count in *surf_count; only the listed pixels are written
+    const float4* surf;
+    const uint32_t* surf_count;
 };
 
-__global__ void __launch_bounds__(256) denoise_infer_kernel(InferParams P) {
-    extern __shared__ __align__(16) unsigned char sm_raw[];
-    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(sm_raw);
-    float* sbias = reinterpret_cast<float*>(sm_raw + pFwdEnd * 2);
-    __nv_bfloat16* stage_all = reinterpret_cast<__nv_bfloat16*>(sm_raw + pFwdEnd * 2 + kBias * 4);
-    for (int i = threadIdx.x; i < pFwdEnd / 8; i += blockDim.x)
-        reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(P.wpack)[i];
-    for (int i = threadIdx.x; i < kBias; i += blockDim.x) sbias[i] = P.bias[i];
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    __nv_bfloat16* stage = stage_all + warp * 16 * sW1;
-    const uint32_t total = P.G.pixels * P.G.images;
-    const uint32_t tiles = (total + kTile - 1) / kTile;
-    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        uint32_t base = tile * kTile + warp * 16;
-        uint32_t valid;
-        gather_tile(P.feat, P.lin_depth, P.G, base, stage, valid);
-        if (valid == 0) {   // no lit pixel in this warp's 16: nothing to filter (warp-uniform)
-            if (lane < 16 && base + lane < total) P.out[base + lane] = 0.0f;
-            __syncwarp();
-            continue;
-        }
-        uint32_t a0[5][4];
+// ---------------------------------------------------------------- inference on tcgen05
+// The four layers of a 128-pixel tile as tcgen05.mma products (M = 128 pixels, N = 64,
+// BF16 operands, FP32 accumulator in tensor memory): the activation tile A [128 x K]
+// and the weights B [64 x K] sit in shared memory, K-major in the no-swizzle layout of
+// 8-row x 16-byte core matrices ((r / 8) * K/8 + k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2;
+// one thread issues the K/16 products of a layer and commits them to an mbarrier, then
+// every thread reads its pixel's row of the accumulator (tcgen05.ld, lane = pixel),
+// adds the bias, applies ReLU, rounds to BF16 and writes the row back as the next A.
+// The last layer's 49 logits go through the softmax and 7x7 filter in registers.
+//
+// A block holds the weights once and kTcGroups warpgroups, each with its own tile,
+// A buffer, 64 accumulator columns, mbarrier and named barrier: while one group waits
+// for its products the others gather, or run their epilogues.
+constexpr int kTcGroups = 8;                    // warpgroups (tiles in flight) per block
+constexpr int kTcThreads = 128 * kTcGroups;
+constexpr uint32_t kTcCols = 64;                // accumulator columns of one group (N)
+constexpr uint32_t kTcAlloc = 512;              // power of two >= kTcGroups * kTcCols
+constexpr int kTcW1 = 0, kTcW2 = kTcW1 + 64 * 80 * 2, kTcW3 = kTcW2 + 64 * 64 * 2, kTcW4 = kTcW3 + 64 * 64 * 2;
+constexpr int kTcABytes = 128 * 80 * 2;
+constexpr int kTcA = kTcW4 + 64 * 64 * 2, kTcBias = kTcA + kTcGroups * kTcABytes, kTcBar = kTcBias + kBias * 4;
+constexpr int kTcSmem = kTcBar + 8 * kTcGroups + 16;
+constexpr int kTcBlocksPerSm = 1;
+static_assert(kTcBlocksPerSm * kTcAlloc <= 512, "tensor-memory columns per SM");
+static_assert(kTcGroups * kTcCols <= kTcAlloc, "groups must fit in the allocation");
+static_assert(kTcBlocksPerSm * (kTcSmem + 1024) <= 232448, "blocks per SM must fit in shared memory");
+constexpr uint32_t kTcWaitCap = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t core_offset(uint32_t r, uint32_t kb, uint32_t kblocks) {
+    return ((r >> 3) * kblocks + kb) * 128u + (r & 7u) * 16u;
+}
+// Shared-memory matrix descriptor, no swizzle: start, leading (K) and stride (8-row)
+// byte offsets, descriptor version 1.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major,
+// N = 64, M = 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((kTcCols >> 3) << 17) | ((128u >> 4) << 24);
+
+// One layer: D[tmem] = A[128 x 16*ksteps] * W^T, issued by the calling thread.
+__device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_addr, uint32_t w_addr, int ksteps) {
+    const uint32_t kblocks = (uint32_t)ksteps * 2u;
+    for (int s = 0; s < ksteps; ++s) {
+        const uint64_t da = umma_desc(a_addr + (uint32_t)s * 256u, 128u, kblocks * 128u);
+        const uint64_t db = umma_desc(w_addr + (uint32_t)s * 256u, 128u, kblocks * 128u);
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                     :: "r"(tmem), "l"(da), "l"(db), "r"(kTcIdesc), "r"(s > 0 ? 1u : 0u));
+    }
+}
+
+// Waits (bounded) for the mbarrier phase; false when the cap ran out.
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t phase) {
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kTcWaitCap && !done; ++it)
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n" : "=r"(done) : "r"(bar), "r"(phase));
+    return done != 0;
+}
+
+// 16 accumulator columns of this thread's lane.
+__device__ __forceinline__ void tc_load16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-        for (int kk = 0; kk < 5; ++kk) load_a(stage, sW1, kk, a0[kk]);
-        float c[8][4];
-        layer<5, 8>(a0, sw + pW1, sW1, sbias, c);
-        uint32_t a1[4][4];
-        to_a_relu<4>(c, a1);
-        layer<4, 8>(a1, sw + pW2, sW, sbias + 64, c);
-        to_a_relu<4>(c, a1);
-        layer<4, 8>(a1, sw + pW3, sW, sbias + 128, c);
-        to_a_relu<4>(c, a1);
-        float z[7][4], aok[7][4], y[2];
-        layer<4, 7>(a1, sw + pW4, sW, sbias + 192, z);
-        softmax_filter(z, P.ao, P.G, base, y, aok);
-        if (t == 0) {
-            for (int h = 0; h < 2; ++h) {
-                uint32_t gp = base + g + 8 * h;
-                if (gp < total) P.out[gp] = ((valid >> (g + 8 * h)) & 1u) ? y[h] : 0.0f;
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Barrier of one warpgroup (named barrier 1 + group; 0 is the block's).
+__device__ __forceinline__ void group_sync(uint32_t group) {
+    asm volatile("bar.sync %0, 128;" :: "r"(group + 1u) : "memory");
+}
+
+// Barrier of one warpgroup that also ORs a flag over its threads (uniform result).
+__device__ __forceinline__ bool group_sync_or(uint32_t group, uint32_t flag) {
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, %2, 128, q;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}\n" : "=r"(r) : "r"(flag), "r"(group + 1u) : "memory");
+    return r != 0;
+}
+
+// Issues a layer from the group's first thread after the group's shared-memory writes
+// and accumulator reads, commits it and waits (that thread alone, bounded); the
+// group's barrier then hands the accumulator, and the outcome, to every lane. A wait
+// that ran out raises the status, waits once more (bounded) for the products in
+// flight, and stops the group (false).
+__device__ __forceinline__ bool tc_run_layer(uint32_t group, uint32_t tmem, uint32_t a_addr, uint32_t w_addr,
+                                             int ksteps, uint32_t bar, uint32_t& phase, uint32_t* status) {
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    group_sync(group);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    uint32_t failed = 0;
+    if ((threadIdx.x & 127u) == 0) {
+        tc_layer(tmem, a_addr, w_addr, ksteps);
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar));
+        if (!tc_wait(bar, phase)) {
+            atomicOr(status, (uint32_t)LUZ_DEV_MMA_WAIT);
+            failed = 1u;
+            tc_wait(bar, phase);
+        }
+    }
+    phase ^= 1u;
+    const bool stop = group_sync_or(group, failed);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    return !stop;
+}
+
+// relu(lo + b.x), relu(hi + b.y) rounded to BF16 and packed (lo in the low half): one
+// packed FP32 add and one converting ReLU (rounding commutes with the clamp at 0).
+__device__ __forceinline__ uint32_t bias_relu_bf16x2(float lo, float hi, float2 b) {
+    uint32_t d;
+    asm("{\n\t.reg .b64 x, y, z;\n\t.reg .f32 l, h;\n\tmov.b64 x, {%1, %2};\n\tmov.b64 y, {%3, %4};\n\t"
+        "add.rn.f32x2 z, x, y;\n\tmov.b64 {l, h}, z;\n\tcvt.rn.relu.bf16x2.f32 %0, h, l;\n\t}\n"
+        : "=r"(d) : "f"(lo), "f"(hi), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+// Bias + ReLU + BF16 of this thread's 64 accumulator columns into row `row` of A (K = 64).
+__device__ __forceinline__ void tc_relu_to_a(uint32_t tmem_lane, const float* sbias, unsigned char* a, uint32_t row) {
+    const float2* b2 = reinterpret_cast<const float2*>(sbias);
+#pragma unroll
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+        float v[16];
+        tc_load16(tmem_lane + (uint32_t)c0, v);
+        uint32_t w[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) w[j] = bias_relu_bf16x2(v[2 * j], v[2 * j + 1], b2[c0 / 2 + j]);
+        *reinterpret_cast<uint4*>(a + core_offset(row, (uint32_t)c0 / 8u, 8u)) = make_uint4(w[0], w[1], w[2], w[3]);
+        *reinterpret_cast<uint4*>(a + core_offset(row, (uint32_t)c0 / 8u + 1u, 8u)) = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_kernel(InferParams P, uint32_t* status) {
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    float* sbias = reinterpret_cast<float*>(tsm + kTcBias);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + kTcBar + 8 * kTcGroups);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, group = tid >> 7, row = tid & 127u;
+    const uint32_t bar = smem_u32(tsm + kTcBar + 8 * group);
+    // weights into the core-matrix layout (rows of the packed n-major copies)
+    for (uint32_t e = tid; e < 64 * 10; e += kTcThreads) {           // W1: K = 80
+        const uint32_t n = e / 10, kb = e % 10;
+        *reinterpret_cast<uint4*>(tsm + kTcW1 + core_offset(n, kb, 10)) =
+            *reinterpret_cast<const uint4*>(P.wpack + pW1 + n * sW1 + kb * 8);
+    }
+    for (uint32_t e = tid; e < 64 * 8; e += kTcThreads) {            // W2, W3, W4: K = 64
+        const uint32_t n = e / 8, kb = e % 8;
+        *reinterpret_cast<uint4*>(tsm + kTcW2 + core_offset(n, kb, 8)) =
+            *reinterpret_cast<const uint4*>(P.wpack + pW2 + n * sW + kb * 8);
+        *reinterpret_cast<uint4*>(tsm + kTcW3 + core_offset(n, kb, 8)) =
+            *reinterpret_cast<const uint4*>(P.wpack + pW3 + n * sW + kb * 8);
+        *reinterpret_cast<uint4*>(tsm + kTcW4 + core_offset(n, kb, 8)) =
+            n < 56 ? *reinterpret_cast<const uint4*>(P.wpack + pW4 + n * sW + kb * 8) : make_uint4(0, 0, 0, 0);
+    }
+    for (uint32_t i = tid; i < (uint32_t)kBias; i += kTcThreads) sbias[i] = P.bias[i];
+    if (row == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(tslot)),
+                     "r"(kTcAlloc));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tslot + group * kTcCols;               // this group's columns
+    const uint32_t tmem_lane = tmem + (((warp & 3u) * 32u) << 16); // this warp's 32 lanes
+    unsigned char* a = tsm + kTcA + group * kTcABytes;
+    const uint32_t a_addr = smem_u32(a);
+    uint32_t phase = 0;
+    const uint32_t total = P.surf ? *P.surf_count : P.G.pixels * P.G.images;
+    const uint32_t tiles = (total + 127) / 128;
+    for (uint32_t tile = blockIdx.x * kTcGroups + group; tile < tiles; tile += gridDim.x * kTcGroups) {
+        // features of pixel `row`: 9 taps of 8 channels (relative depth in channel 5), then 8 zeros
+        const uint32_t item = tile * 128 + row;
+        const bool has = item < total;
+        bool valid = false;
+        uint32_t img = 0, gp = 0;
+        int x = 0, y = 0;
+        float dc = 0.f, inv_dc = 0.f;
+        if (has) {
+            if (P.surf) {
+                const uint32_t xy = __float_as_uint(__ldg(&P.surf[2 * (size_t)item + 1].w));
+                x = (int)(xy & 0xFFFFu);
+                y = (int)(xy >> 16);
+                gp = (uint32_t)y * P.G.width + (uint32_t)x;
+            } else {
+                gp = item;
+                img = gp / P.G.pixels;
+                const uint32_t local = gp - img * P.G.pixels;
+                x = (int)(local % P.G.width);
+                y = (int)(local / P.G.width);
+            }
+            dc = P.lin_depth[gp];
+            valid = dc > 0.0f;
+            inv_dc = valid ? 1.0f / dc : 0.0f;
+        }
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (valid) {
+                const int qx = min(max(x + tap % 3 - 1, 0), (int)P.G.width - 1);
+                const int qy = min(max(y + tap / 3 - 1, 0), (int)P.G.height - 1);
+                const uint32_t q = img * P.G.pixels + (uint32_t)qy * P.G.width + (uint32_t)qx;
+                v = P.feat[q];
+                const float dq = P.lin_depth[q];
+                const float rel = dq > 0.0f ? relative_depth(dq, dc, inv_dc) : 0.0f;
+                v.z = (v.z & 0xFFFFu) | (pack2(0.0f, rel) & 0xFFFF0000u);
+            }
+            *reinterpret_cast<uint4*>(a + core_offset(row, (uint32_t)tap, 10)) = v;
+        }
+        *reinterpret_cast<uint4*>(a + core_offset(row, 9, 10)) = make_uint4(0, 0, 0, 0);
+        if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW1), 5, bar, phase, status)) break;
+        tc_relu_to_a(tmem_lane, sbias, a, row);
+        if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW2), 4, bar, phase, status)) break;
+        tc_relu_to_a(tmem_lane, sbias + 64, a, row);
+        if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW3), 4, bar, phase, status)) break;
+        tc_relu_to_a(tmem_lane, sbias + 128, a, row);
+        if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW4), 4, bar, phase, status)) break;
+        // softmax over the 49 logits and the 7x7 filter of the noisy AO
+        float m = -3.0e38f;
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+            float v[16];
+            tc_load16(tmem_lane + (uint32_t)c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                if (c0 + j < 49) m = fmaxf(m, v[j] + sbias[192 + c0 + j]);
+        }
+        float ssum = 0.f, acc = 0.f;
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+            float v[16];
+            tc_load16(tmem_lane + (uint32_t)c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int k = c0 + j;
+                if (k < 49) {
+                    const float e = __expf(v[j] + sbias[192 + k] - m);
+                    ssum += e;
+                    float ao = 0.f;
+                    if (has) {
+                        const int qx = min(max(x + k % 7 - 3, 0), (int)P.G.width - 1);
+                        const int qy = min(max(y + k / 7 - 3, 0), (int)P.G.height - 1);
+                        ao = __ldg(P.ao + img * P.G.pixels + (uint32_t)qy * P.G.width + (uint32_t)qx);
+                    }
+                    acc += e * ao;
+                }
             }
         }
-        __syncwarp();
+        if (has) P.out[gp] = valid ? acc * (1.0f / ssum) : 0.0f;
     }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(*tslot), "r"(kTcAlloc));
 }
 
 // ---------------------------------------------------------------- training
@@ -646,7 +876,6 @@ static luz_status repack(luz_ctx* ctx, luz_denoiser* d) {
     return LUZ_OK;
 }
 
-static size_t infer_smem() { return (size_t)pFwdEnd * 2 + kBias * 4 + 8 * 16 * sW1 * 2; }
 static size_t train_smem() { return (size_t)pEnd * 2 + kBias * 4 + sizeof(TrainSmem); }
 
 static luz_status check_batch(luz_ctx* ctx, const luz_denoise_batch* b) {
@@ -657,11 +886,14 @@ static luz_status check_batch(luz_ctx* ctx, const luz_denoise_batch* b) {
     return LUZ_OK;
 }
 
-static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* out) {
+// Dense over the batch's pixels, or over the lit-pixel list of one image when `surf`
+// is given (the other pixels of `out` are then written by the features pass).
+static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* out,
+                            const float4* surf = nullptr, const uint32_t* surf_count = nullptr) {
     static bool attr = false;
     if (!attr) {
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)infer_smem()));
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           kTcSmem));
         attr = true;
     }
     InferParams P;
@@ -672,10 +904,12 @@ static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_bat
     P.ao = b->noisy_ao;
     P.G = ImageGeom{b->width, b->height, b->width * b->height, b->images};
     P.out = out;
-    uint32_t tiles = (P.G.pixels * P.G.images + kTile - 1) / kTile;
-    uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)ctx->sm_count * 3);
-    denoise_infer_kernel<<<grid, 256, infer_smem(), ctx->stream>>>(P);
-    LUZ_LAUNCHED(ctx, "denoise_infer_kernel");
+    P.surf = surf;
+    P.surf_count = surf_count;
+    uint32_t tiles = (P.G.pixels * P.G.images + 127) / 128;
+    uint32_t grid = std::min<uint32_t>((tiles + kTcGroups - 1) / kTcGroups, (uint32_t)ctx->sm_count * kTcBlocksPerSm);
+    denoise_infer_tc_kernel<<<grid, kTcThreads, kTcSmem, ctx->stream>>>(P, ctx->d_status);
+    LUZ_LAUNCHED(ctx, "denoise_infer_tc_kernel");
     return LUZ_OK;
 }
 
@@ -819,8 +1053,8 @@ luz_status luz_denoise_batch_infer(luz_ctx* ctx, luz_denoiser* d, const luz_deno
     return run_infer(ctx, d, b, d_out);
 }
 
-luz_status luz_denoise_features(luz_ctx* ctx, luz_frame* f) {
-    if (!ctx || !f) return LUZ_ERR_INVALID;
+// Feature planes of a frame; `denoised`, if set, receives 0 at the background pixels.
+static luz_status launch_features(luz_ctx* ctx, luz_frame* f, float* denoised) {
     luz_status s = upload_lut(ctx);
     if (s != LUZ_OK) return s;
     FeatParams F;
@@ -841,17 +1075,24 @@ luz_status luz_denoise_features(luz_ctx* ctx, luz_frame* f) {
     F.feat = (uint4*)f->features;
     F.lin_depth = f->lin_depth;
     F.ao = f->ao;
+    F.denoised = denoised;
     features_kernel<<<(f->pixels + 255) / 256, 256, 0, ctx->stream>>>(F);
     LUZ_LAUNCHED(ctx, "denoise_features_kernel");
     return LUZ_OK;
 }
 
+luz_status luz_denoise_features(luz_ctx* ctx, luz_frame* f) {
+    if (!ctx || !f) return LUZ_ERR_INVALID;
+    return launch_features(ctx, f, nullptr);
+}
+
 luz_status luz_denoise(luz_ctx* ctx, luz_denoiser* d, luz_frame* f) {
     if (!ctx || !d || !f) return LUZ_ERR_INVALID;
-    luz_status s = luz_denoise_features(ctx, f);
+    luz_status s = launch_features(ctx, f, f->ao_denoised);
     if (s != LUZ_OK) return s;
+    if ((s = ensure_lit_list(ctx, f)) != LUZ_OK) return s;
     luz_denoise_batch b{f->features, f->lin_depth, f->ao, nullptr, f->width, f->height, 1};
-    return run_infer(ctx, d, &b, f->ao_denoised);
+    return run_infer(ctx, d, &b, f->ao_denoised, f->surf, f->lit_count);
 }
 
 }  // extern "C"

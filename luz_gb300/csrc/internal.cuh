@@ -223,6 +223,8 @@ luz_status set_error(luz_ctx* ctx, luz_status st, const std::string& msg);
 luz_status cuda_error(luz_ctx* ctx, cudaError_t e, const char* what);
 luz_status ensure_scratch(luz_ctx* ctx, size_t bytes);
 luz_status check_launch(luz_ctx* ctx, const char* what);
+// Rebuilds the frame's lit-pixel list when its planes or scene constants changed.
+luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f);
 }  // namespace luz
 
 #define LUZ_CUDA(ctx, call)                                          \

@@ -184,7 +184,6 @@ __global__ void __launch_bounds__(256) ao_resolve_kernel(const float4* normal, c
     ao[pix] = (float)misses / (float)samples;
 }
 
-luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f);
 
 luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
     luz_status st = ensure_lit_list(ctx, f);

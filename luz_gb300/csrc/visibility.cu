@@ -579,7 +579,6 @@ luz_status clear_visibility(luz_ctx* ctx, luz_frame* f) {
     return LUZ_OK;
 }
 
-luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f);
 
 luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int frame_index,
                              unsigned long long* d_stats) {

@@ -79,3 +79,39 @@ def test_trained_network_beats_plain_one_sample():
         assert r["denoised_1spp"] < 0.5 * r["raw_1spp"], r
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("size", [(200, 120), (64, 64)])
+def test_frame_path_over_lit_pixels_matches_dense_batch(size):
+    """luz_denoise filters only the frame's lit pixels (its compacted list) and leaves 0
+    at the background; the batch entry point runs over every pixel of the same planes.
+    Both must agree bit for bit."""
+    torch = pytest.importorskip("torch")
+    from luz_gb300 import denoiser as D
+    from luz_gb300 import _abi
+    ctx = L.Context(0)
+    try:
+        w, h = size
+        g = L.GPUScene(ctx, L.HostScene(1, width=w, height=h))
+        g.render(0)
+        fr = g.frame
+        first, second = D.Denoiser(ctx, seed=21), D.Denoiser(ctx, seed=22)
+        first.denoise(fr)            # leaves other values in the plane for the second pass to replace
+        second.denoise(fr)
+        b = _abi.DenoiseBatch()
+        b.features = fr.device_ptr(L.PLANE_FEATURES)
+        b.lin_depth = fr.device_ptr(L.PLANE_LIN_DEPTH)
+        b.noisy_ao = fr.device_ptr(L.PLANE_AO)
+        b.target_ao = None
+        b.width, b.height, b.images = w, h, 1
+        out = torch.full((h, w), float("nan"), dtype=torch.float32, device="cuda")
+        second.infer(b, out.data_ptr())
+        ctx.synchronize()
+        assert ctx.device_status() == 0
+        dense = out.cpu().numpy().reshape(-1)
+        framed = fr.read(L.PLANE_AO_DENOISED).reshape(-1)
+        assert np.array_equal(dense.view(np.uint32), framed.view(np.uint32))
+        lit = fr.read(L.PLANE_LIN_DEPTH).reshape(-1) > 0
+        assert lit.sum() > 0 and np.all(framed[~lit] == 0.0)
+    finally:
+        ctx.close()
