@@ -54,7 +54,7 @@ static void free_frame_buffers(luz_frame* f) {
     void* ptrs[] = {f->albedo, f->normal, f->material, f->emission, f->depth, f->light,
                     f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->surf,
                     f->features, f->lin_depth, f->taa, f->taa_next, f->compose, f->hist, f->hist_state,
-                    f->block_counts, f->lit_count, f->d_scene, f->d_lights, f->d_models,
+                    f->block_counts, f->lit_count, f->dn_list, f->dn_count, f->d_scene, f->d_lights, f->d_models,
                     f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter, f->d_textures,
                     f->d_texels, f->d_shadow_lights, f->d_shadow_maps, f->rays_a, f->rays_b};
     for (void* p : ptrs)
@@ -309,6 +309,8 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     A((void**)&f->ao_denoised, P * 4);
     A((void**)&f->features, P * 16);
     A((void**)&f->lin_depth, P * 4);
+    A((void**)&f->dn_list, P * 4);
+    A((void**)&f->dn_count, 4);
     A((void**)&f->taa, P * 16);
     A((void**)&f->taa_next, P * 16);
     A((void**)&f->compose, P * 4);

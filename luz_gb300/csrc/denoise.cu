@@ -75,43 +75,73 @@ struct FeatParams {
     float* lin_depth;  // distance to the camera (0 = background)
     float* ao;         // noisy AO value
     float* denoised;   // if set: 0 written here for background pixels (the denoiser skips them)
+    uint32_t* list;    // if set: lit pixels appended (x | y << 16), row-major within a block
+    uint32_t* list_count;
 };
 
 __constant__ float c_lin_lut[256];   // pow(i/255, 2.2)
 
+// For lane j of a warp: how many of the `planes` bit planes have bit j of word `w` set.
+// Lane s loads plane s of each group of 32 (one load latency per group); the words
+// then pass through the warp by shuffles.
+__device__ __forceinline__ uint32_t column_count(const uint32_t* __restrict__ bits, uint32_t planes, uint32_t words,
+                                                 uint32_t w) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t mine = 0;
+    for (uint32_t c = 0; c < planes; c += 32) {
+        const uint32_t s = c + lane;
+        const uint32_t word = s < planes ? __ldg(bits + (size_t)s * words + w) : 0u;
+        const uint32_t n = min(32u, planes - c);
+#pragma unroll 8
+        for (uint32_t j = 0; j < n; ++j) mine += (__shfl_sync(0xFFFFFFFFu, word, j) >> lane) & 1u;
+    }
+    return mine;
+}
+
 __global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
-    uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= F.width * F.height) return;
-    float4 n = F.normal[pix];
-    if (length(V3{n.x, n.y, n.z}) == 0.0f) {
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_base;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t x = pix % F.width, y = pix / F.width;
+    const bool inside = pix < F.width * F.height;
+    float4 n = inside ? F.normal[pix] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool lit = inside && !(length(V3{n.x, n.y, n.z}) == 0.0f);
+    if (F.list) {   // block-aggregated append, in pixel order within the block
+        const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const uint32_t mask = __ballot_sync(0xFFFFFFFFu, lit);
+        if (lane == 0) s_warp[warp] = __popc(mask);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int w = 0; w < 8; ++w) { const uint32_t c = s_warp[w]; s_warp[w] = t; t += c; }
+            s_base = t ? atomicAdd(F.list_count, t) : 0u;
+        }
+        __syncthreads();
+        if (lit) F.list[s_base + s_warp[warp] + __popc(mask & ((1u << lane) - 1u))] = x | (y << 16);
+    }
+    uint32_t ao_hits = 0, shadow_hits = 0;
+    if (__any_sync(0xFFFFFFFFu, lit)) {   // a warp's 32 pixels are the 32 bits of one word
+        ao_hits = column_count(F.ao_bits, F.ao_samples, F.words, pix >> 5);
+        shadow_hits = column_count(F.shadow_bits, F.shadow_slots, F.words, pix >> 5);
+    }
+    if (!inside) return;
+    if (!lit) {
         F.feat[pix] = make_uint4(0, 0, 0, 0);
         F.lin_depth[pix] = 0.0f;
         F.ao[pix] = 0.0f;
         if (F.denoised) F.denoised[pix] = 0.0f;
         return;
     }
-    uint32_t w = pix >> 5, bit = 1u << (pix & 31);
-    float ao = 1.0f;
-    if (F.ao_samples) {
-        uint32_t m = 0;
-        for (uint32_t s = 0; s < F.ao_samples; ++s) m += (F.ao_bits[(size_t)s * F.words + w] & bit) ? 1u : 0u;
-        ao = (float)m / (float)F.ao_samples;
-    }
-    float lit = 1.0f;
-    if (F.shadow_slots) {
-        uint32_t h = 0;
-        for (uint32_t s = 0; s < F.shadow_slots; ++s) h += (F.shadow_bits[(size_t)s * F.words + w] & bit) ? 1u : 0u;
-        lit = 1.0f - (float)h / (float)F.shadow_slots;
-    }
+    const float ao = F.ao_samples ? (float)ao_hits / (float)F.ao_samples : 1.0f;
+    const float lit_frac = F.shadow_slots ? 1.0f - (float)shadow_hits / (float)F.shadow_slots : 1.0f;
     uint32_t a8 = F.albedo[pix], m8 = F.material[pix];
     float lum = 0.2127f * c_lin_lut[a8 & 0xFF] + 0.7152f * c_lin_lut[(a8 >> 8) & 0xFF] +
                 0.0722f * c_lin_lut[(a8 >> 16) & 0xFF];
     float rough = (float)(m8 & 0xFF) / 255.0f;
-    uint32_t x = pix % F.width, y = pix / F.width;
     V3 p = depth_to_world(F.inverse_proj, F.inverse_view, pixel_uv(x, F.width), pixel_uv(y, F.height), F.depth[pix]);
     float d = length(p - V3{F.cam[0], F.cam[1], F.cam[2]});
     uint4 v;
-    v.x = pack2(ao, lit);
+    v.x = pack2(ao, lit_frac);
     v.y = pack2(n.x, n.y);
     v.z = pack2(n.z, 0.0f);
     v.w = pack2(rough, lum);
@@ -275,10 +305,10 @@ struct InferParams {
     const float* ao;
     ImageGeom G;
     float* out;
-    // optional pixel list (one image): entry i's x | y << 16 in surf[2 * i + 1].w, the
-    // count in *surf_count; only the listed pixels are written
-    const float4* surf;
-    const uint32_t* surf_count;
+    // optional pixel list (one image): x | y << 16 per entry, the count in *list_count;
+    // only the listed pixels are written
+    const uint32_t* list;
+    const uint32_t* list_count;
 };
 
 // ---------------------------------------------------------------- inference on tcgen05
@@ -420,6 +450,70 @@ __device__ __forceinline__ void tc_relu_to_a(uint32_t tmem_lane, const float* sb
     }
 }
 
+// Packed FP32 pairs (one instruction for both lanes of the pair).
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+        "add.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n\t}\n"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 x, y, z, w;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\tmov.b64 z, {%6, %7};\n\t"
+        "fma.rn.f32x2 w, x, y, z;\n\tmov.b64 {%0, %1}, w;\n\t}\n"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+__device__ __forceinline__ float exp2_approx(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Second pass of the softmax and the 7x7 filter: (sum of w_k * ao_k, sum of w_k) with
+// w_k = 2^((z_k - m) * log2 e), z_k = logit + bias. kInterior: every tap of the
+// thread's pixel is inside the image (rows addressed directly); otherwise clamped.
+template <bool kInterior>
+__device__ __forceinline__ float2 ao_filter(uint32_t tmem_lane, const float2* b4, float b48, float m,
+                                           const float* __restrict__ ao, uint32_t base, int x, int y,
+                                           const ImageGeom& G) {
+    constexpr float kLog2e = 1.4426950408889634f;
+    const float2 l2e = make_float2(kLog2e, kLog2e);
+    const float nm = -m * kLog2e;
+    const float2 nm2 = make_float2(nm, nm);
+    const float* rows[7];
+    int qx[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+        if (kInterior) {
+            rows[d] = ao + base + (uint32_t)(y + d - 3) * G.width + (uint32_t)(x - 3);
+        } else {
+            rows[d] = ao + base + (uint32_t)min(max(y + d - 3, 0), (int)G.height - 1) * G.width;
+            qx[d] = min(max(x + d - 3, 0), (int)G.width - 1);
+        }
+    }
+    auto tap = [&](int k) -> float { return __ldg(rows[k / 7] + (kInterior ? k % 7 : qx[k % 7])); };
+    float2 s = make_float2(0.f, 0.f), acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int c0 = 0; c0 < 48; c0 += 16) {
+        float v[16];
+        tc_load16(tmem_lane + (uint32_t)c0, v);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int k = c0 + 2 * j;
+            const float2 t = fma2(add2(make_float2(v[2 * j], v[2 * j + 1]), b4[k / 2]), l2e, nm2);
+            const float2 e = make_float2(exp2_approx(t.x), exp2_approx(t.y));
+            s = add2(s, e);
+            acc = fma2(e, make_float2(tap(k), tap(k + 1)), acc);
+        }
+    }
+    float v[16];
+    tc_load16(tmem_lane + 48u, v);
+    const float e48 = exp2_approx(fmaf(v[0] + b48, kLog2e, nm));
+    return make_float2(fmaf(e48, tap(48), acc.x + acc.y), e48 + s.x + s.y);
+}
+
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_kernel(InferParams P, uint32_t* status) {
     extern __shared__ __align__(1024) unsigned char tsm[];
     float* sbias = reinterpret_cast<float*>(tsm + kTcBias);
@@ -459,7 +553,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_k
     unsigned char* a = tsm + kTcA + group * kTcABytes;
     const uint32_t a_addr = smem_u32(a);
     uint32_t phase = 0;
-    const uint32_t total = P.surf ? *P.surf_count : P.G.pixels * P.G.images;
+    const uint32_t total = P.list ? *P.list_count : P.G.pixels * P.G.images;
     const uint32_t tiles = (total + 127) / 128;
     for (uint32_t tile = blockIdx.x * kTcGroups + group; tile < tiles; tile += gridDim.x * kTcGroups) {
         // features of pixel `row`: 9 taps of 8 channels (relative depth in channel 5), then 8 zeros
@@ -470,8 +564,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_k
         int x = 0, y = 0;
         float dc = 0.f, inv_dc = 0.f;
         if (has) {
-            if (P.surf) {
-                const uint32_t xy = __float_as_uint(__ldg(&P.surf[2 * (size_t)item + 1].w));
+            if (P.list) {
+                const uint32_t xy = P.list[item];
                 x = (int)(xy & 0xFFFFu);
                 y = (int)(xy >> 16);
                 gp = (uint32_t)y * P.G.width + (uint32_t)x;
@@ -509,37 +603,29 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_k
         tc_relu_to_a(tmem_lane, sbias + 128, a, row);
         if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW4), 4, bar, phase, status)) break;
         // softmax over the 49 logits and the 7x7 filter of the noisy AO
+        const float2* b4 = reinterpret_cast<const float2*>(sbias + 192);
         float m = -3.0e38f;
 #pragma unroll
-        for (int c0 = 0; c0 < 64; c0 += 16) {
+        for (int c0 = 0; c0 < 48; c0 += 16) {
             float v[16];
             tc_load16(tmem_lane + (uint32_t)c0, v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
-                if (c0 + j < 49) m = fmaxf(m, v[j] + sbias[192 + c0 + j]);
-        }
-        float ssum = 0.f, acc = 0.f;
-#pragma unroll
-        for (int c0 = 0; c0 < 64; c0 += 16) {
-            float v[16];
-            tc_load16(tmem_lane + (uint32_t)c0, v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int k = c0 + j;
-                if (k < 49) {
-                    const float e = __expf(v[j] + sbias[192 + k] - m);
-                    ssum += e;
-                    float ao = 0.f;
-                    if (has) {
-                        const int qx = min(max(x + k % 7 - 3, 0), (int)P.G.width - 1);
-                        const int qy = min(max(y + k / 7 - 3, 0), (int)P.G.height - 1);
-                        ao = __ldg(P.ao + img * P.G.pixels + (uint32_t)qy * P.G.width + (uint32_t)qx);
-                    }
-                    acc += e * ao;
-                }
+            for (int j = 0; j < 8; ++j) {
+                const float2 z = add2(make_float2(v[2 * j], v[2 * j + 1]), b4[c0 / 2 + j]);
+                m = fmaxf(m, fmaxf(z.x, z.y));
             }
         }
-        if (has) P.out[gp] = valid ? acc * (1.0f / ssum) : 0.0f;
+        {
+            float v[16];
+            tc_load16(tmem_lane + 48u, v);
+            m = fmaxf(m, v[0] + sbias[192 + 48]);
+        }
+        const uint32_t base = img * P.G.pixels;
+        const bool interior = has && x >= 3 && y >= 3 && x + 3 < (int)P.G.width && y + 3 < (int)P.G.height;
+        const float2 r = __all_sync(0xFFFFFFFFu, interior)
+                             ? ao_filter<true>(tmem_lane, b4, sbias[192 + 48], m, P.ao, base, x, y, P.G)
+                             : ao_filter<false>(tmem_lane, b4, sbias[192 + 48], m, P.ao, base, x, y, P.G);
+        if (has) P.out[gp] = valid ? r.x * (1.0f / r.y) : 0.0f;
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
@@ -886,10 +972,10 @@ static luz_status check_batch(luz_ctx* ctx, const luz_denoise_batch* b) {
     return LUZ_OK;
 }
 
-// Dense over the batch's pixels, or over the lit-pixel list of one image when `surf`
+// Dense over the batch's pixels, or over the lit-pixel list of one image when `list`
 // is given (the other pixels of `out` are then written by the features pass).
 static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* out,
-                            const float4* surf = nullptr, const uint32_t* surf_count = nullptr) {
+                            const uint32_t* list = nullptr, const uint32_t* list_count = nullptr) {
     static bool attr = false;
     if (!attr) {
         LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -904,8 +990,8 @@ static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_bat
     P.ao = b->noisy_ao;
     P.G = ImageGeom{b->width, b->height, b->width * b->height, b->images};
     P.out = out;
-    P.surf = surf;
-    P.surf_count = surf_count;
+    P.list = list;
+    P.list_count = list_count;
     uint32_t tiles = (P.G.pixels * P.G.images + 127) / 128;
     uint32_t grid = std::min<uint32_t>((tiles + kTcGroups - 1) / kTcGroups, (uint32_t)ctx->sm_count * kTcBlocksPerSm);
     denoise_infer_tc_kernel<<<grid, kTcThreads, kTcSmem, ctx->stream>>>(P, ctx->d_status);
@@ -1053,8 +1139,9 @@ luz_status luz_denoise_batch_infer(luz_ctx* ctx, luz_denoiser* d, const luz_deno
     return run_infer(ctx, d, b, d_out);
 }
 
-// Feature planes of a frame; `denoised`, if set, receives 0 at the background pixels.
-static luz_status launch_features(luz_ctx* ctx, luz_frame* f, float* denoised) {
+// Feature planes of a frame. With `for_denoise` the pass also writes 0 to the denoised
+// plane at the background pixels and lists the lit pixels for the denoiser.
+static luz_status launch_features(luz_ctx* ctx, luz_frame* f, bool for_denoise) {
     luz_status s = upload_lut(ctx);
     if (s != LUZ_OK) return s;
     FeatParams F;
@@ -1075,7 +1162,10 @@ static luz_status launch_features(luz_ctx* ctx, luz_frame* f, float* denoised) {
     F.feat = (uint4*)f->features;
     F.lin_depth = f->lin_depth;
     F.ao = f->ao;
-    F.denoised = denoised;
+    F.denoised = for_denoise ? f->ao_denoised : nullptr;
+    F.list = for_denoise ? f->dn_list : nullptr;
+    F.list_count = f->dn_count;
+    if (for_denoise) LUZ_CUDA(ctx, cudaMemsetAsync(f->dn_count, 0, 4, ctx->stream));
     features_kernel<<<(f->pixels + 255) / 256, 256, 0, ctx->stream>>>(F);
     LUZ_LAUNCHED(ctx, "denoise_features_kernel");
     return LUZ_OK;
@@ -1083,16 +1173,15 @@ static luz_status launch_features(luz_ctx* ctx, luz_frame* f, float* denoised) {
 
 luz_status luz_denoise_features(luz_ctx* ctx, luz_frame* f) {
     if (!ctx || !f) return LUZ_ERR_INVALID;
-    return launch_features(ctx, f, nullptr);
+    return launch_features(ctx, f, false);
 }
 
 luz_status luz_denoise(luz_ctx* ctx, luz_denoiser* d, luz_frame* f) {
     if (!ctx || !d || !f) return LUZ_ERR_INVALID;
-    luz_status s = launch_features(ctx, f, f->ao_denoised);
+    luz_status s = launch_features(ctx, f, true);
     if (s != LUZ_OK) return s;
-    if ((s = ensure_lit_list(ctx, f)) != LUZ_OK) return s;
     luz_denoise_batch b{f->features, f->lin_depth, f->ao, nullptr, f->width, f->height, 1};
-    return run_infer(ctx, d, &b, f->ao_denoised, f->surf, f->lit_count);
+    return run_infer(ctx, d, &b, f->ao_denoised, f->dn_list, f->dn_count);
 }
 
 }  // extern "C"

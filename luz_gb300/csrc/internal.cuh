@@ -175,6 +175,8 @@ struct luz_frame {
     float* ao_denoised = nullptr;
     void* features = nullptr;       // 8 x bf16 per pixel (denoiser input)
     float* lin_depth = nullptr;
+    uint32_t* dn_list = nullptr;    // lit pixels in row-major order (x | y << 16), from the features pass
+    uint32_t* dn_count = nullptr;   // its length (device counter)
     float4* taa = nullptr;          // TAA output = next frame's history
     float4* taa_next = nullptr;
     uint32_t* compose = nullptr;    // BGRA8 tone-mapped output

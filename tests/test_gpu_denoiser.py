@@ -115,3 +115,42 @@ def test_frame_path_over_lit_pixels_matches_dense_batch(size):
         assert lit.sum() > 0 and np.all(framed[~lit] == 0.0)
     finally:
         ctx.close()
+
+
+def test_features_count_the_sample_bits():
+    """The features pass counts, per lit pixel, the set AO bits and the occluded shadow
+    bits over all sample planes (more than 32 of each: two groups of the per-lane load)."""
+    from oracle import denoiser as OD
+    ctx = L.Context(0)
+    try:
+        w, h = 200, 120
+        s = L.HostScene(1, width=w, height=h)
+        s.set_sampling(40, light_samples=8)           # 40 AO planes, 5 lights x 8 shadow planes
+        g = L.GPUScene(ctx, s)
+        g.render(0)
+        fr = g.frame
+        fr.denoise_features()
+        ctx.synchronize()
+        assert ctx.device_status() == 0
+        P, words = w * h, (w * h + 31) // 32
+
+        def counts(plane):
+            raw = fr.read(plane).reshape(-1).view(np.uint32)
+            planes = raw.size // words
+            bits = (raw.reshape(planes, words)[:, :, None] >> np.arange(32, dtype=np.uint32)) & 1
+            return bits.reshape(planes, -1)[:, :P].sum(0), planes
+
+        ao_hits, n_ao = counts(L.PLANE_AO_BITS)
+        sh_hits, n_sh = counts(L.PLANE_SHADOW_BITS)
+        assert n_ao == 40 and n_sh == 40
+        lit = np.linalg.norm(fr.read(L.PLANE_NORMAL).reshape(-1, 4)[:, :3], axis=1) > 0
+        assert lit.any()
+        ao = np.where(lit, ao_hits.astype(np.float32) / np.float32(n_ao), np.float32(0)).astype(np.float32)
+        assert np.array_equal(fr.read(L.PLANE_AO).reshape(-1), ao)
+        feat = fr.read(L.PLANE_FEATURES).reshape(-1, 8)
+        lit_frac = np.float32(1) - sh_hits.astype(np.float32) / np.float32(n_sh)
+        assert np.array_equal(OD.bf16_bits_to_f32(feat[lit, 0]), OD.bf16_round(ao[lit]))
+        assert np.array_equal(OD.bf16_bits_to_f32(feat[lit, 1]), OD.bf16_round(lit_frac[lit]))
+        assert np.all(feat[~lit] == 0)
+    finally:
+        ctx.close()
