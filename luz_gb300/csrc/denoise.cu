@@ -119,6 +119,13 @@ __global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
         __syncthreads();
         if (lit) F.list[s_base + s_warp[warp] + __popc(mask & ((1u << lane) - 1u))] = x | (y << 16);
     }
+    uint32_t a8 = 0, m8 = 0;
+    float depth = 0.f;
+    if (lit) {   // issued before the bit counts so that both wait on memory together
+        a8 = F.albedo[pix];
+        m8 = F.material[pix];
+        depth = F.depth[pix];
+    }
     uint32_t ao_hits = 0, shadow_hits = 0;
     if (__any_sync(0xFFFFFFFFu, lit)) {   // a warp's 32 pixels are the 32 bits of one word
         ao_hits = column_count(F.ao_bits, F.ao_samples, F.words, pix >> 5);
@@ -134,11 +141,10 @@ __global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
     }
     const float ao = F.ao_samples ? (float)ao_hits / (float)F.ao_samples : 1.0f;
     const float lit_frac = F.shadow_slots ? 1.0f - (float)shadow_hits / (float)F.shadow_slots : 1.0f;
-    uint32_t a8 = F.albedo[pix], m8 = F.material[pix];
     float lum = 0.2127f * c_lin_lut[a8 & 0xFF] + 0.7152f * c_lin_lut[(a8 >> 8) & 0xFF] +
                 0.0722f * c_lin_lut[(a8 >> 16) & 0xFF];
     float rough = (float)(m8 & 0xFF) / 255.0f;
-    V3 p = depth_to_world(F.inverse_proj, F.inverse_view, pixel_uv(x, F.width), pixel_uv(y, F.height), F.depth[pix]);
+    V3 p = depth_to_world(F.inverse_proj, F.inverse_view, pixel_uv(x, F.width), pixel_uv(y, F.height), depth);
     float d = length(p - V3{F.cam[0], F.cam[1], F.cam[2]});
     uint4 v;
     v.x = pack2(ao, lit_frac);
@@ -324,7 +330,7 @@ struct InferParams {
 // A block holds the weights once and kTcGroups warpgroups, each with its own tile,
 // A buffer, 64 accumulator columns, mbarrier and named barrier: while one group waits
 // for its products the others gather, or run their epilogues.
-constexpr int kTcGroups = 8;                    // warpgroups (tiles in flight) per block
+constexpr int kTcGroups = 6;                    // warpgroups (tiles in flight) per block
 constexpr int kTcThreads = 128 * kTcGroups;
 constexpr uint32_t kTcCols = 64;                // accumulator columns of one group (N)
 constexpr uint32_t kTcAlloc = 512;              // power of two >= kTcGroups * kTcCols
@@ -390,39 +396,28 @@ __device__ __forceinline__ void group_sync(uint32_t group) {
     asm volatile("bar.sync %0, 128;" :: "r"(group + 1u) : "memory");
 }
 
-// Barrier of one warpgroup that also ORs a flag over its threads (uniform result).
-__device__ __forceinline__ bool group_sync_or(uint32_t group, uint32_t flag) {
-    uint32_t r;
-    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, %2, 128, q;\n\t"
-                 "selp.u32 %0, 1, 0, p;\n\t}\n" : "=r"(r) : "r"(flag), "r"(group + 1u) : "memory");
-    return r != 0;
-}
-
 // Issues a layer from the group's first thread after the group's shared-memory writes
-// and accumulator reads, commits it and waits (that thread alone, bounded); the
-// group's barrier then hands the accumulator, and the outcome, to every lane. A wait
-// that ran out raises the status, waits once more (bounded) for the products in
-// flight, and stops the group (false).
-__device__ __forceinline__ bool tc_run_layer(uint32_t group, uint32_t tmem, uint32_t a_addr, uint32_t w_addr,
-                                             int ksteps, uint32_t bar, uint32_t& phase, uint32_t* status) {
+// and accumulator reads, commits it to the group's mbarrier, and every thread waits
+// (bounded) for the products. A thread whose wait runs out raises the status and waits
+// no more from then on (its results are then meaningless, but every barrier is still
+// met and every access stays in bounds); `failed` carries that across layers.
+__device__ __forceinline__ void tc_run_layer(uint32_t group, uint32_t tmem, uint32_t a_addr, uint32_t w_addr,
+                                             int ksteps, uint32_t bar, uint32_t& phase, bool& failed,
+                                             uint32_t* status) {
     asm volatile("fence.proxy.async.shared::cta;");
     asm volatile("tcgen05.fence::before_thread_sync;");
     group_sync(group);
     asm volatile("tcgen05.fence::after_thread_sync;");
-    uint32_t failed = 0;
     if ((threadIdx.x & 127u) == 0) {
         tc_layer(tmem, a_addr, w_addr, ksteps);
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar));
-        if (!tc_wait(bar, phase)) {
-            atomicOr(status, (uint32_t)LUZ_DEV_MMA_WAIT);
-            failed = 1u;
-            tc_wait(bar, phase);
-        }
+    }
+    if (!failed && !tc_wait(bar, phase)) {
+        atomicOr(status, (uint32_t)LUZ_DEV_MMA_WAIT);
+        failed = true;
     }
     phase ^= 1u;
-    const bool stop = group_sync_or(group, failed);
     asm volatile("tcgen05.fence::after_thread_sync;");
-    return !stop;
 }
 
 // relu(lo + b.x), relu(hi + b.y) rounded to BF16 and packed (lo in the low half): one
@@ -553,55 +548,61 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_k
     unsigned char* a = tsm + kTcA + group * kTcABytes;
     const uint32_t a_addr = smem_u32(a);
     uint32_t phase = 0;
+    bool failed = false;
     const uint32_t total = P.list ? *P.list_count : P.G.pixels * P.G.images;
     const uint32_t tiles = (total + 127) / 128;
-    for (uint32_t tile = blockIdx.x * kTcGroups + group; tile < tiles; tile += gridDim.x * kTcGroups) {
+    const uint32_t stride = gridDim.x * kTcGroups;
+    uint32_t tile = blockIdx.x * kTcGroups + group;
+    uint32_t next_xy = (P.list && tile * 128 + row < total) ? P.list[tile * 128 + row] : 0u;
+    for (; tile < tiles; tile += stride) {
         // features of pixel `row`: 9 taps of 8 channels (relative depth in channel 5), then 8 zeros
         const uint32_t item = tile * 128 + row;
         const bool has = item < total;
-        bool valid = false;
         uint32_t img = 0, gp = 0;
         int x = 0, y = 0;
-        float dc = 0.f, inv_dc = 0.f;
-        if (has) {
-            if (P.list) {
-                const uint32_t xy = P.list[item];
-                x = (int)(xy & 0xFFFFu);
-                y = (int)(xy >> 16);
-                gp = (uint32_t)y * P.G.width + (uint32_t)x;
-            } else {
-                gp = item;
-                img = gp / P.G.pixels;
-                const uint32_t local = gp - img * P.G.pixels;
-                x = (int)(local % P.G.width);
-                y = (int)(local / P.G.width);
-            }
-            dc = P.lin_depth[gp];
-            valid = dc > 0.0f;
-            inv_dc = valid ? 1.0f / dc : 0.0f;
+        if (P.list) {
+            x = (int)(next_xy & 0xFFFFu);
+            y = (int)(next_xy >> 16);
+            gp = (uint32_t)y * P.G.width + (uint32_t)x;
+            const uint32_t nitem = item + stride * 128;   // this thread's entry of the next tile
+            next_xy = nitem < total ? P.list[nitem] : 0u;
+        } else if (has) {
+            gp = item;
+            img = gp / P.G.pixels;
+            const uint32_t local = gp - img * P.G.pixels;
+            x = (int)(local % P.G.width);
+            y = (int)(local / P.G.width);
         }
+        // the centre depth and the 9 taps are loaded without waiting on one another
+        // (clamped, always in bounds); background centres get a zero row
+        const float dc = has ? P.lin_depth[gp] : 0.0f;
+        uint32_t tq[9];
+        float td[9];
 #pragma unroll
         for (int tap = 0; tap < 9; ++tap) {
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (valid) {
-                const int qx = min(max(x + tap % 3 - 1, 0), (int)P.G.width - 1);
-                const int qy = min(max(y + tap / 3 - 1, 0), (int)P.G.height - 1);
-                const uint32_t q = img * P.G.pixels + (uint32_t)qy * P.G.width + (uint32_t)qx;
-                v = P.feat[q];
-                const float dq = P.lin_depth[q];
-                const float rel = dq > 0.0f ? relative_depth(dq, dc, inv_dc) : 0.0f;
-                v.z = (v.z & 0xFFFFu) | (pack2(0.0f, rel) & 0xFFFF0000u);
-            }
+            const int qx = min(max(x + tap % 3 - 1, 0), (int)P.G.width - 1);
+            const int qy = min(max(y + tap / 3 - 1, 0), (int)P.G.height - 1);
+            tq[tap] = img * P.G.pixels + (uint32_t)qy * P.G.width + (uint32_t)qx;
+            td[tap] = has ? P.lin_depth[tq[tap]] : 0.0f;
+        }
+        const bool valid = dc > 0.0f;
+        const float inv_dc = valid ? 1.0f / dc : 0.0f;
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            uint4 v = has ? P.feat[tq[tap]] : make_uint4(0, 0, 0, 0);
+            const float rel = td[tap] > 0.0f ? relative_depth(td[tap], dc, inv_dc) : 0.0f;
+            v.z = (v.z & 0xFFFFu) | (pack2(0.0f, rel) & 0xFFFF0000u);
+            if (!valid) v = make_uint4(0, 0, 0, 0);
             *reinterpret_cast<uint4*>(a + core_offset(row, (uint32_t)tap, 10)) = v;
         }
         *reinterpret_cast<uint4*>(a + core_offset(row, 9, 10)) = make_uint4(0, 0, 0, 0);
-        if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW1), 5, bar, phase, status)) break;
+        tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW1), 5, bar, phase, failed, status);
         tc_relu_to_a(tmem_lane, sbias, a, row);
-        if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW2), 4, bar, phase, status)) break;
+        tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW2), 4, bar, phase, failed, status);
         tc_relu_to_a(tmem_lane, sbias + 64, a, row);
-        if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW3), 4, bar, phase, status)) break;
+        tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW3), 4, bar, phase, failed, status);
         tc_relu_to_a(tmem_lane, sbias + 128, a, row);
-        if (!tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW4), 4, bar, phase, status)) break;
+        tc_run_layer(group, tmem, a_addr, smem_u32(tsm + kTcW4), 4, bar, phase, failed, status);
         // softmax over the 49 logits and the 7x7 filter of the noisy AO
         const float2* b4 = reinterpret_cast<const float2*>(sbias + 192);
         float m = -3.0e38f;
@@ -627,6 +628,7 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_k
                              : ao_filter<false>(tmem_lane, b4, sbias[192 + 48], m, P.ao, base, x, y, P.G);
         if (has) P.out[gp] = valid ? r.x * (1.0f / r.y) : 0.0f;
     }
+    if (failed) tc_wait(bar, phase ^ 1u);   // products still in flight before the columns are freed
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(*tslot), "r"(kTcAlloc));
