@@ -45,33 +45,12 @@ struct LightParams {
     float4* out;
 };
 
-// light.frag:17-26
-__device__ __forceinline__ float distribution_ggx(V3 N, V3 H, float roughness) {
-    float a = roughness * roughness;
-    float a2 = a * a;
-    float NdotH = fmax_(dot(N, H), 0.0f);
-    float NdotH2 = NdotH * NdotH;
-    float nom = a2;
-    float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
-    denom = kPi * denom * denom;
-    return nom / denom;
-}
-// light.frag:28-36
-__device__ __forceinline__ float geometry_schlick_ggx(float NdotV, float roughness) {
-    float r = (roughness + 1.0f);
-    float k = (r * r) / 8.0f;
-    float nom = NdotV;
-    float denom = NdotV * (1.0f - k) + k;
-    return nom / denom;
-}
-// light.frag:38-45
-__device__ __forceinline__ float geometry_smith(V3 N, V3 V, V3 L, float roughness) {
-    float NdotV = fmax_(dot(N, V), 0.0f);
-    float NdotL = fmax_(dot(N, L), 0.0f);
-    float ggx2 = geometry_schlick_ggx(NdotV, roughness);
-    float ggx1 = geometry_schlick_ggx(NdotL, roughness);
-    return ggx1 * ggx2;
-}
+// The Cook-Torrance terms of light.frag:17-45 (DistributionGGX, GeometrySchlickGGX,
+// GeometrySmith) are evaluated inline in light_pass_kernel, their quotients folded into
+// one division per light: D * G / (4 NdotV NdotL + 1e-4) =
+// a2 NdotV NdotL / (pi dd^2 gv gl (4 NdotV NdotL + 1e-4)).
+constexpr float kInvPi = 1.0f / kPi;
+
 // light.frag:47-49; pow(x, 5.0) evaluated as x^4 * x.
 __device__ __forceinline__ V3 fresnel_schlick(float cos_theta, V3 F0) {
     float x = clamp01(1.0f - cos_theta);
@@ -121,6 +100,12 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     V3 V = normalize(cam - p);
     V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + albedo * metallic;
     V3 Lo = V3{0.0f, 0.0f, 0.0f};
+    // per-pixel parts of the Cook-Torrance terms (light.frag:17-49, 210-229)
+    const float a = roughness * roughness, a2 = a * a;
+    const float r1 = roughness + 1.0f, k = (r1 * r1) / 8.0f;
+    const float NdotV = fmax_(dot(N, V), 0.0f);
+    const float gv = NdotV * (1.0f - k) + k;                 // GeometrySchlickGGX(NdotV) denominator
+    const V3 diffuse_albedo = albedo * ((1.0f - metallic) * kInvPi);
     // EvaluateShadow's origin (light.frag:138-139), used by the 2D shadow maps
     const V3 shadow_origin = p + N * fmax_(length(p - cam) * 0.01f, 0.05f);
     for (uint32_t i = 0; i < P.light_count; ++i) {
@@ -145,15 +130,18 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
         V3 color = V3{lt.color[0], lt.color[1], lt.color[2]};
         V3 radiance = ((color * lt.intensity) * attenuation) * (1.0f - shadow);
         V3 H = normalize(V + L);
-        float NDF = distribution_ggx(N, H, roughness);
-        float G = geometry_smith(N, V, L, roughness);
+        const float NdotH = fmax_(dot(N, H), 0.0f);
+        const float NdotL = fmax_(dot(N, L), 0.0f);
+        const float dd = NdotH * NdotH * (a2 - 1.0f) + 1.0f;
+        const float gl = NdotL * (1.0f - k) + k;
         V3 F = fresnel_schlick(clamp01(dot(H, V)), F0);
-        V3 num = (NDF * G) * F;
-        float denom = (4.0f * fmax_(dot(N, V), 0.0f)) * fmax_(dot(N, L), 0.0f) + 0.0001f;
-        V3 spec = num / denom;
-        V3 kD = (V3{1.0f, 1.0f, 1.0f} - F) * (1.0f - metallic);
-        float NdotL = fmax_(dot(N, L), 0.0f);
-        Lo = Lo + ((kD * albedo) / kPi + spec) * radiance * NdotL;
+        // D * G / (4 NdotV NdotL + 1e-4) with D = a2 / (pi dd^2) and
+        // G = NdotV NdotL / (gv gl), as one quotient
+        const float spec_scale = (a2 * (NdotV * NdotL)) /
+                                 ((kPi * dd * dd) * (gv * gl) * ((4.0f * NdotV) * NdotL + 0.0001f));
+        V3 spec = F * spec_scale;
+        V3 diffuse = (V3{1.0f, 1.0f, 1.0f} - F) * diffuse_albedo;
+        Lo = Lo + (diffuse + spec) * radiance * NdotL;
     }
     float ao;
     if (P.use_denoised) {
