@@ -367,17 +367,13 @@ __global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, un
     const unsigned long long total = (unsigned long long)lit * (S.shadow_slots + S.ao_samples);
     if (k0 >= total) return;
     const unsigned long long end = min(total, k0 + chunk);
-    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const uint32_t stride = gridDim.x * blockDim.x;
     const float ninf = __int_as_float(0xff800000);
-    for (unsigned long long item = k0 + blockIdx.x * blockDim.x + threadIdx.x; item < end; item += stride) {
-        uint32_t slot, j;
-        if (total <= 0xFFFFFFFFull) {
-            slot = (uint32_t)item / lit;
-            j = (uint32_t)item - slot * lit;
-        } else {
-            slot = (uint32_t)(item / lit);
-            j = (uint32_t)(item - (unsigned long long)slot * lit);
-        }
+    // (slot, j) of the thread's first item by one division, then stepped by the stride
+    unsigned long long item = k0 + blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t slot = (uint32_t)(item / lit), j = (uint32_t)(item - (unsigned long long)slot * lit);
+    const uint32_t step_slot = stride / lit, step_j = stride - step_slot * lit;
+    for (; item < end; item += stride) {
         V3 wo, wd;
         float tmin, tmax;
         uint32_t* out;
@@ -386,6 +382,9 @@ __global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, un
         bool ok = gen_ray(S, C, slot, j, wo, wd, tmin, tmax, out, record_hit, pix);
         rays_a[item - k0] = make_float4(wo.x, wo.y, wo.z, ok ? tmax : ninf);
         if (ok) rays_b[item - k0] = make_float4(wd.x, wd.y, wd.z, __uint_as_float(pix));   // read only for rays
+        slot += step_slot;
+        j += step_j;
+        if (j >= lit) { j -= lit; ++slot; }
     }
 }
 
@@ -617,8 +616,14 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         f->rays_cap = need;
     }
     const unsigned long long chunk = std::min<unsigned long long>(max_items, f->rays_cap);
+    static int raygen_blocks = 0;   // resident 256-thread blocks per SM: the grid is one wave
+    if (raygen_blocks == 0) {
+        LUZ_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&raygen_blocks, raygen_kernel, 256, 0));
+        raygen_blocks = std::max(raygen_blocks, 1);
+    }
     for (unsigned long long k0 = 0; k0 < max_items; k0 += chunk) {
-        raygen_kernel<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b);
+        raygen_kernel<<<(uint32_t)(ctx->sm_count * raygen_blocks), 256, 0, st>>>(S, C, k0, chunk, f->rays_a,
+                                                                                  f->rays_b);
         LUZ_LAUNCHED(ctx, "raygen_kernel");
         if (d_stats) {
             if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, d_stats);
