@@ -72,6 +72,47 @@ __device__ __forceinline__ float sample1(const float* __restrict__ img, uint32_t
 }
 
 // ---------------------------------------------------------------- TAA (taa.comp)
+// A 16x16 block of pixels stages a 20x20 tile of the light image and of the depth
+// (texel origin - 2, wrapped with the sampler's repeat addressing): every tap of
+// find_closest_3x3, get_motion_vector and get_neighbor_3x3 lies at an offset of -1, 0
+// or +1 pixel, whose bilinear footprint spans texels x - 2 .. x + 2. Tile slot t of a
+// row holds texel wrap(origin + t), so the footprint's texels wrap(fx), wrap(fx + 1)
+// sit in slots fx - origin and fx - origin + 1: the same values, the same arithmetic.
+// The history sample follows the motion vector and reads global memory.
+constexpr int kTaaTile = 16, kTaaSpan = kTaaTile + 4;
+
+__device__ __forceinline__ int taa_slot(int f, int origin) { return min(max(f - origin, 0), kTaaSpan - 2); }
+
+// One axis of bilinear(): the footprint's first tile slot and the two weights. The
+// taps of a pixel share three u and three v positions, so a 3x3 neighbourhood needs
+// three of each (the same operations bilinear() performs per tap).
+struct TapAxis {
+    int slot;
+    float a, b;
+};
+__device__ __forceinline__ TapAxis tap_axis(float u, uint32_t n, int origin) {
+    float x = u * (float)n - 0.5f;
+    if (!isfinite(x)) x = 0.0f;
+    const float f = floorf(x);
+    TapAxis t;
+    t.a = x - f;
+    t.b = 1.0f - t.a;
+    t.slot = taa_slot((int)f, origin);
+    return t;
+}
+__device__ __forceinline__ float tap1(const float* tile, TapAxis X, TapAxis Y) {
+    const float* r0 = tile + Y.slot * kTaaSpan + X.slot;
+    return (r0[0] * X.b + r0[1] * X.a) * Y.b + (r0[kTaaSpan] * X.b + r0[kTaaSpan + 1] * X.a) * Y.a;
+}
+__device__ __forceinline__ float4 tap4(const float4* tile, TapAxis X, TapAxis Y) {
+    const float4* r0 = tile + Y.slot * kTaaSpan + X.slot;
+    const float4 c00 = r0[0], c10 = r0[1], c01 = r0[kTaaSpan], c11 = r0[kTaaSpan + 1];
+    return make_float4((c00.x * X.b + c10.x * X.a) * Y.b + (c01.x * X.b + c11.x * X.a) * Y.a,
+                       (c00.y * X.b + c10.y * X.a) * Y.b + (c01.y * X.b + c11.y * X.a) * Y.a,
+                       (c00.z * X.b + c10.z * X.a) * Y.b + (c01.z * X.b + c11.z * X.a) * Y.a,
+                       (c00.w * X.b + c10.w * X.a) * Y.b + (c01.w * X.b + c11.w * X.a) * Y.a);
+}
+
 struct TaaParams {
     const float4* input;     // this frame's light image
     const float4* history;   // last frame's TAA output
@@ -95,9 +136,9 @@ __device__ __forceinline__ float luminance(float r, float g, float b) {
     return r * 0.2127f + g * 0.7152f + b * 0.0722f;
 }
 
-// taa.comp:16-26 (get_motion_vector): screen-space motion of the surface at uv.
-__device__ __forceinline__ void motion_vector(const TaaParams& P, float u, float v, float& mx, float& my) {
-    float depth = sample1(P.depth, P.w, P.h, u, v);
+// taa.comp:16-26 (get_motion_vector): screen-space motion of the surface at (u, v),
+// given the depth sampled there.
+__device__ __forceinline__ void motion_at(const TaaParams& P, float u, float v, float depth, float& mx, float& my) {
     V3 wp = depth_to_world(P.inverse_proj, P.inverse_view, u, v, depth);
     float p4[4] = {wp.x, wp.y, wp.z, 1.0f}, prev[4], cur[4];
     mat4_mul_vec4(P.prev_view_proj, p4, prev);
@@ -106,28 +147,6 @@ __device__ __forceinline__ void motion_vector(const TaaParams& P, float u, float
     float cx = cur[0] / cur[3], cy = cur[1] / cur[3];
     mx = ((cx - P.jitter[0]) - (px - P.prev_jitter[0])) * 0.5f;
     my = ((cy - P.jitter[1]) - (py - P.prev_jitter[1])) * 0.5f;
-}
-
-// taa.comp:111-132 (find_closest_3x3): uv of the nearest depth in the 3x3 around uv.
-__device__ __forceinline__ void closest_3x3(const TaaParams& P, float u, float v, float& cu, float& cv) {
-    const float ddx = fabsf(1.0f / (float)P.w), ddy = fabsf(1.0f / (float)P.h);
-    float best_x = -1.0f, best_y = -1.0f, best_z = 0.0f;
-    bool first = true;
-    for (int dy = -1; dy <= 1; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-            // uv -/+ dv -/+ du, one component at a time as the GLSL vec2 arithmetic does
-            float su = dx < 0 ? u - ddx : (dx > 0 ? u + ddx : u);
-            float sv = dy < 0 ? v - ddy : (dy > 0 ? v + ddy : v);
-            float z = sample1(P.depth, P.w, P.h, su, sv);
-            if (first || best_z > z) {
-                best_x = (float)dx;
-                best_y = (float)dy;
-                best_z = z;
-                first = false;
-            }
-        }
-    cu = u + ddx * best_x;
-    cv = v + ddy * best_y;
 }
 
 // taa.comp:134-157 (clip_aabb, vec4 form).
@@ -147,24 +166,50 @@ __device__ __forceinline__ float4 clip_aabb(float mnx, float mny, float mnz, flo
 }
 
 __global__ void __launch_bounds__(256) taa_kernel(TaaParams P) {
-    uint32_t x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+    __shared__ float4 s_light[kTaaSpan * kTaaSpan];
+    __shared__ float s_depth[kTaaSpan * kTaaSpan];
+    const int ox = (int)(blockIdx.x * kTaaTile) - 2, oy = (int)(blockIdx.y * kTaaTile) - 2;
+    for (int i = threadIdx.x; i < kTaaSpan * kTaaSpan; i += blockDim.x) {
+        const uint32_t tx = repeat_index((float)(ox + i % kTaaSpan), P.w);
+        const uint32_t ty = repeat_index((float)(oy + i / kTaaSpan), P.h);
+        s_light[i] = __ldg(P.input + (size_t)ty * P.w + tx);
+        s_depth[i] = __ldg(P.depth + (size_t)ty * P.w + tx);
+    }
+    __syncthreads();
+    uint32_t x = blockIdx.x * kTaaTile + (threadIdx.x & 15), y = blockIdx.y * kTaaTile + (threadIdx.x >> 4);
     if (x >= P.w || y >= P.h) return;
     const float su = ((float)x + 0.5f) / (float)P.w, sv = ((float)y + 0.5f) / (float)P.h;
-    float cu, cv, mx, my;
-    closest_3x3(P, su, sv, cu, cv);
-    motion_vector(P, cu, cv, mx, my);
+    // the three u and v of the 3x3 taps (uv -/+ 1/size, one component at a time as the
+    // GLSL vec2 arithmetic does; find_closest_3x3 and get_neighbor_3x3 use the same)
+    const float du = 1.0f / (float)P.w, dv = 1.0f / (float)P.h;
+    const float us[3] = {su - du, su, su + du}, vs[3] = {sv - dv, sv, sv + dv};
+    TapAxis ax[3], ay[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        ax[k] = tap_axis(us[k], P.w, ox);
+        ay[k] = tap_axis(vs[k], P.h, oy);
+    }
+    // find_closest_3x3 (taa.comp:111-132); the motion vector's depth sample at the
+    // chosen tap is that tap's depth (taa.comp:16-26)
+    int bi = 0, bj = 0;
+    float best_z = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float z = tap1(s_depth, ax[i], ay[j]);
+            if ((i == 0 && j == 0) || best_z > z) { bi = i; bj = j; best_z = z; }
+        }
+    const float cu = su + du * (float)(bi - 1), cv = sv + dv * (float)(bj - 1);
+    float mx, my;
+    motion_at(P, cu, cv, best_z, mx, my);
     const float hu = su - mx, hv = sv - my;
     float4 hist = sample4(P.history, P.w, P.h, hu, hv);
     // get_neighbor_3x3 (taa.comp:28-93)
-    const float du = 1.0f / (float)P.w, dv = 1.0f / (float)P.h;
     float4 c[9];
     const float mw[3] = {mitchell(sqrtf(2.0f)), mitchell(1.0f), mitchell(0.0f)};   // |d| = sqrt2, 1, 0
-    for (int k = 0; k < 9; ++k) {
-        int dx = k % 3 - 1, dy = k / 3 - 1;
-        float u = dx < 0 ? su - du : (dx > 0 ? su + du : su);
-        float v = dy < 0 ? sv - dv : (dy > 0 ? sv + dv : sv);
-        c[k] = sample4(P.input, P.w, P.h, u, v);
-    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) c[k] = tap4(s_light, ax[k % 3], ay[k / 3]);
     // order tl tc tr ml mc mr bl bc br = c[0..8]
     float4 cmin = gmin4(c[0], gmin4(c[1], gmin4(c[2], gmin4(c[3], gmin4(c[4], gmin4(c[5], gmin4(c[6], gmin4(c[7], c[8]))))))));
     float4 cmax = gmax4(c[0], gmax4(c[1], gmax4(c[2], gmax4(c[3], gmax4(c[4], gmax4(c[5], gmax4(c[6], gmax4(c[7], c[8]))))))));
@@ -188,7 +233,7 @@ __global__ void __launch_bounds__(256) taa_kernel(TaaParams P) {
         }
         src = div4(src, wsum);
     }
-    if (P.reconstruct == 0 || anynan4(src)) src = sample4(P.input, P.w, P.h, su, sv);
+    if (P.reconstruct == 0 || anynan4(src)) src = c[4];   // the centre tap is texture(input, uv)
     float4 out;
     if (hu > 1.0f || hv > 1.0f || hu < 0.0f || hv < 0.0f) {
         out = src;
@@ -225,7 +270,7 @@ luz_status launch_taa(luz_ctx* ctx, luz_frame* f, int reconstruct) {
     memcpy(P.prev_view_proj, s.prev_view_proj, 64);
     memcpy(P.jitter, s.jitter, 8);
     memcpy(P.prev_jitter, s.prev_jitter, 8);
-    dim3 grid((f->width + 15) / 16, (f->height + 15) / 16);
+    dim3 grid((f->width + kTaaTile - 1) / kTaaTile, (f->height + kTaaTile - 1) / kTaaTile);
     taa_kernel<<<grid, 256, 0, ctx->stream>>>(P);
     LUZ_LAUNCHED(ctx, "taa_kernel");
     std::swap(f->taa, f->taa_next);   // the output is the next frame's history

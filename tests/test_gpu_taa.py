@@ -18,11 +18,12 @@ def _frame(g, s):
     return light, depth
 
 
+@pytest.mark.parametrize("size", [(96, 72), (13, 10)])   # partial 16x16 blocks; an image narrower than a tile
 @pytest.mark.parametrize("reconstruct", [True, False])
-def test_taa_sequence_matches_oracle(reconstruct):
+def test_taa_sequence_matches_oracle(reconstruct, size):
     ctx = L.Context(0)
     try:
-        s = L.HostScene(1, width=96, height=72)
+        s = L.HostScene(1, width=size[0], height=size[1])
         g = L.GPUScene(ctx, s)
         hist = np.zeros((s.height, s.width, 4), np.float32)
         cam = s.camera()
@@ -35,7 +36,7 @@ def test_taa_sequence_matches_oracle(reconstruct):
             s.next_frame(jitter=True)
             light, depth = _frame(g, s)
             if k == 3:
-                light[5, 7, 1] = np.nan   # a NaN source texel
+                light[5, 7 % s.width, 1] = np.nan   # a NaN source texel
                 g.frame.write(L.PLANE_LIGHT, light)
             g.frame.taa(reconstruct)
             ctx.synchronize()
