@@ -486,8 +486,12 @@ luz_status luz_denoiser_set_weights(luz_ctx* ctx, luz_denoiser* d, const float* 
 luz_status luz_denoiser_get_weights(luz_ctx* ctx, luz_denoiser* d, float* params);
 /* Computes the features, distances and noisy AO planes of a traced frame. */
 luz_status luz_denoise_features(luz_ctx* ctx, luz_frame* frame);
-/* Features + network + filter: writes LUZ_PLANE_AO_DENOISED. */
+/* Features + network + filter: writes LUZ_PLANE_AO_DENOISED. The network runs over the
+ * frame's lit pixels only (length(N) != 0); background pixels receive 0. */
 luz_status luz_denoise(luz_ctx* ctx, luz_denoiser* d, luz_frame* frame);
+/* The network + filter over every pixel of a batch into d_out (W x H x images floats);
+ * pixels with lin_depth <= 0 receive 0. Agrees bit for bit with luz_denoise on the same
+ * planes. */
 luz_status luz_denoise_batch_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* d_out);
 /* Mean squared error against target_ao and its gradient (host array of
  * LUZ_DENOISER_PARAMS, may be NULL); deterministic. */
