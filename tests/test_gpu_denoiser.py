@@ -154,3 +154,27 @@ def test_features_count_the_sample_bits():
         assert np.all(feat[~lit] == 0)
     finally:
         ctx.close()
+
+
+def test_frame_with_nothing_lit_denoises_to_zero():
+    """An empty lit-pixel list: the network runs over no tile and every pixel of the
+    denoised plane is the background's 0."""
+    ctx = L.Context(0)
+    try:
+        from luz_gb300 import denoiser as D
+        s = L.HostScene(1, width=64, height=48)
+        cam = s.camera()
+        cam.mode = 2
+        cam.eye[:] = (0.0, 50.0, 0.0)
+        cam.center[:] = (0.0, 100.0, 1.0)       # looking up into empty sky
+        s.set_camera(cam)
+        g = L.GPUScene(ctx, s)
+        g.render(0)
+        den = D.Denoiser(ctx, seed=4)
+        den.denoise(g.frame)
+        ctx.synchronize()
+        assert ctx.device_status() == 0
+        assert g.frame.lit_count() == 0
+        assert np.all(g.frame.read(L.PLANE_AO_DENOISED) == 0.0)
+    finally:
+        ctx.close()

@@ -18,7 +18,7 @@ def _frame(g, s):
     return light, depth
 
 
-@pytest.mark.parametrize("size", [(96, 72), (13, 10)])   # partial 16x16 blocks; an image narrower than a tile
+@pytest.mark.parametrize("size", [(96, 72), (13, 10), (3, 2)])   # partial blocks; images narrower than a tile
 @pytest.mark.parametrize("reconstruct", [True, False])
 def test_taa_sequence_matches_oracle(reconstruct, size):
     ctx = L.Context(0)
@@ -36,7 +36,7 @@ def test_taa_sequence_matches_oracle(reconstruct, size):
             s.next_frame(jitter=True)
             light, depth = _frame(g, s)
             if k == 3:
-                light[5, 7 % s.width, 1] = np.nan   # a NaN source texel
+                light[5 % s.height, 7 % s.width, 1] = np.nan   # a NaN source texel
                 g.frame.write(L.PLANE_LIGHT, light)
             g.frame.taa(reconstruct)
             ctx.synchronize()
