@@ -235,7 +235,9 @@ uint32_t luz_blas_primitive_count(const luz_blas* blas);
  * buffers: vertices (luz_vertex, 48-B stride) and u32 indices as input; as output
  * nodes (max(n-1,1) x 64 B), triangles (n x 48 B), sorted Morton codes and sorted
  * primitive order (n x 4 B each), n = index_count / 3. The result is byte-identical
- * to luz_blas_build's (same layouts as luz_blas_download).
+ * to luz_blas_build's (same layouts as luz_blas_download): the binary LBVH only.
+ * It is not a luz_blas: the 4-wide nodes that the visibility and G-buffer traversals
+ * walk are not built, and no entry point takes these buffers as a TLAS instance.
  *
  * Every temporary lives in one file-scope device array of LUZ_NOALLOC_SCRATCH_BYTES
  * (about 10.3 MiB), which every GPU that loads the library holds until the process
@@ -243,14 +245,20 @@ uint32_t luz_blas_primitive_count(const luz_blas* blas);
  * work. No cudaMalloc, cudaFree or allocating library routine is called.
  *
  * `stream` is a cudaStream_t (NULL = the legacy default stream); the call waits for
- * its own work on that stream before it returns. The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) with that device current; make
- * that first call before any stream capture. All calls share the one array and it
+ * its own work on that stream before it returns. Every call outside a stream capture
+ * looks up the array's device address (cudaGetSymbolAddress) with the current device
+ * current, so a context torn down and created again after an earlier call is served
+ * at the array's new address; a call inside a capture reuses the address of the last
+ * call outside one, so make the first call on a device before any stream capture
+ * (LUZ_ERR_INVALID otherwise). All calls share the one array and it
  * keeps the last call's contents (each call resets what it reads before writing):
  * calls that overlap on the GPU, from several host threads or streams, race.
  * Returns LUZ_ERR_INVALID for bad arguments or an index outside the vertex buffer
  * (checked on the device, the bad index is never dereferenced), LUZ_ERR_DEVICE if a
- * kernel raised its status word, LUZ_ERR_CUDA if a CUDA call failed. */
+ * kernel raised its status word, LUZ_ERR_CUDA if a CUDA call failed. After
+ * LUZ_ERR_INVALID from the index check, LUZ_ERR_DEVICE or LUZ_ERR_CUDA the output
+ * buffers hold undefined contents (the build ran with the bad indices replaced by 0).
+ * n = 0 writes one empty root node (inverted boxes) and nothing else. */
 #define LUZ_NOALLOC_MAX_TRIANGLES (1u << 17)
 #define LUZ_NOALLOC_SCRATCH_BYTES 10756608u
 luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint32_t vertex_count,

@@ -117,19 +117,26 @@ extern "C" luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint3
     int dev = 0;
     NOALLOC_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return LUZ_ERR_LIMIT;
-    // Set-up, once per device with that device current: the address of g_scratch as
-    // the device sees it (the symbol itself is only a host-side stand-in).
+    cudaStream_t st = (cudaStream_t)stream;
+    // The address of g_scratch as the device sees it (the symbol itself is only a
+    // host-side stand-in), looked up with this device current. Outside a stream
+    // capture it is looked up on every call, so a context that was torn down and
+    // created again (cudaDeviceReset) gets the array's new address; inside a capture
+    // the address of the last call outside one is used.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    NOALLOC_CUDA(cudaStreamIsCapturing(st, &capture));
     unsigned char* base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_mutex);
-        if (!g_scratch_ptr[dev]) {
+        if (capture == cudaStreamCaptureStatusNone) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return LUZ_ERR_CUDA;
             g_scratch_ptr[dev] = p;
+        } else if (!g_scratch_ptr[dev]) {
+            return LUZ_ERR_INVALID;   // first call on this device inside a capture
         }
         base = (unsigned char*)g_scratch_ptr[dev];
     }
-    cudaStream_t st = (cudaStream_t)stream;
     Header* h = (Header*)(base + kOffHeader);
     uint32_t* status = &h->status;
     uint32_t* zero = &h->zero;

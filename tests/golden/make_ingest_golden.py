@@ -15,7 +15,7 @@ ref` from the reference tree) and stores what the reference produced:
                         point/spot/directional.obj) through its importer
 
 Run from the repository root where the reference tree exists:
-    python tests/golden/make_ingest_golden.py [--reference /root/reference]
+    python tests/golden/make_ingest_golden.py [--reference <reference tree>]
 """
 import argparse
 import base64
@@ -32,6 +32,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "ingest")
 ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle.reference_tree import reference_root  # noqa: E402
 
 
 def png_bytes(rgba: np.ndarray) -> bytes:
@@ -237,8 +239,10 @@ def mesh_digest(v: np.ndarray, i: np.ndarray) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("LUZ_REF_ROOT", "/root/reference"))
+    ap.add_argument("--reference", default=reference_root())
     args = ap.parse_args()
+    if not args.reference:
+        sys.exit("the reference tree was not found: set LUZ_REF_ROOT or pass --reference")
     os.makedirs(OUT, exist_ok=True)
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"LUZ_REF_ROOT={args.reference}"],
                    check=True)

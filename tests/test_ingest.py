@@ -20,10 +20,11 @@ import numpy as np
 import pytest
 
 import luz_gb300 as L
+from oracle.reference_tree import reference_root
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden", "ingest")
-REF_ROOT = os.environ.get("LUZ_REF_ROOT", "/root/reference")
+REF_ROOT = reference_root()
 REF_LIB = os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libluz_ref_ingest.so")
 
 
@@ -183,8 +184,8 @@ def _digest(v, i):
 @pytest.mark.parametrize("name", ["cube.glb", "point.obj", "spot.obj", "directional.obj"])
 def test_reference_assets(name):
     """The reference repository's own assets: digests of what its importer made."""
-    path = os.path.join(REF_ROOT, "assets", name)
-    if not os.path.exists(path):
+    path = os.path.join(REF_ROOT, "assets", name) if REF_ROOT else None
+    if path is None or not os.path.exists(path):
         pytest.skip("reference assets not present")
     g = gold("ref_assets.json")[name]
     s = L.HostScene.import_file(path, 64, 64)
