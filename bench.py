@@ -28,7 +28,6 @@ import argparse
 import ctypes as C
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -80,16 +79,6 @@ def measured_peaks():
             d = json.load(f)
         return d.get("hbm_gbs", FALLBACK_HBM_GBS), "measured"
     return FALLBACK_HBM_GBS, "fallback"
-
-
-def profiled(key: str):
-    """A figure of the committed ncu summary of the visibility kernel (full 1080p
-    launch): dram_bytes_per_launch, issue_active_frac."""
-    p = os.path.join(ROOT, "profiles", "visibility_kernel_config2.md")
-    if not os.path.exists(p):
-        return None
-    m = re.search(key + r":\s*([0-9.eE+]+)", open(p).read())
-    return float(m.group(1)) if m else None
 
 
 class Clocks:
@@ -542,11 +531,17 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     clocks.start()
     launches0 = ctx.launch_count()
+    ctx.profile(True)          # an event pair around each launch of the instrumented kernels
     for k in range(K):
         flush.zero_()
         frame(args.warmup + k, evs[k])
     torch.cuda.synchronize()
     launches = ctx.launch_count() - launches0
+    kernel_ms = {}
+    for name in ("tlas_build", "gbuffer", "raygen", "traversal", "light_pass"):
+        tot, n = ctx.profile_read(name)
+        kernel_ms[name] = {"ms_per_launch": tot / max(n, 1), "launches": n}
+    ctx.profile(False)
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
@@ -562,24 +557,35 @@ def run_ours(args, rank, world, local):
     if ctx.device_status() != 0:
         raise RuntimeError("device status word raised during timing")
 
-    # roofline of the dominant stage (visibility: ray generation + traversal):
-    # algorithmic bytes per frame. Every item's 32-B ray record is written and read;
-    # a traversed ray writes its bit, a 4-wide node visit reads 7 of its 8 float4
-    # (112 B), a triangle test 48 B, an instance entry 80 B.
-    vis_bytes = (lit * S * 64 + stats["rays"] * 0.125 + (stats["tlas_nodes"] + stats["blas_nodes"]) * 112 +
-                 stats["tris"] * 48 + stats["instances"] * 80)
-    vis_s = stage_ms["visibility"] * 1e-3
+    # Roofline of the dominant kernel, the traversal (visibility_kernel): algorithmic
+    # bytes per launch = ray records read (32 B per item, written by ray generation) +
+    # hit bits (1/8 B per traversed ray) + 4-wide node visits x 112 B (7 of the 8
+    # float4) + triangle tests x 48 B + instance entries x 80 B, with the visits counted
+    # by the counting build of the same kernel over the same frame. The node and triangle
+    # loads are served by L1 and L2 (the BVH is read from HBM about once per frame), so
+    # the bound is the L2 read bandwidth, measured in this run by L2-only 16-B loads
+    # over a 48 MiB buffer on every SM.
+    trav_bytes = (lit * S * 32 + stats["rays"] * 0.125 + (stats["tlas_nodes"] + stats["blas_nodes"]) * 112 +
+                  stats["tris"] * 48 + stats["instances"] * 80)
+    trav_ms = kernel_ms["traversal"]["ms_per_launch"]
+    l2_gbs = ctx.probe_l2_read_gbs(48 << 20, 50)
     peak, peak_kind = measured_peaks()
-    achieved = vis_bytes / vis_s / 1e9
-    roofline = {"bound": "hbm", "kernel": "visibility_kernel", "achieved": achieved, "peak": peak,
-                "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profiled("dram_bytes_per_launch"), "algorithmic_bytes": vis_bytes,
-                "note": "visibility stage = raygen_kernel + visibility_kernel (CUDA events around both); "
-                        "algorithmic bytes are served 98% by L1/L2 (traffic = DRAM bytes of the traversal "
-                        "launch); the traversal is issue-bound",
-                "issue_active_frac": profiled("issue_active_frac"),
+    achieved = trav_bytes / (trav_ms * 1e-3) / 1e9
+    roofline = {"bound": "l2", "kernel": "visibility_kernel", "achieved": achieved, "peak": l2_gbs,
+                "peak_source": "measured in this run (L2-only loads, 48 MiB, every SM)", "unit": "GB/s",
+                "frac": achieved / l2_gbs, "traffic": None, "algorithmic_bytes": trav_bytes,
+                "ms_per_launch": trav_ms,
+                "note": "traffic (DRAM bytes per launch) comes from an ncu capture, not from this run; "
+                        "the kernel is issue-bound (about 73 % of issue slots, half the lanes active)",
                 "per_ray": {k: stats[k] / max(stats["rays"], 1) for k in
                             ("tlas_nodes", "blas_nodes", "tris", "instances")}}
+    # the light pass against HBM: per lit pixel the 32-B surface record, albedo /
+    # material / emission (12 B), its shadow and AO bits and the 16-B RGBA32F result
+    lp_bytes = lit * (32 + 12 + 16 + S / 8.0)
+    lp_ms = kernel_ms["light_pass"]["ms_per_launch"]
+    light_pass = {"bound": "hbm", "achieved": lp_bytes / (lp_ms * 1e-3) / 1e9, "peak": peak,
+                  "peak_source": peak_kind, "unit": "GB/s", "algorithmic_bytes": lp_bytes, "ms_per_launch": lp_ms}
+    light_pass["frac"] = light_pass["achieved"] / peak
 
     # e2e through the C ABI from pinned host buffers
     e2e = None
@@ -658,10 +664,17 @@ def run_ours(args, rank, world, local):
                              "the light pass cannot depend on it (weight max(dot(N, L), 0) = 0 or zero "
                              "unshadowed radiance) is resolved at generation without traversal, the "
                              "image is unchanged; rays_traversed_per_frame are the rays actually traced.",
-                "lit_pixels": lit, "stage_ms": stage_ms,
-                "blas_build": {"ms": g.blas_build_ms, "triangles": g.blas_prims, "meshes": len(g.blas),
-                               "note": "one batched device build, host->device vertex/index copies included"},
-                "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "traversed_grays_per_s": world * (scene.width * scene.height + stats["rays"]) / (ms * 1e-3) / 1e9,
+                "lit_pixels": lit, "stage_ms": stage_ms, "kernel_ms": kernel_ms,
+                "blas_build": {"ms": g.blas_build_ms, "device_ms": g.blas_build_device_ms,
+                               "triangles": g.blas_prims, "meshes": len(g.blas),
+                               "algorithmic_bytes_per_triangle": 248,
+                               "device_gbs": 248.0 * g.blas_prims / (g.blas_build_device_ms * 1e-3) / 1e9,
+                               "hbm_frac": 248.0 * g.blas_prims / (g.blas_build_device_ms * 1e-3) / 1e9 / peak,
+                               "note": "one batched build; ms includes the host->device vertex/index copies, "
+                                       "device_ms is the device pipeline after them (CUDA events)"},
+                "gpu_launches": launches, "roofline": roofline, "light_pass_roofline": light_pass,
+                "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk, "denoised_vs_plain": denoised, "batched_uneven_64": batched,
                 "stress_4k_4096_instances": stress, "post_passes_1080p": post}
         print(json.dumps(line), flush=True)

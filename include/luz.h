@@ -214,6 +214,33 @@ typedef struct luz_vis_tuning {
 luz_status luz_ctx_set_vis_tuning(luz_ctx* ctx, const luz_vis_tuning* tuning);
 luz_status luz_ctx_get_vis_tuning(const luz_ctx* ctx, luz_vis_tuning* tuning);
 
+/* Measurement hooks (no counterpart in the reference, which times passes with GPU
+ * timestamp queries, source/Core/main.cpp:236-308). luz_ctx_last_blas_build_ms: the
+ * device time of the last luz_blas_build[_batch] of this context from the end of its
+ * host->device copies to its last kernel (CUDA events on the context's stream).
+ * luz_ctx_probe_l2_read: the L2 read bandwidth in GB/s, from `reps` passes of 16-B
+ * L2-only loads over a `bytes` buffer (allocated and freed by the call; keep it below
+ * the L2 size, e.g. 48 MiB) on every SM. */
+luz_status luz_ctx_last_blas_build_ms(luz_ctx* ctx, float* device_ms);
+luz_status luz_ctx_probe_l2_read(luz_ctx* ctx, uint64_t bytes, uint32_t reps, float* gbs);
+/* Per-kernel device time: with profiling on, every launch of the kernels below is
+ * bracketed by a pair of CUDA events on the context's stream (not while the stream is
+ * being captured into a graph). luz_ctx_profile(ctx, 1) clears earlier records and
+ * starts, (ctx, 0) stops; luz_ctx_profile_read waits for the stream and returns the
+ * summed milliseconds and the launch count of one kernel since the start. */
+enum {
+    LUZ_KERNEL_TLAS_BUILD = 0,  /* fused single-CTA TLAS build                      */
+    LUZ_KERNEL_GBUFFER = 1,     /* primary closest-hit G-buffer                      */
+    LUZ_KERNEL_RAYGEN = 2,      /* shadow / AO ray generation                        */
+    LUZ_KERNEL_TRAVERSAL = 3,   /* persistent shadow / AO any-hit traversal          */
+    LUZ_KERNEL_LIGHT_PASS = 4,  /* deferred light pass (every mode)                  */
+    LUZ_KERNEL_FEATURES = 5,    /* denoiser features                                 */
+    LUZ_KERNEL_DENOISE = 6,     /* denoiser network + filter                         */
+    LUZ_KERNEL_TAA = 7
+};
+luz_status luz_ctx_profile(luz_ctx* ctx, int32_t on);
+luz_status luz_ctx_profile_read(luz_ctx* ctx, int32_t kernel, float* total_ms, uint32_t* launches);
+
 /* ------------------------------------------------------------------ BLAS
  * Replaces vkw::CreateBLAS + vkw::CmdBuildBLAS (source/Graphics/VulkanWrapper.h:236,
  * :229; VulkanWrapper.cpp:743-836, 1089-1104) as called by GPUScene::AddMesh

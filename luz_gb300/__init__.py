@@ -515,6 +515,36 @@ class Context:
     def launch_count(self) -> int:
         return lib.luz_ctx_launch_count(self._h)
 
+    def last_blas_build_ms(self) -> float:
+        """Device time of the last BLAS build, host->device copies excluded."""
+        ms = C.c_float()
+        _check(lib.luz_ctx_last_blas_build_ms(self._h, C.byref(ms)), self._h, "build timing")
+        return ms.value
+
+    KERNELS = {"tlas_build": 0, "gbuffer": 1, "raygen": 2, "traversal": 3, "light_pass": 4, "features": 5,
+               "denoise": 6, "taa": 7}
+
+    def profile(self, on: bool) -> None:
+        """Per-kernel event timing of the instrumented kernels (on clears the records)."""
+        _check(lib.luz_ctx_profile(self._h, 1 if on else 0), self._h, "profile")
+
+    def profile_read(self, kernel: str) -> tuple[float, int]:
+        """(summed ms, launches) of one kernel since profiling was switched on."""
+        ms, n = C.c_float(), C.c_uint32()
+        _check(lib.luz_ctx_profile_read(self._h, self.KERNELS[kernel], C.byref(ms), C.byref(n)), self._h,
+               "profile read")
+        return ms.value, n.value
+
+    def probe_l2_read_gbs(self, nbytes: int = 48 << 20, reps: int = 50) -> float:
+        """L2 read bandwidth (GB/s) from L2-only 16-B loads over an nbytes buffer."""
+        g = C.c_float()
+        _check(lib.luz_ctx_probe_l2_read(self._h, nbytes, reps, C.byref(g)), self._h, "L2 probe")
+        return g.value
+
+    def set_stream_default(self) -> None:
+        """Back to the context's own stream."""
+        _check(lib.luz_ctx_set_stream(self._h, None), self._h, "set stream")
+
     def close(self):
         if self._h:
             for child in list(self._children):
@@ -622,6 +652,7 @@ class GPUScene:
         t0 = time.perf_counter()
         self.blas = ctx.build_blas(meshes)                          # AddMesh for every mesh
         self.blas_build_ms = (time.perf_counter() - t0) * 1e3       # synchronous, host copies included
+        self.blas_build_device_ms = ctx.last_blas_build_ms() if meshes else 0.0
         self.blas_prims = sum(len(i) // 3 for _, i in meshes)
         self.tlas = ctx.tlas(max(scene.instance_count, 1))          # CreateTLAS
         self.frame = ctx.frame(scene.width, scene.height)           # DeferredRenderer::CreateImages

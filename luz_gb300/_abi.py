@@ -148,6 +148,10 @@ SIGNATURES = [
     ("luz_ctx_set_blue_noise", C.c_int32, [P, c_u8_p, C.c_uint32]),
     ("luz_ctx_set_vis_tuning", C.c_int32, [P, C.POINTER(C.c_uint32 * 4)]),
     ("luz_ctx_get_vis_tuning", C.c_int32, [P, C.POINTER(C.c_uint32 * 4)]),
+    ("luz_ctx_last_blas_build_ms", C.c_int32, [P, c_float_p]),
+    ("luz_ctx_probe_l2_read", C.c_int32, [P, C.c_uint64, C.c_uint32, c_float_p]),
+    ("luz_ctx_profile", C.c_int32, [P, C.c_int32]),
+    ("luz_ctx_profile_read", C.c_int32, [P, C.c_int32, c_float_p, c_u32_p]),
     ("luz_blas_build", C.c_int32, [P, C.POINTER(BlasDesc), C.POINTER(P)]),
     ("luz_blas_build_batch", C.c_int32, [P, C.c_uint32, C.POINTER(BlasDesc), C.POINTER(P)]),
     ("luz_blas_destroy", None, [P]),

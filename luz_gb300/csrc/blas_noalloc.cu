@@ -175,7 +175,7 @@ extern "C" luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint3
         noalloc_indices_kernel<<<cdiv(index_count, 256), 256, 0, st>>>(d_indices, index_count, vertex_count,
                                                                         idx, status);
         NOALLOC_LAUNCHED();
-        blas_bounds_kernel<<<cdiv(n, 256), 256, 0, st>>>(d_seg, zero, 1, n, bounds);
+        blas_bounds_kernel<<<cdiv(n, 256 * kBoundsIters), 256, 0, st>>>(d_seg, zero, 1, n, bounds);
         NOALLOC_LAUNCHED();
         blas_morton_kernel<<<cdiv(n, 256), 256, 0, st>>>(d_seg, zero, 1, n, bounds, keys[0], vals[0]);
         NOALLOC_LAUNCHED();

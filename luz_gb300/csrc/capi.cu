@@ -36,6 +36,28 @@ luz_status check_launch(luz_ctx* ctx, const char* what) {
     if (e != cudaSuccess) return cuda_error(ctx, e, what);
     return LUZ_OK;
 }
+void prof_begin(luz_ctx* ctx, int32_t kernel) {
+    if (!ctx->prof_on) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    while (ctx->prof_pool.size() < ctx->prof_used + 2) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        ctx->prof_pool.push_back(e);
+    }
+    luz_ctx::ProfRec r{kernel, ctx->prof_pool[ctx->prof_used], nullptr};   // b: set by prof_end
+    ctx->prof_used += 2;
+    cudaEventRecord(r.a, ctx->stream);
+    ctx->prof_recs.push_back(r);
+}
+
+void prof_end(luz_ctx* ctx) {
+    if (!ctx->prof_on || ctx->prof_recs.empty() || ctx->prof_recs.back().b) return;
+    cudaEvent_t b = ctx->prof_pool[ctx->prof_used - 1];
+    cudaEventRecord(b, ctx->stream);
+    ctx->prof_recs.back().b = b;
+}
+
 luz_status ensure_scratch(luz_ctx* ctx, size_t bytes) {
     if (bytes <= ctx->scratch_bytes) return LUZ_OK;
     if (ctx->d_scratch) {
@@ -97,6 +119,8 @@ luz_status luz_ctx_create(int device, luz_ctx** out) {
     ctx->stream = ctx->own_stream;
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (cudaMalloc(&ctx->d_status, 4) != cudaSuccess) return fail(LUZ_ERR_OOM);
+    for (auto& ev : ctx->build_ev)
+        if (cudaEventCreate(&ev) != cudaSuccess) return fail(LUZ_ERR_CUDA);
     cudaMemset(ctx->d_status, 0, 4);
     float lut[256];
     for (int i = 0; i < 256; ++i) lut[i] = (float)std::pow((double)((float)i / 255.0f), 2.2);
@@ -116,7 +140,97 @@ void luz_ctx_destroy(luz_ctx* ctx) {
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    for (auto ev : ctx->build_ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto ev : ctx->prof_pool) cudaEventDestroy(ev);
     delete ctx;
+}
+
+luz_status luz_ctx_last_blas_build_ms(luz_ctx* ctx, float* device_ms) {
+    if (!ctx || !device_ms) return LUZ_ERR_INVALID;
+    if (!ctx->build_timed) return set_error(ctx, LUZ_ERR_INVALID, "no BLAS build on this context yet");
+    LUZ_CUDA(ctx, cudaEventSynchronize(ctx->build_ev[1]));
+    LUZ_CUDA(ctx, cudaEventElapsedTime(device_ms, ctx->build_ev[0], ctx->build_ev[1]));
+    return LUZ_OK;
+}
+
+luz_status luz_ctx_profile(luz_ctx* ctx, int32_t on) {
+    if (!ctx) return LUZ_ERR_INVALID;
+    if (on) {
+        LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));   // the pool's events are free again
+        ctx->prof_recs.clear();
+        ctx->prof_used = 0;
+    }
+    ctx->prof_on = on != 0;
+    return LUZ_OK;
+}
+
+luz_status luz_ctx_profile_read(luz_ctx* ctx, int32_t kernel, float* total_ms, uint32_t* launches) {
+    if (!ctx || !total_ms || !launches) return LUZ_ERR_INVALID;
+    LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double sum = 0.0;
+    uint32_t n = 0;
+    for (const auto& r : ctx->prof_recs) {
+        if (r.kernel != kernel || !r.b) continue;
+        float ms = 0.f;
+        LUZ_CUDA(ctx, cudaEventElapsedTime(&ms, r.a, r.b));
+        sum += ms;
+        ++n;
+    }
+    *total_ms = (float)sum;
+    *launches = n;
+    return LUZ_OK;
+}
+
+namespace {
+// Streams `words` 16-B words of a buffer `reps` times through L2 (ld.global.cg: cached
+// in L2 only, so L1 serves none of it); one XOR per block keeps the loads live.
+__global__ void __launch_bounds__(512) l2_read_probe_kernel(const uint4* __restrict__ buf, size_t words,
+                                                            uint32_t reps, uint32_t* sink) {
+    uint32_t x = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (uint32_t r = 0; r < reps; ++r)
+        for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += stride) {
+            const uint4 v = __ldcg(buf + i);
+            x ^= v.x ^ v.y ^ v.z ^ v.w;
+        }
+    x = __reduce_xor_sync(0xFFFFFFFFu, x);
+    if ((threadIdx.x & 31) == 0 && x == 0x9E3779B9u) atomicXor(sink, x);   // practically never taken
+}
+}  // namespace
+
+luz_status luz_ctx_probe_l2_read(luz_ctx* ctx, uint64_t bytes, uint32_t reps, float* gbs) {
+    if (!ctx || !gbs || bytes < (1u << 20) || reps == 0) return LUZ_ERR_INVALID;
+    const size_t words = (size_t)(bytes / 16);
+    void* buf = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto run = [&]() -> luz_status {
+        LUZ_CUDA(ctx, cudaMalloc(&buf, words * 16 + 256));
+        LUZ_CUDA(ctx, cudaMemsetAsync(buf, 0x5A, words * 16 + 256, ctx->stream));
+        LUZ_CUDA(ctx, cudaEventCreate(&e0));
+        LUZ_CUDA(ctx, cudaEventCreate(&e1));
+        uint32_t* sink = (uint32_t*)((char*)buf + words * 16);
+        const uint32_t grid = (uint32_t)ctx->sm_count * 4;
+        l2_read_probe_kernel<<<grid, 512, 0, ctx->stream>>>((const uint4*)buf, words, 2, sink);   // warm L2
+        LUZ_LAUNCHED(ctx, "l2_read_probe_kernel");
+        LUZ_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        l2_read_probe_kernel<<<grid, 512, 0, ctx->stream>>>((const uint4*)buf, words, reps, sink);
+        LUZ_LAUNCHED(ctx, "l2_read_probe_kernel");
+        LUZ_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        LUZ_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0.f;
+        LUZ_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        *gbs = (float)((double)words * 16.0 * reps / (ms * 1e-3) / 1e9);
+        return LUZ_OK;
+    };
+    const luz_status st = run();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (buf) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(buf);
+    }
+    return st;
 }
 
 const char* luz_last_error(const luz_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
@@ -558,7 +672,9 @@ luz_status luz_frame_write(luz_ctx* ctx, luz_frame* f, int32_t plane, const void
     if (need == 0) return LUZ_OK;
     LUZ_CUDA(ctx, cudaMemcpyAsync(dst, src, need, cudaMemcpyHostToDevice, ctx->stream));
     LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (plane == LUZ_PLANE_NORMAL || plane == LUZ_PLANE_DEPTH) f->surf_valid = false;
+    // the lit list comes from the normal and depth planes, and its pass writes the
+    // background pixels of the light plane
+    if (plane == LUZ_PLANE_NORMAL || plane == LUZ_PLANE_DEPTH || plane == LUZ_PLANE_LIGHT) f->surf_valid = false;
     return LUZ_OK;
 }
 

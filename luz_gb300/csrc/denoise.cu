@@ -996,7 +996,9 @@ static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_bat
     P.list_count = list_count;
     uint32_t tiles = (P.G.pixels * P.G.images + 127) / 128;
     uint32_t grid = std::min<uint32_t>((tiles + kTcGroups - 1) / kTcGroups, (uint32_t)ctx->sm_count * kTcBlocksPerSm);
+    prof_begin(ctx, LUZ_KERNEL_DENOISE);
     denoise_infer_tc_kernel<<<grid, kTcThreads, kTcSmem, ctx->stream>>>(P, ctx->d_status);
+    prof_end(ctx);
     LUZ_LAUNCHED(ctx, "denoise_infer_tc_kernel");
     return LUZ_OK;
 }
@@ -1168,7 +1170,9 @@ static luz_status launch_features(luz_ctx* ctx, luz_frame* f, bool for_denoise) 
     F.list = for_denoise ? f->dn_list : nullptr;
     F.list_count = f->dn_count;
     if (for_denoise) LUZ_CUDA(ctx, cudaMemsetAsync(f->dn_count, 0, 4, ctx->stream));
+    prof_begin(ctx, LUZ_KERNEL_FEATURES);
     features_kernel<<<(f->pixels + 255) / 256, 256, 0, ctx->stream>>>(F);
+    prof_end(ctx);
     LUZ_LAUNCHED(ctx, "denoise_features_kernel");
     return LUZ_OK;
 }

@@ -120,6 +120,15 @@ struct luz_ctx {
     size_t pinned_bytes = 0;
     int sm_count = 0;
     luz::VisTuning vis_tuning{0, 0, 0, 0, 0};   // set == 0: library defaults
+    // device pipeline of the last batched BLAS build (after its host->device copies)
+    cudaEvent_t build_ev[2] = {nullptr, nullptr};
+    bool build_timed = false;
+    // per-kernel timing (luz_ctx_profile): an event pair around each instrumented launch
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_pool;
+    size_t prof_used = 0;
+    struct ProfRec { int32_t kernel; cudaEvent_t a, b; };
+    std::vector<ProfRec> prof_recs;
 };
 
 struct luz_blas {
@@ -227,6 +236,11 @@ luz_status ensure_scratch(luz_ctx* ctx, size_t bytes);
 luz_status check_launch(luz_ctx* ctx, const char* what);
 // Rebuilds the frame's lit-pixel list when its planes or scene constants changed.
 luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f);
+// Per-kernel timing: prof_begin records an event before a launch of kernel `kernel`
+// (LUZ_KERNEL_*), prof_end one after it, both on the context's stream; nothing when
+// profiling is off or the stream is being captured.
+void prof_begin(luz_ctx* ctx, int32_t kernel);
+void prof_end(luz_ctx* ctx);
 }  // namespace luz
 
 #define LUZ_CUDA(ctx, call)                                          \

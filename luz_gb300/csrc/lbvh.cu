@@ -60,44 +60,66 @@ __device__ __forceinline__ float leaf_pad(float lo, float hi) {
 
 // ---------------------------------------------------------------- bounds + morton
 // seg_bounds: 6 ordered uints per segment (min xyz, max xyz); init min=~0, max=0.
-// Min/max of the ordered centroid keys: reduced across the warp (redux.sync) when
-// all of its lanes belong to one segment, so one lane issues the six atomics.
-__global__ void blas_bounds_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
-                                   uint32_t total, uint32_t* seg_bounds) {
-    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    bool in = g < total;
-    int s = in ? find_seg(seg_prim_off, nseg, g) : -1;
-    uint32_t k[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
-    if (in) {
-        const SegDesc sd = segs[s];
-        uint32_t p = g - sd.prim_off;
-        uint32_t i0 = sd.indices[3 * p], i1 = sd.indices[3 * p + 1], i2 = sd.indices[3 * p + 2];
-        V3 lo, hi;
-        tri_box(load_pos(sd.vertices, i0), load_pos(sd.vertices, i1), load_pos(sd.vertices, i2), lo, hi);
-        V3 c = V3{(lo.x + hi.x) * 0.5f + 0.0f, (lo.y + hi.y) * 0.5f + 0.0f, (lo.z + hi.z) * 0.5f + 0.0f};
-        if (finite3(c)) {
-            k[0] = k[3] = float_to_ordered(c.x);
-            k[1] = k[4] = float_to_ordered(c.y);
-            k[2] = k[5] = float_to_ordered(c.z);
-        }
-    }
+// A block walks kBoundsIters rows of 256 consecutive primitives. Per row, a warp whose
+// lanes all belong to one segment reduces its ordered centroid keys (redux.sync) and
+// lane 0 merges them into a running min/max of that segment, which goes to the global
+// words (six atomics) only when the segment changes or the block's range ends; a warp
+// that straddles a segment boundary issues per-lane atomics. Min and max do not
+// depend on the order, so the result is the one of any reduction order.
+__global__ void __launch_bounds__(256) blas_bounds_kernel(const SegDesc* segs, const uint32_t* seg_prim_off,
+                                                          int nseg, uint32_t total, uint32_t* seg_bounds) {
     const uint32_t full = 0xFFFFFFFFu;
-    int s0 = __shfl_sync(full, s, 0);
-    bool uniform = __all_sync(full, s == s0 || s < 0);
-    if (uniform) {
-        uint32_t r[6];
-        for (int a = 0; a < 3; ++a) r[a] = __reduce_min_sync(full, k[a]);
-        for (int a = 3; a < 6; ++a) r[a] = __reduce_max_sync(full, k[a]);
-        if ((threadIdx.x & 31) == 0 && s0 >= 0) {
-            uint32_t* b = seg_bounds + 6 * s0;
-            for (int a = 0; a < 3; ++a) if (r[a] != 0xFFFFFFFFu) atomicMin(b + a, r[a]);
-            for (int a = 3; a < 6; ++a) if (r[a] != 0u) atomicMax(b + a, r[a]);
+    const bool leader = (threadIdx.x & 31) == 0;
+    int acc_s = -1;
+    uint32_t acc[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+    auto flush = [&]() {
+        if (acc_s < 0) return;
+        uint32_t* b = seg_bounds + 6 * acc_s;
+        for (int a = 0; a < 3; ++a) if (acc[a] != 0xFFFFFFFFu) atomicMin(b + a, acc[a]);
+        for (int a = 3; a < 6; ++a) if (acc[a] != 0u) atomicMax(b + a, acc[a]);
+    };
+    const uint32_t base = blockIdx.x * (blockDim.x * kBoundsIters);
+    for (int it = 0; it < kBoundsIters; ++it) {
+        const uint32_t row = base + (uint32_t)it * blockDim.x;
+        if (row >= total) break;   // uniform across the block
+        const uint32_t g = row + threadIdx.x;
+        const bool in = g < total;
+        const int s = in ? find_seg(seg_prim_off, nseg, g) : -1;
+        uint32_t k[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+        if (in) {
+            const SegDesc sd = segs[s];
+            const uint32_t p = g - sd.prim_off;
+            const uint32_t i0 = sd.indices[3 * p], i1 = sd.indices[3 * p + 1], i2 = sd.indices[3 * p + 2];
+            V3 lo, hi;
+            tri_box(load_pos(sd.vertices, i0), load_pos(sd.vertices, i1), load_pos(sd.vertices, i2), lo, hi);
+            V3 c = V3{(lo.x + hi.x) * 0.5f + 0.0f, (lo.y + hi.y) * 0.5f + 0.0f, (lo.z + hi.z) * 0.5f + 0.0f};
+            if (finite3(c)) {
+                k[0] = k[3] = float_to_ordered(c.x);
+                k[1] = k[4] = float_to_ordered(c.y);
+                k[2] = k[5] = float_to_ordered(c.z);
+            }
         }
-    } else if (s >= 0 && k[0] != 0xFFFFFFFFu) {
-        uint32_t* b = seg_bounds + 6 * s;
-        for (int a = 0; a < 3; ++a) atomicMin(b + a, k[a]);
-        for (int a = 3; a < 6; ++a) atomicMax(b + a, k[a]);
+        const int s0 = __shfl_sync(full, s, 0);
+        if (__all_sync(full, s == s0 || s < 0)) {
+            uint32_t r[6];
+            for (int a = 0; a < 3; ++a) r[a] = __reduce_min_sync(full, k[a]);
+            for (int a = 3; a < 6; ++a) r[a] = __reduce_max_sync(full, k[a]);
+            if (leader && s0 >= 0) {
+                if (s0 != acc_s) {
+                    flush();
+                    acc_s = s0;
+                    for (int a = 0; a < 3; ++a) { acc[a] = 0xFFFFFFFFu; acc[a + 3] = 0u; }
+                }
+                for (int a = 0; a < 3; ++a) acc[a] = min(acc[a], r[a]);
+                for (int a = 3; a < 6; ++a) acc[a] = max(acc[a], r[a]);
+            }
+        } else if (s >= 0 && k[0] != 0xFFFFFFFFu) {
+            uint32_t* b = seg_bounds + 6 * s;
+            for (int a = 0; a < 3; ++a) atomicMin(b + a, k[a]);
+            for (int a = 3; a < 6; ++a) atomicMax(b + a, k[a]);
+        }
     }
+    if (leader) flush();
 }
 
 __device__ __forceinline__ void decode_bounds(const uint32_t* b, V3& cmin, V3& ext) {
@@ -1136,11 +1158,12 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
     for (uint32_t s = 0; s < count; ++s)
         for (int k = 0; k < 6; ++k) binit[s * 6 + k] = k < 3 ? 0xFFFFFFFFu : 0u;
     LUZ_CUDA(ctx, cudaMemcpyAsync(d_bounds, binit.data(), count * 24, cudaMemcpyHostToDevice, st));
+    LUZ_CUDA(ctx, cudaEventRecord(ctx->build_ev[0], st));   // device pipeline starts here
     LUZ_CUDA(ctx, cudaMemsetAsync(d_node_parent, 0xFF, (size_t)M * 4, st));
     LUZ_CUDA(ctx, cudaMemsetAsync(d_leaf_parent, 0xFF, (size_t)std::max(N, 1u) * 4, st));
     LUZ_CUDA(ctx, cudaMemsetAsync(d_flags, 0, (size_t)M * 4, st));
     if (N > 0) {
-        blas_bounds_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, d_bounds);
+        blas_bounds_kernel<<<cdiv(N, 256 * kBoundsIters), 256, 0, st>>>(d_segs, d_prim_off, count, N, d_bounds);
         LUZ_LAUNCHED(ctx, "blas_bounds_kernel");
         blas_morton_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, d_bounds,
                                                          sb.keys[0], sb.vals[0]);
@@ -1190,6 +1213,8 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
             LUZ_CUDA(ctx, cudaMemcpyAsync(ab + off_ord[s], d_ord + prim_off[s], (size_t)n * 4,
                                           cudaMemcpyDeviceToDevice, st));
     }
+    LUZ_CUDA(ctx, cudaEventRecord(ctx->build_ev[1], st));
+    ctx->build_timed = true;
     LUZ_CUDA(ctx, cudaStreamSynchronize(st));
     uint32_t bits = 0;
     LUZ_CUDA(ctx, cudaMemcpy(&bits, ctx->d_status, 4, cudaMemcpyDeviceToHost));
@@ -1307,9 +1332,11 @@ luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t) {
     uint32_t* d_zero = (uint32_t*)p; p += align256(4);
 
     if (n <= kFusedTlasMax) {
+        prof_begin(ctx, LUZ_KERNEL_TLAS_BUILD);
         tlas_fused_kernel<<<1, 1024, 0, st>>>(t->d_input, n, inst_box, t->shade, sb.keys[0], sb.vals[0], karras_nodes,
                                               node_parent, leaf_parent, flags, t->instances, leaf_box, t->morton,
                                               t->order, t->nodes, queue, newidx, t->levels, t->nodes4, ctx->d_status);
+        prof_end(ctx);
         LUZ_LAUNCHED(ctx, "tlas_fused_kernel");
         return LUZ_OK;
     }

@@ -31,8 +31,11 @@ constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1;
 constexpr uint32_t kLookbackSpinLimit = 1u << 22;
 
-__global__ void blas_bounds_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
-                                   uint32_t total, uint32_t* seg_bounds);
+// Rows of 256 primitives one block of blas_bounds_kernel reduces (launch 256 threads
+// and ceil(total / (256 * kBoundsIters)) blocks).
+constexpr int kBoundsIters = 16;
+__global__ void __launch_bounds__(256) blas_bounds_kernel(const SegDesc* segs, const uint32_t* seg_prim_off,
+                                                          int nseg, uint32_t total, uint32_t* seg_bounds);
 __global__ void blas_morton_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                                    uint32_t total, const uint32_t* seg_bounds,
                                    unsigned long long* keys, uint32_t* vals);

@@ -1,8 +1,8 @@
 // lightpass.cu — the deferred light pass: light.frag main (light.frag:171-235) over
 // the G-buffer planes and the visibility bit planes. Thread t shades the t-th lit
 // pixel of the compacted list the G-buffer pass wrote (world position and normal;
-// every lane of a warp runs the same light loop) and writes the background colour
-// of pixel t if that pixel is unlit.
+// every lane of a warp runs the same light loop). The pass that compacted that list
+// wrote the background colour of the unlit pixels.
 #include <cstring>
 
 #include "internal.cuh"
@@ -71,14 +71,7 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lit = *P.lit_count;
     const V3 amb = V3{P.ambient[0], P.ambient[1], P.ambient[2]};
-    // background (light.frag:178-181) of pixel t
-    if (t < P.width * P.height) {
-        float4 nb = P.normal[t];
-        if (length(V3{nb.x, nb.y, nb.z}) == 0.0f) {
-            V3 c = amb * P.ambient_intensity;
-            P.out[t] = make_float4(c.x, c.y, c.z, 1.0f);
-        }
-    }
+    // the background (light.frag:178-181) was written by the lit-list pass
     if (blockIdx.x * blockDim.x >= lit) return;   // no lit pixel in this block
     for (uint32_t i = threadIdx.x; i < P.light_count; i += blockDim.x) s_lights[i] = P.lights[i];
     __syncthreads();
@@ -207,7 +200,9 @@ luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     uint32_t blocks = (f->pixels + 255) / 256;
+    prof_begin(ctx, LUZ_KERNEL_LIGHT_PASS);
     light_pass_kernel<<<blocks, 256, smem, ctx->stream>>>(P);
+    prof_end(ctx);
     LUZ_LAUNCHED(ctx, "light_pass_kernel");
     return LUZ_OK;
 }

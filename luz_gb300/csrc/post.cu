@@ -271,7 +271,9 @@ luz_status launch_taa(luz_ctx* ctx, luz_frame* f, int reconstruct) {
     memcpy(P.jitter, s.jitter, 8);
     memcpy(P.prev_jitter, s.prev_jitter, 8);
     dim3 grid((f->width + kTaaTile - 1) / kTaaTile, (f->height + kTaaTile - 1) / kTaaTile);
+    prof_begin(ctx, LUZ_KERNEL_TAA);
     taa_kernel<<<grid, 256, 0, ctx->stream>>>(P);
+    prof_end(ctx);
     LUZ_LAUNCHED(ctx, "taa_kernel");
     std::swap(f->taa, f->taa_next);   // the output is the next frame's history
     return LUZ_OK;

@@ -305,14 +305,24 @@ __global__ void __launch_bounds__(1024) lit_scan_kernel(uint32_t* chunk_counts, 
     if (threadIdx.x == 0) *total = s_carry;
 }
 
+// Also writes light.frag's background colour (light.frag:178-181: ambient colour x
+// intensity, alpha 1) into the light plane at every unlit pixel, so the light pass
+// touches lit pixels only.
 __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, const float* depth,
                                                         uint32_t width, uint32_t height,
                                                         const uint32_t* chunk_offsets,
                                                         const float* inverse_proj,
-                                                        const float* inverse_view, float4* surf) {
+                                                        const float* inverse_view, const float* ambient,
+                                                        float4* surf, float4* light) {
     __shared__ uint32_t s_tmp[8];
     __shared__ float s_ip[16], s_iv[16];
+    __shared__ float4 s_bg;
     if (threadIdx.x < 16) { s_ip[threadIdx.x] = inverse_proj[threadIdx.x]; s_iv[threadIdx.x] = inverse_view[threadIdx.x]; }
+    if (threadIdx.x == 0) {
+        // ambient = (ambientLightColor, ambientLightIntensity), the first 16 B of the scene block
+        const V3 c = V3{ambient[0], ambient[1], ambient[2]} * ambient[3];
+        s_bg = make_float4(c.x, c.y, c.z, 1.0f);
+    }
     __syncthreads();
     uint32_t base = blockIdx.x * kChunk + threadIdx.x * 4;
     bool lit[4];
@@ -325,7 +335,10 @@ __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, co
     }
     uint32_t pos = chunk_offsets[blockIdx.x] + block_excl(c, s_tmp);
     for (int k = 0; k < 4; ++k) {
-        if (!lit[k]) continue;
+        if (!lit[k]) {
+            if (px[k] != ~0u) light[px[k]] = s_bg;
+            continue;
+        }
         uint32_t pix = px[k];
         uint32_t x = pix % width, y = pix / width;
         V3 p = depth_to_world(s_ip, s_iv, pixel_uv(x, width), pixel_uv(y, height), depth[pix]);
@@ -369,7 +382,9 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
     if (f->max_map_index >= (int32_t)f->texture_count)
         return set_error(ctx, LUZ_ERR_INVALID, "a ModelBlock map index is beyond the frame's textures");
     uint32_t tiles = ((f->width + kGbTile - 1) / kGbTile) * ((f->height + kGbTile - 1) / kGbTile);
+    prof_begin(ctx, LUZ_KERNEL_GBUFFER);
     gbuffer_kernel<<<tiles, kGbTile * kGbTile, 0, ctx->stream>>>(G);
+    prof_end(ctx);
     LUZ_LAUNCHED(ctx, "gbuffer_kernel");
     return launch_lit_compaction(ctx, f);
 }
@@ -392,7 +407,8 @@ luz_status launch_lit_compaction(luz_ctx* ctx, luz_frame* f) {
                                                       f->block_counts,
                                                       (const float*)((const char*)f->d_scene + offsetof(luz_scene, inverse_proj)),
                                                       (const float*)((const char*)f->d_scene + offsetof(luz_scene, inverse_view)),
-                                                      f->surf);
+                                                      (const float*)((const char*)f->d_scene + offsetof(luz_scene, ambient_light_color)),
+                                                      f->surf, f->light);
     LUZ_LAUNCHED(ctx, "lit_write_kernel");
     f->surf_valid = true;
     return LUZ_OK;

@@ -622,16 +622,20 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         raygen_blocks = std::max(raygen_blocks, 1);
     }
     for (unsigned long long k0 = 0; k0 < max_items; k0 += chunk) {
+        prof_begin(ctx, LUZ_KERNEL_RAYGEN);
         raygen_kernel<<<(uint32_t)(ctx->sm_count * raygen_blocks), 256, 0, st>>>(S, C, k0, chunk, f->rays_a,
                                                                                   f->rays_b);
+        prof_end(ctx);
         LUZ_LAUNCHED(ctx, "raygen_kernel");
         if (d_stats) {
             if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, d_stats);
             else visibility_kernel<true, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, d_stats);
             LUZ_LAUNCHED(ctx, "visibility_kernel<stats>");
         } else {
+            prof_begin(ctx, LUZ_KERNEL_TRAVERSAL);
             if (staged) visibility_kernel<false, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, nullptr);
             else visibility_kernel<false, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, nullptr);
+            prof_end(ctx);
             LUZ_LAUNCHED(ctx, "visibility_kernel");
         }
     }
