@@ -390,19 +390,26 @@ luz_status luz_frame_read_shadow_map(luz_ctx* ctx, luz_frame* frame, uint32_t li
 luz_status luz_gbuffer_primary(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas);
 /* Shadow (light.frag:86-109,137-146) and AO (light.frag:111-135) any-hit rays of
  * every lit pixel; writes the visibility bit planes (shadow: 1 = occluded, AO: 1 =
- * miss). A shadow sample of a light with max(dot(N, L), 0) = 0 at the pixel keeps
- * bit 0 without a ray: the light pass multiplies that light's shadowed radiance by
- * the same max(dot(N, L), 0) (light.frag:209-226), so the image is the one of
- * tracing every ray. */
+ * miss). By default a shadow sample keeps bit 0 without a ray when the light pass's
+ * term of its light cannot depend on the shadow factor (light.frag:209-226 adds
+ * ((kD * albedo / pi + spec) * radiance) * max(dot(N, L), 0) with radiance =
+ * ((color * intensity) * attenuation) * (1 - shadow)): (a) max(dot(N, L), 0) is 0 or
+ * NaN (the light is behind the surface), or (b) every channel of (color * intensity)
+ * * attenuation is +-0 (outside a spot light's cone, a black light). The light pass
+ * output is then the one of tracing every ray, but the exported bit planes are not
+ * light.frag's per-ray results for those samples; luz_frame_set_shadow_cull(frame, 0)
+ * traces every sample as light.frag does. */
 luz_status luz_trace_visibility(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas,
                                 int32_t frame_index);
+/* enable != 0 (the default): leave out the shadow rays of conditions (a) and (b) above;
+ * 0: trace every shadow sample, so that LUZ_PLANE_SHADOW_BITS holds light.frag's
+ * per-ray hit results. */
+luz_status luz_frame_set_shadow_cull(luz_frame* frame, int32_t enable);
 /* The same trace with per-ray work counters (a separate kernel build, for
  * roofline accounting): out[0] rays traversed, out[1] TLAS node visits, out[2] BLAS
  * node visits, out[3] triangle tests, out[4] instance entries. Rays with nothing to
- * trace are not counted: a shadow ray whose light has max(dot(N, L), 0) = 0 at the
- * pixel (the light pass weights its shadow factor by that, light.frag:209-226, so
- * the ray cannot change the image; its bit stays 0), a ray with a non-finite origin
- * or direction or tMin > tMax (AO: recorded as a miss). */
+ * trace are not counted: a shadow ray left out by the cull above, a ray with a
+ * non-finite origin or direction or tMin > tMax (AO: recorded as a miss). */
 luz_status luz_trace_visibility_stats(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas,
                                       int32_t frame_index, uint64_t out[5]);
 /* Per-pixel AO value (mean of the miss bits) into LUZ_PLANE_AO. */

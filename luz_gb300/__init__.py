@@ -372,6 +372,11 @@ class Frame:
                self.ctx.handle, "trace stats")
         return {"rays": out[0], "tlas_nodes": out[1], "blas_nodes": out[2], "tris": out[3], "instances": out[4]}
 
+    def set_shadow_cull(self, enable: bool) -> None:
+        """False: trace every shadow sample light.frag traces (exact per-ray bit planes);
+        True (default): leave out the samples whose light's term cannot depend on them."""
+        _check(lib.luz_frame_set_shadow_cull(self._h, int(enable)), self.ctx.handle, "shadow cull")
+
     def ao_resolve(self) -> None:
         _check(lib.luz_ao_resolve(self.ctx.handle, self._h), self.ctx.handle, "ao resolve")
 

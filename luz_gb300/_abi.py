@@ -179,6 +179,7 @@ SIGNATURES = [
     ("luz_trace_visibility", C.c_int32, [P, P, P, C.c_int32]),
     ("luz_trace_visibility_stats", C.c_int32, [P, P, P, C.c_int32, C.POINTER(C.c_uint64)]),
     ("luz_ao_resolve", C.c_int32, [P, P]),
+    ("luz_frame_set_shadow_cull", C.c_int32, [P, C.c_int32]),
     ("luz_frame_lit_count", C.c_int32, [P, P, c_u32_p]),
     ("luz_light_pass", C.c_int32, [P, P, C.c_int32]),
     ("luz_render_frame", C.c_int32, [P, P, P, C.POINTER(Instance), C.c_uint32, C.c_int32]),

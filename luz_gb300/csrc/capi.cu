@@ -573,6 +573,12 @@ luz_status luz_trace_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, i
     return launch_visibility(ctx, f, t, frame_index, nullptr);
 }
 
+luz_status luz_frame_set_shadow_cull(luz_frame* f, int32_t enable) {
+    if (!f) return LUZ_ERR_INVALID;
+    f->shadow_cull = enable != 0;
+    return LUZ_OK;
+}
+
 luz_status luz_trace_visibility_stats(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int32_t frame_index,
                                       uint64_t out[5]) {
     if (!ctx || !f || !t || !out) return LUZ_ERR_INVALID;

@@ -182,6 +182,7 @@ struct luz_frame {
     uint32_t* ao_bits = nullptr;
     float* ao = nullptr;
     float* ao_denoised = nullptr;
+    bool shadow_cull = true;        // leave out shadow rays that cannot change the image
     void* features = nullptr;       // 8 x bf16 per pixel (denoiser input)
     float* lin_depth = nullptr;
     uint32_t* dn_list = nullptr;    // lit pixels in row-major order (x | y << 16), from the features pass

@@ -130,7 +130,7 @@ __device__ __forceinline__ bool gen_ray(const SceneVis& S, const VisCommon& C, u
         // When the light pass's term of this light cannot depend on its shadow factor
         // (zero weight max(dot(N, L), 0) or zero unshadowed radiance, computed as the
         // light pass computes them), the ray is not traced and its bit stays 0.
-        if (shadow_has_no_effect(S.lights[li], p, N, L)) return false;
+        if (S.cull && shadow_has_no_effect(S.lights[li], p, N, L)) return false;
         sample_rg(C.blue_noise, C.bn_size, S.sampler, px, py, (int)si, S.frame, li + 1, &rx, &ry);
         shadow_ray(S.lights[li], p, N, cam, rx, ry, L, wo, wd, tmax);
         tmin = 0.001f;
@@ -553,6 +553,7 @@ SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index) 
     S.words = f->words;
     S.shadow_bits = f->shadow_bits;
     S.ao_bits = f->ao_bits;
+    S.cull = f->shadow_cull ? 1 : 0;
     return S;
 }
 

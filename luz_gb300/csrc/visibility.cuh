@@ -18,6 +18,7 @@ struct SceneVis {
     float cam[3];
     float ao_min, ao_max;
     int sampler, frame;
+    int cull;                 // leave out shadow rays that cannot change the light pass's output
     uint32_t width, words;
     uint32_t* shadow_bits;
     uint32_t* ao_bits;

@@ -143,3 +143,55 @@ def test_negative_ao_min_is_rejected(ctx):
     g = L.GPUScene(ctx, s)
     with pytest.raises(L.LuzError, match="ao_min is negative"):
         g.update_resources_gpu()
+
+
+@pytest.mark.parametrize("scene", ["config1", "config2_small"])
+def test_every_shadow_ray_traced_matches_oracle(ctx, scene):
+    """With the shadow-ray cull off, every shadow sample light.frag traces is traced
+    (light.frag:93-107): the bit planes equal the oracle's full trace (cull=False) bit
+    for bit, and the light pass output is bit-identical to the culled frame's."""
+    if scene == "config1":
+        s = _cfg1(256, 256)
+    else:
+        s = L.HostScene(2, width=160, height=90, meshes=6, instances=128, subdivisions=4)
+    g = gpu_frame(ctx, s)
+    culled_light = g.frame.read(L.PLANE_LIGHT).copy()
+    culled_bits = g.frame.read(L.PLANE_SHADOW_BITS).copy()
+    g.frame.set_shadow_cull(False)
+    g.render(0)
+    ctx.synchronize()
+    assert ctx.device_status() == 0
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    f.shadow_bits[:] = 0
+    f.ao_bits[:] = 0
+    f.visibility(0, L.blue_noise(), cull=False)
+    full_bits = g.frame.read(L.PLANE_SHADOW_BITS)
+    assert bits_mismatch(full_bits, f.shadow_bits[: f.shadow_slots]) == 0
+    assert bits_mismatch(g.frame.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+    assert bits_mismatch(full_bits, culled_bits) > 0          # the culled samples do hit
+    assert np.array_equal(g.frame.read(L.PLANE_LIGHT).view(np.uint32), culled_light.view(np.uint32))
+    g.frame.set_shadow_cull(True)
+
+
+def test_config2_full_size_frame_parity(ctx):
+    """The benchmark frame itself: 1920x1080, 64 displaced icospheres x 1024 instances, 41
+    lights, 1 shadow ray per light and 16 AO rays per pixel. G-buffer planes and every
+    hit/miss mask bit-exact against the oracle, radiance within 1e-4 relative."""
+    s = L.HostScene(2)
+    assert (s.width, s.height, s.instance_count, s.light_count) == (1920, 1080, 1024, 41)
+    g = gpu_frame(ctx, s)
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    fr = g.frame
+    assert np.array_equal(fr.read(L.PLANE_ALBEDO).ravel(), f.albedo)
+    assert np.array_equal(fr.read(L.PLANE_MATERIAL).ravel(), f.material)
+    assert np.array_equal(fr.read(L.PLANE_NORMAL).reshape(-1, 4).view(np.uint32), f.normal.view(np.uint32))
+    assert np.array_equal(fr.read(L.PLANE_DEPTH).ravel().view(np.uint32), f.depth.view(np.uint32))
+    assert np.array_equal(fr.read(L.PLANE_PRIMARY_HIT).reshape(-1, 2), f.primary_hit)
+    assert bits_mismatch(fr.read(L.PLANE_SHADOW_BITS), f.shadow_bits[: f.shadow_slots]) == 0
+    assert bits_mismatch(fr.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+    gl = fr.read(L.PLANE_LIGHT)
+    ol = f.light_pass()
+    rel = np.abs(gl - ol) / np.maximum(np.abs(ol), 1e-6)
+    assert rel.max() <= RADIANCE_RTOL, rel.max()
