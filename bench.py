@@ -200,10 +200,17 @@ def run_reference(args, rank):
 
 
 # ---------------------------------------------------------------------------- denoised vs plain
-def denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=16, curve_spp=(1, 2, 4, 8, 16, 32, 64, 128, 256)):
-    """AO RMSE against 1024 samples (lit pixels, stratified samples) for the denoised
-    single sample and the plain path; the smallest plain sample count with an RMSE at
-    or below the denoised one; ms/frame of both frames (1 shadow ray per light each)."""
+def denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=16, curve_spp=(1, 2, 4, 8, 16, 32, 64),
+                      target_spp=1024):
+    """The headline comparison. The denoised frame traces 1 AO ray and 1 shadow ray per
+    light per lit pixel and filters the shadow ratio and AO with the network; the plain
+    frame traces N AO rays and N shadow rays per light (the reference's one sample-count
+    knob, lightSamples, sets every light's numShadowSamples: GPUScene.cpp:248). RMSE
+    over the lit pixels against the target_spp-sample frame, for the AO value and for
+    the radiance (RGB light-pass output); the equal-quality N is the smallest plain
+    sample count whose AO RMSE and radiance RMSE are both at or below the denoised
+    frame's; ms/frame of both frames (TLAS build, G-buffer, visibility, denoiser / light
+    pass), CUDA events, L2 flushed between frames."""
     import numpy as np
     import torch
 
@@ -215,49 +222,60 @@ def denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=16, curve_spp=(1, 
     den = D.Denoiser(ctx)
     den.load(D.DEFAULT_WEIGHTS)
     fr, tl, sc = g.frame, g.tlas, g.scene
-    shadow_spp = 1
-
-    def setup(ao, light):
-        sc.set_sampling(ao, light_samples=light, sampler=L.SAMPLER_STRATIFIED)
-        fr.upload(sc.block(), sc.lights(), sc.light_count, sc.models(), sc.instance_count)
-
+    t0 = time.perf_counter()
     tl.build(g.instances, g.n_instances)
     fr.gbuffer(tl)
     lit = np.linalg.norm(fr.read(L.PLANE_NORMAL)[..., :3], axis=-1) > 0
-    setup(1024, 0)
-    fr.trace(tl, 1_000_007)
-    fr.ao_resolve()
-    target = fr.read(L.PLANE_AO).copy()
+    t_rad, t_sig = D.reference(fr, tl, sc, target_spp, per_trace=16)   # torch and the context share `stream`
+    t_ao = t_sig[..., 3]
+    t_target = time.perf_counter() - t0
 
-    def plain_rmse(n):
-        setup(n, 0)
+    def rmse_pair(ao_plane):
+        return (D.lit_rmse(fr.read(ao_plane), t_ao, lit), D.lit_rmse(fr.read(L.PLANE_LIGHT)[..., :3], t_rad, lit))
+
+    def plain(n):
+        D.set_samples(fr, sc, n, n)
         fr.trace(tl, 7)
+        fr.light_pass(L.LIGHT_PASS_PLAIN)
         fr.ao_resolve()
-        return D.lit_rmse(fr.read(L.PLANE_AO), target, lit)
+        return rmse_pair(L.PLANE_AO)
 
-    curve = {n: plain_rmse(n) for n in curve_spp}
-    setup(1, shadow_spp)
+    curve = {n: plain(n) for n in curve_spp}
+    D.set_samples(fr, sc, 1, 1)
     fr.trace(tl, 7)
     den.denoise(fr)
-    r_den = D.lit_rmse(fr.read(L.PLANE_AO_DENOISED), target, lit)
-    # smallest N with plain RMSE <= denoised: bracket on the measured curve, then walk up
-    ns = sorted(curve)
-    n_star = ns[-1]
-    for a, b in zip(ns, ns[1:]):
-        if curve[b] <= r_den:
-            slope = np.log(curve[a] / curve[b]) / np.log(b / a)
-            n_star = max(a, int(np.floor(a * (curve[a] / r_den) ** (1.0 / max(slope, 1e-3)))))
-            break
-    while n_star < 4096:
-        r = curve.get(n_star) if n_star in curve else plain_rmse(n_star)
-        curve[n_star] = r
-        if r <= r_den:
-            break
-        n_star += 1
+    fr.light_pass(L.LIGHT_PASS_DENOISED)
+    r_den = rmse_pair(L.PLANE_AO_DENOISED)
 
-    def timed(fn):
+    def passes(n):
+        r = curve[n] if n in curve else curve.setdefault(n, plain(n))
+        return r[0] <= r_den[0] and r[1] <= r_den[1]
+
+    # smallest N that matches the denoised frame on both: first passing point of the
+    # measured curve, then a bisection over the integers below it
+    ns = sorted(curve)
+    hi = next((n for n in ns if passes(n)), None)
+    matched = hi is not None
+    if matched:
+        lo = max([n for n in ns if n < hi] or [0])
+        while hi - lo > 1:
+            mid = (lo + hi) // 2
+            if passes(mid):
+                hi = mid
+            else:
+                lo = mid
+        n_star = hi
+    else:
+        n_star = ns[-1]          # the denoised frame beats every measured N: a lower bound
+    ao_curve = {n: v[0] for n, v in curve.items()}
+    rad_curve = {n: v[1] for n, v in curve.items()}
+
+    def timed(fn, profile=False):
         for w in range(W):
             fn(w)
+        torch.cuda.synchronize()
+        if profile:
+            ctx.profile(True)
         ts = []
         for k in range(K):
             flush.zero_()
@@ -274,45 +292,41 @@ def denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=16, curve_spp=(1, 
         fr.gbuffer(tl)
         fr.trace(tl, fi)
         den.denoise(fr)
-        fr.light_pass(True)
+        fr.light_pass(L.LIGHT_PASS_DENOISED)
 
     def frame_plain(fi):
         tl.build(g.instances, g.n_instances)
         fr.gbuffer(tl)
         fr.trace(tl, fi)
-        fr.light_pass(False)
+        fr.light_pass(L.LIGHT_PASS_PLAIN)
 
-    def ao_denoised(fi):
-        fr.trace(tl, fi)
-        den.denoise(fr)
-
-    def ao_plain(fi):
-        fr.trace(tl, fi)
-
-    setup(1, shadow_spp)
-    ms_den = timed(frame_denoised)
-    ms_denoise_only = timed(lambda fi: den.denoise(fr))
-    setup(n_star, shadow_spp)
+    D.set_samples(fr, sc, 1, 1)
+    ms_den = timed(frame_denoised, profile=True)
+    stages = {}
+    for name in ("tlas_build", "gbuffer", "raygen", "traversal", "features", "light_pass", "denoise"):
+        tot, n = ctx.profile_read(name)
+        stages[name] = tot / K
+    ctx.profile(False)
+    D.set_samples(fr, sc, n_star, n_star)
     ms_plain = timed(frame_plain)
-    setup(1, 0)
-    ms_ao_den = timed(ao_denoised)
-    setup(n_star, 0)
-    ms_ao_plain = timed(ao_plain)
-    setup(restore_ao, shadow_spp)   # back to the benchmark's sampling
+    # back to the benchmark's sampling
     sc.set_sampling(restore_ao, light_samples=1, sampler=L.SAMPLER_PARITY)
     fr.upload(sc.block(), sc.lights(), sc.light_count, sc.models(), sc.instance_count)
-    lit = fr.lit_count()   # the frame path filters the lit pixels only
-    flops = 2.0 * (72 * 64 + 64 * 64 + 64 * 64 + 64 * 49) * lit
-    return {"rmse_vs_1024spp": {"denoised_1spp": r_den, "plain": {str(k): v for k, v in sorted(curve.items())}},
-            "equal_rmse_spp": n_star,
+    nlit = int(lit.sum())
+    flops = 2.0 * (72 * 64 + 64 * 64 + 64 * 64 + 64 * 49) * nlit
+    return {"target_spp": target_spp, "target": f"{target_spp // 16} traces of 16 AO + 16 shadow samples per light",
+            "target_s": t_target,
+            "rmse_vs_target": {"denoised_1spp": {"ao": r_den[0], "radiance": r_den[1]},
+                               "plain": {str(k): {"ao": v[0], "radiance": v[1]} for k, v in sorted(curve.items())}},
+            "equal_rmse_spp": n_star, "equal_rmse_matched": matched,
+            "equal_rmse_spp_interpolated": {"ao": D.equal_rmse_spp(ao_curve, r_den[0]),
+                                            "radiance": D.equal_rmse_spp(rad_curve, r_den[1])},
             "ms_per_frame_denoised": ms_den, "ms_per_frame_plain_equal_rmse": ms_plain,
             "frame_speedup": ms_plain / ms_den,
-            "ao_only": {"ms_denoised_1spp": ms_ao_den, "ms_plain_equal_rmse": ms_ao_plain,
-                        "speedup": ms_ao_plain / ms_ao_den},
-            "denoiser_ms": ms_denoise_only, "denoised_pixels": lit,
-            "denoiser_tflops_bf16": flops / (ms_denoise_only * 1e-3) / 1e12,
-            "shadow_rays_per_light": shadow_spp, "sampler": "stratified (8x8-block R2)",
-            "weights": D.DEFAULT_WEIGHTS.name}
+            "denoised_frame_kernel_ms": stages,
+            "denoiser_tflops_bf16": flops / (stages["denoise"] * 1e-3) / 1e12 if stages["denoise"] else None,
+            "denoised_pixels": nlit, "plain_rays_per_px": "N AO + N shadow per light",
+            "sampler": "stratified (8x8-block R2)", "weights": D.DEFAULT_WEIGHTS.name}
 
 
 # ---------------------------------------------------------------------------- post passes

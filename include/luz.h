@@ -47,7 +47,7 @@ enum {
 };
 
 /* ------------------------------------------------------------------ limits */
-#define LUZ_MAX_SHADOW_SLOTS 1024   /* Σ_lights numShadowSamples per pixel      */
+#define LUZ_MAX_SHADOW_SLOTS 16384  /* Σ_lights numShadowSamples per pixel      */
 #define LUZ_MAX_AO_SAMPLES 4096     /* aoNumSamples per pixel                   */
 #define LUZ_BLUE_NOISE_SIZE 128     /* substitute blue-noise texture, RGBA8     */
 
@@ -184,7 +184,10 @@ enum {
     LUZ_PLANE_LIN_DEPTH = 12,   /* F32 distance to the camera, 0 for background          */
     LUZ_PLANE_TAA = 13,         /* RGBA32F temporal anti-aliasing output (= next history)  */
     LUZ_PLANE_COMPOSE = 14,     /* BGRA8 UNORM composed, tone-mapped output (bytes B,G,R,A) */
-    LUZ_PLANE_COUNT = 15
+    LUZ_PLANE_SIGNAL = 15,      /* RGBA32F denoiser input: shadowed direct light S r, g, b, AO */
+    LUZ_PLANE_UNSHADOWED = 16,  /* RGBA32F unshadowed direct light U r, g, b, lum(S)/lum(U)    */
+    LUZ_PLANE_DENOISED = 17,    /* RGBA32F denoiser output: shadow ratio R r, g, b, AO         */
+    LUZ_PLANE_COUNT = 18
 };
 
 /* ------------------------------------------------------------------ context */
@@ -418,8 +421,17 @@ luz_status luz_ao_resolve(luz_ctx* ctx, luz_frame* frame);
 luz_status luz_frame_lit_count(luz_ctx* ctx, luz_frame* frame, uint32_t* count);
 /* DeferredRenderer::LightPass (source/Graphics/DeferredRenderer.cpp:324-345) running
  * light.frag main (light.frag:171-235) over the G-buffer and visibility planes.
- * use_denoised_ao != 0 reads LUZ_PLANE_AO_DENOISED instead of the AO bit planes. */
-luz_status luz_light_pass(luz_ctx* ctx, luz_frame* frame, int32_t use_denoised_ao);
+ * LUZ_LIGHT_PASS_PLAIN: shadow factors and AO from the bit planes, as light.frag.
+ * LUZ_LIGHT_PASS_DENOISED_AO: AO from LUZ_PLANE_AO_DENOISED, shadows from the bits.
+ * LUZ_LIGHT_PASS_DENOISED: the frame from the denoiser's output (run luz_denoise
+ * first): ambient * AO + U * R + emission per channel, where U is the unshadowed
+ * direct light (LUZ_PLANE_UNSHADOWED), R the filtered shadow ratio and AO the filtered
+ * AO (LUZ_PLANE_DENOISED). Unlit pixels keep the background colour that the G-buffer
+ * pass's lit-pixel compaction wrote (light.frag:178-181). */
+#define LUZ_LIGHT_PASS_PLAIN 0
+#define LUZ_LIGHT_PASS_DENOISED_AO 1
+#define LUZ_LIGHT_PASS_DENOISED 2
+luz_status luz_light_pass(luz_ctx* ctx, luz_frame* frame, int32_t mode);
 /* One whole frame: TLAS build, primary G-buffer, visibility, light pass. */
 luz_status luz_render_frame(luz_ctx* ctx, luz_frame* frame, luz_tlas* tlas,
                             const luz_instance* instances, uint32_t instance_count,
@@ -501,41 +513,66 @@ luz_status luz_batch_autotune(luz_ctx* ctx, luz_batch* b, uint32_t reps, luz_vis
                               float* best_ms);
 
 /* ------------------------------------------------------------------ denoiser
- * Learned kernel-predicting AO denoiser; no counterpart in the reference, which
- * integrates AO with aoSamples rays per pixel (light.frag:111-135). Per pixel an MLP
- * 72 -> 64 -> 64 -> 64 -> 49 (BF16 tensor cores, FP32 accumulation) reads 8 channels
- * over a 3x3 neighbourhood (noisy AO, noisy shadow lit fraction, normal, relative
- * depth, roughness, albedo luminance) and predicts softmax weights of a 7x7 filter
- * applied to the noisy AO. Parameters: LUZ_DENOISER_PARAMS FP32 values, row-major
- * [out][in] weights then biases per layer: W1[64][72] b1[64] W2[64][64] b2[64]
- * W3[64][64] b3[64] W4[49][64] b4[49]. */
+ * Learned kernel-predicting denoiser of the 1-sample shadow and AO terms; no
+ * counterpart in the reference, which integrates them with lightSamples shadow rays
+ * per light (light.frag:86-109) and aoSamples AO rays (light.frag:111-135) per pixel.
+ *
+ * Its input is the split of the direct light (luz_denoise_features): per lit pixel the
+ * shadowed sum S of light.frag's light loop (r, g, b) with the AO value
+ * (LUZ_PLANE_SIGNAL), and the same sum U with every shadow factor 0 (r, g, b) with
+ * lum(S) / lum(U) (LUZ_PLANE_UNSHADOWED). One predicted 7x7 kernel w filters both
+ * terms: AO' = sum(w AO) / sum(w), and per channel the ratio estimator
+ * R = sum(w S) / sum(w U) (1 where sum(w U) = 0), so that neighbours count by their
+ * unshadowed light. The frame is then ambient * AO' + U * R + emission
+ * (luz_light_pass with LUZ_LIGHT_PASS_DENOISED): the material and light detail of U
+ * stay unfiltered.
+ *
+ * Per pixel an MLP 72 -> 64 -> 64 -> 64 -> 49 (BF16 tensor cores, FP32 accumulation)
+ * reads 8 channels over a 3x3 neighbourhood (noisy AO, lum(S) / lum(U), normal,
+ * relative depth, roughness, albedo luminance) and predicts the softmax weights of the
+ * 7x7 kernel. Parameters: LUZ_DENOISER_PARAMS FP32 values, row-major [out][in]
+ * weights then biases per layer: W1[64][72] b1[64] W2[64][64] b2[64] W3[64][64]
+ * b3[64] W4[49][64] b4[49]. Training loss per pixel: sum over the outputs (R r, g, b
+ * and AO') of weight x (y - t)^2, mean over the batch; the weights come with the
+ * batch, else they are the shadow weight w (1/3 unless set,
+ * luz_denoiser_set_shadow_weight) for the ratio outputs and 1 for AO. */
 #define LUZ_DENOISER_PARAMS 16177
 typedef struct luz_denoiser luz_denoiser;
 /* A batch of images in device memory: features (LUZ_PLANE_FEATURES layout),
- * distances (LUZ_PLANE_LIN_DEPTH), noisy AO, and for training the target AO;
- * `images` images of width x height stored one after the other. */
+ * distances (LUZ_PLANE_LIN_DEPTH), the noisy split (LUZ_PLANE_SIGNAL and
+ * LUZ_PLANE_UNSHADOWED layouts: 4 floats per pixel each), for training the target
+ * (shadow ratio r, g, b and AO per pixel) and optionally a per-pixel loss weight of
+ * each output (4 floats per pixel; NULL = the shadow weight for the ratio outputs, 1
+ * for AO); `images` images of width x height stored one after the other. */
 typedef struct luz_denoise_batch {
     const void* features;
     const float* lin_depth;
-    const float* noisy_ao;
-    const float* target_ao;
+    const float* noisy;
+    const float* unshadowed;
+    const float* target;
+    const float* weight;
     uint32_t width, height, images;
 } luz_denoise_batch;
 luz_status luz_denoiser_create(luz_ctx* ctx, uint64_t seed, luz_denoiser** out);
 void luz_denoiser_destroy(luz_denoiser* d);
+/* Loss weight w of each shadow-ratio output in training (the AO output weighs 1). */
+luz_status luz_denoiser_set_shadow_weight(luz_ctx* ctx, luz_denoiser* d, float weight);
 /* Sets / reads the FP32 parameters (resets the Adam moments). */
 luz_status luz_denoiser_set_weights(luz_ctx* ctx, luz_denoiser* d, const float* params);
 luz_status luz_denoiser_get_weights(luz_ctx* ctx, luz_denoiser* d, float* params);
-/* Computes the features, distances and noisy AO planes of a traced frame. */
+/* Computes the network inputs of a traced frame: the split of the direct light
+ * (LUZ_PLANE_SIGNAL, LUZ_PLANE_UNSHADOWED), then features, distances and the noisy AO
+ * (LUZ_PLANE_AO); background pixels get zeros. */
 luz_status luz_denoise_features(luz_ctx* ctx, luz_frame* frame);
-/* Features + network + filter: writes LUZ_PLANE_AO_DENOISED. The network runs over the
- * frame's lit pixels only (length(N) != 0); background pixels receive 0. */
+/* Inputs + network + filter over the frame's lit pixels (length(N) != 0): writes
+ * LUZ_PLANE_DENOISED (R r, g, b and AO') and its AO channel to LUZ_PLANE_AO_DENOISED;
+ * background pixels receive 0. */
 luz_status luz_denoise(luz_ctx* ctx, luz_denoiser* d, luz_frame* frame);
-/* The network + filter over every pixel of a batch into d_out (W x H x images floats);
- * pixels with lin_depth <= 0 receive 0. Agrees bit for bit with luz_denoise on the same
- * planes. */
+/* The network + filter over every pixel of a batch into d_out (4 floats per pixel,
+ * W x H x images); pixels with lin_depth <= 0 receive 0. Agrees bit for bit with
+ * luz_denoise on the same planes. */
 luz_status luz_denoise_batch_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* d_out);
-/* Mean squared error against target_ao and its gradient (host array of
+/* The training loss against `target` and its gradient (host array of
  * LUZ_DENOISER_PARAMS, may be NULL); deterministic. */
 luz_status luz_denoiser_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* grad,
                                  float* loss);

@@ -21,7 +21,8 @@ from . import _abi
 from ._abi import (BLUE_NOISE_SIZE, LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_SPOT, PLANE_ALBEDO, PLANE_AO,
                    PLANE_AO_BITS, PLANE_AO_DENOISED, PLANE_DEPTH, PLANE_DTYPES, PLANE_EMISSION, PLANE_LIGHT,
                    PLANE_MATERIAL, PLANE_NORMAL, PLANE_PRIMARY_HIT, PLANE_SHADOW_BITS, PLANE_TAA, PLANE_COMPOSE,
-                   PLANE_FEATURES, PLANE_LIN_DEPTH, SAMPLER_PARITY,
+                   PLANE_FEATURES, PLANE_LIN_DEPTH, PLANE_SIGNAL, PLANE_UNSHADOWED, PLANE_DENOISED,
+                   LIGHT_PASS_PLAIN, LIGHT_PASS_DENOISED_AO, LIGHT_PASS_DENOISED, SAMPLER_PARITY,
                    SAMPLER_STRATIFIED, SHADOW_RAYTRACING, BlasDesc, Camera, GenParams, Instance, Light, Model,
                    Scene, Vertex)
 
@@ -385,8 +386,11 @@ class Frame:
         _check(lib.luz_frame_lit_count(self.ctx.handle, self._h, C.byref(n)), self.ctx.handle, "lit count")
         return n.value
 
-    def light_pass(self, use_denoised_ao: bool = False) -> None:
-        _check(lib.luz_light_pass(self.ctx.handle, self._h, int(use_denoised_ao)), self.ctx.handle, "light pass")
+    def light_pass(self, mode: int = LIGHT_PASS_PLAIN) -> None:
+        """mode: LIGHT_PASS_PLAIN (light.frag from the bit planes), LIGHT_PASS_DENOISED_AO
+        (AO from the denoised plane; True also selects it), LIGHT_PASS_DENOISED (the frame
+        composed from the denoiser's filtered shadow ratio and AO)."""
+        _check(lib.luz_light_pass(self.ctx.handle, self._h, int(mode)), self.ctx.handle, "light pass")
 
     def taa(self, reconstruct: bool = True) -> None:
         """Temporal anti-aliasing of the light image into PLANE_TAA (the next history)."""

@@ -29,11 +29,14 @@ BLUE_NOISE_SIZE = 128
 PLANE_ALBEDO, PLANE_NORMAL, PLANE_MATERIAL, PLANE_EMISSION, PLANE_DEPTH, PLANE_LIGHT = range(6)
 PLANE_SHADOW_BITS, PLANE_AO_BITS, PLANE_AO, PLANE_AO_DENOISED, PLANE_PRIMARY_HIT = range(6, 11)
 PLANE_TAA, PLANE_COMPOSE = 13, 14
+PLANE_SIGNAL, PLANE_UNSHADOWED, PLANE_DENOISED = 15, 16, 17
+LIGHT_PASS_PLAIN, LIGHT_PASS_DENOISED_AO, LIGHT_PASS_DENOISED = 0, 1, 2
 PLANE_DTYPES = {PLANE_ALBEDO: (np.uint32, 1), PLANE_NORMAL: (np.float32, 4), PLANE_MATERIAL: (np.uint32, 1),
                 PLANE_EMISSION: (np.uint32, 1), PLANE_DEPTH: (np.float32, 1), PLANE_LIGHT: (np.float32, 4),
                 PLANE_SHADOW_BITS: (np.uint32, 1), PLANE_AO_BITS: (np.uint32, 1), PLANE_AO: (np.float32, 1),
                 PLANE_AO_DENOISED: (np.float32, 1), PLANE_PRIMARY_HIT: (np.uint32, 2),
-                PLANE_TAA: (np.float32, 4), PLANE_COMPOSE: (np.uint32, 1)}
+                PLANE_TAA: (np.float32, 4), PLANE_COMPOSE: (np.uint32, 1), PLANE_SIGNAL: (np.float32, 4),
+                PLANE_UNSHADOWED: (np.float32, 4), PLANE_DENOISED: (np.float32, 4)}
 
 
 class Vertex(C.Structure):
@@ -125,8 +128,9 @@ class BatchScene(C.Structure):
 
 
 class DenoiseBatch(C.Structure):
-    _fields_ = [("features", C.c_void_p), ("lin_depth", C.c_void_p), ("noisy_ao", C.c_void_p),
-                ("target_ao", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32), ("images", C.c_uint32)]
+    _fields_ = [("features", C.c_void_p), ("lin_depth", C.c_void_p), ("noisy", C.c_void_p),
+                ("unshadowed", C.c_void_p), ("target", C.c_void_p), ("weight", C.c_void_p), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("images", C.c_uint32)]
 
 
 DENOISER_PARAMS = 16177
@@ -200,6 +204,7 @@ SIGNATURES = [
     ("luz_denoiser_destroy", None, [P]),
     ("luz_denoiser_set_weights", C.c_int32, [P, P, c_float_p]),
     ("luz_denoiser_get_weights", C.c_int32, [P, P, c_float_p]),
+    ("luz_denoiser_set_shadow_weight", C.c_int32, [P, P, C.c_float]),
     ("luz_denoise_features", C.c_int32, [P, P]),
     ("luz_denoise", C.c_int32, [P, P, P]),
     ("luz_denoise_batch_infer", C.c_int32, [P, P, C.POINTER(DenoiseBatch), P]),

@@ -13,7 +13,7 @@ namespace luz {
 luz_status pack_tlas_input(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint32_t n);
 luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t);
 luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t);
-luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised);
+luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode);
 }  // namespace luz
 
 struct luz_batch {

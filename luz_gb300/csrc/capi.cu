@@ -15,7 +15,7 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t);
 luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int frame_index,
                              unsigned long long* d_stats);
 luz_status frame_lit_count(luz_ctx* ctx, luz_frame* f, uint32_t* count);
-luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised);
+luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode);
 uint32_t lit_chunks(uint32_t width, uint32_t height);
 luz_status launch_ao_resolve(luz_ctx* ctx, luz_frame* f);
 luz_status upload_srgb_lut(luz_ctx* ctx, const float* lut);
@@ -74,7 +74,8 @@ luz_status ensure_scratch(luz_ctx* ctx, size_t bytes) {
 
 static void free_frame_buffers(luz_frame* f) {
     void* ptrs[] = {f->albedo, f->normal, f->material, f->emission, f->depth, f->light,
-                    f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->surf,
+                    f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->signal,
+                    f->unshadowed, f->denoised, f->surf,
                     f->features, f->lin_depth, f->taa, f->taa_next, f->compose, f->hist, f->hist_state,
                     f->block_counts, f->lit_count, f->dn_list, f->dn_count, f->d_scene, f->d_lights, f->d_models,
                     f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter, f->d_textures,
@@ -421,6 +422,9 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     A((void**)&f->primary_hit, P * 8);
     A((void**)&f->ao, P * 4);
     A((void**)&f->ao_denoised, P * 4);
+    A((void**)&f->signal, P * 16);
+    A((void**)&f->unshadowed, P * 16);
+    A((void**)&f->denoised, P * 16);
     A((void**)&f->features, P * 16);
     A((void**)&f->lin_depth, P * 4);
     A((void**)&f->dn_list, P * 4);
@@ -441,6 +445,9 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
         return cuda_error(ctx, e, "cudaMalloc(frame)");
     }
     cudaMemset(f->ao_denoised, 0, P * 4);
+    cudaMemset(f->signal, 0, P * 16);
+    cudaMemset(f->unshadowed, 0, P * 16);
+    cudaMemset(f->denoised, 0, P * 16);
     cudaMemset(f->taa, 0, P * 16);
     cudaMemset(f->compose, 0, P * 4);
     cudaMemset(f->hist_state, 0, 16);
@@ -607,9 +614,12 @@ luz_status luz_frame_lit_count(luz_ctx* ctx, luz_frame* f, uint32_t* count) {
     return frame_lit_count(ctx, f, count);
 }
 
-luz_status luz_light_pass(luz_ctx* ctx, luz_frame* f, int32_t use_denoised_ao) {
+luz_status luz_light_pass(luz_ctx* ctx, luz_frame* f, int32_t mode) {
     if (!ctx || !f) return LUZ_ERR_INVALID;
-    return launch_light_pass(ctx, f, use_denoised_ao);
+    // public modes 0, 1, 2 -> plain, denoised AO, composed from the denoiser's output
+    if (mode < LUZ_LIGHT_PASS_PLAIN || mode > LUZ_LIGHT_PASS_DENOISED)
+        return set_error(ctx, LUZ_ERR_INVALID, "unknown light pass mode");
+    return launch_light_pass(ctx, f, mode == LUZ_LIGHT_PASS_DENOISED ? 3 : mode);
 }
 
 luz_status luz_render_frame(luz_ctx* ctx, luz_frame* f, luz_tlas* t, const luz_instance* instances,
@@ -629,7 +639,8 @@ size_t luz_frame_plane_bytes(const luz_frame* f, int32_t plane) {
         case LUZ_PLANE_ALBEDO: case LUZ_PLANE_MATERIAL: case LUZ_PLANE_EMISSION: case LUZ_PLANE_DEPTH:
         case LUZ_PLANE_AO: case LUZ_PLANE_AO_DENOISED: case LUZ_PLANE_LIN_DEPTH:
         case LUZ_PLANE_COMPOSE: return P * 4;
-        case LUZ_PLANE_NORMAL: case LUZ_PLANE_LIGHT: case LUZ_PLANE_FEATURES: case LUZ_PLANE_TAA: return P * 16;
+        case LUZ_PLANE_NORMAL: case LUZ_PLANE_LIGHT: case LUZ_PLANE_FEATURES: case LUZ_PLANE_TAA:
+        case LUZ_PLANE_SIGNAL: case LUZ_PLANE_UNSHADOWED: case LUZ_PLANE_DENOISED: return P * 16;
         case LUZ_PLANE_PRIMARY_HIT: return P * 8;
         case LUZ_PLANE_SHADOW_BITS: return (size_t)f->shadow_slots * f->words * 4;
         case LUZ_PLANE_AO_BITS: return (size_t)f->ao_samples * f->words * 4;
@@ -655,6 +666,9 @@ void* luz_frame_plane_device_ptr(luz_frame* f, int32_t plane) {
         case LUZ_PLANE_LIN_DEPTH: return f->lin_depth;
         case LUZ_PLANE_TAA: return f->taa;
         case LUZ_PLANE_COMPOSE: return f->compose;
+        case LUZ_PLANE_SIGNAL: return f->signal;
+        case LUZ_PLANE_UNSHADOWED: return f->unshadowed;
+        case LUZ_PLANE_DENOISED: return f->denoised;
         default: return nullptr;
     }
 }

@@ -13,8 +13,8 @@
 // fixed order, writes one partial per CTA, and a second kernel sums the partials in
 // CTA order — the gradient is deterministic. Adam keeps FP32 master weights.
 //
-// Feature channels per pixel: 0 noisy AO, 1 noisy shadow (mean lit fraction over the
-// shadow samples), 2-4 normal, 5 depth relative to the centre pixel
+// Feature channels per pixel: 0 noisy AO, 1 noisy shadow ratio of the direct light's
+// luminance (lum(S) / lum(U)), 2-4 normal, 5 depth relative to the centre pixel
 // ((d_q - d_p)/d_p, clamped to [-1,1]), 6 roughness, 7 albedo luminance.
 #include <cuda_bf16.h>
 
@@ -65,9 +65,6 @@ struct FeatParams {
     const float4* normal;
     const uint32_t* material;
     const float* depth;
-    const uint32_t* shadow_bits;
-    const uint32_t* ao_bits;
-    uint32_t shadow_slots, ao_samples, words;
     uint32_t width, height;
     float inverse_proj[16], inverse_view[16];
     float cam[3];
@@ -75,29 +72,17 @@ struct FeatParams {
     float* lin_depth;  // distance to the camera (0 = background)
     float* ao;         // noisy AO value
     float* denoised;   // if set: 0 written here for background pixels (the denoiser skips them)
+    float4* denoised4; // if set: the same for the filtered plane
+    float4* signal;    // read at lit pixels (written by the split pass), zeroed at background pixels
+    float4* unshadowed;
     uint32_t* list;    // if set: lit pixels appended (x | y << 16), row-major within a block
     uint32_t* list_count;
 };
 
 __constant__ float c_lin_lut[256];   // pow(i/255, 2.2)
 
-// For lane j of a warp: how many of the `planes` bit planes have bit j of word `w` set.
-// Lane s loads plane s of each group of 32 (one load latency per group); the words
-// then pass through the warp by shuffles.
-__device__ __forceinline__ uint32_t column_count(const uint32_t* __restrict__ bits, uint32_t planes, uint32_t words,
-                                                 uint32_t w) {
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t mine = 0;
-    for (uint32_t c = 0; c < planes; c += 32) {
-        const uint32_t s = c + lane;
-        const uint32_t word = s < planes ? __ldg(bits + (size_t)s * words + w) : 0u;
-        const uint32_t n = min(32u, planes - c);
-#pragma unroll 8
-        for (uint32_t j = 0; j < n; ++j) mine += (__shfl_sync(0xFFFFFFFFu, word, j) >> lane) & 1u;
-    }
-    return mine;
-}
-
+// Channels 0 and 1 come from the split pass: the AO value and the shadow ratio of
+// the direct light's luminance, lum(S) / lum(U).
 __global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
     __shared__ uint32_t s_warp[8];
     __shared__ uint32_t s_base;
@@ -119,35 +104,29 @@ __global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
         __syncthreads();
         if (lit) F.list[s_base + s_warp[warp] + __popc(mask & ((1u << lane) - 1u))] = x | (y << 16);
     }
-    uint32_t a8 = 0, m8 = 0;
-    float depth = 0.f;
-    if (lit) {   // issued before the bit counts so that both wait on memory together
-        a8 = F.albedo[pix];
-        m8 = F.material[pix];
-        depth = F.depth[pix];
-    }
-    uint32_t ao_hits = 0, shadow_hits = 0;
-    if (__any_sync(0xFFFFFFFFu, lit)) {   // a warp's 32 pixels are the 32 bits of one word
-        ao_hits = column_count(F.ao_bits, F.ao_samples, F.words, pix >> 5);
-        shadow_hits = column_count(F.shadow_bits, F.shadow_slots, F.words, pix >> 5);
-    }
     if (!inside) return;
     if (!lit) {
         F.feat[pix] = make_uint4(0, 0, 0, 0);
         F.lin_depth[pix] = 0.0f;
         F.ao[pix] = 0.0f;
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        F.signal[pix] = z4;
+        F.unshadowed[pix] = z4;
         if (F.denoised) F.denoised[pix] = 0.0f;
+        if (F.denoised4) F.denoised4[pix] = z4;
         return;
     }
-    const float ao = F.ao_samples ? (float)ao_hits / (float)F.ao_samples : 1.0f;
-    const float lit_frac = F.shadow_slots ? 1.0f - (float)shadow_hits / (float)F.shadow_slots : 1.0f;
+    const uint32_t a8 = F.albedo[pix], m8 = F.material[pix];
+    const float depth = F.depth[pix];
+    const float ao = F.signal[pix].w;
+    const float shadow = F.unshadowed[pix].w;   // lum(S) / lum(U) of the split pass
     float lum = 0.2127f * c_lin_lut[a8 & 0xFF] + 0.7152f * c_lin_lut[(a8 >> 8) & 0xFF] +
                 0.0722f * c_lin_lut[(a8 >> 16) & 0xFF];
     float rough = (float)(m8 & 0xFF) / 255.0f;
     V3 p = depth_to_world(F.inverse_proj, F.inverse_view, pixel_uv(x, F.width), pixel_uv(y, F.height), depth);
     float d = length(p - V3{F.cam[0], F.cam[1], F.cam[2]});
     uint4 v;
-    v.x = pack2(ao, lit_frac);
+    v.x = pack2(ao, shadow);
     v.y = pack2(n.x, n.y);
     v.z = pack2(n.z, 0.0f);
     v.w = pack2(rough, lum);
@@ -241,10 +220,29 @@ __device__ __forceinline__ void to_a_relu(const float c[2 * KS][4], uint32_t a[K
     }
 }
 
+// Filtered shadow ratio of one channel: sum(w S) / sum(w U); 1 where sum(w U) = 0 (no
+// neighbour receives direct light in that channel: the pixel's own U is 0 then too).
+__device__ __forceinline__ float filtered_ratio(float ws, float wu) {
+    return wu > 0.0f ? fminf(fmaxf(ws / wu, 0.0f), 1.0f) : 1.0f;
+}
+
+// Tap k of the 7x7 filter around pixel (x, y) of image img (image-clamped); zeros when
+// !ok or k >= 49.
+__device__ __forceinline__ float4 signal_tap(const float4* __restrict__ sig, const ImageGeom& G, bool ok,
+                                             uint32_t img, int x, int y, int k) {
+    if (!ok || k >= 49) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const int qx = min(max(x + k % 7 - 3, 0), (int)G.width - 1);
+    const int qy = min(max(y + k / 7 - 3, 0), (int)G.height - 1);
+    return __ldg(sig + img * G.pixels + (uint32_t)qy * G.width + (uint32_t)qx);
+}
+
 // Softmax over the 49 logits of rows g and g+8 (4 lanes share a row) and the 7x7
-// filter of the noisy AO. w[7][4] receives the weights; returns y for both rows.
-__device__ __forceinline__ void softmax_filter(float z[7][4], const float* __restrict__ ao, const ImageGeom& G,
-                                               uint32_t base, float y[2], float aok[7][4]) {
+// filter. z[7][4] receives the normalised weights w_k; for row g + 8h, y[h] = (ratio
+// r, g, b, AO) with ratio_c = sum(w S_c) / sum(w U_c) and AO = sum(w AO), and
+// du[h] = sum(w U) (r, g, b).
+__device__ __forceinline__ void softmax_filter(float z[7][4], const float4* __restrict__ sig,
+                                               const float4* __restrict__ uns, const ImageGeom& G, uint32_t base,
+                                               float4 y[2], float3 du[2]) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const uint32_t total = G.pixels * G.images;
 #pragma unroll
@@ -270,35 +268,47 @@ __device__ __forceinline__ void softmax_filter(float z[7][4], const float* __res
         s += __shfl_xor_sync(0xFFFFFFFFu, s, 2);
         float inv = 1.0f / s;
         uint32_t gp = base + g + 8 * h;
-        float acc = 0.f;
-        uint32_t img = 0, local = 0;
+        uint32_t img = 0;
         int x = 0, yy = 0;
-        bool ok = gp < total;
+        const bool ok = gp < total;
         if (ok) {
             img = gp / G.pixels;
-            local = gp - img * G.pixels;
+            const uint32_t local = gp - img * G.pixels;
             x = (int)(local % G.width);
             yy = (int)(local / G.width);
         }
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        float3 au = make_float3(0.f, 0.f, 0.f);
 #pragma unroll
         for (int nt = 0; nt < 7; ++nt)
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
-                int k = nt * 8 + 2 * t + j;
-                float wk = z[nt][2 * h + j] * inv;
+                const int k = nt * 8 + 2 * t + j;
+                const float wk = z[nt][2 * h + j] * inv;
                 z[nt][2 * h + j] = wk;
-                float a = 0.f;
-                if (k < 49 && ok) {
-                    int qx = min(max(x + k % 7 - 3, 0), (int)G.width - 1);
-                    int qy = min(max(yy + k / 7 - 3, 0), (int)G.height - 1);
-                    a = __ldg(ao + img * G.pixels + (uint32_t)qy * G.width + (uint32_t)qx);
-                }
-                aok[nt][2 * h + j] = a;
-                acc += wk * a;
+                const float4 a = signal_tap(sig, G, ok, img, x, yy, k);
+                const float4 u = signal_tap(uns, G, ok, img, x, yy, k);
+                acc.x += wk * a.x;
+                acc.y += wk * a.y;
+                acc.z += wk * a.z;
+                acc.w += wk * a.w;
+                au.x += wk * u.x;
+                au.y += wk * u.y;
+                au.z += wk * u.z;
             }
-        acc += __shfl_xor_sync(0xFFFFFFFFu, acc, 1);
-        acc += __shfl_xor_sync(0xFFFFFFFFu, acc, 2);
-        y[h] = acc;
+#pragma unroll
+        for (int o = 1; o <= 2; o <<= 1) {
+            acc.x += __shfl_xor_sync(0xFFFFFFFFu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xFFFFFFFFu, acc.y, o);
+            acc.z += __shfl_xor_sync(0xFFFFFFFFu, acc.z, o);
+            acc.w += __shfl_xor_sync(0xFFFFFFFFu, acc.w, o);
+            au.x += __shfl_xor_sync(0xFFFFFFFFu, au.x, o);
+            au.y += __shfl_xor_sync(0xFFFFFFFFu, au.y, o);
+            au.z += __shfl_xor_sync(0xFFFFFFFFu, au.z, o);
+        }
+        y[h] = make_float4(filtered_ratio(acc.x, au.x), filtered_ratio(acc.y, au.y), filtered_ratio(acc.z, au.z),
+                           acc.w);
+        du[h] = au;
     }
 }
 
@@ -308,9 +318,11 @@ struct InferParams {
     const float* bias;
     const uint4* feat;
     const float* lin_depth;
-    const float* ao;
+    const float4* sig;       // noisy (shadowed direct light S r, g, b, AO)
+    const float4* uns;       // unshadowed direct light U (r, g, b, -)
     ImageGeom G;
-    float* out;
+    float4* out;             // filtered shadow ratio sum(w S) / sum(w U) (r, g, b) and AO
+    float* out_ao;           // if set: its AO channel as well
     // optional pixel list (one image): x | y << 16 per entry, the count in *list_count;
     // only the listed pixels are written
     const uint32_t* list;
@@ -330,10 +342,10 @@ struct InferParams {
 // A block holds the weights once and kTcGroups warpgroups, each with its own tile,
 // A buffer, 64 accumulator columns, mbarrier and named barrier: while one group waits
 // for its products the others gather, or run their epilogues.
-constexpr int kTcGroups = 6;                    // warpgroups (tiles in flight) per block
+constexpr int kTcGroups = 4;                    // warpgroups (tiles in flight) per block
 constexpr int kTcThreads = 128 * kTcGroups;
 constexpr uint32_t kTcCols = 64;                // accumulator columns of one group (N)
-constexpr uint32_t kTcAlloc = 512;              // power of two >= kTcGroups * kTcCols
+constexpr uint32_t kTcAlloc = 256;              // power of two >= kTcGroups * kTcCols
 constexpr int kTcW1 = 0, kTcW2 = kTcW1 + 64 * 80 * 2, kTcW3 = kTcW2 + 64 * 64 * 2, kTcW4 = kTcW3 + 64 * 64 * 2;
 constexpr int kTcABytes = 128 * 80 * 2;
 constexpr int kTcA = kTcW4 + 64 * 64 * 2, kTcBias = kTcA + kTcGroups * kTcABytes, kTcBar = kTcBias + kBias * 4;
@@ -466,30 +478,35 @@ __device__ __forceinline__ float exp2_approx(float x) {
     return r;
 }
 
-// Second pass of the softmax and the 7x7 filter: (sum of w_k * ao_k, sum of w_k) with
-// w_k = 2^((z_k - m) * log2 e), z_k = logit + bias. kInterior: every tap of the
-// thread's pixel is inside the image (rows addressed directly); otherwise clamped.
+// Second pass of the softmax and the 7x7 filter: with w_k = 2^((z_k - m) * log2 e),
+// z_k = logit + bias, sums of w_k x the shadowed light S_k (r, g, b) and AO_k (acc),
+// of w_k x the unshadowed light U_k (accu, r, g, b) and of w_k (the return value).
+// kInterior: every tap of the thread's pixel is inside the image (rows addressed
+// directly); otherwise clamped.
 template <bool kInterior>
-__device__ __forceinline__ float2 ao_filter(uint32_t tmem_lane, const float2* b4, float b48, float m,
-                                           const float* __restrict__ ao, uint32_t base, int x, int y,
-                                           const ImageGeom& G) {
+__device__ __forceinline__ float signal_filter(uint32_t tmem_lane, const float2* b4, float b48, float m,
+                                               const float4* __restrict__ sig, const float4* __restrict__ uns,
+                                               uint32_t base, int x, int y, const ImageGeom& G, float4& acc,
+                                               float3& accu) {
     constexpr float kLog2e = 1.4426950408889634f;
     const float2 l2e = make_float2(kLog2e, kLog2e);
     const float nm = -m * kLog2e;
     const float2 nm2 = make_float2(nm, nm);
-    const float* rows[7];
+    uint32_t rows[7];
     int qx[7];
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
         if (kInterior) {
-            rows[d] = ao + base + (uint32_t)(y + d - 3) * G.width + (uint32_t)(x - 3);
+            rows[d] = base + (uint32_t)(y + d - 3) * G.width + (uint32_t)(x - 3);
         } else {
-            rows[d] = ao + base + (uint32_t)min(max(y + d - 3, 0), (int)G.height - 1) * G.width;
+            rows[d] = base + (uint32_t)min(max(y + d - 3, 0), (int)G.height - 1) * G.width;
             qx[d] = min(max(x + d - 3, 0), (int)G.width - 1);
         }
     }
-    auto tap = [&](int k) -> float { return __ldg(rows[k / 7] + (kInterior ? k % 7 : qx[k % 7])); };
-    float2 s = make_float2(0.f, 0.f), acc = make_float2(0.f, 0.f);
+    auto at = [&](int k) -> uint32_t { return rows[k / 7] + (uint32_t)(kInterior ? k % 7 : qx[k % 7]); };
+    float2 s = make_float2(0.f, 0.f);
+    float2 a_xy = make_float2(0.f, 0.f), a_zw = make_float2(0.f, 0.f), u_xy = make_float2(0.f, 0.f);
+    float u_z = 0.f;
 #pragma unroll
     for (int c0 = 0; c0 < 48; c0 += 16) {
         float v[16];
@@ -500,13 +517,28 @@ __device__ __forceinline__ float2 ao_filter(uint32_t tmem_lane, const float2* b4
             const float2 t = fma2(add2(make_float2(v[2 * j], v[2 * j + 1]), b4[k / 2]), l2e, nm2);
             const float2 e = make_float2(exp2_approx(t.x), exp2_approx(t.y));
             s = add2(s, e);
-            acc = fma2(e, make_float2(tap(k), tap(k + 1)), acc);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t q = at(k + h);
+                const float4 x4 = __ldg(sig + q), u4 = __ldg(uns + q);
+                const float eh = h ? e.y : e.x;
+                const float2 e2 = make_float2(eh, eh);
+                a_xy = fma2(e2, make_float2(x4.x, x4.y), a_xy);
+                a_zw = fma2(e2, make_float2(x4.z, x4.w), a_zw);
+                u_xy = fma2(e2, make_float2(u4.x, u4.y), u_xy);
+                u_z = fmaf(eh, u4.z, u_z);
+            }
         }
     }
     float v[16];
     tc_load16(tmem_lane + 48u, v);
     const float e48 = exp2_approx(fmaf(v[0] + b48, kLog2e, nm));
-    return make_float2(fmaf(e48, tap(48), acc.x + acc.y), e48 + s.x + s.y);
+    const uint32_t q = at(48);
+    const float4 x48 = __ldg(sig + q), u48 = __ldg(uns + q);
+    acc = make_float4(fmaf(e48, x48.x, a_xy.x), fmaf(e48, x48.y, a_xy.y), fmaf(e48, x48.z, a_zw.x),
+                      fmaf(e48, x48.w, a_zw.y));
+    accu = make_float3(fmaf(e48, u48.x, u_xy.x), fmaf(e48, u48.y, u_xy.y), fmaf(e48, u48.z, u_z));
+    return e48 + s.x + s.y;
 }
 
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_kernel(InferParams P, uint32_t* status) {
@@ -623,10 +655,20 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) denoise_infer_tc_k
         }
         const uint32_t base = img * P.G.pixels;
         const bool interior = has && x >= 3 && y >= 3 && x + 3 < (int)P.G.width && y + 3 < (int)P.G.height;
-        const float2 r = __all_sync(0xFFFFFFFFu, interior)
-                             ? ao_filter<true>(tmem_lane, b4, sbias[192 + 48], m, P.ao, base, x, y, P.G)
-                             : ao_filter<false>(tmem_lane, b4, sbias[192 + 48], m, P.ao, base, x, y, P.G);
-        if (has) P.out[gp] = valid ? r.x * (1.0f / r.y) : 0.0f;
+        float4 acc;
+        float3 accu;
+        const float wsum = __all_sync(0xFFFFFFFFu, interior)
+                               ? signal_filter<true>(tmem_lane, b4, sbias[192 + 48], m, P.sig, P.uns, base, x, y,
+                                                     P.G, acc, accu)
+                               : signal_filter<false>(tmem_lane, b4, sbias[192 + 48], m, P.sig, P.uns, base, x, y,
+                                                      P.G, acc, accu);
+        if (has) {
+            const float4 r = valid ? make_float4(filtered_ratio(acc.x, accu.x), filtered_ratio(acc.y, accu.y),
+                                                 filtered_ratio(acc.z, accu.z), acc.w * (1.0f / wsum))
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+            P.out[gp] = r;
+            if (P.out_ao) P.out_ao[gp] = r.w;
+        }
     }
     if (failed) tc_wait(bar, phase ^ 1u);   // products still in flight before the columns are freed
     asm volatile("tcgen05.fence::before_thread_sync;");
@@ -640,10 +682,13 @@ struct TrainParams {
     const float* bias;
     const uint4* feat;
     const float* lin_depth;
-    const float* ao;
-    const float* target;
+    const float4* sig;         // noisy (shadowed direct light S r, g, b, AO)
+    const float4* uns;         // unshadowed direct light U (r, g, b, -)
+    const float4* target;      // many-sample shadow ratio (r, g, b) and AO
+    const float4* weight;      // per-pixel loss weight of each output, or null (shadow_weight, AO: 1)
     ImageGeom G;
     float grad_scale;          // 2 / number of pixels (mean squared error)
+    float shadow_weight;       // loss weight of each shadow-ratio output (AO: 1)
     float* partial;            // [gridDim.x][kParams]
     float* partial_loss;       // [gridDim.x]
 };
@@ -742,33 +787,63 @@ __global__ void __launch_bounds__(256, 1) denoise_train_kernel(TrainParams P) {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
                 S.h3T[nt * 8 + 2 * t + (j & 1)][px0 + g + 8 * (j >> 1)] = __float2bfloat16(fmaxf(c[nt][j], 0.f));
-        float z[7][4], aok[7][4], y[2];
+        float z[7][4];
+        float4 y[2];
+        float3 du[2];
         layer<4, 7>(a1, sw + pW4, sW, sbias + 192, z);
-        softmax_filter(z, P.ao, P.G, base, y, aok);   // z now holds the softmax weights
-        // ---- loss and dL/dz (softmax + filter backward)
+        softmax_filter(z, P.sig, P.uns, P.G, base, y, du);   // z now holds the softmax weights
+        // ---- loss and dL/dz (softmax + filter backward): with dy the loss gradient of
+        // the outputs, g_k = dy_ao AO_k + sum_c dy_c (S_kc - ratio_c U_kc) / sum(w U_c)
+        // (the derivative of the ratio of sums) and dz_k = w_k (g_k - sum_j w_j g_j)
         float dz[8][4];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            uint32_t gp = base + g + 8 * h;
-            bool ok = ((valid >> (g + 8 * h)) & 1u) != 0;
-            float tgt = ok ? P.target[gp] : 0.f;
-            float err = ok ? (y[h] - tgt) : 0.f;
-            if (t == 0) loss += err * err * (0.5f * P.grad_scale);   // mean over the batch's pixels
-            float dy = err * P.grad_scale;
+            const uint32_t gp = base + g + 8 * h;
+            const bool ok = ((valid >> (g + 8 * h)) & 1u) != 0;
+            const float4 tg = ok ? P.target[gp] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 err = ok ? make_float4(y[h].x - tg.x, y[h].y - tg.y, y[h].z - tg.z, y[h].w - tg.w)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 cw = (P.weight && ok) ? P.weight[gp]
+                                               : make_float4(P.shadow_weight, P.shadow_weight, P.shadow_weight, 1.0f);
+            if (t == 0)   // mean over the batch's pixels
+                loss += (cw.w * err.w * err.w + cw.x * err.x * err.x + cw.y * err.y * err.y + cw.z * err.z * err.z) *
+                        (0.5f * P.grad_scale);
+            const float4 dy = make_float4(cw.x * err.x * P.grad_scale, cw.y * err.y * P.grad_scale,
+                                          cw.z * err.z * P.grad_scale, cw.w * err.w * P.grad_scale);
+            // d ratio_c / d w_k = (S_kc - ratio_c U_kc) / sum(w U_c); 0 where the sum is 0
+            const float3 dq = make_float3(du[h].x > 0.f ? dy.x / du[h].x : 0.f, du[h].y > 0.f ? dy.y / du[h].y : 0.f,
+                                          du[h].z > 0.f ? dy.z / du[h].z : 0.f);
+            const float3 dr = make_float3(dq.x * y[h].x, dq.y * y[h].y, dq.z * y[h].z);
+            uint32_t img = 0;
+            int px = 0, py = 0;
+            const bool in = gp < P.G.pixels * P.G.images;
+            if (in) {
+                img = gp / P.G.pixels;
+                const uint32_t local = gp - img * P.G.pixels;
+                px = (int)(local % P.G.width);
+                py = (int)(local / P.G.width);
+            }
+            float gk[7][2];
             float sdot = 0.f;
 #pragma unroll
             for (int nt = 0; nt < 7; ++nt)
 #pragma unroll
-                for (int j = 0; j < 2; ++j) sdot += z[nt][2 * h + j] * (dy * aok[nt][2 * h + j]);
+                for (int j = 0; j < 2; ++j) {
+                    const float4 a = signal_tap(P.sig, P.G, in, img, px, py, nt * 8 + 2 * t + j);
+                    const float4 u = signal_tap(P.uns, P.G, in, img, px, py, nt * 8 + 2 * t + j);
+                    gk[nt][j] = dy.w * a.w + (dq.x * a.x - dr.x * u.x) + (dq.y * a.y - dr.y * u.y) +
+                                (dq.z * a.z - dr.z * u.z);
+                    sdot += z[nt][2 * h + j] * gk[nt][j];
+                }
             sdot += __shfl_xor_sync(0xFFFFFFFFu, sdot, 1);
             sdot += __shfl_xor_sync(0xFFFFFFFFu, sdot, 2);
 #pragma unroll
             for (int nt = 0; nt < 7; ++nt)
 #pragma unroll
                 for (int j = 0; j < 2; ++j) {
-                    int k = nt * 8 + 2 * t + j;
-                    float w = z[nt][2 * h + j];
-                    dz[nt][2 * h + j] = (k < 49) ? w * (dy * aok[nt][2 * h + j] - sdot) : 0.f;
+                    const int k = nt * 8 + 2 * t + j;
+                    const float w = z[nt][2 * h + j];
+                    dz[nt][2 * h + j] = (k < 49) ? w * (gk[nt][j] - sdot) : 0.f;
                 }
             dz[7][2 * h] = dz[7][2 * h + 1] = 0.f;
         }
@@ -943,9 +1018,11 @@ struct luz_denoiser {
     float* loss = nullptr;
     int ctas = 0;
     uint64_t step = 0;
+    float shadow_weight = 1.0f / 3.0f;
 };
 
 namespace luz {
+luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode);
 namespace dn {
 
 static luz_status upload_lut(luz_ctx* ctx) {
@@ -967,7 +1044,8 @@ static luz_status repack(luz_ctx* ctx, luz_denoiser* d) {
 static size_t train_smem() { return (size_t)pEnd * 2 + kBias * 4 + sizeof(TrainSmem); }
 
 static luz_status check_batch(luz_ctx* ctx, const luz_denoise_batch* b) {
-    if (!b || !b->features || !b->lin_depth || !b->noisy_ao || b->width == 0 || b->height == 0 || b->images == 0)
+    if (!b || !b->features || !b->lin_depth || !b->noisy || !b->unshadowed || b->width == 0 || b->height == 0 ||
+        b->images == 0)
         return set_error(ctx, LUZ_ERR_INVALID, "incomplete denoiser batch");
     if ((uint64_t)b->width * b->height * b->images >= (1ull << 31))
         return set_error(ctx, LUZ_ERR_LIMIT, "denoiser batch larger than 2^31 pixels");
@@ -976,8 +1054,9 @@ static luz_status check_batch(luz_ctx* ctx, const luz_denoise_batch* b) {
 
 // Dense over the batch's pixels, or over the lit-pixel list of one image when `list`
 // is given (the other pixels of `out` are then written by the features pass).
-static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float* out,
-                            const uint32_t* list = nullptr, const uint32_t* list_count = nullptr) {
+static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float4* out,
+                            float* out_ao = nullptr, const uint32_t* list = nullptr,
+                            const uint32_t* list_count = nullptr) {
     static bool attr = false;
     if (!attr) {
         LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -989,9 +1068,11 @@ static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_bat
     P.bias = d->bias;
     P.feat = (const uint4*)b->features;
     P.lin_depth = b->lin_depth;
-    P.ao = b->noisy_ao;
+    P.sig = (const float4*)b->noisy;
+    P.uns = (const float4*)b->unshadowed;
     P.G = ImageGeom{b->width, b->height, b->width * b->height, b->images};
     P.out = out;
+    P.out_ao = out_ao;
     P.list = list;
     P.list_count = list_count;
     uint32_t tiles = (P.G.pixels * P.G.images + 127) / 128;
@@ -1004,7 +1085,7 @@ static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_bat
 }
 
 static luz_status run_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b) {
-    if (!b->target_ao) return set_error(ctx, LUZ_ERR_INVALID, "training batch without targets");
+    if (!b->target) return set_error(ctx, LUZ_ERR_INVALID, "training batch without targets");
     static bool attr = false;
     if (!attr) {
         LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1016,10 +1097,13 @@ static luz_status run_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_
     P.bias = d->bias;
     P.feat = (const uint4*)b->features;
     P.lin_depth = b->lin_depth;
-    P.ao = b->noisy_ao;
-    P.target = b->target_ao;
+    P.sig = (const float4*)b->noisy;
+    P.uns = (const float4*)b->unshadowed;
+    P.target = (const float4*)b->target;
+    P.weight = (const float4*)b->weight;
     P.G = ImageGeom{b->width, b->height, b->width * b->height, b->images};
     P.grad_scale = 2.0f / (float)((double)P.G.pixels * P.G.images);
+    P.shadow_weight = d->shadow_weight;
     P.partial = d->partial;
     P.partial_loss = d->partial_loss;
     LUZ_CUDA(ctx, cudaMemsetAsync(d->partial, 0, (size_t)d->ctas * kParams * 4, ctx->stream));
@@ -1140,24 +1224,22 @@ luz_status luz_denoise_batch_infer(luz_ctx* ctx, luz_denoiser* d, const luz_deno
     if (!ctx || !d || !d_out) return LUZ_ERR_INVALID;
     luz_status s = check_batch(ctx, b);
     if (s != LUZ_OK) return s;
-    return run_infer(ctx, d, b, d_out);
+    return run_infer(ctx, d, b, (float4*)d_out);
 }
 
-// Feature planes of a frame. With `for_denoise` the pass also writes 0 to the denoised
-// plane at the background pixels and lists the lit pixels for the denoiser.
+// Network inputs of a traced frame: the split pass (shadowed and unshadowed direct
+// light and AO of the lit pixels), then the feature planes. With `for_denoise` the
+// features pass also writes 0 to the denoised planes at the background pixels and
+// lists the lit pixels for the denoiser.
 static luz_status launch_features(luz_ctx* ctx, luz_frame* f, bool for_denoise) {
     luz_status s = upload_lut(ctx);
+    if (s == LUZ_OK) s = launch_light_pass(ctx, f, 2);
     if (s != LUZ_OK) return s;
     FeatParams F;
     F.albedo = f->albedo;
     F.normal = f->normal;
     F.material = f->material;
     F.depth = f->depth;
-    F.shadow_bits = f->shadow_bits;
-    F.ao_bits = f->ao_bits;
-    F.shadow_slots = f->shadow_slots;
-    F.ao_samples = f->ao_samples;
-    F.words = f->words;
     F.width = f->width;
     F.height = f->height;
     memcpy(F.inverse_proj, f->h_scene.inverse_proj, 64);
@@ -1167,6 +1249,9 @@ static luz_status launch_features(luz_ctx* ctx, luz_frame* f, bool for_denoise) 
     F.lin_depth = f->lin_depth;
     F.ao = f->ao;
     F.denoised = for_denoise ? f->ao_denoised : nullptr;
+    F.denoised4 = for_denoise ? f->denoised : nullptr;
+    F.signal = f->signal;
+    F.unshadowed = f->unshadowed;
     F.list = for_denoise ? f->dn_list : nullptr;
     F.list_count = f->dn_count;
     if (for_denoise) LUZ_CUDA(ctx, cudaMemsetAsync(f->dn_count, 0, 4, ctx->stream));
@@ -1186,8 +1271,15 @@ luz_status luz_denoise(luz_ctx* ctx, luz_denoiser* d, luz_frame* f) {
     if (!ctx || !d || !f) return LUZ_ERR_INVALID;
     luz_status s = launch_features(ctx, f, true);
     if (s != LUZ_OK) return s;
-    luz_denoise_batch b{f->features, f->lin_depth, f->ao, nullptr, f->width, f->height, 1};
-    return run_infer(ctx, d, &b, f->ao_denoised, f->dn_list, f->dn_count);
+    luz_denoise_batch b{f->features, f->lin_depth, (const float*)f->signal, (const float*)f->unshadowed, nullptr,
+                        nullptr, f->width, f->height, 1};
+    return run_infer(ctx, d, &b, f->denoised, f->ao_denoised, f->dn_list, f->dn_count);
+}
+
+luz_status luz_denoiser_set_shadow_weight(luz_ctx* ctx, luz_denoiser* d, float weight) {
+    if (!ctx || !d || !(weight >= 0.0f) || !(weight <= 1e6f)) return LUZ_ERR_INVALID;
+    d->shadow_weight = weight;
+    return LUZ_OK;
 }
 
 }  // extern "C"

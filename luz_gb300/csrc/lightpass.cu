@@ -29,7 +29,9 @@ struct LightParams {
     const uint32_t* shadow_bits;
     const uint32_t* ao_bits;
     const float* ao_denoised;
-    int use_denoised;
+    const float4* denoised;      // kCompose: filtered (shadow ratio rgb, AO)
+    float4* signal;              // kSplit: (S rgb, AO)
+    float4* unshadowed;          // kSplit: written (U rgb, lum(S) / lum(U)); kCompose: read
     const luz_light* lights;
     const uint32_t* light_slot;
     uint32_t light_count;
@@ -66,6 +68,17 @@ __device__ __forceinline__ uint32_t bit_at(const uint32_t* __restrict__ planes, 
     return (__ldg(planes + (size_t)plane * words + (pix >> 5)) >> (pix & 31)) & 1u;
 }
 
+// Modes of the light pass. kPlain: light.frag main with the ray-traced shadow factors
+// and AO from the bit planes. kDenoisedAo: the same with AO from the denoised plane.
+// kSplit (the denoiser's input pass): the direct light twice, shadowed as light.frag
+// sums it (S) and unshadowed (U, every shadow factor 0), written as (S, AO) and
+// (U, lum(S) / lum(U)); no light-plane write. kCompose: the frame from the filtered
+// shadow ratio R and AO: ambient * AO + U * R + emission.
+enum : int { kPlain = 0, kDenoisedAo = 1, kSplit = 2, kCompose = 3 };
+
+__device__ __forceinline__ float luminance(V3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+template <int kMode>
 __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     extern __shared__ luz_light s_lights[];
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -93,6 +106,7 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     V3 V = normalize(cam - p);
     V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + albedo * metallic;
     V3 Lo = V3{0.0f, 0.0f, 0.0f};
+    V3 Lu = V3{0.0f, 0.0f, 0.0f};   // kSplit: unshadowed direct light
     // per-pixel parts of the Cook-Torrance terms (light.frag:17-49, 210-229)
     const float a = roughness * roughness, a2 = a * a;
     const float r1 = roughness + 1.0f, k = (r1 * r1) / 8.0f;
@@ -101,7 +115,7 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     const V3 diffuse_albedo = albedo * ((1.0f - metallic) * kInvPi);
     // EvaluateShadow's origin (light.frag:138-139), used by the 2D shadow maps
     const V3 shadow_origin = p + N * fmax_(length(p - cam) * 0.01f, 0.05f);
-    for (uint32_t i = 0; i < P.light_count; ++i) {
+    for (uint32_t i = 0; i < (kMode == kCompose ? 0u : P.light_count); ++i) {
         const luz_light& lt = s_lights[i];
         const V3 L = light_vector(lt, p);                    // light.frag:194-198
         const float attenuation = light_attenuation(lt, p, L);   // light.frag:199-208
@@ -135,9 +149,14 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
         V3 spec = F * spec_scale;
         V3 diffuse = (V3{1.0f, 1.0f, 1.0f} - F) * diffuse_albedo;
         Lo = Lo + (diffuse + spec) * radiance * NdotL;
+        if constexpr (kMode == kSplit) Lu = Lu + (diffuse + spec) * ((color * lt.intensity) * attenuation) * NdotL;
     }
     float ao;
-    if (P.use_denoised) {
+    if constexpr (kMode == kCompose) {
+        const float4 d = P.denoised[pix], u = P.unshadowed[pix];
+        Lo = V3{u.x * d.x, u.y * d.y, u.z * d.z};
+        ao = d.w;
+    } else if constexpr (kMode == kDenoisedAo) {
         ao = P.ao_denoised[pix];
     } else if (P.ao_samples == 0) {
         ao = 1.0f;
@@ -145,6 +164,13 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
         uint32_t misses = 0;
         for (uint32_t s = 0; s < P.ao_samples; ++s) misses += bit_at(P.ao_bits, s, P.words, pix);
         ao = (float)misses / (float)P.ao_samples;
+    }
+    if constexpr (kMode == kSplit) {
+        const float lu = luminance(Lu);
+        const float ratio = lu > 0.0f ? fminf(fmaxf(luminance(Lo) / lu, 0.0f), 1.0f) : 1.0f;
+        P.signal[pix] = make_float4(Lo.x, Lo.y, Lo.z, ao);
+        P.unshadowed[pix] = make_float4(Lu.x, Lu.y, Lu.z, ratio);
+        return;
     }
     V3 ambient = (((amb * P.ambient_intensity) * albedo) * occlusion) * ao;
     V3 c = (ambient + Lo) + emission;
@@ -166,7 +192,8 @@ __global__ void __launch_bounds__(256) ao_resolve_kernel(const float4* normal, c
 }
 
 
-luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
+luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode) {
+    if (mode < kPlain || mode > kCompose) return set_error(ctx, LUZ_ERR_INVALID, "unknown light pass mode");
     luz_status st = ensure_lit_list(ctx, f);
     if (st != LUZ_OK) return st;
     LightParams P;
@@ -179,7 +206,9 @@ luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
     P.shadow_bits = f->shadow_bits;
     P.ao_bits = f->ao_bits;
     P.ao_denoised = f->ao_denoised;
-    P.use_denoised = use_denoised;
+    P.denoised = f->denoised;
+    P.signal = f->signal;
+    P.unshadowed = f->unshadowed;
     P.lights = f->d_lights;
     P.light_slot = f->d_light_slot;
     P.light_count = f->light_count;
@@ -195,13 +224,16 @@ luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int use_denoised) {
     P.height = f->height;
     P.out = f->light;
     size_t smem = (size_t)f->light_count * sizeof(luz_light);
-    if (smem > 48 * 1024) {
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(light_pass_kernel,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    void (*kernels[4])(LightParams) = {light_pass_kernel<kPlain>, light_pass_kernel<kDenoisedAo>,
+                                       light_pass_kernel<kSplit>, light_pass_kernel<kCompose>};
+    static size_t attr_bytes[4] = {48 * 1024, 48 * 1024, 48 * 1024, 48 * 1024};
+    if (smem > attr_bytes[mode]) {
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(kernels[mode], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_bytes[mode] = smem;
     }
     uint32_t blocks = (f->pixels + 255) / 256;
     prof_begin(ctx, LUZ_KERNEL_LIGHT_PASS);
-    light_pass_kernel<<<blocks, 256, smem, ctx->stream>>>(P);
+    kernels[mode]<<<blocks, 256, smem, ctx->stream>>>(P);
     prof_end(ctx);
     LUZ_LAUNCHED(ctx, "light_pass_kernel");
     return LUZ_OK;

@@ -48,6 +48,8 @@ def load() -> C.CDLL:
                                                C.c_int]),
             "oracle_light_pass": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32, P,
                                             C.c_int, C.c_uint32, C.c_uint32]),
+            "oracle_light_split": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32, P,
+                                             C.c_int]),
             "oracle_light_pass_f64": (C.c_int, [P, P, C.c_uint32, P, P, P, P, P, P, P, P, C.c_uint32, C.c_uint32,
                                                 P, C.c_int, C.c_uint32, C.c_uint32]),
             "oracle_trace_ray": (C.c_int, [P, P, P, C.c_float, C.c_float, C.c_int, C.c_int, P]),
@@ -225,6 +227,17 @@ class OracleFrame:
            _p(self.material), _p(self.emission), _p(self.depth), _p(self.shadow_bits), _p(self.ao_bits), _p(ao),
            self.W, self.H, _p(out), nthreads or threads(), y0, self.H if y1 is None else y1)
         return out.reshape(self.H, self.W, 4)
+
+    def light_split(self, nthreads=None) -> tuple[np.ndarray, np.ndarray]:
+        """The denoiser's split of the direct light: (signal [H, W, 4] = shadowed direct
+        light S r, g, b and AO; unshadowed [H, W, 4] = U r, g, b and lum(S) / lum(U))."""
+        out = np.zeros((self.W * self.H, 8), np.float32)
+        load().oracle_light_split(scene_bytes(self.scene), C.cast(self.lights, C.c_void_p), self.nl, _p(self.albedo),
+                                  _p(self.normal), _p(self.material), _p(self.emission), _p(self.depth),
+                                  _p(self.shadow_bits), _p(self.ao_bits), self.W, self.H, _p(out),
+                                  nthreads or threads())
+        out = out.reshape(self.H, self.W, 8)
+        return out[..., :4].copy(), out[..., 4:].copy()
 
 
 K_EMPTY_CHILD = -2147483647   # 0x80000001: a child slot with an inverted box

@@ -1,8 +1,10 @@
-"""FP64 numpy restatement of the learned AO denoiser (test infrastructure).
+"""FP64 numpy restatement of the learned shadow + AO denoiser (test infrastructure).
 
 Same network, feature gather (3x3 taps, clamped to the image, channel 5 replaced by
 the depth relative to the centre pixel, zero rows for background pixels), softmax
-7x7 filter and mean-squared-error loss as luz_gb300/csrc/denoise.cu, evaluated in
+7x7 filter (the AO average and the ratio estimator sum(w S) / sum(w U) of the
+shadowed over the unshadowed direct light) and weighted squared-error loss as
+luz_gb300/csrc/denoise.cu, evaluated in
 double precision with exact backpropagation. Inputs are the device's BF16 feature
 planes and weights rounded to BF16, as the device uses them; the device also rounds
 activations to BF16 between layers, so agreement is to BF16 accuracy.
@@ -57,26 +59,39 @@ def gather(feat_bits: np.ndarray, lin_depth: np.ndarray) -> tuple[np.ndarray, np
     return X, valid
 
 
-def neighbours(ao: np.ndarray) -> np.ndarray:
-    """[N,H,W] → [N,H,W,49] noisy AO at the 7x7 taps (clamped)."""
-    N, H, W = ao.shape
+# Loss weight of each shadow-ratio output (the AO output has weight 1).
+SHADOW_WEIGHT = 1.0 / 3.0
+
+
+def neighbours(sig: np.ndarray) -> np.ndarray:
+    """[N,H,W,4] → [N,H,W,49,4] at the 7x7 taps (clamped)."""
+    N, H, W, C4 = sig.shape
     ys, xs = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
-    out = np.zeros((N, H, W, 49), np.float64)
+    out = np.zeros((N, H, W, 49, C4), np.float64)
     for k in range(49):
         qy = np.clip(ys + k // 7 - 3, 0, H - 1)
         qx = np.clip(xs + k % 7 - 3, 0, W - 1)
-        out[..., k] = ao[:, qy, qx]
+        out[..., k, :] = sig[:, qy, qx, :]
     return out
 
 
-def forward_backward(params: np.ndarray, feat_bits, lin_depth, noisy_ao, target_ao):
-    """Returns (y [N,H,W], loss, grad [16177]); loss = sum over valid pixels of
-    (y - t)^2 divided by the number of pixels (background pixels count as zero error)."""
+def forward_backward(params: np.ndarray, feat_bits, lin_depth, noisy, unshadowed, target, weight=None,
+                     shadow_weight: float = SHADOW_WEIGHT):
+    """noisy: [N,H,W,4] shadowed direct light S (r, g, b) and AO; unshadowed: [N,H,W,4]
+    unshadowed direct light U (r, g, b, -); target: [N,H,W,4] shadow ratio (r, g, b) and
+    AO. Outputs per pixel: the ratio estimator R_c = sum(w S_c) / sum(w U_c) (1 where
+    the sum is 0) and AO' = sum(w AO). Returns (y [N,H,W,4], loss, grad [16177]);
+    loss = sum over valid pixels and outputs of weight x (y - t)^2 divided by the
+    number of pixels (background pixels count as zero error); weight [N,H,W,4] per
+    pixel, or shadow_weight for the ratio outputs and 1 for AO."""
     layers = [(bf16_round(W).astype(np.float64), b.astype(np.float64)) for W, b in unpack(params)]
     X, valid = gather(feat_bits, lin_depth)
     x = X[valid].astype(np.float64)                       # [P, 72]
-    A = neighbours(noisy_ao)[valid]                       # [P, 49]
-    t = target_ao[valid].astype(np.float64)
+    A = neighbours(noisy)[valid]                          # [P, 49, 4]
+    Uk = neighbours(unshadowed)[valid][..., :3]           # [P, 49, 3]
+    t = target[valid].astype(np.float64)                  # [P, 4]
+    cw = (np.asarray(weight, np.float64)[valid] if weight is not None else
+          np.array([shadow_weight, shadow_weight, shadow_weight, 1.0]))
     hs = [x]
     h = x
     for W, b in layers[:3]:
@@ -87,12 +102,17 @@ def forward_backward(params: np.ndarray, feat_bits, lin_depth, noisy_ao, target_
     z -= z.max(axis=1, keepdims=True)
     e = np.exp(z)
     w = e / e.sum(axis=1, keepdims=True)
-    y = (w * A).sum(axis=1)
-    npx = noisy_ao.size   # every pixel of the batch, as the device's mean
+    sums = (w[:, :, None] * A).sum(axis=1)                # [P, 4]: sum(w S), sum(w AO)
+    du = (w[:, :, None] * Uk).sum(axis=1)                 # [P, 3]: sum(w U)
+    lit = du > 0
+    ratio = np.where(lit, np.clip(sums[:, :3] / np.where(lit, du, 1.0), 0.0, 1.0), 1.0)
+    y = np.concatenate([ratio, sums[:, 3:4]], axis=1)     # [P, 4]
+    npx = noisy.shape[0] * noisy.shape[1] * noisy.shape[2]   # every pixel of the batch, as the device's mean
     err = y - t
-    loss = float((err ** 2).sum()) / npx
-    dy = 2.0 * err / npx
-    dw = dy[:, None] * A
+    loss = float((cw * err ** 2).sum()) / npx
+    dy = 2.0 * cw * err / npx
+    dq = np.where(lit, dy[:, :3] / np.where(lit, du, 1.0), 0.0)      # d loss / d sum(w S)
+    dw = dy[:, None, 3] * A[..., 3] + (dq[:, None, :] * (A[..., :3] - ratio[:, None, :] * Uk)).sum(axis=2)
     dz = w * (dw - (w * dw).sum(axis=1, keepdims=True))
     grads = []
     d = dz
@@ -104,6 +124,6 @@ def forward_backward(params: np.ndarray, feat_bits, lin_depth, noisy_ao, target_
             d = (d @ W) * (hs[li] > 0)
     grads.reverse()
     g = np.concatenate([np.concatenate([gw.ravel(), gb]) for gw, gb in grads])
-    yfull = np.zeros(noisy_ao.shape)
+    yfull = np.zeros(noisy.shape)
     yfull[valid] = y
     return yfull, loss, g

@@ -832,13 +832,15 @@ static bool shadow_has_no_effect(const luz_light& lt, v3 p, v3 N, v3 L) {
 template <typename T>
 static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl, const std::vector<uint32_t>& first_slot,
                         const Planes& P, uint32_t W, uint32_t H, uint32_t words, uint32_t ao_n, uint32_t pix,
-                        T out[4], const std::vector<T>& lut) {
+                        T out[4], const std::vector<T>& lut, T* split = nullptr) {
     const T pi = std::is_same<T, float>::value ? (T)PI_F : (T)3.14159265359;
     vec3<T> N = {(T)P.normal[4 * pix], (T)P.normal[4 * pix + 1], (T)P.normal[4 * pix + 2]};
     vec3<T> amb = {(T)S.ambient_light_color[0], (T)S.ambient_light_color[1], (T)S.ambient_light_color[2]};
     if (length(N) == T(0)) {   // light.frag:178-181
         vec3<T> c = amb * (T)S.ambient_light_intensity;
         out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = T(1);
+        if (split)
+            for (int k = 0; k < 8; ++k) split[k] = T(0);
         return;
     }
     uint32_t a8 = P.albedo[pix], m8 = P.material[pix], e8 = P.emission[pix];
@@ -862,6 +864,7 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
     vec3<T> V = normalize(cam - fragPos);                                                   // light.frag:187
     vec3<T> F0 = vec3<T>{(T)0.04f, (T)0.04f, (T)0.04f} * (T(1) - metallic) + albedo * metallic;   // 188-189
     vec3<T> Lo = {T(0), T(0), T(0)};
+    vec3<T> Lu = {T(0), T(0), T(0)};   // the same sum with every shadow factor 0 (for `split`)
     for (uint32_t i = 0; i < nl; ++i) {                                                    // light.frag:192
         const luz_light& lt = lights[i];
         vec3<T> L = light_vector<T>(lt, fragPos);                                           // light.frag:194-198
@@ -895,6 +898,7 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
         vec3<T> kD = (vec3<T>{T(1), T(1), T(1)} - F) * (T(1) - metallic);
         T NdotL = tmax_(dot(N, L), T(0));
         Lo = Lo + ((kD * albedo) / pi + spec) * radiance * NdotL;                           // light.frag:226
+        if (split) Lu = Lu + ((kD * albedo) / pi + spec) * ((color * (T)lt.intensity) * attenuation) * NdotL;
     }
     T ao;
     if (P.ao_override) ao = (T)P.ao_override[pix];
@@ -903,6 +907,13 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
         uint32_t misses = 0;
         for (uint32_t s = 0; s < ao_n; ++s) misses += (P.ao_bits[(size_t)s * words + (pix >> 5)] >> (pix & 31)) & 1u;
         ao = (T)misses / (T)ao_n;                                                            // light.frag:134
+    }
+    if (split) {   // S, AO, U, lum(S) / lum(U) (1 where lum(U) = 0, clamped to [0, 1])
+        const T ls = T(0.2126f) * Lo.x + T(0.7152f) * Lo.y + T(0.0722f) * Lo.z;
+        const T lu = T(0.2126f) * Lu.x + T(0.7152f) * Lu.y + T(0.0722f) * Lu.z;
+        split[0] = Lo.x; split[1] = Lo.y; split[2] = Lo.z; split[3] = ao;
+        split[4] = Lu.x; split[5] = Lu.y; split[6] = Lu.z;
+        split[7] = lu > T(0) ? std::min(std::max(ls / lu, T(0)), T(1)) : T(1);
     }
     vec3<T> ambient = (((amb * (T)S.ambient_light_intensity) * albedo) * occlusion) * ao;   // light.frag:232
     vec3<T> c = (ambient + Lo) + emission;                                                  // light.frag:233
@@ -1639,6 +1650,32 @@ static void light_pass_impl(const luz_scene* S, const luz_light* lights, uint32_
             if (outd) light_pixel<double>(*S, lights, nl, first, P, W, H, words, ao_n, pix, &outd[4 * (size_t)pix], lutd);
         }
     });
+}
+
+// The split of the direct light that feeds the denoiser, per pixel 8 values: S (r, g,
+// b), the AO value, U (r, g, b), lum(S) / lum(U); S is light.frag's shadowed sum over
+// the lights, U the same with every shadow factor 0. Background pixels get zeros.
+int oracle_light_split(const luz_scene* S, const luz_light* lights, uint32_t nl, const uint32_t* albedo,
+                       const float* normal, const uint32_t* material, const uint32_t* emission, const float* depth,
+                       const uint32_t* shadow_bits, const uint32_t* ao_bits, uint32_t W, uint32_t H, float* out8,
+                       int threads) {
+    uint32_t words = (W * H + 31) / 32;
+    std::vector<uint32_t> first(nl, 0);
+    uint32_t acc = 0;
+    for (uint32_t l = 0; l < nl; ++l) {
+        first[l] = acc;
+        acc += S->shadow_type == LUZ_SHADOW_RAYTRACING ? (uint32_t)std::max(0, lights[l].num_shadow_samples) : 0u;
+    }
+    std::vector<float> lutf(256);
+    for (int i = 0; i < 256; ++i) lutf[i] = (float)std::pow((double)((float)i / 255.0f), 2.2);
+    Planes P{albedo, normal, material, emission, depth, shadow_bits, ao_bits, nullptr};
+    uint32_t ao_n = (uint32_t)std::max(0, S->ao_num_samples);
+    parallel_for(W * H, threads, [&](uint32_t b, uint32_t e) {
+        float rgba[4];
+        for (uint32_t pix = b; pix < e; ++pix)
+            light_pixel<float>(*S, lights, nl, first, P, W, H, words, ao_n, pix, rgba, lutf, &out8[8 * (size_t)pix]);
+    });
+    return LUZ_OK;
 }
 
 int oracle_light_pass(const luz_scene* S, const luz_light* lights, uint32_t nl, const uint32_t* albedo,
