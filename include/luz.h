@@ -185,7 +185,7 @@ enum {
     LUZ_PLANE_TAA = 13,         /* RGBA32F temporal anti-aliasing output (= next history)  */
     LUZ_PLANE_COMPOSE = 14,     /* BGRA8 UNORM composed, tone-mapped output (bytes B,G,R,A) */
     LUZ_PLANE_SIGNAL = 15,      /* RGBA32F denoiser input: shadowed direct light S r, g, b, AO */
-    LUZ_PLANE_UNSHADOWED = 16,  /* RGBA32F unshadowed direct light U r, g, b, lum(S)/lum(U)    */
+    LUZ_PLANE_UNSHADOWED = 16,  /* RGBA32F unshadowed direct light U r, g, b, lit fraction     */
     LUZ_PLANE_DENOISED = 17,    /* RGBA32F denoiser output: shadow ratio R r, g, b, AO         */
     LUZ_PLANE_COUNT = 18
 };
@@ -520,7 +520,7 @@ luz_status luz_batch_autotune(luz_ctx* ctx, luz_batch* b, uint32_t reps, luz_vis
  * Its input is the split of the direct light (luz_denoise_features): per lit pixel the
  * shadowed sum S of light.frag's light loop (r, g, b) with the AO value
  * (LUZ_PLANE_SIGNAL), and the same sum U with every shadow factor 0 (r, g, b) with
- * lum(S) / lum(U) (LUZ_PLANE_UNSHADOWED). One predicted 7x7 kernel w filters both
+ * the unoccluded fraction of all the pixel's shadow samples (LUZ_PLANE_UNSHADOWED). One predicted 7x7 kernel w filters both
  * terms: AO' = sum(w AO) / sum(w), and per channel the ratio estimator
  * R = sum(w S) / sum(w U) (1 where sum(w U) = 0), so that neighbours count by their
  * unshadowed light. The frame is then ambient * AO' + U * R + emission
@@ -528,7 +528,7 @@ luz_status luz_batch_autotune(luz_ctx* ctx, luz_batch* b, uint32_t reps, luz_vis
  * stay unfiltered.
  *
  * Per pixel an MLP 72 -> 64 -> 64 -> 64 -> 49 (BF16 tensor cores, FP32 accumulation)
- * reads 8 channels over a 3x3 neighbourhood (noisy AO, lum(S) / lum(U), normal,
+ * reads 8 channels over a 3x3 neighbourhood (noisy AO, unoccluded shadow fraction, normal,
  * relative depth, roughness, albedo luminance) and predicts the softmax weights of the
  * 7x7 kernel. Parameters: LUZ_DENOISER_PARAMS FP32 values, row-major [out][in]
  * weights then biases per layer: W1[64][72] b1[64] W2[64][64] b2[64] W3[64][64]

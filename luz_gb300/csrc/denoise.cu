@@ -13,8 +13,8 @@
 // fixed order, writes one partial per CTA, and a second kernel sums the partials in
 // CTA order — the gradient is deterministic. Adam keeps FP32 master weights.
 //
-// Feature channels per pixel: 0 noisy AO, 1 noisy shadow ratio of the direct light's
-// luminance (lum(S) / lum(U)), 2-4 normal, 5 depth relative to the centre pixel
+// Feature channels per pixel: 0 noisy AO, 1 unoccluded fraction of the shadow
+// samples, 2-4 normal, 5 depth relative to the centre pixel
 // ((d_q - d_p)/d_p, clamped to [-1,1]), 6 roughness, 7 albedo luminance.
 #include <cuda_bf16.h>
 
@@ -81,8 +81,8 @@ struct FeatParams {
 
 __constant__ float c_lin_lut[256];   // pow(i/255, 2.2)
 
-// Channels 0 and 1 come from the split pass: the AO value and the shadow ratio of
-// the direct light's luminance, lum(S) / lum(U).
+// Channels 0 and 1 come from the split pass: the AO value and the unoccluded
+// fraction of all the pixel's shadow samples.
 __global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
     __shared__ uint32_t s_warp[8];
     __shared__ uint32_t s_base;
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(256) features_kernel(FeatParams F) {
     const uint32_t a8 = F.albedo[pix], m8 = F.material[pix];
     const float depth = F.depth[pix];
     const float ao = F.signal[pix].w;
-    const float shadow = F.unshadowed[pix].w;   // lum(S) / lum(U) of the split pass
+    const float shadow = F.unshadowed[pix].w;   // unoccluded shadow fraction of the split pass
     float lum = 0.2127f * c_lin_lut[a8 & 0xFF] + 0.7152f * c_lin_lut[(a8 >> 8) & 0xFF] +
                 0.0722f * c_lin_lut[(a8 >> 16) & 0xFF];
     float rough = (float)(m8 & 0xFF) / 255.0f;

@@ -184,7 +184,7 @@ struct luz_frame {
     float* ao_denoised = nullptr;
     bool shadow_cull = true;        // leave out shadow rays that cannot change the image
     float4* signal = nullptr;       // shadowed direct light S (r, g, b) and AO per pixel: denoiser input
-    float4* unshadowed = nullptr;   // unshadowed direct light U (r, g, b) and lum(S) / lum(U) per pixel
+    float4* unshadowed = nullptr;   // unshadowed direct light U (r, g, b) and lit shadow fraction per pixel
     float4* denoised = nullptr;     // filtered shadow ratio (r, g, b) and AO
     void* features = nullptr;       // 8 x bf16 per pixel (denoiser input)
     float* lin_depth = nullptr;

@@ -31,7 +31,7 @@ struct LightParams {
     const float* ao_denoised;
     const float4* denoised;      // kCompose: filtered (shadow ratio rgb, AO)
     float4* signal;              // kSplit: (S rgb, AO)
-    float4* unshadowed;          // kSplit: written (U rgb, lum(S) / lum(U)); kCompose: read
+    float4* unshadowed;          // kSplit: written (U rgb, lit shadow fraction); kCompose: read
     const luz_light* lights;
     const uint32_t* light_slot;
     uint32_t light_count;
@@ -72,11 +72,9 @@ __device__ __forceinline__ uint32_t bit_at(const uint32_t* __restrict__ planes, 
 // and AO from the bit planes. kDenoisedAo: the same with AO from the denoised plane.
 // kSplit (the denoiser's input pass): the direct light twice, shadowed as light.frag
 // sums it (S) and unshadowed (U, every shadow factor 0), written as (S, AO) and
-// (U, lum(S) / lum(U)); no light-plane write. kCompose: the frame from the filtered
+// (U, unoccluded fraction of the shadow samples); no light-plane write. kCompose: the frame from the filtered
 // shadow ratio R and AO: ambient * AO + U * R + emission.
 enum : int { kPlain = 0, kDenoisedAo = 1, kSplit = 2, kCompose = 3 };
-
-__device__ __forceinline__ float luminance(V3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
 
 template <int kMode>
 __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
@@ -107,6 +105,8 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
     V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + albedo * metallic;
     V3 Lo = V3{0.0f, 0.0f, 0.0f};
     V3 Lu = V3{0.0f, 0.0f, 0.0f};   // kSplit: unshadowed direct light
+    uint32_t hits_all = 0, slots_all = 0;   // kSplit: occluded shadow samples over all lights
+    float shadow_sum = 0.0f;                // kSplit: sum of the shadow factors (other shadow types)
     // per-pixel parts of the Cook-Torrance terms (light.frag:17-49, 210-229)
     const float a = roughness * roughness, a2 = a * a;
     const float r1 = roughness + 1.0f, k = (r1 * r1) / 8.0f;
@@ -130,10 +130,15 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
                 uint32_t hits = 0;
                 for (int s = 0; s < ns; ++s) hits += bit_at(P.shadow_bits, first + s, P.words, pix);
                 shadow = (float)hits / (float)ns;
+                if constexpr (kMode == kSplit) {
+                    hits_all += hits;
+                    slots_all += (uint32_t)ns;
+                }
             }
         } else if (P.shadow_type == LUZ_SHADOW_MAP && i < P.shadow_count && P.shadow_lights[i].faces) {
             shadow = shadow_map_factor(P.shadow_lights[i], p, shadow_origin);   // light.frag:147-164
         }
+        if constexpr (kMode == kSplit) shadow_sum += shadow;
         V3 color = V3{lt.color[0], lt.color[1], lt.color[2]};
         V3 radiance = ((color * lt.intensity) * attenuation) * (1.0f - shadow);
         V3 H = normalize(V + L);
@@ -166,10 +171,16 @@ __global__ void __launch_bounds__(256) light_pass_kernel(LightParams P) {
         ao = (float)misses / (float)P.ao_samples;
     }
     if constexpr (kMode == kSplit) {
-        const float lu = luminance(Lu);
-        const float ratio = lu > 0.0f ? fminf(fmaxf(luminance(Lo) / lu, 0.0f), 1.0f) : 1.0f;
+        // the denoiser's shadow feature: the unoccluded fraction of all shadow samples of
+        // the pixel (1 - hits / samples; with other shadow types 1 - the mean shadow factor)
+        float lit_fraction = 1.0f;
+        if (P.shadow_type == LUZ_SHADOW_RAYTRACING) {
+            if (slots_all) lit_fraction = 1.0f - (float)hits_all / (float)slots_all;
+        } else if (P.light_count) {
+            lit_fraction = 1.0f - shadow_sum / (float)P.light_count;
+        }
         P.signal[pix] = make_float4(Lo.x, Lo.y, Lo.z, ao);
-        P.unshadowed[pix] = make_float4(Lu.x, Lu.y, Lu.z, ratio);
+        P.unshadowed[pix] = make_float4(Lu.x, Lu.y, Lu.z, lit_fraction);
         return;
     }
     V3 ambient = (((amb * P.ambient_intensity) * albedo) * occlusion) * ao;

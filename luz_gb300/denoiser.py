@@ -2,9 +2,10 @@
 and RMSE.
 
 Pairs follow the training recipe of the path: scenes of the config-1 generator with
-seeded cameras (config 3), as 256x256 crops of 1920x1080 images; input = 1 AO sample
-and 1 shadow sample per light per pixel, target = the 1024-sample estimate of the
-same pixels (shadow ratio of the direct light and AO). Samples come from the
+seeded cameras (config 3), 256x256 (whole images by default; crops of 1920x1080
+images on request); input = 1 AO sample and 1 shadow sample per light per pixel,
+target = the 1024-sample estimate of the same pixels (shadow ratio of the direct
+light and AO). Samples come from the
 stratified sequence (LUZ_SAMPLER_STRATIFIED): the reference's float recurrence
 repeats values long before 1024 samples.
 
@@ -106,7 +107,7 @@ class Denoiser:
 
 class PairSet:
     """N images of W x H in device memory: features, distances, the noisy split of the
-    direct light (S r, g, b and AO; U r, g, b and lum(S) / lum(U)) and the many-sample
+    direct light (S r, g, b and AO; U r, g, b and the lit shadow fraction) and the many-sample
     target (shadow ratio r, g, b and AO)."""
 
     def __init__(self, n: int, width: int, height: int, device: int = 0):
@@ -218,7 +219,7 @@ def crop_camera(scene: HostScene, full=(1920, 1080), rng=None) -> None:
 
 
 def render_pairs(ctx: Context, n: int, size: int = 256, seed0: int = 20000, target_spp: int = 1024,
-                 per_trace: int = 32, crop_of=(1920, 1080), log=None) -> PairSet:
+                 per_trace: int = 32, crop_of=None, log=None) -> PairSet:
     """Renders n config-3 scenes (one BLAS set, a fresh TLAS per scene) as size x size
     crops of crop_of-sized images (None: whole size x size images): the 1-sample input
     (1 AO ray, 1 shadow ray per light) and the target_spp-sample target."""

@@ -3,8 +3,8 @@
     python -m luz_gb300.train_denoiser --scenes 2000 --size 256 --epochs 20 \
         --out luz_gb300/weights/denoiser_config3.bin
 
-Pairs: config-3 scenes (config-1 generator, seeded cameras) as 256x256 crops of
-1920x1080 images, 1-sample input (1 AO ray and 1 shadow ray per light) and the
+Pairs: config-3 scenes (config-1 generator, seeded cameras), 256x256 images (crops
+of 1920x1080 images with --crops), 1-sample input (1 AO ray and 1 shadow ray per light) and the
 1024-sample target (shadow ratio of the direct light and AO). Evaluation: a held-out
 config-3 scene at 1920x1080, AO and radiance RMSE against 1024 samples for the
 denoised single sample and the plain path (AO and shadow rays per light alike).
@@ -33,8 +33,8 @@ def main():
     ap.add_argument("--radiance-weights", action="store_true",
                     help="weight each pixel's shadow-ratio error by its squared unshadowed direct light "
                          "(relative to the set's RMS), so that it counts as the radiance error it causes")
-    ap.add_argument("--whole", action="store_true",
-                    help="train on whole size x size images instead of crops of 1920x1080 images")
+    ap.add_argument("--crops", action="store_true",
+                    help="train on size x size crops of 1920x1080 images instead of whole size x size images")
     ap.add_argument("--out", default=str(D.DEFAULT_WEIGHTS))
     ap.add_argument("--resume", default=None, help="checkpoint to start from")
     ap.add_argument("--no-eval", action="store_true")
@@ -45,7 +45,7 @@ def main():
     log = lambda m: print(m, flush=True)  # noqa: E731
     t0 = time.perf_counter()
     pairs = D.render_pairs(ctx, a.scenes, size=a.size, seed0=20000, target_spp=a.target_spp,
-                           crop_of=None if a.whole else (1920, 1080), log=log)
+                           crop_of=(1920, 1080) if a.crops else None, log=log)
     t_pairs = time.perf_counter() - t0
     den = D.Denoiser(ctx, seed=a.seed)
     if a.resume:
@@ -62,7 +62,7 @@ def main():
     px = steps * a.batch * a.size * a.size
     record = {"scenes": a.scenes, "size": a.size, "target_spp": a.target_spp, "epochs": a.epochs,
               "batch": a.batch, "lr": a.lr, "seed": a.seed, "shadow_weight": a.shadow_weight,
-              "radiance_weights": a.radiance_weights, "crops_of": None if a.whole else [1920, 1080],
+              "radiance_weights": a.radiance_weights, "crops_of": [1920, 1080] if a.crops else None,
               "loss_history": hist,
               "pair_generation_s": t_pairs, "train_s": t_train, "train_steps": steps,
               "train_pixels_per_s": px / t_train,

@@ -230,7 +230,8 @@ class OracleFrame:
 
     def light_split(self, nthreads=None) -> tuple[np.ndarray, np.ndarray]:
         """The denoiser's split of the direct light: (signal [H, W, 4] = shadowed direct
-        light S r, g, b and AO; unshadowed [H, W, 4] = U r, g, b and lum(S) / lum(U))."""
+        light S r, g, b and AO; unshadowed [H, W, 4] = U r, g, b and the unoccluded
+        fraction of all shadow samples)."""
         out = np.zeros((self.W * self.H, 8), np.float32)
         load().oracle_light_split(scene_bytes(self.scene), C.cast(self.lights, C.c_void_p), self.nl, _p(self.albedo),
                                   _p(self.normal), _p(self.material), _p(self.emission), _p(self.depth),

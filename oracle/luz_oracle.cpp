@@ -865,6 +865,8 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
     vec3<T> F0 = vec3<T>{(T)0.04f, (T)0.04f, (T)0.04f} * (T(1) - metallic) + albedo * metallic;   // 188-189
     vec3<T> Lo = {T(0), T(0), T(0)};
     vec3<T> Lu = {T(0), T(0), T(0)};   // the same sum with every shadow factor 0 (for `split`)
+    uint32_t hits_all = 0, slots_all = 0;   // occluded shadow samples over all lights (for `split`)
+    T shadow_sum = T(0);
     for (uint32_t i = 0; i < nl; ++i) {                                                    // light.frag:192
         const luz_light& lt = lights[i];
         vec3<T> L = light_vector<T>(lt, fragPos);                                           // light.frag:194-198
@@ -878,6 +880,8 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
                 for (int s = 0; s < ns; ++s)
                     hits += (P.shadow_bits[(size_t)(first_slot[i] + s) * words + (pix >> 5)] >> (pix & 31)) & 1u;
                 shadow = (T)hits / (T)ns;                                                    // light.frag:108
+                hits_all += hits;
+                slots_all += (uint32_t)ns;
             }
         } else if (S.shadow_type == LUZ_SHADOW_MAP && i < g_shadow.size() && g_shadow[i].faces) {   // 147-164
             v3 fp = {(float)fragPos.x, (float)fragPos.y, (float)fragPos.z};
@@ -886,6 +890,7 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
             v3 origin = fp + nf * fmax_(length(fp - camf) * 0.01f, 0.05f);
             shadow = (T)shadow_map_factor(g_shadow[i], fp, origin);
         }
+        shadow_sum += shadow;
         vec3<T> color = {(T)lt.color[0], (T)lt.color[1], (T)lt.color[2]};
         vec3<T> radiance = ((color * (T)lt.intensity) * attenuation) * (T(1) - shadow);    // light.frag:210
         vec3<T> Hh = normalize(V + L);
@@ -908,12 +913,15 @@ static void light_pixel(const luz_scene& S, const luz_light* lights, uint32_t nl
         for (uint32_t s = 0; s < ao_n; ++s) misses += (P.ao_bits[(size_t)s * words + (pix >> 5)] >> (pix & 31)) & 1u;
         ao = (T)misses / (T)ao_n;                                                            // light.frag:134
     }
-    if (split) {   // S, AO, U, lum(S) / lum(U) (1 where lum(U) = 0, clamped to [0, 1])
-        const T ls = T(0.2126f) * Lo.x + T(0.7152f) * Lo.y + T(0.0722f) * Lo.z;
-        const T lu = T(0.2126f) * Lu.x + T(0.7152f) * Lu.y + T(0.0722f) * Lu.z;
+    if (split) {   // S, AO, U, unoccluded fraction of all shadow samples
+        T lit_fraction = T(1);
+        if (S.shadow_type == LUZ_SHADOW_RAYTRACING) {
+            if (slots_all) lit_fraction = T(1) - (T)hits_all / (T)slots_all;
+        } else if (nl) {
+            lit_fraction = T(1) - shadow_sum / (T)nl;
+        }
         split[0] = Lo.x; split[1] = Lo.y; split[2] = Lo.z; split[3] = ao;
-        split[4] = Lu.x; split[5] = Lu.y; split[6] = Lu.z;
-        split[7] = lu > T(0) ? std::min(std::max(ls / lu, T(0)), T(1)) : T(1);
+        split[4] = Lu.x; split[5] = Lu.y; split[6] = Lu.z; split[7] = lit_fraction;
     }
     vec3<T> ambient = (((amb * (T)S.ambient_light_intensity) * albedo) * occlusion) * ao;   // light.frag:232
     vec3<T> c = (ambient + Lo) + emission;                                                  // light.frag:233
@@ -1653,8 +1661,9 @@ static void light_pass_impl(const luz_scene* S, const luz_light* lights, uint32_
 }
 
 // The split of the direct light that feeds the denoiser, per pixel 8 values: S (r, g,
-// b), the AO value, U (r, g, b), lum(S) / lum(U); S is light.frag's shadowed sum over
-// the lights, U the same with every shadow factor 0. Background pixels get zeros.
+// b), the AO value, U (r, g, b), the unoccluded fraction of all shadow samples; S is
+// light.frag's shadowed sum over the lights, U the same with every shadow factor 0.
+// Background pixels get zeros.
 int oracle_light_split(const luz_scene* S, const luz_light* lights, uint32_t nl, const uint32_t* albedo,
                        const float* normal, const uint32_t* material, const uint32_t* emission, const float* depth,
                        const uint32_t* shadow_bits, const uint32_t* ao_bits, uint32_t W, uint32_t H, float* out8,

@@ -141,8 +141,8 @@ def test_frame_path_over_lit_pixels_matches_dense_batch(size):
 
 def test_features_count_the_sample_bits():
     """The network inputs per lit pixel: the AO value is the mean of the AO miss bits over
-    all sample planes (40 here), the shadow feature lum(S) / lum(U) of the split pass,
-    both rounded to BF16; background pixels are zero."""
+    all sample planes (40 here), the shadow feature the unoccluded fraction of all shadow
+    samples, both rounded to BF16; background pixels are zero."""
     from oracle import denoiser as OD
     ctx = L.Context(0)
     try:
@@ -172,7 +172,9 @@ def test_features_count_the_sample_bits():
         assert np.array_equal(fr.read(L.PLANE_AO).reshape(-1), ao)
         assert np.array_equal(fr.read(L.PLANE_SIGNAL).reshape(-1, 4)[:, 3], ao)
         feat = fr.read(L.PLANE_FEATURES).reshape(-1, 8)
-        shadow = fr.read(L.PLANE_UNSHADOWED).reshape(-1, 4)[:, 3]     # lum(S) / lum(U)
+        sh_hits, _ = counts(L.PLANE_SHADOW_BITS)
+        shadow = np.float32(1) - sh_hits.astype(np.float32) / np.float32(n_sh)
+        assert np.array_equal(fr.read(L.PLANE_UNSHADOWED).reshape(-1, 4)[lit, 3], shadow[lit])
         assert np.array_equal(OD.bf16_bits_to_f32(feat[lit, 0]), OD.bf16_round(ao[lit]))
         assert np.array_equal(OD.bf16_bits_to_f32(feat[lit, 1]), OD.bf16_round(shadow[lit]))
         assert np.all(feat[~lit] == 0)
@@ -207,9 +209,9 @@ def test_frame_with_nothing_lit_denoises_to_zero():
 
 def test_split_of_the_direct_light_matches_oracle():
     """The denoiser's input pass: per lit pixel light.frag's direct light S (shadowed)
-    and U (every shadow factor 0), the AO value and lum(S) / lum(U), against the
-    oracle's restatement on the same frame (bit-exact visibility). S and U within 1e-4
-    relative, as the radiance; the luminance ratio within 3e-4."""
+    and U (every shadow factor 0), the AO value and the unoccluded fraction of the
+    shadow samples, against the oracle's restatement on the same frame (bit-exact
+    visibility). S and U within 1e-4 relative, as the radiance; the counts exact."""
     from tests.pathutil import oracle_frame, oracle_scene
     ctx = L.Context(0)
     try:
@@ -230,7 +232,7 @@ def test_split_of_the_direct_light_matches_oracle():
         for a, b in ((u[..., :3], o_u[..., :3]), (sig[..., :3], o_sig[..., :3])):
             rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-6)
             assert rel[lit].max() <= 1e-4, rel[lit].max()
-        assert np.abs(u[..., 3] - o_u[..., 3])[lit].max() <= 3e-4
+        assert np.array_equal(u[..., 3][lit], o_u[..., 3][lit])
         assert np.array_equal(sig[..., 3][lit], o_sig[..., 3][lit])          # AO = misses / samples
         ratio = u[..., 3][lit]
         assert (ratio < 1).any() and (ratio == 1).any()                        # shadowed and lit pixels
