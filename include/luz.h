@@ -194,11 +194,19 @@ enum {
 luz_status luz_ctx_create(int device, luz_ctx** out);
 void luz_ctx_destroy(luz_ctx* ctx);
 const char* luz_last_error(const luz_ctx* ctx);
+/* Waits for the context's stream; LUZ_ERR_DEVICE when a kernel has raised the device
+ * status word since it was last read (luz_ctx_device_status reads and clears it). */
 luz_status luz_ctx_synchronize(luz_ctx* ctx);
 /* Reads and clears the device status word (LUZ_DEV_* bits). */
 luz_status luz_ctx_device_status(luz_ctx* ctx, uint32_t* bits);
 /* Number of kernels this context has launched so far. */
 uint64_t luz_ctx_launch_count(const luz_ctx* ctx);
+/* Debug knob, off by default (no counterpart in the reference): the traversal steps a
+ * shadow / AO ray may take before the visibility kernel ends it (counted as not
+ * occluded, AO: a miss) and raises LUZ_DEV_TRAVERSAL_CAP; 0 restores the library's cap
+ * (2^22 steps). For testing that a cap which runs out ends the kernel with a status
+ * instead of a hang. */
+luz_status luz_ctx_set_debug_step_cap(luz_ctx* ctx, uint32_t steps);
 /* Uses `stream` (a cudaStream_t) for all later work; NULL = the context's own. */
 luz_status luz_ctx_set_stream(luz_ctx* ctx, void* stream);
 /* Uploads the substitute blue-noise texture (RGBA8, size*size texels). */

@@ -550,6 +550,11 @@ class Context:
         _check(lib.luz_ctx_probe_l2_read(self._h, nbytes, reps, C.byref(g)), self._h, "L2 probe")
         return g.value
 
+    def set_debug_step_cap(self, steps: int) -> None:
+        """Debug: traversal steps per shadow / AO ray before it is ended with
+        LUZ_DEV_TRAVERSAL_CAP raised; 0 restores the library's cap."""
+        _check(lib.luz_ctx_set_debug_step_cap(self._h, steps), self._h, "debug step cap")
+
     def set_stream_default(self) -> None:
         """Back to the context's own stream."""
         _check(lib.luz_ctx_set_stream(self._h, None), self._h, "set stream")

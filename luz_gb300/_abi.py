@@ -149,6 +149,7 @@ SIGNATURES = [
     ("luz_ctx_device_status", C.c_int32, [P, c_u32_p]),
     ("luz_ctx_launch_count", C.c_uint64, [P]),
     ("luz_ctx_set_stream", C.c_int32, [P, P]),
+    ("luz_ctx_set_debug_step_cap", C.c_int32, [P, C.c_uint32]),
     ("luz_ctx_set_blue_noise", C.c_int32, [P, c_u8_p, C.c_uint32]),
     ("luz_ctx_set_vis_tuning", C.c_int32, [P, C.POINTER(C.c_uint32 * 4)]),
     ("luz_ctx_get_vis_tuning", C.c_int32, [P, C.POINTER(C.c_uint32 * 4)]),

@@ -2,6 +2,7 @@
 // handles, frames, uploads and read-back.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 
@@ -239,6 +240,19 @@ const char* luz_last_error(const luz_ctx* ctx) { return ctx ? ctx->last_error.c_
 luz_status luz_ctx_synchronize(luz_ctx* ctx) {
     if (!ctx) return LUZ_ERR_INVALID;
     LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t bits = 0;
+    LUZ_CUDA(ctx, cudaMemcpy(&bits, ctx->d_status, 4, cudaMemcpyDeviceToHost));
+    if (bits) {
+        char msg[96];
+        snprintf(msg, sizeof(msg), "a kernel raised the device status word (LUZ_DEV_* bits 0x%x)", bits);
+        return set_error(ctx, LUZ_ERR_DEVICE, msg);
+    }
+    return LUZ_OK;
+}
+
+luz_status luz_ctx_set_debug_step_cap(luz_ctx* ctx, uint32_t steps) {
+    if (!ctx) return LUZ_ERR_INVALID;
+    ctx->debug_step_cap = steps;
     return LUZ_OK;
 }
 

@@ -120,6 +120,7 @@ struct luz_ctx {
     size_t pinned_bytes = 0;
     int sm_count = 0;
     luz::VisTuning vis_tuning{0, 0, 0, 0, 0};   // set == 0: library defaults
+    uint32_t debug_step_cap = 0;                // traversal steps per ray, 0 = the library's cap
     // device pipeline of the last batched BLAS build (after its host->device copies)
     cudaEvent_t build_ev[2] = {nullptr, nullptr};
     bool build_timed = false;

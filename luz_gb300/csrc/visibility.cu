@@ -210,13 +210,15 @@ __device__ __forceinline__ float4 node_load(const float4* p) {
 // Up to `steps` traversal steps of one lane's ray; clears `active` when it ends.
 // tlas / insts: the scene's TLAS nodes and instances (kernel parameters in the
 // single-scene kernel, the lane's own scene in the batched one). The step cap of a
-// ray is charged `steps` per call, so a ray ends after at most kRayStepCap + steps.
+// ray (kRayStepCap unless a debug cap is set) is charged `steps` per call, so a ray
+// ends after at most step_cap + steps; a ray that reaches it ends unoccluded (shadow)
+// or as a miss (AO) and raises LUZ_DEV_TRAVERSAL_CAP.
 template <bool kStats, bool kStaged>
 __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& active, const float4* smem_tlas,
                                           uint32_t staged, const float4* tlas, const DevInstance* insts,
-                                          uint32_t* s_stack, int* lstack, uint32_t steps, uint32_t& err,
-                                          TraceCounters& cnt) {
-    if (active && (r.budget += steps) > kRayStepCap) {
+                                          uint32_t* s_stack, int* lstack, uint32_t steps, uint32_t step_cap,
+                                          uint32_t& err, TraceCounters& cnt) {
+    if (active && (r.budget += steps) > step_cap) {
         err |= LUZ_DEV_TRAVERSAL_CAP;
         finish_ray(c, active, false);
     }
@@ -452,7 +454,8 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
             }
         }
         if (exhausted && __ballot_sync(full, active) == 0) break;
-        run_steps<kStats, kStaged>(r, c, active, smem, staged, S.tlas_nodes, S.instances, s_stack, lstack, C.steps, err,
+        run_steps<kStats, kStaged>(r, c, active, smem, staged, S.tlas_nodes, S.instances, s_stack, lstack, C.steps,
+                                   C.step_cap, err,
                                    cnt);
     }
     if (err) atomicOr(C.status, err);
@@ -504,7 +507,8 @@ visibility_batch_kernel(const SceneVis* __restrict__ scenes, uint32_t n, const u
             }
         }
         if (exhausted && __ballot_sync(full, active) == 0) break;
-        run_steps<kStats, false>(r, c, active, nullptr, 0u, r.tlas, r.insts, s_stack, lstack, C.steps, err, cnt);
+        run_steps<kStats, false>(r, c, active, nullptr, 0u, r.tlas, r.insts, s_stack, lstack, C.steps, C.step_cap, err,
+                                 cnt);
     }
     if (err) atomicOr(C.status, err);
     if (kStats) flush_stats(stats, rays, cnt);
@@ -567,6 +571,7 @@ VisCommon make_vis_common(luz_ctx* ctx, unsigned long long* work_counter) {
     C.refill = tu.refill;
     C.steps = tu.steps;
     C.smem_nodes = tu.smem_nodes;
+    C.step_cap = ctx->debug_step_cap ? ctx->debug_step_cap : kRayStepCap;
     return C;
 }
 

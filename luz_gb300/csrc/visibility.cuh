@@ -30,6 +30,7 @@ struct VisCommon {
     unsigned long long* work_counter;
     uint32_t* status;
     uint32_t refill, steps, smem_nodes;
+    uint32_t step_cap;        // traversal steps per ray before it is ended (LUZ_DEV_TRAVERSAL_CAP)
 };
 
 // The context's visibility launch shape (the library defaults until one is set).
