@@ -89,7 +89,7 @@ def load_ref():
     f = lib.ref_light_pass
     f.restype = C.c_int
     f.argtypes = [P, P, C.c_int, P, P, P, P, P, P, C.c_int, C.c_int, C.c_int, C.c_int, P, P, P, P, C.c_uint64,
-                  C.POINTER(C.c_uint64)]
+                  C.POINTER(C.c_uint64), P, P, C.c_int, C.c_int]
     return lib
 
 

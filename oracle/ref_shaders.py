@@ -192,11 +192,33 @@ extern "C" int ref_light_pass(const luz_scene* S, const luz_light* L, int nl, co
                               const float* normal, const uint32_t* material, const uint32_t* emission,
                               const float* depth, const uint8_t* bn, int bn_size, int W, int H, int frame,
                               refshim::AnyHitFn fn, const void* user, float* out, float* ray_log,
-                              uint64_t ray_log_cap, uint64_t* ray_count) {
+                              uint64_t ray_log_cap, uint64_t* ray_count, const luz_shadow_light* sl,
+                              const float* maps, int sl_count, int map_res) {
     if (nl < 0 || nl > LUZ_MAX_LIGHTS) return 1;
     SceneBlock& sb = g_scene;
     memset(&sb, 0, sizeof(sb));
     for (int i = 0; i < nl; ++i) memcpy(&sb.lights[i], &L[i], sizeof(luz_light));   // head of LightBlock
+    // Shadow maps (scene shadow type MAP): the LightBlock tail (viewProj, zFar) and the
+    // map as a cube texture (point lights) or a 2D texture read through the bilinear,
+    // repeat-addressed sampler; maps of the lights are concatenated in light order.
+    for (int i = 0; i < nl; ++i) {
+        sb.lights[i].shadowMap = -1;
+        cubeTextures[i] = samplerCube{};
+    }
+    const float* m = maps;
+    for (int i = 0; sl && maps && i < sl_count && i < nl; ++i) {
+        if (!sl[i].faces) continue;
+        for (int f = 0; f < 6; ++f) memcpy(&sb.lights[i].viewProj[f], sl[i].view_proj[f], 64);
+        sb.lights[i].zFar = sl[i].z_far;
+        if (sl[i].faces == 6) {
+            cubeTextures[i] = samplerCube{m, map_res};
+            sb.lights[i].shadowMap = i;
+        } else {
+            textures[8 + i] = {m, map_res, map_res, 2, 1};
+            sb.lights[i].shadowMap = 8 + i;
+        }
+        m += (size_t)sl[i].faces * map_res * map_res;
+    }
     memcpy((char*)&sb + sizeof(LightBlock) * LUZ_MAX_LIGHTS, S, sizeof(luz_scene));
     sb.numLights = nl;
     sb.blueNoiseTexture = 5;
@@ -245,8 +267,8 @@ def main():
         '#include "luz.h"',
         "namespace refshim { Env g_env; }",
         "SceneBlock g_scene;",
-        "sampler2D textures[8];",
-        "samplerCube cubeTextures[1];",
+        "sampler2D textures[8 + LUZ_MAX_LIGHTS];",
+        "samplerCube cubeTextures[LUZ_MAX_LIGHTS];",
         "LightConstants ctx;",
         "vec2 fragTexCoord;",
         "vec4 outColor;",

@@ -39,7 +39,11 @@ struct sampler2D {
     const void* data = nullptr;
     int w = 1, h = 1, kind = 0, filter = 0;
 };
-struct samplerCube {};
+// A cube shadow map: six R32F faces of res x res texels (+x, -x, +y, -y, +z, -z).
+struct samplerCube {
+    const float* faces = nullptr;
+    int res = 1;
+};
 
 inline vec4 fetch(const sampler2D& s, int x, int y) {
     x = x < 0 ? 0 : (x >= s.w ? s.w - 1 : x);
@@ -113,7 +117,42 @@ inline void imageStore(image2D& im, ivec2 p, vec4 v) {
     float* o = im.data + 4 * ((size_t)p.y * im.w + p.x);
     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
 }
-inline vec4 texture(const samplerCube&, vec3) { return vec4(0.0f); }
+// Cube-map lookup for the shadow maps: the face of the major axis of the direction
+// (ties to x, then y) with the face coordinates of Vulkan's cube-face table, then
+// bilinear filtering clamped to the face's edges (the reference's sampler is linear;
+// edge texels are not blended across faces here).
+inline vec4 texture(const samplerCube& s, vec3 d) {
+    if (!s.faces) return vec4(0.0f);
+    const float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+    int face;
+    float ma, sc, tc;
+    if (ax >= ay && ax >= az) {
+        face = d.x >= 0.0f ? 0 : 1; ma = ax; sc = d.x >= 0.0f ? -d.z : d.z; tc = -d.y;
+    } else if (ay >= az) {
+        face = d.y >= 0.0f ? 2 : 3; ma = ay; sc = d.x; tc = d.y >= 0.0f ? d.z : -d.z;
+    } else {
+        face = d.z >= 0.0f ? 4 : 5; ma = az; sc = d.z >= 0.0f ? d.x : -d.x; tc = -d.y;
+    }
+    float u = 0.5f, v = 0.5f;
+    if (ma != 0.0f) {
+        u = 0.5f * (sc / ma + 1.0f);
+        v = 0.5f * (tc / ma + 1.0f);
+    } else {
+        face = 0;
+    }
+    const int n = s.res;
+    const float* f = s.faces + (size_t)face * n * n;
+    float x = u * (float)n - 0.5f, y = v * (float)n - 0.5f;
+    if (!std::isfinite(x)) x = 0.0f;
+    if (!std::isfinite(y)) y = 0.0f;
+    const float fx = std::floor(x), fy = std::floor(y);
+    const float wx = x - fx, wy = y - fy;
+    auto clampi = [n](float c) { return c <= 0.0f ? 0 : (c >= (float)(n - 1) ? n - 1 : (int)c); };
+    const int x0 = clampi(fx), x1 = clampi(fx + 1.0f), y0 = clampi(fy), y1 = clampi(fy + 1.0f);
+    const float c00 = f[(size_t)y0 * n + x0], c10 = f[(size_t)y0 * n + x1];
+    const float c01 = f[(size_t)y1 * n + x0], c11 = f[(size_t)y1 * n + x1];
+    return vec4((c00 * (1.0f - wx) + c10 * wx) * (1.0f - wy) + (c01 * (1.0f - wx) + c11 * wx) * wy, 0.0f, 0.0f, 1.0f);
+}
 inline ivec2 textureSize(const sampler2D& s, int) { return ivec2(s.w, s.h); }
 inline vec4 texelFetch(const sampler2D& s, ivec2 p, int) { return refshim::fetch(s, p.x, p.y); }
 

@@ -23,17 +23,21 @@ REF = O.load_ref()
 pytestmark = pytest.mark.skipif(REF is None, reason="oracle/_ref not built (reference tree absent)")
 
 
-def _run_ref(s, f, bn, frame=0, log_cap=0):
+def _run_ref(s, f, bn, frame=0, log_cap=0, shadow=None):
+    """shadow: (luz_shadow_light array, [maps], resolution) for a shadow-map scene."""
     lib = O.load()
     W, H = s.width, s.height
     out = np.zeros((H, W, 4), np.float32)
     log = np.zeros((max(log_cap, 1), 8), np.float32)
     cnt = C.c_uint64()
     fn = C.cast(lib.oracle_trace_ray, C.c_void_p)
+    sl, maps, res = shadow if shadow else (None, None, 0)
+    flat = np.ascontiguousarray(np.concatenate([m.reshape(-1) for m in maps])) if maps else None
     st = REF.ref_light_pass(C.byref(f.scene), C.cast(f.lights, C.c_void_p), f.nl, O._p(f.albedo),
                             O._p(f.normal), O._p(f.material), O._p(f.emission), O._p(f.depth), O._p(bn),
                             bn.shape[0], W, H, frame, fn, f.tlas.handle, O._p(out), O._p(log), log_cap,
-                            C.byref(cnt))
+                            C.byref(cnt), C.cast(sl, C.c_void_p) if sl is not None else None, O._p(flat),
+                            len(sl) if sl is not None else 0, res)
     assert st == 0
     return out, log[: min(cnt.value, log_cap)], cnt.value
 
@@ -68,6 +72,34 @@ def test_reference_light_pass_matches_oracle():
     # a handful of pixels may see a grazing ray flip between hit and miss
     assert close.mean() > 0.995, close.mean()
     assert np.median(rel[..., :3]) < 1e-6
+
+
+def test_reference_shadow_map_lookups_match_oracle():
+    """light.frag:147-165 from the reference's code: the point lights' cube-map test
+    (distance - 0.05 against depth x zFar) and the directional light's 2D map test
+    (NDC depth of the biased origin through viewProj[0]), over the oracle's rasterised
+    maps, against the oracle's light pass with the same maps. The cube texture
+    lookup (face selection, bilinear within a face) is the shim's, the rest is the
+    reference's."""
+    s = L.HostScene(1, width=96, height=96)
+    s.set_shadow_type(L._abi.SHADOW_MAP)
+    _, tl = oracle_scene(s)
+    lights = s.shadow_lights()
+    res = 256
+    maps = O.render_shadow_maps(tl, lights, res)
+    try:
+        f = oracle_frame(s, tl)
+        ref, _, _ = _run_ref(s, f, L.blue_noise(), shadow=(lights, maps, res))   # only AO rays are traced
+        mine = f.light_pass()
+        rel = np.abs(ref - mine) / np.maximum(np.abs(mine), 1e-6)
+        close = (rel[..., :3] <= 1e-4).all(axis=-1)
+        assert close.mean() > 0.995, close.mean()
+        # the maps shadow some pixels: the frame differs from the one without maps
+        O.clear_shadow_maps()
+        unshadowed = f.light_pass()
+        assert (np.abs(unshadowed - mine)[..., :3].max(axis=-1) > 1e-3).mean() > 0.01
+    finally:
+        O.clear_shadow_maps()
 
 
 # ---------------------------------------------------------------- post-processing passes
