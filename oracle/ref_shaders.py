@@ -2,6 +2,7 @@
 """Recipe: compile the reference's own light-pass shader code for the CPU.
 
 Reads source/Shaders/light.frag and source/Shaders/utils.glsl from the reference tree
+(and taa.comp, present.frag, histogram.comp, histogramAverage.comp for the post passes)
 (where they lie; nothing is copied into the repository), keeps the functions of the
 ray-traced light pass (main, EvaluateShadow, TraceShadowRay, TraceAORays,
 BlueNoiseSample, DiskSample, HemisphereSample, the GGX terms, DepthToWorld), rewrites
@@ -30,6 +31,8 @@ TAA_UTIL_FUNCS = ["DepthToWorld", "MitchellFilter", "rcp", "Luminance"]
 TAA_FUNCS = ["get_uv", "get_motion_vector", "get_neighbor_3x3", "find_closest_3x3", "clip_aabb", "anti_flicker",
              "main"]
 COMPOSE_FUNCS = ["LinearizeDepth", "Tonemap", "TonemapACES", "TonemapExposure", "main"]
+HIST_UTIL_FUNCS = ["Luminance"]
+HIST_FUNCS = ["HDRToHistogramBin"]
 
 
 def extract(src: str, name: str) -> str:
@@ -172,6 +175,59 @@ extern "C" void ref_compose(const float* light, const uint32_t* albedo, const fl
 }
 """
 
+HIST_HEAD = """// Generated by oracle/ref_shaders.py from the reference's histogram.comp,
+// histogramAverage.comp and utils.glsl.
+#include <cstddef>
+#include "ref_shim.hpp"
+#include "luz.h"
+static PostProcessingConstants h_ctx;
+struct HistFloatBuffer { float* data; };
+static HistFloatBuffer h_floatBuffers[2];
+static float HistogramShared[LUZ_HISTOGRAM_BINS];
+#define ctx h_ctx
+#define floatBuffers h_floatBuffers
+"""
+
+HIST_WRAPPER = r"""
+#undef ctx
+#undef floatBuffers
+// DeferredRenderer.cpp:447-466: histogramMinLog -10, histogramOneOverLog 1/12.
+static void hist_constants(float width, float height, float delta_time) {
+    memset(&h_ctx, 0, sizeof(h_ctx));
+    h_ctx.size = vec2(width, height);
+    h_ctx.deltaTime = delta_time;
+    h_ctx.histogramMinLog = -10.0f;
+    h_ctx.histogramOneOverLog = 1.0f / 12.0f;
+    h_ctx.histogramRID = 0;
+    h_ctx.histogramAverageRID = 1;
+}
+
+// The bin of every pixel of an RGBA32F image (histogram.comp's HDRToHistogramBin).
+extern "C" void ref_histogram_bins(const float* rgba, int n, uint32_t* bins) {
+    hist_constants((float)n, 1.0f, 0.0f);
+    for (int i = 0; i < n; ++i) bins[i] = HDRToHistogramBin(vec3(rgba[4 * i], rgba[4 * i + 1], rgba[4 * i + 2]));
+}
+
+// histogramAverage.comp's one workgroup of 256 threads over the bin counts, run phase
+// by phase between its barriers: each thread's count x bin index, the halving tree
+// sum, then thread 0's block. out: the weighted sum, weightedLogAverage,
+// weightedAverageLuminance, adaptedLuminance and the value the shader stores in the
+// average buffer.
+extern "C" void ref_histogram_average(const uint32_t* counts, int width, int height, float delta_time,
+                                      float last_luminance, float* out) {
+    hist_constants((float)width, (float)height, delta_time);
+    float bins[LUZ_HISTOGRAM_BINS * 4] = {}, average[4] = {last_luminance, 0.0f, 0.0f, 0.0f};
+    for (int i = 0; i < LUZ_HISTOGRAM_BINS; ++i) bins[i * 4] = (float)counts[i];
+    h_floatBuffers[0].data = bins;
+    h_floatBuffers[1].data = average;
+    for (uint32_t g = 0; g < LUZ_HISTOGRAM_BINS; ++g) hist_avg_init(g);
+    for (uint32_t k = (LUZ_HISTOGRAM_BINS >> 1); k > 0; k >>= 1)
+        for (uint32_t g = 0; g < LUZ_HISTOGRAM_BINS; ++g) hist_avg_step(g, k);
+    hist_average_final(bins[0], out);
+    out[4] = average[0];
+}
+"""
+
 WRAPPER = r"""
 #undef scene
 #undef tlas
@@ -293,6 +349,36 @@ def main():
     cbody = swizzles(float_literals(cbody))
     (out / "ref_compose.cpp").write_text(COMPOSE_HEAD + "namespace {\n" + cbody + "\n}  // namespace\n" +
                                          COMPOSE_WRAPPER)
+
+    # histogram.comp's bin function and histogramAverage.comp's phases
+    hist = (ref / "histogram.comp").read_text()
+    havg = (ref / "histogramAverage.comp").read_text()
+    hbody = "\n\n".join([extract(utils, f) for f in HIST_UTIL_FUNCS] + [extract(hist, f) for f in HIST_FUNCS])
+    amain = extract(havg, "main")
+    init = re.search(r"float countForThisBin = (.*?);\s*HistogramShared\[groupIndex\] = (.*?);", amain, re.S)
+    step = re.search(r"if \(groupIndex < histogramSampleIndex\) \{\s*(.*?;)\s*\}", amain, re.S)
+    blk = re.search(r"if \(groupIndex == 0\) \{", amain)
+    if not (init and step and blk):
+        raise SystemExit("histogramAverage.comp: unexpected main")
+    i = amain.index("{", blk.start())
+    depth, j = 0, i
+    for j in range(i, len(amain)):
+        depth += {"{": 1, "}": -1}.get(amain[j], 0)
+        if depth == 0:
+            break
+    final = amain[i + 1:j]
+    phases = "\n".join([
+        "void hist_avg_init(uint groupIndex) { float countForThisBin = " + init.group(1) +
+        "; HistogramShared[groupIndex] = " + init.group(2) + "; }",
+        "void hist_avg_step(uint groupIndex, uint histogramSampleIndex) { if (groupIndex < histogramSampleIndex) { " +
+        step.group(1) + " } }",
+        "void hist_average_final(float countForThisBin, float* out) {" + final +
+        "\n    out[0] = HistogramShared[0]; out[1] = weightedLogAverage; out[2] = weightedAverageLuminance;"
+        " out[3] = adaptedLuminance;\n}",
+    ])
+    hsrc = swizzles(float_literals(hbody + "\n\n" + phases))
+    (out / "ref_histogram.cpp").write_text(HIST_HEAD + "namespace {\n" + hsrc + "\n}  // namespace\n" +
+                                           HIST_WRAPPER)
 
 
 if __name__ == "__main__":

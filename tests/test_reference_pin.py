@@ -159,3 +159,37 @@ def test_compose_matches_reference_shader():
         q = (np.clip(np.nan_to_num(ref, nan=0.0), 0, 1) * 255 + 0.5).astype(np.uint32)
         words = q[..., 2] | (q[..., 1] << 8) | (q[..., 0] << 16) | (255 << 24)
         assert np.array_equal(words, ours), t
+
+
+def test_histogram_matches_reference_shaders():
+    """histogram.comp and histogramAverage.comp from the reference tree. The bin of every
+    pixel comes from the shader's HDRToHistogramBin: the oracle's counts equal the
+    count of the reference's bins, bin for bin. histogramAverage.comp's workgroup runs
+    phase by phase over those counts: its weighted sum, log average, average and adapted
+    luminance equal the oracle's. Two deliberate deviations are checked as such: the
+    shader stores the weighted bin sum where the next frame reads its adapted luminance
+    (here the adapted luminance is carried), and every workgroup of histogram.comp
+    zeroes the global bins before adding its own (here the bins are exact counts)."""
+    lib = REF
+    lib.ref_histogram_bins.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+    lib.ref_histogram_average.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_void_p]
+    rng = np.random.default_rng(3)
+    H, W = 48, 64
+    img = np.zeros((H, W, 4), np.float32)
+    img[..., :3] = np.exp2(rng.uniform(-14.0, 5.0, size=(H, W, 3))).astype(np.float32)
+    img[:2] = 0.0                                   # below LUZ_EPS: bin 0
+    img[2, :8, :3] = 1e30                           # clamped to the top bin
+    ref_bins = np.zeros(H * W, np.uint32)
+    lib.ref_histogram_bins(O._p(img), H * W, O._p(ref_bins))
+    counts = np.bincount(ref_bins, minlength=256).astype(np.uint32)
+    state = np.array([0.37], np.float32)
+    want, _ = O.histogram(img, 1.0 / 60.0, state.copy())
+    assert np.array_equal(want["bins"], counts)
+    assert counts[0] >= 2 * W and counts[255] >= 8
+    out = np.zeros(5, np.float32)
+    lib.ref_histogram_average(O._p(counts), W, H, C.c_float(1.0 / 60.0), C.c_float(state[0]), O._p(out))
+    assert out[0] == np.float32(want["weighted_sum"])
+    assert out[1] == np.float32(want["log_average"])
+    assert np.isclose(out[2], want["average_luminance"], rtol=1e-6)
+    assert np.isclose(out[3], want["adapted_luminance"], rtol=1e-6)
+    assert out[4] == out[0] and out[4] != np.float32(want["adapted_luminance"])   # what the shader stores
