@@ -329,6 +329,44 @@ def denoised_vs_plain(g, ctx, stream, flush, K, W, restore_ao=16, curve_spp=(1, 
             "sampler": "stratified (8x8-block R2)", "weights": D.DEFAULT_WEIGHTS.name}
 
 
+# ---------------------------------------------------------------------------- denoiser training
+def denoiser_training(ctx, stream, steps=20, scenes=32):
+    """Training throughput of the denoiser: Adam steps on batches of 16 config-3 pairs at
+    256x256 (1-sample input, 64-sample target: the target count does not change the
+    step's work). Per step the tcgen05 forward + backward + weight-gradient kernel, the
+    partial sum, Adam and the BF16 repack; the kernel's own time from the event pairs
+    around its launches."""
+    import torch
+
+    from luz_gb300 import denoiser as D
+
+    pairs = D.render_pairs(ctx, scenes, size=256, target_spp=64, per_trace=32)
+    ctx.set_stream(stream.cuda_stream)      # render_pairs ran on a stream of its own
+    torch.cuda.set_stream(stream)
+    den = D.Denoiser(ctx, seed=2)
+    batch = 16
+    for w in range(3):
+        den.train_step(pairs.batch((w * batch) % (scenes - batch + 1), batch), 1e-3)
+    torch.cuda.synchronize()
+    ctx.profile(True)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        den.train_step(pairs.batch((k * batch) % (scenes - batch + 1), batch), 1e-3)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / steps
+    kern, n = ctx.profile_read("denoise_train")
+    ctx.profile(False)
+    px = batch * 256 * 256
+    flop = 3.0 * 2.0 * (72 * 64 + 64 * 64 + 64 * 64 + 64 * 49) * px    # forward + backward (dX and dW)
+    kms = kern / max(n, 1)
+    den.close()
+    return {"pixels_per_step": px, "ms_per_step": wall * 1e3, "kernel_ms_per_step": kms,
+            "kernel_tflops_bf16": flop / (kms * 1e-3) / 1e12, "step_tflops_bf16": flop / wall / 1e12,
+            "kernel": "denoise_train_tc_kernel (tcgen05, TMEM accumulators)",
+            "note": "FLOP = 3 x forward (forward, dX, dW); the step also runs the partial sum, Adam, the repack "
+                    "and a 4-byte loss read-back"}
+
+
 # ---------------------------------------------------------------------------- post passes
 def post_passes(g, stream, flush, K, W):
     """TAA (taa.comp), compose / ACES (present.frag) and the luminance histogram on the
@@ -650,6 +688,12 @@ def run_ours(args, rank, world, local):
         if ctx.device_status() != 0:
             raise RuntimeError("device status word raised during the denoised comparison")
 
+    training = None
+    if not args.no_denoise:
+        training = denoiser_training(ctx, stream)
+        if ctx.device_status() != 0:
+            raise RuntimeError("device status word raised during denoiser training")
+
     batched = None
     if not args.no_batch:
         saved = ctx.vis_tuning()
@@ -689,7 +733,8 @@ def run_ours(args, rank, world, local):
                                        "device_ms is the device pipeline after them (CUDA events)"},
                 "gpu_launches": launches, "roofline": roofline, "light_pass_roofline": light_pass,
                 "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk, "denoised_vs_plain": denoised, "batched_uneven_64": batched,
+                "clocks": clk, "denoised_vs_plain": denoised, "denoiser_training": training,
+                "batched_uneven_64": batched,
                 "stress_4k_4096_instances": stress, "post_passes_1080p": post}
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -247,7 +247,8 @@ enum {
     LUZ_KERNEL_LIGHT_PASS = 4,  /* deferred light pass (every mode)                  */
     LUZ_KERNEL_FEATURES = 5,    /* denoiser features                                 */
     LUZ_KERNEL_DENOISE = 6,     /* denoiser network + filter                         */
-    LUZ_KERNEL_TAA = 7
+    LUZ_KERNEL_TAA = 7,
+    LUZ_KERNEL_DENOISE_TRAIN = 8 /* denoiser forward + backward + weight gradients    */
 };
 luz_status luz_ctx_profile(luz_ctx* ctx, int32_t on);
 luz_status luz_ctx_profile_read(luz_ctx* ctx, int32_t kernel, float* total_ms, uint32_t* launches);

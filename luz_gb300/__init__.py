@@ -531,7 +531,7 @@ class Context:
         return ms.value
 
     KERNELS = {"tlas_build": 0, "gbuffer": 1, "raygen": 2, "traversal": 3, "light_pass": 4, "features": 5,
-               "denoise": 6, "taa": 7}
+               "denoise": 6, "taa": 7, "denoise_train": 8}
 
     def profile(self, on: bool) -> None:
         """Per-kernel event timing of the instrumented kernels (on clears the records)."""

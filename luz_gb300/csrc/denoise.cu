@@ -1,17 +1,16 @@
-// denoise.cu — learned kernel-predicting AO denoiser (no counterpart in the
-// reference renderer): per pixel, 72 features (8 channels over a 3x3 neighbourhood)
-// → 64 → 64 → 64 (ReLU) → 49 logits → softmax → 7x7 filter of the noisy AO.
+// denoise.cu — learned kernel-predicting denoiser of the 1-sample shadow and AO terms
+// (no counterpart in the reference renderer): per pixel, 72 features (8 channels over
+// a 3x3 neighbourhood) → 64 → 64 → 64 (ReLU) → 49 logits → softmax → one 7x7 kernel
+// that filters the AO and, as the ratio sum(w S) / sum(w U), the shadowed over the
+// unshadowed direct light.
 //
-// BF16 tensor-core matrix products (mma.sync m16n8k16, FP32 accumulation). A warp
-// owns 16 pixels; activations stay in registers from layer to layer (the FP32
-// accumulator fragment of one layer is the BF16 A fragment of the next). Weights are
-// staged in shared memory, n-major with padded strides (conflict-free fragments).
-//
-// Training: one persistent kernel runs forward and backward over fixed pixel tiles;
-// every CTA accumulates its weight gradients with tensor-core products over the
-// tile's pixels (activations and gradients stored transposed in shared memory) in a
-// fixed order, writes one partial per CTA, and a second kernel sums the partials in
-// CTA order — the gradient is deterministic. Adam keeps FP32 master weights.
+// BF16 tcgen05 matrix products with FP32 accumulators in tensor memory, operands in
+// shared memory in the K-major no-swizzle core-matrix layout. Inference: a block per
+// SM, warpgroups with a 128-pixel tile each (thread = pixel row). Training: one
+// persistent kernel runs forward, backward and the weight-gradient products over fixed
+// pixel tiles; every block accumulates its weight gradients in tensor memory in a
+// fixed tile order, writes one partial, and a second kernel sums the partials in block
+// order — the gradient is deterministic. Adam keeps FP32 master weights.
 //
 // Feature channels per pixel: 0 noisy AO, 1 unoccluded fraction of the shadow
 // samples, 2-4 normal, 5 depth relative to the centre pixel
@@ -30,7 +29,8 @@ namespace dn {
 
 constexpr int kParams = 16177;
 constexpr int oW1 = 0, ob1 = 4608, oW2 = 4672, ob2 = 8768, oW3 = 8832, ob3 = 12928, oW4 = 12992, ob4 = 16128;
-// packed BF16 weights (elements), n-major with padded k strides
+// packed BF16 weights (elements), n-major with padded k strides; the kernels copy them
+// into the core-matrix layout
 constexpr int sW1 = 88, sW = 72;
 constexpr int pW1 = 0;
 constexpr int pW2 = pW1 + 64 * sW1;
@@ -41,23 +41,11 @@ constexpr int pW3T = pW2T + 64 * sW;
 constexpr int pW4T = pW3T + 64 * sW;
 constexpr int pEnd = pW4T + 64 * sW;
 constexpr int kBias = 64 + 64 + 64 + 56;   // b1 | b2 | b3 | b4 (padded)
-constexpr int kTile = 128;                 // pixels per CTA tile (8 warps x 16)
-constexpr int sT = kTile + 8;              // stride of the transposed activation tiles
-
-__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&v);
 }
-__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-__device__ __forceinline__ float bf(__nv_bfloat16 v) { return __bfloat162float(v); }
 
 // ---------------------------------------------------------------- features
 struct FeatParams {
@@ -147,79 +135,6 @@ __device__ __forceinline__ float relative_depth(float dq, float dc, float inv_dc
     return fminf(fmaxf((dq - dc) * inv_dc, -1.0f), 1.0f);
 }
 
-// Gathers the 16 x 80 feature tile of a warp into `stage` ([16][sW1] bf16) for the
-// pixels base..base+15 (global index over images). Invalid pixels get zeros.
-__device__ __forceinline__ void gather_tile(const uint4* __restrict__ feat, const float* __restrict__ ld,
-                                            const ImageGeom& G, uint32_t base, __nv_bfloat16* stage,
-                                            uint32_t& valid_mask) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t total = G.pixels * G.images;
-    valid_mask = 0;
-    for (int e = lane; e < 16 * 9; e += 32) {
-        int r = e / 9, tap = e % 9;
-        uint32_t gp = base + r;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (gp < total) {
-            uint32_t img = gp / G.pixels, local = gp - img * G.pixels;
-            int x = (int)(local % G.width), y = (int)(local / G.width);
-            float dc = ld[gp];
-            if (dc > 0.0f) {
-                int qx = min(max(x + tap % 3 - 1, 0), (int)G.width - 1);
-                int qy = min(max(y + tap / 3 - 1, 0), (int)G.height - 1);
-                uint32_t q = img * G.pixels + (uint32_t)qy * G.width + (uint32_t)qx;
-                v = feat[q];
-                float dq = ld[q];
-                float rel = dq > 0.0f ? relative_depth(dq, dc, 1.0f / dc) : 0.0f;
-                // channel 5 (upper half of v.z) carries the relative depth
-                v.z = (v.z & 0xFFFFu) | (pack2(0.0f, rel) & 0xFFFF0000u);
-            }
-        }
-        *reinterpret_cast<uint4*>(stage + r * sW1 + tap * 8) = v;
-    }
-    for (int e = lane; e < 16; e += 32)
-        *reinterpret_cast<uint4*>(stage + e * sW1 + 72) = make_uint4(0, 0, 0, 0);
-    for (int r = 0; r < 16; ++r) {
-        uint32_t gp = base + r;
-        if (gp < total && ld[gp] > 0.0f) valid_mask |= 1u << r;
-    }
-    __syncwarp();
-}
-
-__device__ __forceinline__ void load_a(const __nv_bfloat16* stage, int stride, int kk, uint32_t a[4]) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    a[0] = ld32(stage + g * stride + 16 * kk + 2 * t);
-    a[1] = ld32(stage + (g + 8) * stride + 16 * kk + 2 * t);
-    a[2] = ld32(stage + g * stride + 16 * kk + 2 * t + 8);
-    a[3] = ld32(stage + (g + 8) * stride + 16 * kk + 2 * t + 8);
-}
-
-// c[NT][4] = A[16 x 16*KS] * W^T (+ bias), W n-major [NT*8][stride] in shared memory.
-template <int KS, int NT>
-__device__ __forceinline__ void layer(const uint32_t a[KS][4], const __nv_bfloat16* W, int stride, const float* bias,
-                                      float c[NT][4]) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-        float b0 = bias ? bias[nt * 8 + 2 * t] : 0.f, b1 = bias ? bias[nt * 8 + 2 * t + 1] : 0.f;
-        c[nt][0] = b0; c[nt][1] = b1; c[nt][2] = b0; c[nt][3] = b1;
-        const __nv_bfloat16* wr = W + (nt * 8 + g) * stride + 2 * t;
-#pragma unroll
-        for (int kk = 0; kk < KS; ++kk) mma16816(c[nt], a[kk], ld32(wr + 16 * kk), ld32(wr + 16 * kk + 8));
-    }
-}
-
-// ReLU + BF16: accumulator fragments of 2*KS n-tiles → A fragments of KS k-steps.
-template <int KS>
-__device__ __forceinline__ void to_a_relu(const float c[2 * KS][4], uint32_t a[KS][4]) {
-#pragma unroll
-    for (int kk = 0; kk < KS; ++kk) {
-        a[kk][0] = pack2(fmaxf(c[2 * kk][0], 0.f), fmaxf(c[2 * kk][1], 0.f));
-        a[kk][1] = pack2(fmaxf(c[2 * kk][2], 0.f), fmaxf(c[2 * kk][3], 0.f));
-        a[kk][2] = pack2(fmaxf(c[2 * kk + 1][0], 0.f), fmaxf(c[2 * kk + 1][1], 0.f));
-        a[kk][3] = pack2(fmaxf(c[2 * kk + 1][2], 0.f), fmaxf(c[2 * kk + 1][3], 0.f));
-    }
-}
-
 // Filtered shadow ratio of one channel: sum(w S) / sum(w U); 1 where sum(w U) = 0 (no
 // neighbour receives direct light in that channel: the pixel's own U is 0 then too).
 __device__ __forceinline__ float filtered_ratio(float ws, float wu) {
@@ -234,82 +149,6 @@ __device__ __forceinline__ float4 signal_tap(const float4* __restrict__ sig, con
     const int qx = min(max(x + k % 7 - 3, 0), (int)G.width - 1);
     const int qy = min(max(y + k / 7 - 3, 0), (int)G.height - 1);
     return __ldg(sig + img * G.pixels + (uint32_t)qy * G.width + (uint32_t)qx);
-}
-
-// Softmax over the 49 logits of rows g and g+8 (4 lanes share a row) and the 7x7
-// filter. z[7][4] receives the normalised weights w_k; for row g + 8h, y[h] = (ratio
-// r, g, b, AO) with ratio_c = sum(w S_c) / sum(w U_c) and AO = sum(w AO), and
-// du[h] = sum(w U) (r, g, b).
-__device__ __forceinline__ void softmax_filter(float z[7][4], const float4* __restrict__ sig,
-                                               const float4* __restrict__ uns, const ImageGeom& G, uint32_t base,
-                                               float4 y[2], float3 du[2]) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const uint32_t total = G.pixels * G.images;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        float m = -3.0e38f;
-#pragma unroll
-        for (int nt = 0; nt < 7; ++nt)
-#pragma unroll
-            for (int j = 0; j < 2; ++j)
-                if (nt * 8 + 2 * t + j < 49) m = fmaxf(m, z[nt][2 * h + j]);
-        m = fmaxf(m, __shfl_xor_sync(0xFFFFFFFFu, m, 1));
-        m = fmaxf(m, __shfl_xor_sync(0xFFFFFFFFu, m, 2));
-        float s = 0.f;
-#pragma unroll
-        for (int nt = 0; nt < 7; ++nt)
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                float e = (nt * 8 + 2 * t + j < 49) ? __expf(z[nt][2 * h + j] - m) : 0.f;
-                z[nt][2 * h + j] = e;
-                s += e;
-            }
-        s += __shfl_xor_sync(0xFFFFFFFFu, s, 1);
-        s += __shfl_xor_sync(0xFFFFFFFFu, s, 2);
-        float inv = 1.0f / s;
-        uint32_t gp = base + g + 8 * h;
-        uint32_t img = 0;
-        int x = 0, yy = 0;
-        const bool ok = gp < total;
-        if (ok) {
-            img = gp / G.pixels;
-            const uint32_t local = gp - img * G.pixels;
-            x = (int)(local % G.width);
-            yy = (int)(local / G.width);
-        }
-        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        float3 au = make_float3(0.f, 0.f, 0.f);
-#pragma unroll
-        for (int nt = 0; nt < 7; ++nt)
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const int k = nt * 8 + 2 * t + j;
-                const float wk = z[nt][2 * h + j] * inv;
-                z[nt][2 * h + j] = wk;
-                const float4 a = signal_tap(sig, G, ok, img, x, yy, k);
-                const float4 u = signal_tap(uns, G, ok, img, x, yy, k);
-                acc.x += wk * a.x;
-                acc.y += wk * a.y;
-                acc.z += wk * a.z;
-                acc.w += wk * a.w;
-                au.x += wk * u.x;
-                au.y += wk * u.y;
-                au.z += wk * u.z;
-            }
-#pragma unroll
-        for (int o = 1; o <= 2; o <<= 1) {
-            acc.x += __shfl_xor_sync(0xFFFFFFFFu, acc.x, o);
-            acc.y += __shfl_xor_sync(0xFFFFFFFFu, acc.y, o);
-            acc.z += __shfl_xor_sync(0xFFFFFFFFu, acc.z, o);
-            acc.w += __shfl_xor_sync(0xFFFFFFFFu, acc.w, o);
-            au.x += __shfl_xor_sync(0xFFFFFFFFu, au.x, o);
-            au.y += __shfl_xor_sync(0xFFFFFFFFu, au.y, o);
-            au.z += __shfl_xor_sync(0xFFFFFFFFu, au.z, o);
-        }
-        y[h] = make_float4(filtered_ratio(acc.x, au.x), filtered_ratio(acc.y, au.y), filtered_ratio(acc.z, au.z),
-                           acc.w);
-        du[h] = au;
-    }
 }
 
 // ---------------------------------------------------------------- inference
@@ -693,259 +532,375 @@ struct TrainParams {
     float* partial_loss;       // [gridDim.x]
 };
 
-constexpr int kDwTiles = 40 + 36 * 3;    // (layer, 16-row, 8-col) tiles of dW (bias as an extra column)
-constexpr int kDwPerWarp = (kDwTiles + 7) / 8;
+// ---------------------------------------------------------------- training on tcgen05
+// Forward, backward and the weight gradients of a 128-pixel tile as tcgen05.mma
+// products (M = 128, BF16 operands in shared memory, FP32 accumulators in tensor
+// memory), one warpgroup per SM, thread p = pixel p of the tile:
+//   forward   D = A * W^T for the four layers (A = X, H1, H2, H3; as inference);
+//   backward  dH_l = dZ_{l+1} * W_{l+1} (B = the transposed weights W^T, K = outputs);
+//   gradients dW_l += dZ_l^T * [H_{l-1} | 1]^T over the tile's pixels (M = outputs,
+//             rows 64..127 of A zero; N = 80 with the bias column of ones; K = the 128
+//             pixels), accumulated in tensor memory over all tiles of the block.
+// Every operand sits in the K-major no-swizzle core-matrix layout of the inference
+// kernel; the activations and dZ are written twice by their threads: as a row of the
+// next product's A and as a column of the transposed copy (dW's A and B). One
+// partial per block in the FP32 parameter layout, summed in block order.
+constexpr int kTtW1 = 0;                            // [64 x 80] forward B
+constexpr int kTtW2 = kTtW1 + 64 * 80 * 2;          // [64 x 64]
+constexpr int kTtW3 = kTtW2 + 64 * 64 * 2;
+constexpr int kTtW4 = kTtW3 + 64 * 64 * 2;          // rows >= 49 zero
+constexpr int kTtW4T = kTtW4 + 64 * 64 * 2;         // [64 hidden x 64 outputs] backward B
+constexpr int kTtW3T = kTtW4T + 64 * 64 * 2;
+constexpr int kTtW2T = kTtW3T + 64 * 64 * 2;
+constexpr int kTtA = kTtW2T + 64 * 64 * 2;          // [128 x 80] X, then H1, H2, H3
+constexpr int kTtXT = kTtA + 128 * 80 * 2;          // [80 x 128] X^T, row 72 ones
+constexpr int kTtHT = kTtXT + 80 * 128 * 2;         // 3 x [80 x 128] H^T, row 64 ones
+constexpr int kTtDZ = kTtHT + 3 * 80 * 128 * 2;     // [128 x 64] dZ
+constexpr int kTtDZT = kTtDZ + 128 * 64 * 2;        // [128 x 128] dZ^T in rows 0..63
+constexpr int kTtBias = kTtDZT + 128 * 128 * 2;
+constexpr int kTtBar = kTtBias + kBias * 4;
+constexpr int kTtSmem = kTtBar + 32;
+static_assert(kTtSmem + 1024 <= 232448, "training tile must fit in shared memory");
+// tensor-memory columns: forward D, backward dH, dW1..dW4 (80 each)
+constexpr uint32_t kTtFwd = 0, kTtDH = 64, kTtDW1 = 128, kTtDW2 = 208, kTtDW3 = 288, kTtDW4 = 368;
+constexpr uint32_t kTtAlloc = 512;
 
-struct TrainSmem {
-    // transposed tiles: [unit][pixel]
-    __nv_bfloat16 xT[80][sT];     // features, row 72 = ones (bias column of dW1)
-    __nv_bfloat16 h1T[72][sT];    // rows 64 = ones, 65..71 = 0
-    __nv_bfloat16 h2T[72][sT];
-    __nv_bfloat16 h3T[72][sT];
-    __nv_bfloat16 d4T[64][sT];    // rows 49..63 = 0
-    __nv_bfloat16 d3T[64][sT];
-    __nv_bfloat16 d2T[64][sT];
-    __nv_bfloat16 d1T[64][sT];
-};
-
-// dW tile t -> (layer, m-tile, n-tile, A rows, B rows)
-__device__ __forceinline__ void dw_tile(int id, int& l, int& mt, int& nt) {
-    if (id < 40) { l = 0; mt = id / 10; nt = id % 10; return; }
-    id -= 40;
-    l = 1 + id / 36;
-    id %= 36;
-    mt = id / 9;
-    nt = id % 9;
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
 }
 
-__global__ void __launch_bounds__(256, 1) denoise_train_kernel(TrainParams P) {
-    extern __shared__ __align__(16) unsigned char sm_raw[];
-    __nv_bfloat16* sw = reinterpret_cast<__nv_bfloat16*>(sm_raw);
-    float* sbias = reinterpret_cast<float*>(sm_raw + pEnd * 2);
-    TrainSmem& S = *reinterpret_cast<TrainSmem*>(sm_raw + pEnd * 2 + kBias * 4);
-    // The per-warp feature tiles live in d3T/d2T, which are written only after every
-    // warp has loaded its features (barrier below).
-    __nv_bfloat16* stage_all = &S.d3T[0][0];
-    static_assert(2 * sizeof(S.d3T) >= 8 * 16 * sW1 * 2, "staging tiles must fit in d3T+d2T");
-    for (int i = threadIdx.x; i < pEnd / 8; i += blockDim.x)
-        reinterpret_cast<uint4*>(sw)[i] = reinterpret_cast<const uint4*>(P.wpack)[i];
-    for (int i = threadIdx.x; i < kBias; i += blockDim.x) sbias[i] = P.bias[i];
-    // constant rows: ones for the bias columns, zeros for padding
-    for (int i = threadIdx.x; i < sT; i += blockDim.x) {
-        __nv_bfloat16 one = __float2bfloat16(1.0f), zero = __float2bfloat16(0.0f);
-        S.xT[72][i] = one;
-        for (int r = 73; r < 80; ++r) S.xT[r][i] = zero;
-        S.h1T[64][i] = one; S.h2T[64][i] = one; S.h3T[64][i] = one;
-        for (int r = 65; r < 72; ++r) { S.h1T[r][i] = zero; S.h2T[r][i] = zero; S.h3T[r][i] = zero; }
-        for (int r = 49; r < 64; ++r) S.d4T[r][i] = zero;
+// D[tmem] (+)= A[128 x 16 ksteps] * B[N x 16 ksteps]^T; a / b: shared addresses,
+// ka / kb: their core-matrix columns (K / 8).
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint32_t a, uint32_t ka, uint32_t b, uint32_t kb, int ksteps,
+                                       uint32_t idesc, bool accumulate) {
+    for (int s = 0; s < ksteps; ++s) {
+        const uint64_t da = umma_desc(a + (uint32_t)s * 256u, 128u, ka * 128u);
+        const uint64_t db = umma_desc(b + (uint32_t)s * 256u, 128u, kb * 128u);
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                     :: "r"(tmem), "l"(da), "l"(db), "r"(idesc), "r"((s > 0 || accumulate) ? 1u : 0u));
     }
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    __nv_bfloat16* stage = stage_all + warp * 16 * sW1;
-    const uint32_t total = P.G.pixels * P.G.images;
-    const uint32_t tiles = (total + kTile - 1) / kTile;
-    float dw[kDwPerWarp][4];
-#pragma unroll
-    for (int i = 0; i < kDwPerWarp; ++i) dw[i][0] = dw[i][1] = dw[i][2] = dw[i][3] = 0.f;
-    float loss = 0.f;
-    const int px0 = warp * 16;   // this warp's pixel rows inside the tile
+}
 
+// Makes the block's shared-memory writes and tensor-memory reads visible to the
+// products that thread 0 issues next.
+__device__ __forceinline__ void tt_before_issue() {
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+}
+
+// Commits the issued products to the mbarrier and waits for them (bounded; see
+// tc_run_layer).
+__device__ __forceinline__ void tt_commit_wait(uint32_t bar, uint32_t& phase, bool& failed, uint32_t* status) {
+    if (threadIdx.x == 0)
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar));
+    if (!failed && !tc_wait(bar, phase)) {
+        atomicOr(status, (uint32_t)LUZ_DEV_MMA_WAIT);
+        failed = true;
+    }
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+}
+
+// Element (r, k) of a core-matrix tile with kblocks core columns, as a 2-byte offset.
+__device__ __forceinline__ uint32_t elem_offset(uint32_t r, uint32_t k, uint32_t kblocks) {
+    return core_offset(r, k >> 3, kblocks) + (k & 7u) * 2u;
+}
+
+__device__ __forceinline__ void st_bf16(unsigned char* base, uint32_t off, float v) {
+    *reinterpret_cast<__nv_bfloat16*>(base + off) = __float2bfloat16(v);
+}
+
+// Forward epilogue of layers 1-3: bias + ReLU + BF16 of this thread's 64 accumulator
+// columns into row `row` of A (the next layer's input) and column `row` of the
+// transposed copy ht; bit j of mask = (h_j > 0).
+__device__ __forceinline__ void tt_relu_out(uint32_t tl, const float* sb, unsigned char* a, unsigned char* ht,
+                                            uint32_t row, uint64_t& mask) {
+    mask = 0;
+#pragma unroll
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+        float v[16];
+        tc_load16(tl + (uint32_t)c0, v);
+        uint32_t w[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float lo = fmaxf(v[2 * j] + sb[c0 + 2 * j], 0.0f), hi = fmaxf(v[2 * j + 1] + sb[c0 + 2 * j + 1], 0.0f);
+            w[j] = pack2(lo, hi);
+            const __nv_bfloat162 q = *reinterpret_cast<const __nv_bfloat162*>(&w[j]);
+            *reinterpret_cast<__nv_bfloat16*>(ht + elem_offset((uint32_t)(c0 + 2 * j), row, 16)) = q.x;
+            *reinterpret_cast<__nv_bfloat16*>(ht + elem_offset((uint32_t)(c0 + 2 * j + 1), row, 16)) = q.y;
+            mask |= (uint64_t)(__bfloat162float(q.x) > 0.0f) << (c0 + 2 * j);
+            mask |= (uint64_t)(__bfloat162float(q.y) > 0.0f) << (c0 + 2 * j + 1);
+        }
+        *reinterpret_cast<uint4*>(a + core_offset(row, (uint32_t)c0 / 8u, 8u)) = make_uint4(w[0], w[1], w[2], w[3]);
+        *reinterpret_cast<uint4*>(a + core_offset(row, (uint32_t)c0 / 8u + 1u, 8u)) = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+// Backward epilogue of layers 3-1: dZ = dH * ReLU'(h) of this thread's 64 columns into
+// row `row` of dZ (when dz != null) and column `row` of dZ^T.
+__device__ __forceinline__ void tt_dz_out(uint32_t tl, uint64_t mask, unsigned char* dz, unsigned char* dzt,
+                                          uint32_t row) {
+#pragma unroll
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+        float v[16];
+        tc_load16(tl + (uint32_t)c0, v);
+        uint32_t w[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float lo = ((mask >> (c0 + 2 * j)) & 1u) ? v[2 * j] : 0.0f;
+            const float hi = ((mask >> (c0 + 2 * j + 1)) & 1u) ? v[2 * j + 1] : 0.0f;
+            w[j] = pack2(lo, hi);
+            const __nv_bfloat162 q = *reinterpret_cast<const __nv_bfloat162*>(&w[j]);
+            *reinterpret_cast<__nv_bfloat16*>(dzt + elem_offset((uint32_t)(c0 + 2 * j), row, 16)) = q.x;
+            *reinterpret_cast<__nv_bfloat16*>(dzt + elem_offset((uint32_t)(c0 + 2 * j + 1), row, 16)) = q.y;
+        }
+        if (dz) {
+            *reinterpret_cast<uint4*>(dz + core_offset(row, (uint32_t)c0 / 8u, 8u)) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4*>(dz + core_offset(row, (uint32_t)c0 / 8u + 1u, 8u)) =
+                make_uint4(w[4], w[5], w[6], w[7]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128, 1) denoise_train_tc_kernel(TrainParams P, uint32_t* status) {
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    float* sbias = reinterpret_cast<float*>(tsm + kTtBias);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(tsm + kTtBar + 8);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid;
+    const uint32_t bar = smem_u32(tsm + kTtBar);
+    // weights into the core-matrix layout: forward (n-major W) and backward (W^T)
+    for (uint32_t e = tid; e < 64 * 10; e += 128) {
+        const uint32_t n = e / 10, kb = e % 10;
+        *reinterpret_cast<uint4*>(tsm + kTtW1 + core_offset(n, kb, 10)) =
+            *reinterpret_cast<const uint4*>(P.wpack + pW1 + n * sW1 + kb * 8);
+    }
+    for (uint32_t e = tid; e < 64 * 8; e += 128) {
+        const uint32_t n = e / 8, kb = e % 8;
+        const uint32_t o = core_offset(n, kb, 8);
+        *reinterpret_cast<uint4*>(tsm + kTtW2 + o) = *reinterpret_cast<const uint4*>(P.wpack + pW2 + n * sW + kb * 8);
+        *reinterpret_cast<uint4*>(tsm + kTtW3 + o) = *reinterpret_cast<const uint4*>(P.wpack + pW3 + n * sW + kb * 8);
+        *reinterpret_cast<uint4*>(tsm + kTtW4 + o) =
+            n < 56 ? *reinterpret_cast<const uint4*>(P.wpack + pW4 + n * sW + kb * 8) : make_uint4(0, 0, 0, 0);
+        *reinterpret_cast<uint4*>(tsm + kTtW4T + o) = *reinterpret_cast<const uint4*>(P.wpack + pW4T + n * sW + kb * 8);
+        *reinterpret_cast<uint4*>(tsm + kTtW3T + o) = *reinterpret_cast<const uint4*>(P.wpack + pW3T + n * sW + kb * 8);
+        *reinterpret_cast<uint4*>(tsm + kTtW2T + o) = *reinterpret_cast<const uint4*>(P.wpack + pW2T + n * sW + kb * 8);
+    }
+    for (uint32_t i = tid; i < (uint32_t)kBias; i += 128) sbias[i] = P.bias[i];
+    // constant parts: zero dZ^T (rows 64..127 stay zero, rows 49..63 of the last layer
+    // too) and the ones / zero rows of the transposed activations
+    for (uint32_t i = tid; i < 128 * 128 * 2 / 16; i += 128)
+        reinterpret_cast<uint4*>(tsm + kTtDZT)[i] = make_uint4(0, 0, 0, 0);
+    for (uint32_t i = tid; i < 128 * 64 * 2 / 16; i += 128)
+        reinterpret_cast<uint4*>(tsm + kTtDZ)[i] = make_uint4(0, 0, 0, 0);
+    {
+        const __nv_bfloat16 one = __float2bfloat16(1.0f), zero = __float2bfloat16(0.0f);
+        for (uint32_t k = 72; k < 80; ++k)
+            *reinterpret_cast<__nv_bfloat16*>(tsm + kTtXT + elem_offset(k, row, 16)) = k == 72 ? one : zero;
+        for (int l = 0; l < 3; ++l)
+            for (uint32_t k = 64; k < 80; ++k)
+                *reinterpret_cast<__nv_bfloat16*>(tsm + kTtHT + l * 80 * 128 * 2 + elem_offset(k, row, 16)) =
+                    k == 64 ? one : zero;
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" :: "r"(smem_u32(tslot)),
+                     "r"(kTtAlloc));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *tslot;
+    const uint32_t lane_off = ((warp & 3u) * 32u) << 16;
+    unsigned char* a = tsm + kTtA;
+    unsigned char* xt = tsm + kTtXT;
+    unsigned char* ht[3] = {tsm + kTtHT, tsm + kTtHT + 80 * 128 * 2, tsm + kTtHT + 2 * 80 * 128 * 2};
+    unsigned char* dz = tsm + kTtDZ;
+    unsigned char* dzt = tsm + kTtDZT;
+    const uint32_t a_addr = smem_u32(a), dz_addr = smem_u32(dz), dzt_addr = smem_u32(dzt);
+    const uint32_t xt_addr = smem_u32(xt);
+    const uint32_t ht_addr[3] = {smem_u32(ht[0]), smem_u32(ht[1]), smem_u32(ht[2])};
+    const uint32_t wf[4] = {smem_u32(tsm + kTtW1), smem_u32(tsm + kTtW2), smem_u32(tsm + kTtW3), smem_u32(tsm + kTtW4)};
+    const uint32_t wt[3] = {smem_u32(tsm + kTtW2T), smem_u32(tsm + kTtW3T), smem_u32(tsm + kTtW4T)};
+    const uint32_t dw_col[4] = {kTtDW1, kTtDW2, kTtDW3, kTtDW4};
+    uint32_t phase = 0;
+    bool failed = false, accumulated = false;
+    float loss = 0.f;
+    const uint32_t total = P.G.pixels * P.G.images;
+    const uint32_t tiles = (total + 127) / 128;
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        uint32_t base = tile * kTile + px0;
-        uint32_t valid;
-        gather_tile(P.feat, P.lin_depth, P.G, base, stage, valid);
-        // xT: features transposed (rows 0..71)
-        for (int e = lane; e < 16 * 72; e += 32) {
-            int r = e / 72, k = e % 72;
-            S.xT[k][px0 + r] = stage[r * sW1 + k];
+        // ---- features of pixel `row` (9 taps of 8 channels, relative depth in channel 5)
+        const uint32_t gp = tile * 128 + row;
+        const bool has = gp < total;
+        uint32_t img = 0;
+        int x = 0, y = 0;
+        if (has) {
+            img = gp / P.G.pixels;
+            const uint32_t local = gp - img * P.G.pixels;
+            x = (int)(local % P.G.width);
+            y = (int)(local / P.G.width);
         }
-        uint32_t a0[5][4];
+        const float dc = has ? P.lin_depth[gp] : 0.0f;
+        const bool valid = dc > 0.0f;
+        const float inv_dc = valid ? 1.0f / dc : 0.0f;
 #pragma unroll
-        for (int kk = 0; kk < 5; ++kk) load_a(stage, sW1, kk, a0[kk]);
-        __syncthreads();   // every warp's staging tile is consumed before d3T/d2T are written
-        float c[8][4];
-        uint32_t a1[4][4];
-        // ---- forward, keeping h1..h3 (post-ReLU, BF16) transposed in shared memory
-        layer<5, 8>(a0, sw + pW1, sW1, sbias, c);
-        to_a_relu<4>(c, a1);
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                S.h1T[nt * 8 + 2 * t + (j & 1)][px0 + g + 8 * (j >> 1)] = __float2bfloat16(fmaxf(c[nt][j], 0.f));
-        layer<4, 8>(a1, sw + pW2, sW, sbias + 64, c);
-        to_a_relu<4>(c, a1);
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                S.h2T[nt * 8 + 2 * t + (j & 1)][px0 + g + 8 * (j >> 1)] = __float2bfloat16(fmaxf(c[nt][j], 0.f));
-        layer<4, 8>(a1, sw + pW3, sW, sbias + 128, c);
-        to_a_relu<4>(c, a1);
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                S.h3T[nt * 8 + 2 * t + (j & 1)][px0 + g + 8 * (j >> 1)] = __float2bfloat16(fmaxf(c[nt][j], 0.f));
-        float z[7][4];
-        float4 y[2];
-        float3 du[2];
-        layer<4, 7>(a1, sw + pW4, sW, sbias + 192, z);
-        softmax_filter(z, P.sig, P.uns, P.G, base, y, du);   // z now holds the softmax weights
-        // ---- loss and dL/dz (softmax + filter backward): with dy the loss gradient of
-        // the outputs, g_k = dy_ao AO_k + sum_c dy_c (S_kc - ratio_c U_kc) / sum(w U_c)
-        // (the derivative of the ratio of sums) and dz_k = w_k (g_k - sum_j w_j g_j)
-        float dz[8][4];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const uint32_t gp = base + g + 8 * h;
-            const bool ok = ((valid >> (g + 8 * h)) & 1u) != 0;
-            const float4 tg = ok ? P.target[gp] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 err = ok ? make_float4(y[h].x - tg.x, y[h].y - tg.y, y[h].z - tg.z, y[h].w - tg.w)
-                                  : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 cw = (P.weight && ok) ? P.weight[gp]
-                                               : make_float4(P.shadow_weight, P.shadow_weight, P.shadow_weight, 1.0f);
-            if (t == 0)   // mean over the batch's pixels
-                loss += (cw.w * err.w * err.w + cw.x * err.x * err.x + cw.y * err.y * err.y + cw.z * err.z * err.z) *
-                        (0.5f * P.grad_scale);
-            const float4 dy = make_float4(cw.x * err.x * P.grad_scale, cw.y * err.y * P.grad_scale,
-                                          cw.z * err.z * P.grad_scale, cw.w * err.w * P.grad_scale);
-            // d ratio_c / d w_k = (S_kc - ratio_c U_kc) / sum(w U_c); 0 where the sum is 0
-            const float3 dq = make_float3(du[h].x > 0.f ? dy.x / du[h].x : 0.f, du[h].y > 0.f ? dy.y / du[h].y : 0.f,
-                                          du[h].z > 0.f ? dy.z / du[h].z : 0.f);
-            const float3 dr = make_float3(dq.x * y[h].x, dq.y * y[h].y, dq.z * y[h].z);
-            uint32_t img = 0;
-            int px = 0, py = 0;
-            const bool in = gp < P.G.pixels * P.G.images;
-            if (in) {
-                img = gp / P.G.pixels;
-                const uint32_t local = gp - img * P.G.pixels;
-                px = (int)(local % P.G.width);
-                py = (int)(local / P.G.width);
+        for (int tap = 0; tap < 9; ++tap) {
+            const int qx = min(max(x + tap % 3 - 1, 0), (int)P.G.width - 1);
+            const int qy = min(max(y + tap / 3 - 1, 0), (int)P.G.height - 1);
+            const uint32_t q = img * P.G.pixels + (uint32_t)qy * P.G.width + (uint32_t)qx;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (valid) {
+                v = P.feat[q];
+                const float dq = P.lin_depth[q];
+                const float rel = dq > 0.0f ? relative_depth(dq, dc, inv_dc) : 0.0f;
+                v.z = (v.z & 0xFFFFu) | (pack2(0.0f, rel) & 0xFFFF0000u);
             }
-            float gk[7][2];
-            float sdot = 0.f;
+            *reinterpret_cast<uint4*>(a + core_offset(row, (uint32_t)tap, 10)) = v;
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-            for (int nt = 0; nt < 7; ++nt)
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    const float4 a = signal_tap(P.sig, P.G, in, img, px, py, nt * 8 + 2 * t + j);
-                    const float4 u = signal_tap(P.uns, P.G, in, img, px, py, nt * 8 + 2 * t + j);
-                    gk[nt][j] = dy.w * a.w + (dq.x * a.x - dr.x * u.x) + (dq.y * a.y - dr.y * u.y) +
-                                (dq.z * a.z - dr.z * u.z);
-                    sdot += z[nt][2 * h + j] * gk[nt][j];
-                }
-            sdot += __shfl_xor_sync(0xFFFFFFFFu, sdot, 1);
-            sdot += __shfl_xor_sync(0xFFFFFFFFu, sdot, 2);
-#pragma unroll
-            for (int nt = 0; nt < 7; ++nt)
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    const int k = nt * 8 + 2 * t + j;
-                    const float w = z[nt][2 * h + j];
-                    dz[nt][2 * h + j] = (k < 49) ? w * (gk[nt][j] - sdot) : 0.f;
-                }
-            dz[7][2 * h] = dz[7][2 * h + 1] = 0.f;
-        }
-#pragma unroll
-        for (int nt = 0; nt < 7; ++nt)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                int col = nt * 8 + 2 * t + (j & 1);
-                if (col < 49) S.d4T[col][px0 + g + 8 * (j >> 1)] = __float2bfloat16(dz[nt][j]);
-            }
-        // ---- back through layers 4..2: dH = dZ * W, masked by ReLU'
-        uint32_t ad[4][4];
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-            ad[kk][0] = pack2(dz[2 * kk][0], dz[2 * kk][1]);
-            ad[kk][1] = pack2(dz[2 * kk][2], dz[2 * kk][3]);
-            ad[kk][2] = pack2(dz[2 * kk + 1][0], dz[2 * kk + 1][1]);
-            ad[kk][3] = pack2(dz[2 * kk + 1][2], dz[2 * kk + 1][3]);
-        }
-        __nv_bfloat16(*hT[3])[sT] = {S.h3T, S.h2T, S.h1T};
-        __nv_bfloat16(*dT[3])[sT] = {S.d3T, S.d2T, S.d1T};
-        const int wT[3] = {pW4T, pW3T, pW2T};
-#pragma unroll
-        for (int L = 0; L < 3; ++L) {
-            float dh[8][4];
-            layer<4, 8>(ad, sw + wT[L], sW, nullptr, dh);
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    int unit = nt * 8 + 2 * t + (j & 1), px = px0 + g + 8 * (j >> 1);
-                    float hv = bf(hT[L][unit][px]);
-                    float d = hv > 0.f ? dh[nt][j] : 0.f;
-                    dh[nt][j] = d;
-                    dT[L][unit][px] = __float2bfloat16(d);
-                }
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-                ad[kk][0] = pack2(dh[2 * kk][0], dh[2 * kk][1]);
-                ad[kk][1] = pack2(dh[2 * kk][2], dh[2 * kk][3]);
-                ad[kk][2] = pack2(dh[2 * kk + 1][0], dh[2 * kk + 1][1]);
-                ad[kk][3] = pack2(dh[2 * kk + 1][2], dh[2 * kk + 1][3]);
+            for (int c = 0; c < 4; ++c) {
+                *reinterpret_cast<uint16_t*>(xt + elem_offset((uint32_t)(tap * 8 + 2 * c), row, 16)) =
+                    (uint16_t)(w4[c] & 0xFFFFu);
+                *reinterpret_cast<uint16_t*>(xt + elem_offset((uint32_t)(tap * 8 + 2 * c + 1), row, 16)) =
+                    (uint16_t)(w4[c] >> 16);
             }
         }
-        __syncthreads();
-        // ---- dW += dZ^T * H over the tile's 128 pixels (fixed order)
+        *reinterpret_cast<uint4*>(a + core_offset(row, 9, 10)) = make_uint4(0, 0, 0, 0);
+        // ---- forward
+        uint64_t mask[3];
+        const uint32_t tl = tmem + lane_off;
 #pragma unroll
-        for (int i = 0; i < kDwPerWarp; ++i) {
-            int id = warp + 8 * i;
-            if (id >= kDwTiles) break;
-            int l, mt, nt;
-            dw_tile(id, l, mt, nt);
-            const __nv_bfloat16* A;
-            const __nv_bfloat16* B;
-            if (l == 0) { A = &S.d1T[0][0]; B = &S.xT[0][0]; }
-            else if (l == 1) { A = &S.d2T[0][0]; B = &S.h1T[0][0]; }
-            else if (l == 2) { A = &S.d3T[0][0]; B = &S.h2T[0][0]; }
-            else { A = &S.d4T[0][0]; B = &S.h3T[0][0]; }
-#pragma unroll
-            for (int kk = 0; kk < kTile / 16; ++kk) {
-                uint32_t a[4];
-                const __nv_bfloat16* ar = A + (mt * 16 + g) * sT + 16 * kk + 2 * t;
-                a[0] = ld32(ar);
-                a[1] = ld32(ar + 8 * sT);
-                a[2] = ld32(ar + 8);
-                a[3] = ld32(ar + 8 * sT + 8);
-                const __nv_bfloat16* br = B + (nt * 8 + g) * sT + 16 * kk + 2 * t;
-                mma16816(dw[i], a, ld32(br), ld32(br + 8));
-            }
+        for (int l = 0; l < 4; ++l) {
+            tt_before_issue();
+            if (tid == 0) tc_mma(tmem + kTtFwd, a_addr, l == 0 ? 10u : 8u, wf[l], l == 0 ? 10u : 8u, l == 0 ? 5 : 4,
+                                 tc_idesc(64), false);
+            tt_commit_wait(bar, phase, failed, status);
+            if (l < 3) tt_relu_out(tl + kTtFwd, sbias + 64 * l, a, ht[l], row, mask[l]);
         }
-        __syncthreads();
+        // ---- softmax, filter, loss and dL/dz of the last layer (this thread's pixel)
+        const float* b4 = sbias + 192;
+        float z[49];
+#pragma unroll
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+            float v[16];
+            tc_load16(tl + kTtFwd + (uint32_t)c0, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                if (c0 + j < 49) z[c0 + j] = v[j] + b4[c0 + j];
+        }
+        float m = -3.0e38f;
+#pragma unroll
+        for (int k = 0; k < 49; ++k) m = fmaxf(m, z[k]);
+        float sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < 49; ++k) {
+            z[k] = __expf(z[k] - m);
+            sum += z[k];
+        }
+        const float inv = 1.0f / sum;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        float3 au = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < 49; ++k) {
+            z[k] *= inv;   // the normalised weight w_k
+            const float4 sv = signal_tap(P.sig, P.G, has, img, x, y, k);
+            const float4 uv = signal_tap(P.uns, P.G, has, img, x, y, k);
+            acc.x += z[k] * sv.x;
+            acc.y += z[k] * sv.y;
+            acc.z += z[k] * sv.z;
+            acc.w += z[k] * sv.w;
+            au.x += z[k] * uv.x;
+            au.y += z[k] * uv.y;
+            au.z += z[k] * uv.z;
+        }
+        const float4 yv = make_float4(filtered_ratio(acc.x, au.x), filtered_ratio(acc.y, au.y),
+                                      filtered_ratio(acc.z, au.z), acc.w);
+        const float4 tg = valid ? P.target[gp] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 err = valid ? make_float4(yv.x - tg.x, yv.y - tg.y, yv.z - tg.z, yv.w - tg.w)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 cw = (P.weight && valid) ? P.weight[gp]
+                                              : make_float4(P.shadow_weight, P.shadow_weight, P.shadow_weight, 1.0f);
+        loss += (cw.w * err.w * err.w + cw.x * err.x * err.x + cw.y * err.y * err.y + cw.z * err.z * err.z) *
+                (0.5f * P.grad_scale);
+        const float4 dy = make_float4(cw.x * err.x * P.grad_scale, cw.y * err.y * P.grad_scale,
+                                      cw.z * err.z * P.grad_scale, cw.w * err.w * P.grad_scale);
+        const float3 dq = make_float3(au.x > 0.f ? dy.x / au.x : 0.f, au.y > 0.f ? dy.y / au.y : 0.f,
+                                      au.z > 0.f ? dy.z / au.z : 0.f);
+        const float3 dr = make_float3(dq.x * yv.x, dq.y * yv.y, dq.z * yv.z);
+        float g[49];
+        float sdot = 0.f;
+#pragma unroll
+        for (int k = 0; k < 49; ++k) {
+            const float4 sv = signal_tap(P.sig, P.G, has, img, x, y, k);
+            const float4 uv = signal_tap(P.uns, P.G, has, img, x, y, k);
+            g[k] = dy.w * sv.w + (dq.x * sv.x - dr.x * uv.x) + (dq.y * sv.y - dr.y * uv.y) + (dq.z * sv.z - dr.z * uv.z);
+            sdot += z[k] * g[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 64; k += 2) {
+            const float lo = k < 49 ? z[k] * (g[k] - sdot) : 0.0f;
+            const float hi = k + 1 < 49 ? z[k + 1] * (g[k + 1] - sdot) : 0.0f;
+            const uint32_t w = pack2(lo, hi);
+            *reinterpret_cast<uint32_t*>(dz + elem_offset(row, (uint32_t)k, 8)) = w;
+            const __nv_bfloat162 q = *reinterpret_cast<const __nv_bfloat162*>(&w);
+            if (k < 49) *reinterpret_cast<__nv_bfloat16*>(dzt + elem_offset((uint32_t)k, row, 16)) = q.x;
+            if (k + 1 < 49) *reinterpret_cast<__nv_bfloat16*>(dzt + elem_offset((uint32_t)k + 1, row, 16)) = q.y;
+        }
+        // ---- backward: dW_l += dZ_l^T [H_{l-1} | 1]^T and dH_{l-1} = dZ_l W_l, l = 4..2;
+        // dW_1 += dZ_1^T [X | 1]^T
+#pragma unroll
+        for (int l = 3; l >= 0; --l) {
+            tt_before_issue();
+            if (tid == 0) {
+                tc_mma(tmem + dw_col[l], dzt_addr, 16u, l == 0 ? xt_addr : ht_addr[l - 1], 16u, 8, tc_idesc(80),
+                       accumulated);
+                if (l > 0) tc_mma(tmem + kTtDH, dz_addr, 8u, wt[l - 1], 8u, 4, tc_idesc(64), false);
+            }
+            tt_commit_wait(bar, phase, failed, status);
+            if (l > 0) tt_dz_out(tl + kTtDH, mask[l - 1], l > 1 ? dz : nullptr, dzt, row);
+        }
+        accumulated = true;
     }
-    // ---- write this CTA's partial gradient in the FP32 parameter layout
+    // ---- this block's partial gradient: lanes 0..63 of the dW columns (rows = outputs)
     float* out = P.partial + (size_t)blockIdx.x * kParams;
+    const uint32_t tl = tmem + lane_off;
 #pragma unroll
-    for (int i = 0; i < kDwPerWarp; ++i) {
-        int id = warp + 8 * i;
-        if (id >= kDwTiles) break;
-        int l, mt, nt;
-        dw_tile(id, l, mt, nt);
+    for (int l = 0; l < 4; ++l) {
+        const int nin = l == 0 ? 72 : 64, nout = l == 3 ? 49 : 64;
+        const int ow = l == 0 ? oW1 : (l == 1 ? oW2 : (l == 2 ? oW3 : oW4));
+        const int ob = l == 0 ? ob1 : (l == 1 ? ob2 : (l == 2 ? ob3 : ob4));
+        for (int c0 = 0; c0 < 80; c0 += 16) {
+            float v[16];
+            tc_load16(tl + dw_col[l] + (uint32_t)c0, v);
+            if ((int)row < nout && accumulated) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            int row = mt * 16 + g + 8 * (j >> 1), col = nt * 8 + 2 * t + (j & 1);
-            int nin = l == 0 ? 72 : 64, nout = l == 3 ? 49 : 64;
-            int ow = l == 0 ? oW1 : (l == 1 ? oW2 : (l == 2 ? oW3 : oW4));
-            int ob = l == 0 ? ob1 : (l == 1 ? ob2 : (l == 2 ? ob3 : ob4));
-            if (row >= nout) continue;
-            if (col < nin) out[ow + row * nin + col] = dw[i][j];
-            else if (col == nin) out[ob + row] = dw[i][j];
+                for (int j = 0; j < 16; ++j) {
+                    const int c = c0 + j;
+                    if (c < nin) out[ow + (int)row * nin + c] = v[j];
+                    else if (c == nin) out[ob + (int)row] = v[j];
+                }
+            }
         }
     }
+    // loss of the block
+    loss += __shfl_xor_sync(0xFFFFFFFFu, loss, 1);
+    loss += __shfl_xor_sync(0xFFFFFFFFu, loss, 2);
     loss += __shfl_xor_sync(0xFFFFFFFFu, loss, 4);
     loss += __shfl_xor_sync(0xFFFFFFFFu, loss, 8);
     loss += __shfl_xor_sync(0xFFFFFFFFu, loss, 16);
-    __shared__ float s_loss[8];
-    if (lane == 0) s_loss[warp] = loss;
+    __shared__ float s_loss[4];
+    if ((tid & 31) == 0) s_loss[warp] = loss;
+    if (failed) tc_wait(bar, phase ^ 1u);
+    asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float s = 0.f;
-        for (int w = 0; w < 8; ++w) s += s_loss[w];
-        P.partial_loss[blockIdx.x] = s;
-    }
+    if (tid == 0) P.partial_loss[blockIdx.x] = s_loss[0] + s_loss[1] + s_loss[2] + s_loss[3];
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTtAlloc));
 }
 
 // Sums the per-CTA partials in CTA order (deterministic).
@@ -1041,8 +996,6 @@ static luz_status repack(luz_ctx* ctx, luz_denoiser* d) {
     return LUZ_OK;
 }
 
-static size_t train_smem() { return (size_t)pEnd * 2 + kBias * 4 + sizeof(TrainSmem); }
-
 static luz_status check_batch(luz_ctx* ctx, const luz_denoise_batch* b) {
     if (!b || !b->features || !b->lin_depth || !b->noisy || !b->unshadowed || b->width == 0 || b->height == 0 ||
         b->images == 0)
@@ -1086,12 +1039,6 @@ static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_bat
 
 static luz_status run_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b) {
     if (!b->target) return set_error(ctx, LUZ_ERR_INVALID, "training batch without targets");
-    static bool attr = false;
-    if (!attr) {
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)train_smem()));
-        attr = true;
-    }
     TrainParams P;
     P.wpack = d->pack;
     P.bias = d->bias;
@@ -1107,8 +1054,16 @@ static luz_status run_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_
     P.partial = d->partial;
     P.partial_loss = d->partial_loss;
     LUZ_CUDA(ctx, cudaMemsetAsync(d->partial, 0, (size_t)d->ctas * kParams * 4, ctx->stream));
-    denoise_train_kernel<<<d->ctas, 256, train_smem(), ctx->stream>>>(P);
-    LUZ_LAUNCHED(ctx, "denoise_train_kernel");
+    static bool tc_attr = false;
+    if (!tc_attr) {
+        LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           kTtSmem));
+        tc_attr = true;
+    }
+    prof_begin(ctx, LUZ_KERNEL_DENOISE_TRAIN);
+    denoise_train_tc_kernel<<<d->ctas, 128, kTtSmem, ctx->stream>>>(P, ctx->d_status);
+    prof_end(ctx);
+    LUZ_LAUNCHED(ctx, "denoise_train_tc_kernel");
     reduce_partials_kernel<<<(kParams + 255) / 256, 256, 0, ctx->stream>>>(d->partial, d->ctas, d->grad,
                                                                           d->partial_loss, d->loss);
     LUZ_LAUNCHED(ctx, "denoise_reduce_kernel");
