@@ -248,7 +248,8 @@ enum {
     LUZ_KERNEL_FEATURES = 5,    /* denoiser features                                 */
     LUZ_KERNEL_DENOISE = 6,     /* denoiser network + filter                         */
     LUZ_KERNEL_TAA = 7,
-    LUZ_KERNEL_DENOISE_TRAIN = 8 /* denoiser forward + backward + weight gradients    */
+    LUZ_KERNEL_DENOISE_TRAIN = 8, /* denoiser forward + backward + weight gradients   */
+    LUZ_KERNEL_BATCH_FRAME = 9  /* a batch frame in one persistent launch            */
 };
 luz_status luz_ctx_profile(luz_ctx* ctx, int32_t on);
 luz_status luz_ctx_profile_read(luz_ctx* ctx, int32_t kernel, float* total_ms, uint32_t* launches);
@@ -489,13 +490,22 @@ void* luz_frame_plane_device_ptr(luz_frame* frame, int32_t plane);
 
 /* ------------------------------------------------------------------ batches
  * Many independent scenes of uneven size as one unit (no counterpart in the
- * reference, which renders one scene per frame): every TLAS build and G-buffer pass,
- * ONE persistent visibility launch over the shadow/AO rays of all scenes, every light
- * pass. Scene constants and instances are uploaded / packed once at creation (the
- * arrays may be freed after luz_batch_create); luz_batch_capture records a render as
- * one CUDA graph that luz_batch_replay launches; luz_batch_autotune picks the
- * visibility launch shape (ray-batch refill size, steps between refills, CTAs per SM)
- * by timing the batch's own launch. */
+ * reference, which renders one scene per frame). A render runs, by default, ONE
+ * persistent launch (the frame kernel) over every scene: the per-frame TLAS builds,
+ * the clearing of the hit/miss planes, the G-buffer passes with their lit-pixel lists,
+ * the shadow/AO traversal of all scenes' rays from one work counter, and the light
+ * passes; work items are handed out by tickets and wait only on items handed out
+ * before them, each wait bounded (LUZ_DEV_BATCH_QUEUE when one gives up). The meshes'
+ * BLASes are built before, once, by luz_blas_build_batch (the reference builds them
+ * once at load, GPUScene.cpp:108-138). The frame kernel takes scenes of up to 4096
+ * instances and 688 lights; a batch with a larger scene renders staged (every TLAS
+ * build, G-buffer and light pass its own launch around one visibility launch over all
+ * scenes), which luz_batch_set_fused(ctx, b, 0) also selects. Both forms give the same
+ * planes bit for bit. Scene constants and instances are uploaded / packed once at
+ * creation (the arrays may be freed after luz_batch_create); luz_batch_capture records
+ * a render as one CUDA graph that luz_batch_replay launches; luz_batch_autotune picks
+ * the traversal launch shape (ray-batch refill size, steps between refills, CTAs per
+ * SM) by timing the batch's own launch. */
 typedef struct luz_batch luz_batch;
 typedef struct luz_batch_scene {
     const luz_instance* instances;
@@ -520,6 +530,11 @@ luz_status luz_batch_capture(luz_ctx* ctx, luz_batch* b, int32_t frame_index);
 luz_status luz_batch_replay(luz_ctx* ctx, luz_batch* b);
 luz_status luz_batch_autotune(luz_ctx* ctx, luz_batch* b, uint32_t reps, luz_vis_tuning* chosen,
                               float* best_ms);
+/* on = 1: renders run the frame kernel (LUZ_ERR_LIMIT when a scene does not fit it);
+ * on = 0: staged launches. Drops a captured graph. */
+luz_status luz_batch_set_fused(luz_ctx* ctx, luz_batch* b, int32_t on);
+/* 1 when the batch renders with the frame kernel. */
+int32_t luz_batch_fused(const luz_batch* b);
 
 /* ------------------------------------------------------------------ denoiser
  * Learned kernel-predicting denoiser of the 1-sample shadow and AO terms; no

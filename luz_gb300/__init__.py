@@ -531,7 +531,7 @@ class Context:
         return ms.value
 
     KERNELS = {"tlas_build": 0, "gbuffer": 1, "raygen": 2, "traversal": 3, "light_pass": 4, "features": 5,
-               "denoise": 6, "taa": 7, "denoise_train": 8}
+               "denoise": 6, "taa": 7, "denoise_train": 8, "batch_frame": 9}
 
     def profile(self, on: bool) -> None:
         """Per-kernel event timing of the instrumented kernels (on clears the records)."""
@@ -582,8 +582,10 @@ class _BorrowedFrame(Frame):
 
 class Batch:
     """Many scenes rendered as one unit (luz_batch_*): one batched BLAS build over the
-    meshes of every scene, then per render every TLAS and G-buffer, one visibility
-    launch for all scenes, every light pass; optionally as one CUDA graph."""
+    meshes of every scene at creation, then per render ONE persistent launch (the frame
+    kernel: every TLAS build, G-buffer, the traversal of all scenes' rays and every
+    light pass), or the staged launches (set_fused(False)); optionally as one CUDA
+    graph."""
 
     def __init__(self, ctx: "Context", scenes: list[HostScene]):
         self.ctx, self.scenes = ctx, scenes
@@ -633,6 +635,14 @@ class Batch:
 
     def replay(self) -> None:
         _check(lib.luz_batch_replay(self.ctx.handle, self._h), self.ctx.handle, "batch replay")
+
+    @property
+    def fused(self) -> bool:
+        """True when renders run the frame kernel."""
+        return bool(lib.luz_batch_fused(self._h))
+
+    def set_fused(self, on: bool) -> None:
+        _check(lib.luz_batch_set_fused(self.ctx.handle, self._h, 1 if on else 0), self.ctx.handle, "batch mode")
 
     def autotune(self, reps: int = 3):
         arr = (C.c_uint32 * 4)()

@@ -201,6 +201,8 @@ SIGNATURES = [
     ("luz_batch_capture", C.c_int32, [P, P, C.c_int32]),
     ("luz_batch_replay", C.c_int32, [P, P]),
     ("luz_batch_autotune", C.c_int32, [P, P, C.c_uint32, C.POINTER(C.c_uint32 * 4), C.POINTER(C.c_float)]),
+    ("luz_batch_set_fused", C.c_int32, [P, P, C.c_int32]),
+    ("luz_batch_fused", C.c_int32, [P]),
     ("luz_denoiser_create", C.c_int32, [P, C.c_uint64, C.POINTER(P)]),
     ("luz_denoiser_destroy", None, [P]),
     ("luz_denoiser_set_weights", C.c_int32, [P, P, c_float_p]),

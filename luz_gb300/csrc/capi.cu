@@ -19,7 +19,6 @@ luz_status frame_lit_count(luz_ctx* ctx, luz_frame* f, uint32_t* count);
 luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode);
 uint32_t lit_chunks(uint32_t width, uint32_t height);
 luz_status launch_ao_resolve(luz_ctx* ctx, luz_frame* f);
-luz_status upload_srgb_lut(luz_ctx* ctx, const float* lut);
 
 luz_status set_error(luz_ctx* ctx, luz_status st, const std::string& msg) {
     if (ctx) ctx->last_error = msg;
@@ -126,7 +125,9 @@ luz_status luz_ctx_create(int device, luz_ctx** out) {
     cudaMemset(ctx->d_status, 0, 4);
     float lut[256];
     for (int i = 0; i < 256; ++i) lut[i] = (float)std::pow((double)((float)i / 255.0f), 2.2);
-    if (upload_srgb_lut(ctx, lut) != LUZ_OK) return fail(LUZ_ERR_CUDA);
+    if (cudaMalloc(&ctx->d_srgb_lut, sizeof(lut)) != cudaSuccess) return fail(LUZ_ERR_OOM);
+    if (cudaMemcpy(ctx->d_srgb_lut, lut, sizeof(lut), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(LUZ_ERR_CUDA);
     // Default substitute blue noise: a flat mid-grey texel (callers upload the seeded one).
     uint8_t grey[4] = {128, 128, 128, 255};
     if (luz_ctx_set_blue_noise(ctx, grey, 1) != LUZ_OK) return fail(LUZ_ERR_CUDA);
@@ -139,6 +140,7 @@ void luz_ctx_destroy(luz_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_blue_noise) cudaFree(ctx->d_blue_noise);
+    if (ctx->d_srgb_lut) cudaFree(ctx->d_srgb_lut);
     if (ctx->d_scratch) cudaFree(ctx->d_scratch);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);

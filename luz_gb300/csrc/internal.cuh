@@ -112,6 +112,7 @@ struct luz_ctx {
     uint32_t* d_status = nullptr;        // device status word (LUZ_DEV_* bits)
     uint64_t launches = 0;
     uint8_t* d_blue_noise = nullptr;     // RGBA8 size*size
+    float* d_srgb_lut = nullptr;         // pow(i / 255, 2.2), i = 0..255 (albedo decode)
     uint32_t blue_noise_size = 0;
     // reusable scratch
     void* d_scratch = nullptr;

@@ -21,18 +21,11 @@
 #include <vector>
 
 #include "internal.cuh"
-#include "lbvh_kernels.cuh"
+#include "lbvh_device.cuh"
 
 namespace luz {
 
 // ---------------------------------------------------------------- helpers
-__device__ __forceinline__ uint32_t float_to_ordered(float f) {
-    uint32_t u = __float_as_uint(f);
-    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
-}
-__device__ __forceinline__ float ordered_to_float(uint32_t u) {
-    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
-}
 
 __device__ __forceinline__ int find_seg(const uint32_t* offs, int nseg, uint32_t g) {
     int lo = 0, hi = nseg - 1;
@@ -122,11 +115,6 @@ __global__ void __launch_bounds__(256) blas_bounds_kernel(const SegDesc* segs, c
     if (leader) flush();
 }
 
-__device__ __forceinline__ void decode_bounds(const uint32_t* b, V3& cmin, V3& ext) {
-    cmin = V3{ordered_to_float(b[0]), ordered_to_float(b[1]), ordered_to_float(b[2])};
-    V3 cmax = V3{ordered_to_float(b[3]), ordered_to_float(b[4]), ordered_to_float(b[5])};
-    ext = cmax - cmin;
-}
 
 __global__ void blas_morton_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                                    uint32_t total, const uint32_t* seg_bounds,
@@ -306,69 +294,8 @@ onesweep_pass_kernel(const unsigned long long* __restrict__ kin, const uint32_t*
 }
 
 // ---------------------------------------------------------------- Karras hierarchy
-__device__ __forceinline__ int kdelta(const unsigned long long* keys, int n, int i, int j) {
-    if (j < 0 || j >= n) return -1;
-    uint32_t ki = (uint32_t)keys[i] & 0x3FFFFFFFu, kj = (uint32_t)keys[j] & 0x3FFFFFFFu;
-    if (ki != kj) return __clz(ki ^ kj);
-    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
-}
 
-__device__ __forceinline__ void write_inverted_slot(float4* node, int slot) {
-    const float inf = __int_as_float(0x7f800000);
-    if (slot == 0) {
-        node[0] = make_float4(inf, -inf, inf, -inf);
-        node[2].x = inf; node[2].y = -inf;
-    } else {
-        node[1] = make_float4(inf, -inf, inf, -inf);
-        node[2].z = inf; node[2].w = -inf;
-    }
-}
 
-// seg_node_off: first internal node of each segment (global); sorted keys per segment
-// start at seg_prim_off. node_parent / leaf_parent: (local parent << 1) | side.
-// Internal node i of segment sd.
-__device__ __forceinline__ void karras_node(const SegDesc& sd, int i, const unsigned long long* keys,
-                                            uint32_t* node_parent, uint32_t* leaf_parent, uint32_t* dev_status) {
-    int n = (int)sd.prim_count;
-    float4* node = sd.nodes + (size_t)i * kNodeF4;
-    if (n <= 1) {
-        // Single node: child0 = leaf 0 (if any), child1 = empty.
-        write_inverted_slot(node, 0);
-        write_inverted_slot(node, 1);
-        int c0 = n == 1 ? ~0 : kEmptyChild;
-        node[3] = make_float4(__int_as_float(c0), __int_as_float(kEmptyChild), 0.f, 0.f);
-        if (n == 1) leaf_parent[sd.prim_off] = 0u;
-        node_parent[sd.node_off] = 0xFFFFFFFFu;
-        return;
-    }
-    const unsigned long long* k = keys + sd.prim_off;
-    int d = (kdelta(k, n, i, i + 1) - kdelta(k, n, i, i - 1)) >= 0 ? 1 : -1;
-    int dmin = kdelta(k, n, i, i - d);
-    int lmax = 2;
-    int guard = 0;
-    while (kdelta(k, n, i, i + lmax * d) > dmin) {
-        lmax <<= 1;
-        if (++guard > 40) { atomicOr(dev_status, (uint32_t)LUZ_DEV_KARRAS_RANGE); return; }
-    }
-    int l = 0;
-    for (int t = lmax >> 1; t >= 1; t >>= 1)
-        if (kdelta(k, n, i, i + (l + t) * d) > dmin) l += t;
-    int j = i + l * d;
-    int dnode = kdelta(k, n, i, j);
-    int split = 0, step = l;
-    do {
-        step = (step + 1) >> 1;
-        if (kdelta(k, n, i, i + (split + step) * d) > dnode) split += step;
-    } while (step > 1);
-    int gamma = i + split * d + min(d, 0);
-    int lo = min(i, j), hi = max(i, j);
-    int c0, c1;
-    if (lo == gamma) { c0 = ~gamma; leaf_parent[sd.prim_off + gamma] = ((uint32_t)i << 1) | 0u; }
-    else { c0 = gamma; node_parent[sd.node_off + gamma] = ((uint32_t)i << 1) | 0u; }
-    if (hi == gamma + 1) { c1 = ~(gamma + 1); leaf_parent[sd.prim_off + gamma + 1] = ((uint32_t)i << 1) | 1u; }
-    else { c1 = gamma + 1; node_parent[sd.node_off + gamma + 1] = ((uint32_t)i << 1) | 1u; }
-    node[3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
-}
 
 __global__ void karras_kernel(const SegDesc* segs, const uint32_t* seg_node_off, int nseg,
                               uint32_t total_nodes, const unsigned long long* keys,
@@ -407,43 +334,7 @@ __global__ void blas_emit_kernel(const SegDesc* segs, const uint32_t* seg_prim_o
     leaf_box[2 * g + 1] = make_float4(hi.x + px, hi.y + py, hi.z + pz, 0.f);
 }
 
-__device__ __forceinline__ void write_slot(float4* node, int slot, float4 lo, float4 hi) {
-    if (slot == 0) {
-        node[0] = make_float4(lo.x, hi.x, lo.y, hi.y);
-        node[2].x = lo.z; node[2].y = hi.z;
-    } else {
-        node[1] = make_float4(lo.x, hi.x, lo.y, hi.y);
-        node[2].z = lo.z; node[2].w = hi.z;
-    }
-}
 
-// Leaf g (global index) of segment sd: writes its box into its parent and climbs
-// while it is the second child to arrive. kBlock: every leaf of the tree is handled
-// by one CTA, so block-scope fences order the node writes.
-template <bool kBlock>
-__device__ __forceinline__ void refit_leaf(const SegDesc& sd, uint32_t g, const float4* leaf_box,
-                                           const uint32_t* node_parent, const uint32_t* leaf_parent,
-                                           uint32_t* flags) {
-    float4 lo = leaf_box[2 * g], hi = leaf_box[2 * g + 1];
-    uint32_t p = leaf_parent[g];
-    const uint32_t node_count = sd.prim_count > 1 ? sd.prim_count - 1 : 1;
-    // Depth is bounded by the node count; the loop always ends at the root.
-    for (uint32_t guard = 0; guard <= sd.prim_count + 1; ++guard) {
-        uint32_t local = p >> 1;
-        if (p == 0xFFFFFFFFu || local >= node_count) return;
-        float4* node = sd.nodes + (size_t)local * kNodeF4;
-        write_slot(node, p & 1, lo, hi);
-        if (kBlock) __threadfence_block(); else __threadfence();
-        uint32_t old = atomicAdd(flags + sd.node_off + local, 1u);
-        if (old == 0) return;
-        if (kBlock) __threadfence_block(); else __threadfence();
-        float4 n0 = __ldcg(node + 0), n1 = __ldcg(node + 1), n2 = __ldcg(node + 2);
-        lo = make_float4(fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z), 0.f);
-        hi = make_float4(fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w), 0.f);
-        p = node_parent[sd.node_off + local];
-        if (p == 0xFFFFFFFFu) return;
-    }
-}
 
 __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                              uint32_t total, const float4* leaf_box, const uint32_t* node_parent,
@@ -455,12 +346,6 @@ __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, 
 }
 
 // ---------------------------------------------------------------- bounding sphere
-// Centre of a BLAS's root box (the union of the root node's two slots).
-__device__ __forceinline__ V3 root_centre(float4 n0, float4 n1, float4 n2) {
-    V3 lo = V3{fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z)};
-    V3 hi = V3{fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w)};
-    return V3{(lo.x + hi.x) * 0.5f + 0.0f, (lo.y + hi.y) * 0.5f + 0.0f, (lo.z + hi.z) * 0.5f + 0.0f};
-}
 
 // Bounding sphere of every BLAS about its root box centre: the largest squared
 // distance of a triangle vertex from the centre, kept as float bits in the root
@@ -584,38 +469,8 @@ __global__ void __launch_bounds__(256) chunk_apply_kernel(const uint32_t* in, ui
     }
 }
 
-struct Slot4 {
-    float lx[4], hx[4], ly[4], hy[4], lz[4], hz[4];
-    int ch[4];
-    int k;
-};
 
-__device__ __forceinline__ void slot4_put(Slot4& s, const float4* n2, int side, int child) {
-    float4 a = n2[side], z = n2[2];
-    s.lx[s.k] = a.x; s.hx[s.k] = a.y; s.ly[s.k] = a.z; s.hy[s.k] = a.w;
-    s.lz[s.k] = side ? z.z : z.x;
-    s.hz[s.k] = side ? z.w : z.y;
-    s.ch[s.k] = child;
-    ++s.k;
-}
 
-__device__ __forceinline__ void slot4_store(Slot4& s, float4* out) {
-    const float inf = __int_as_float(0x7f800000);
-    for (; s.k < 4; ++s.k) {
-        s.lx[s.k] = s.ly[s.k] = s.lz[s.k] = inf;
-        s.hx[s.k] = s.hy[s.k] = s.hz[s.k] = -inf;
-        s.ch[s.k] = kEmptyChild;
-    }
-    out[0] = make_float4(s.lx[0], s.lx[1], s.lx[2], s.lx[3]);
-    out[1] = make_float4(s.hx[0], s.hx[1], s.hx[2], s.hx[3]);
-    out[2] = make_float4(s.ly[0], s.ly[1], s.ly[2], s.ly[3]);
-    out[3] = make_float4(s.hy[0], s.hy[1], s.hy[2], s.hy[3]);
-    out[4] = make_float4(s.lz[0], s.lz[1], s.lz[2], s.lz[3]);
-    out[5] = make_float4(s.hz[0], s.hz[1], s.hz[2], s.hz[3]);
-    out[6] = make_float4(__int_as_float(s.ch[0]), __int_as_float(s.ch[1]), __int_as_float(s.ch[2]),
-                         __int_as_float(s.ch[3]));
-    out[7] = make_float4(0.f, 0.f, 0.f, 0.f);
-}
 
 // idx4[q]: exclusive prefix of the even-depth flags over all segments' nodes.
 __global__ void bvh4_emit_kernel(const SegDesc* segs, const uint32_t* seg_node_off, int nseg, uint32_t total_nodes,
@@ -645,50 +500,6 @@ __global__ void bvh4_emit_kernel(const SegDesc* segs, const uint32_t* seg_node_o
     slot4_store(s4, sd.nodes4 + (size_t)(idx4[q] - base4) * kNode4F4);
 }
 
-// TLAS: the binary tree is in breadth-first order with level table
-// levels = {L, start_0, ..., start_L}; the 4-wide nodes are the even levels, in order.
-__device__ __forceinline__ void tlas_bvh4_block(const float4* nodes, uint32_t m, const uint32_t* levels,
-                                                float4* nodes4) {
-    __shared__ uint32_t s_start[66], s_even[66];
-    __shared__ uint32_t s_levels;
-    if (threadIdx.x == 0) {
-        uint32_t L = min(levels[0], 64u);
-        s_levels = L;
-        uint32_t acc = 0;
-        for (uint32_t l = 0; l <= L; ++l) s_start[l] = levels[1 + l];
-        for (uint32_t l = 0; l < L; ++l) {
-            s_even[l] = acc;
-            if ((l & 1u) == 0) acc += s_start[l + 1] - s_start[l];
-        }
-    }
-    __syncthreads();
-    const uint32_t L = s_levels;
-    for (uint32_t b = threadIdx.x; b < m; b += blockDim.x) {
-        uint32_t l = 0;
-        while (l + 1 < L && s_start[l + 1] <= b) ++l;
-        if (l & 1u) continue;
-        const float4* n2 = nodes + (size_t)b * kNodeF4;
-        float4 n3 = n2[3];
-        int c[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
-        Slot4 s4;
-        s4.k = 0;
-        for (int side = 0; side < 2; ++side) {
-            if (c[side] < 0) {
-                slot4_put(s4, n2, side, c[side]);
-                continue;
-            }
-            const float4* mm = nodes + (size_t)c[side] * kNodeF4;
-            float4 m3 = mm[3];
-            int g[2] = {__float_as_int(m3.x), __float_as_int(m3.y)};
-            for (int s2 = 0; s2 < 2; ++s2) {
-                int ref = g[s2];
-                if (ref >= 0 && l + 2 < L) ref = (int)(s_even[l + 2] + ((uint32_t)ref - s_start[l + 2]));
-                slot4_put(s4, mm, s2, ref);
-            }
-        }
-        slot4_store(s4, nodes4 + (size_t)(s_even[l] + (b - s_start[l])) * kNode4F4);
-    }
-}
 
 __global__ void __launch_bounds__(1024) tlas_bvh4_kernel(const float4* nodes, uint32_t m, const uint32_t* levels,
                                                          float4* nodes4) {
@@ -696,55 +507,6 @@ __global__ void __launch_bounds__(1024) tlas_bvh4_kernel(const float4* nodes, ui
 }
 
 // ---------------------------------------------------------------- TLAS
-// Instance i: shading record, padded world box; returns false when the box centre
-// is not finite (no contribution to the Morton bounds).
-__device__ __forceinline__ bool tlas_instance_one(const DevInstanceInput* in, uint32_t i, float4* inst_box,
-                                                  DevShadeInstance* shade, V3& c) {
-    const DevInstanceInput ii = in[i];
-    float w2o[12];
-    affine_inverse(ii.o2w, w2o);
-    DevShadeInstance sh;
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) sh.normal_mat[r * 3 + c] = w2o[c * 4 + r];
-    sh.pad0 = 0.f;
-    sh.vertices = ii.vertices;
-    sh.indices = ii.indices;
-    shade[i] = sh;
-    const float inf = __int_as_float(0x7f800000);
-    V3 wlo = V3{inf, inf, inf}, whi = V3{-inf, -inf, -inf};
-    if (ii.blas_prims > 0) {
-        float4 n0 = ii.nodes[0], n1 = ii.nodes[1], n2 = ii.nodes[2];
-        V3 lo = V3{fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z)};
-        V3 hi = V3{fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w)};
-        for (int c = 0; c < 8; ++c) {
-            V3 p = V3{(c & 1) ? hi.x : lo.x, (c & 2) ? hi.y : lo.y, (c & 4) ? hi.z : lo.z};
-            V3 w = xform_point(ii.o2w, p);
-            wlo = V3{fmin_(wlo.x, w.x), fmin_(wlo.y, w.y), fmin_(wlo.z, w.z)};
-            whi = V3{fmax_(whi.x, w.x), fmax_(whi.y, w.y), fmax_(whi.z, w.z)};
-        }
-        // Clip with the axis box of the transformed bounding sphere: an ellipsoid
-        // c' + M u (|u| <= r) reaches r * |row_a(M)| from its centre along world axis a.
-        uint32_t r2 = __float_as_uint(ii.nodes[3].z);
-        if (r2 < 0x7F800000u) {
-            V3 c = root_centre(n0, n1, n2);
-            V3 cw = xform_point(ii.o2w, c);
-            float r = sqrtf(__uint_as_float(r2));
-            const float* m = ii.o2w;
-            float ex = r * sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
-            float ey = r * sqrtf(m[4] * m[4] + m[5] * m[5] + m[6] * m[6]);
-            float ez = r * sqrtf(m[8] * m[8] + m[9] * m[9] + m[10] * m[10]);
-            wlo = V3{fmax_(wlo.x, cw.x - ex), fmax_(wlo.y, cw.y - ey), fmax_(wlo.z, cw.z - ez)};
-            whi = V3{fmin_(whi.x, cw.x + ex), fmin_(whi.y, cw.y + ey), fmin_(whi.z, cw.z + ez)};
-        }
-        float px = box_pad(wlo.x, whi.x), py = box_pad(wlo.y, whi.y), pz = box_pad(wlo.z, whi.z);
-        wlo = V3{wlo.x - px, wlo.y - py, wlo.z - pz};
-        whi = V3{whi.x + px, whi.y + py, whi.z + pz};
-    }
-    inst_box[2 * i] = make_float4(wlo.x, wlo.y, wlo.z, 0.f);
-    inst_box[2 * i + 1] = make_float4(whi.x, whi.y, whi.z, 0.f);
-    c = V3{(wlo.x + whi.x) * 0.5f + 0.0f, (wlo.y + whi.y) * 0.5f + 0.0f, (wlo.z + whi.z) * 0.5f + 0.0f};
-    return finite3(c);
-}
 
 __global__ void tlas_instance_kernel(const DevInstanceInput* in, uint32_t n, float4* inst_box,
                                      DevShadeInstance* shade, uint32_t* seg_bounds) {
@@ -779,27 +541,6 @@ __global__ void tlas_morton_kernel(const float4* inst_box, uint32_t n, const uin
     vals[i] = i;
 }
 
-// Leaf j of the sorted order: instance record, leaf box, sorted Morton key and order.
-__device__ __forceinline__ void tlas_emit_one(const DevInstanceInput* in, const float4* inst_box, uint32_t j,
-                                              unsigned long long key, uint32_t i, DevInstance* inst_out,
-                                              float4* leaf_box, uint32_t* morton_out, uint32_t* order_out) {
-    morton_out[j] = (uint32_t)key & 0x3FFFFFFFu;
-    order_out[j] = i;
-    const DevInstanceInput ii = in[i];
-    DevInstance d;
-    affine_inverse(ii.o2w, d.w2o);
-    d.nodes = ii.nodes;
-    d.nodes4 = ii.nodes4;
-    d.pad = nullptr;
-    d.tris = ii.tris;
-    d.custom_index = ii.custom_index;
-    d.mask = ii.mask;
-    d.input_index = i;
-    d.blas_prims = ii.blas_prims;
-    inst_out[j] = d;
-    leaf_box[2 * j] = inst_box[2 * i];
-    leaf_box[2 * j + 1] = inst_box[2 * i + 1];
-}
 
 __global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_box, uint32_t n,
                                  const unsigned long long* keys, const uint32_t* vals,
@@ -811,83 +552,6 @@ __global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_
 }
 
 
-// Breadth-first relayout of one tree (single block of 1024 threads). Children of a
-// level keep their parents' order, left before right.
-__device__ __forceinline__ void bfs_relayout_block(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
-                                                   uint32_t* newidx, uint32_t* levels) {
-    __shared__ uint32_t s_warp[32];
-    __shared__ uint32_t s_carry;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) { queue[0] = 0; newidx[0] = 0; s_carry = 0; }
-    __syncthreads();
-    uint32_t head = 0, tail = 1, level = 0;
-    while (head < tail && tail <= m) {
-        uint32_t level_end = tail;
-        // level table {L, start_0, ..., start_L} (depth is far below 64 for a TLAS)
-        if (tid == 0 && level < 64) levels[1 + level] = head;
-        ++level;
-        for (uint32_t base = head; base < level_end; base += 1024) {
-            uint32_t q = base + tid;
-            int c0 = 0, c1 = 0;
-            uint32_t cnt = 0;
-            if (q < level_end) {
-                uint32_t old = queue[q];
-                float4 n3 = src[(size_t)old * kNodeF4 + 3];
-                c0 = __float_as_int(n3.x);
-                c1 = __float_as_int(n3.y);
-                cnt = (c0 >= 0) + (c1 >= 0);
-            }
-            // block exclusive scan of cnt
-            uint32_t x = cnt;
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-                if (lane >= o) x += y;
-            }
-            if (lane == 31) s_warp[warp] = x;
-            __syncthreads();
-            uint32_t wpre = 0, total = 0;
-            for (int w = 0; w < 32; ++w) {
-                uint32_t t = s_warp[w];
-                if (w < warp) wpre += t;
-                total += t;
-            }
-            uint32_t pos = tail + s_carry + wpre + x - cnt;
-            if (q < level_end) {
-                // A tree has exactly m nodes: positions and child indices stay below m.
-                if (c0 >= 0) {
-                    if (pos < m && (uint32_t)c0 < m) { queue[pos] = (uint32_t)c0; newidx[c0] = pos; }
-                    ++pos;
-                }
-                if (c1 >= 0 && pos < m && (uint32_t)c1 < m) { queue[pos] = (uint32_t)c1; newidx[c1] = pos; }
-            }
-            __syncthreads();
-            if (tid == 0) s_carry += total;
-            __syncthreads();
-        }
-        head = level_end;
-        tail = level_end + s_carry;
-        __syncthreads();
-        if (tid == 0) s_carry = 0;
-        __syncthreads();
-    }
-    if (tid == 0) {
-        uint32_t L = level < 64 ? level : 64;
-        levels[0] = L;
-        levels[1 + L] = tail;
-    }
-    for (uint32_t old = tid; old < m; old += 1024) {
-        const float4* s = src + (size_t)old * kNodeF4;
-        float4* d = dst + (size_t)newidx[old] * kNodeF4;
-        float4 n3 = s[3];
-        int c0 = __float_as_int(n3.x), c1 = __float_as_int(n3.y);
-        if (c0 >= 0) c0 = (int)newidx[c0];
-        if (c1 >= 0) c1 = (int)newidx[c1];
-        d[0] = s[0];
-        d[1] = s[1];
-        d[2] = s[2];
-        d[3] = make_float4(__int_as_float(c0), __int_as_float(c1), 0.f, 0.f);
-    }
-}
 
 __global__ void __launch_bounds__(1024)
 bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
@@ -895,85 +559,11 @@ bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
     bfs_relayout_block(src, dst, m, queue, newidx, levels);
 }
 
-// The whole TLAS build in one CTA of 1024 threads for up to kFusedTlasMax instances
-// (the per-frame rebuild of GPUScene::UpdateResourcesGPU is otherwise a chain of ten
-// small launches): instance boxes and Morton bounds, Morton keys sorted with their
-// index in shared memory (bitonic network; the (key, index) order is the stable
-// order the radix sort gives), Karras hierarchy, leaves, refit, breadth-first
-// relayout and 4-wide collapse, separated by block barriers. Same results as the
-// multi-kernel path, bit for bit.
-constexpr uint32_t kFusedTlasMax = 4096;
-__global__ void __launch_bounds__(1024)
-tlas_fused_kernel(const DevInstanceInput* __restrict__ in, uint32_t n, float4* inst_box, DevShadeInstance* shade,
-                  unsigned long long* keys, uint32_t* vals, float4* karras_nodes, uint32_t* node_parent,
-                  uint32_t* leaf_parent, uint32_t* flags, DevInstance* inst_out, float4* leaf_box,
-                  uint32_t* morton_out, uint32_t* order_out, float4* nodes_out, uint32_t* queue, uint32_t* newidx,
-                  uint32_t* levels, float4* nodes4, uint32_t* dev_status) {
+// The TLAS build of tlas_build_block as one CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) tlas_fused_kernel(TlasBuildArgs A, uint32_t* dev_status) {
     __shared__ unsigned long long s_keys[kFusedTlasMax];
     __shared__ uint32_t s_bounds[6];
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    const uint32_t m = max(n, 2u) - 1;
-    if (tid < 6) s_bounds[tid] = tid < 3 ? 0xFFFFFFFFu : 0u;
-    for (uint32_t q = tid; q < m; q += nt) { node_parent[q] = 0xFFFFFFFFu; flags[q] = 0u; }
-    for (uint32_t g = tid; g < n; g += nt) leaf_parent[g] = 0xFFFFFFFFu;
-    __syncthreads();
-    for (uint32_t i = tid; i < n; i += nt) {
-        V3 c;
-        if (!tlas_instance_one(in, i, inst_box, shade, c)) continue;
-        atomicMin(s_bounds + 0, float_to_ordered(c.x));
-        atomicMin(s_bounds + 1, float_to_ordered(c.y));
-        atomicMin(s_bounds + 2, float_to_ordered(c.z));
-        atomicMax(s_bounds + 3, float_to_ordered(c.x));
-        atomicMax(s_bounds + 4, float_to_ordered(c.y));
-        atomicMax(s_bounds + 5, float_to_ordered(c.z));
-    }
-    __syncthreads();
-    uint32_t P = 1;
-    while (P < n) P <<= 1;
-    {
-        V3 cmin, ext;
-        decode_bounds(s_bounds, cmin, ext);
-        for (uint32_t i = tid; i < P; i += nt) {
-            if (i < n) {
-                const float4 l = inst_box[2 * i], h = inst_box[2 * i + 1];
-                const unsigned long long key = morton30(V3{l.x, l.y, l.z}, V3{h.x, h.y, h.z}, cmin, ext);
-                s_keys[i] = (key << 32) | i;
-            } else {
-                s_keys[i] = ~0ull;
-            }
-        }
-    }
-    __syncthreads();
-    for (uint32_t k = 2; k <= P; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = tid; i < P; i += nt) {
-                const uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    const unsigned long long a = s_keys[i], b = s_keys[ixj];
-                    if ((a > b) == ((i & k) == 0)) { s_keys[i] = b; s_keys[ixj] = a; }
-                }
-            }
-            __syncthreads();
-        }
-    }
-    for (uint32_t j = tid; j < n; j += nt) {
-        keys[j] = s_keys[j] >> 32;
-        vals[j] = (uint32_t)s_keys[j];
-    }
-    __syncthreads();
-    SegDesc sd{};
-    sd.prim_count = n;
-    sd.nodes = karras_nodes;
-    for (uint32_t q = tid; q < m; q += nt) karras_node(sd, (int)q, keys, node_parent, leaf_parent, dev_status);
-    __syncthreads();
-    for (uint32_t j = tid; j < n; j += nt)
-        tlas_emit_one(in, inst_box, j, keys[j], vals[j], inst_out, leaf_box, morton_out, order_out);
-    __syncthreads();
-    for (uint32_t g = tid; g < n; g += nt) refit_leaf<true>(sd, g, leaf_box, node_parent, leaf_parent, flags);
-    __syncthreads();
-    bfs_relayout_block(karras_nodes, nodes_out, m, queue, newidx, levels);
-    __syncthreads();
-    tlas_bvh4_block(nodes_out, m, levels, nodes4);
+    tlas_build_block(A, s_keys, s_bounds, dev_status);
 }
 
 // ---------------------------------------------------------------- host drivers
@@ -1305,6 +895,49 @@ luz_status build_tlas(luz_ctx* ctx, luz_tlas* t, const luz_instance* inst, uint3
     return launch_tlas_build(ctx, t);
 }
 
+// The TLAS's scratch buffer (t->tmp) carved for a build of up to max_instances.
+struct TlasScratch {
+    TlasBuildArgs a;
+    uint32_t* bounds;
+    SortBuffers sb;
+    SegDesc* d_seg;
+    uint32_t* d_zero;
+};
+
+static TlasScratch carve_tlas(luz_tlas* t) {
+    TlasScratch s;
+    uint32_t cap = std::max(t->max_instances, 1u);
+    uint32_t mcap = std::max(cap, 2u) - 1;
+    char* p = (char*)t->tmp;
+    TlasBuildArgs& a = s.a;
+    a.in = t->d_input;
+    a.n = t->count;
+    a.shade = t->shade;
+    a.inst_box = (float4*)p; p += align256((size_t)cap * 32);
+    s.bounds = (uint32_t*)p; p += align256(24);
+    p = carve_sort(p, cap, 4, s.sb);
+    a.keys = s.sb.keys[0];
+    a.vals = s.sb.vals[0];
+    a.leaf_box = (float4*)p; p += align256((size_t)cap * 32);
+    a.node_parent = (uint32_t*)p; p += align256((size_t)mcap * 4);
+    a.leaf_parent = (uint32_t*)p; p += align256((size_t)cap * 4);
+    a.flags = (uint32_t*)p; p += align256((size_t)mcap * 4);
+    a.karras_nodes = (float4*)p; p += align256((size_t)mcap * 64);
+    a.queue = (uint32_t*)p; p += align256((size_t)mcap * 4);
+    a.newidx = (uint32_t*)p; p += align256((size_t)mcap * 4);
+    s.d_seg = (SegDesc*)p; p += align256(sizeof(SegDesc));
+    s.d_zero = (uint32_t*)p; p += align256(4);
+    a.inst_out = t->instances;
+    a.morton_out = t->morton;
+    a.order_out = t->order;
+    a.nodes_out = t->nodes;
+    a.levels = t->levels;
+    a.nodes4 = t->nodes4;
+    return s;
+}
+
+TlasBuildArgs tlas_build_args(luz_tlas* t) { return carve_tlas(t).a; }
+
 // Device part of a TLAS build from the packed staging buffer: one host-to-device copy
 // from pinned memory and the LBVH kernels; no host synchronisation (graph-capturable).
 luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t) {
@@ -1313,29 +946,25 @@ luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t) {
     if (n == 0) return LUZ_OK;
     LUZ_CUDA(ctx, cudaMemcpyAsync(t->d_input, t->h_input, (size_t)n * sizeof(DevInstanceInput),
                                   cudaMemcpyHostToDevice, st));
-    uint32_t cap = std::max(t->max_instances, 1u);
-    uint32_t mcap = std::max(cap, 2u) - 1;
-    uint32_t m = std::max(n, 2u) - 1;
-    char* p = (char*)t->tmp;
-    float4* inst_box = (float4*)p; p += align256((size_t)cap * 32);
-    uint32_t* bounds = (uint32_t*)p; p += align256(24);
-    SortBuffers sb;
-    p = carve_sort(p, cap, 4, sb);
-    float4* leaf_box = (float4*)p; p += align256((size_t)cap * 32);
-    uint32_t* node_parent = (uint32_t*)p; p += align256((size_t)mcap * 4);
-    uint32_t* leaf_parent = (uint32_t*)p; p += align256((size_t)cap * 4);
-    uint32_t* flags = (uint32_t*)p; p += align256((size_t)mcap * 4);
-    float4* karras_nodes = (float4*)p; p += align256((size_t)mcap * 64);
-    uint32_t* queue = (uint32_t*)p; p += align256((size_t)mcap * 4);
-    uint32_t* newidx = (uint32_t*)p; p += align256((size_t)mcap * 4);
-    SegDesc* d_seg = (SegDesc*)p; p += align256(sizeof(SegDesc));
-    uint32_t* d_zero = (uint32_t*)p; p += align256(4);
+    const uint32_t m = std::max(n, 2u) - 1;
+    TlasScratch ts = carve_tlas(t);
+    const TlasBuildArgs& A = ts.a;
+    float4* inst_box = A.inst_box;
+    uint32_t* bounds = ts.bounds;
+    SortBuffers& sb = ts.sb;
+    float4* leaf_box = A.leaf_box;
+    uint32_t* node_parent = A.node_parent;
+    uint32_t* leaf_parent = A.leaf_parent;
+    uint32_t* flags = A.flags;
+    float4* karras_nodes = A.karras_nodes;
+    uint32_t* queue = A.queue;
+    uint32_t* newidx = A.newidx;
+    SegDesc* d_seg = ts.d_seg;
+    uint32_t* d_zero = ts.d_zero;
 
     if (n <= kFusedTlasMax) {
         prof_begin(ctx, LUZ_KERNEL_TLAS_BUILD);
-        tlas_fused_kernel<<<1, 1024, 0, st>>>(t->d_input, n, inst_box, t->shade, sb.keys[0], sb.vals[0], karras_nodes,
-                                              node_parent, leaf_parent, flags, t->instances, leaf_box, t->morton,
-                                              t->order, t->nodes, queue, newidx, t->levels, t->nodes4, ctx->d_status);
+        tlas_fused_kernel<<<1, 1024, 0, st>>>(A, ctx->d_status);
         prof_end(ctx);
         LUZ_LAUNCHED(ctx, "tlas_fused_kernel");
         return LUZ_OK;

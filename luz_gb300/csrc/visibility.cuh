@@ -35,6 +35,8 @@ struct VisCommon {
 
 // The context's visibility launch shape (the library defaults until one is set).
 const VisTuning& vis_tuning(const luz_ctx* ctx);
+// Launch-independent inputs of the visibility kernels (blue noise, status word, shape).
+VisCommon make_vis_common(luz_ctx* ctx, unsigned long long* work_counter);
 SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index);
 luz_status clear_visibility(luz_ctx* ctx, luz_frame* f);
 luz_status launch_visibility_batch(luz_ctx* ctx, const SceneVis* d_scenes, uint32_t n,
