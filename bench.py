@@ -646,9 +646,10 @@ def run_ours(args, rank, world, local):
                         "the kernel is issue-bound (about 73 % of issue slots, half the lanes active)",
                 "per_ray": {k: stats[k] / max(stats["rays"], 1) for k in
                             ("tlas_nodes", "blas_nodes", "tris", "instances")}}
-    # the light pass against HBM: per lit pixel the 32-B surface record, albedo /
-    # material / emission (12 B), its shadow and AO bits and the 16-B RGBA32F result
-    lp_bytes = lit * (32 + 12 + 16 + S / 8.0)
+    # the light pass against HBM: per lit pixel the 32-B surface record, the 16-B record of
+    # its albedo / material / emission words, its shadow and AO bits and the 16-B
+    # RGBA32F result
+    lp_bytes = lit * (32 + 16 + 16 + S / 8.0)
     lp_ms = kernel_ms["light_pass"]["ms_per_launch"]
     light_pass = {"bound": "hbm", "achieved": lp_bytes / (lp_ms * 1e-3) / 1e9, "peak": peak,
                   "peak_source": peak_kind, "unit": "GB/s", "algorithmic_bytes": lp_bytes, "ms_per_launch": lp_ms}

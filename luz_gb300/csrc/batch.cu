@@ -43,6 +43,7 @@ struct FrameScene {
     LightParams lp;          // plain light pass
     uint32_t* lit_count;
     float4* surf;            // compacted lit pixels (fragPos, pixel), (N, x | y << 16)
+    uint4* surf_mat;         // beside them: (albedo, material, emission, pixel)
     float ambient[4];        // ambientLightColor, ambientLightIntensity
     uint32_t tiles_x;        // 16x16 G-buffer tiles per row
 };
@@ -155,7 +156,7 @@ __device__ __noinline__ void publish_offsets(const FrameArgs& A) {
 // scene's list keep the 4x4-patch order the traversal's warps like. Writes every
 // G-buffer plane, the background colour of light.frag:178-181 at the unlit pixels, and
 // appends the lit pixels (length(N) != 0, light.frag:178) with their DepthToWorld
-// position (light.frag:186) to the list; the list's order between tiles is the order
+// position (light.frag:186) and G-buffer words to the list; the list's order between tiles is the order
 // the tiles finish, and no output depends on it.
 __device__ __noinline__ void frame_gbuffer_item(const FrameScene& F, uint32_t k, uint32_t* s_tmp,
                                                 uint32_t* s_base) {
@@ -166,8 +167,9 @@ __device__ __noinline__ void frame_gbuffer_item(const FrameScene& F, uint32_t k,
     const uint32_t y = ty * kFrameTile + (sub >> 2) * 4u + (w >> 2);
     const uint32_t width = F.gb.width, height = F.gb.height;
     const bool inside = x < width && y < height;
-    float4 nd = make_float4(0.f, 0.f, 0.f, 1.f);
-    if (inside) nd = gbuffer_pixel(F.gb, x, y);
+    GbufPixel gp{make_float4(0.f, 0.f, 0.f, 1.f), 0u, 0u, 0u};
+    if (inside) gp = gbuffer_pixel(F.gb, x, y);
+    const float4 nd = gp.nd;
     const bool lit = inside && !(length(V3{nd.x, nd.y, nd.z}) == 0.0f);
     const uint32_t rank = block_excl(lit ? 1u : 0u, s_tmp);
     if (tid == 0) {
@@ -184,6 +186,7 @@ __device__ __noinline__ void frame_gbuffer_item(const FrameScene& F, uint32_t k,
                                     nd.w);
         F.surf[2 * (size_t)pos] = make_float4(p.x, p.y, p.z, __uint_as_float(pix));
         F.surf[2 * (size_t)pos + 1] = make_float4(nd.x, nd.y, nd.z, __uint_as_float(x | (y << 16)));
+        F.surf_mat[pos] = make_uint4(gp.albedo, gp.material, gp.emission, pix);
     } else {
         const V3 c = V3{F.ambient[0], F.ambient[1], F.ambient[2]} * F.ambient[3];
         F.lp.out[pix] = make_float4(c.x, c.y, c.z, 1.0f);
@@ -457,6 +460,7 @@ static luz_status setup_frame_kernel(luz_ctx* ctx, luz_batch* b) {
         F.lp = make_light_params(ctx, f);
         F.lit_count = f->lit_count;
         F.surf = f->surf;
+        F.surf_mat = f->surf_mat;
         memcpy(F.ambient, f->h_scene.ambient_light_color, 12);
         F.ambient[3] = f->h_scene.ambient_light_intensity;
         F.tiles_x = (f->width + kFrameTile - 1) / kFrameTile;

@@ -75,7 +75,7 @@ luz_status ensure_scratch(luz_ctx* ctx, size_t bytes) {
 static void free_frame_buffers(luz_frame* f) {
     void* ptrs[] = {f->albedo, f->normal, f->material, f->emission, f->depth, f->light,
                     f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->signal,
-                    f->unshadowed, f->denoised, f->surf,
+                    f->unshadowed, f->denoised, f->surf, f->surf_mat,
                     f->features, f->lin_depth, f->taa, f->taa_next, f->compose, f->hist, f->hist_state,
                     f->block_counts, f->lit_count, f->dn_list, f->dn_count, f->d_scene, f->d_lights, f->d_models,
                     f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter, f->d_textures,
@@ -451,6 +451,7 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     A((void**)&f->hist, (256 + 260) * 4);
     A((void**)&f->hist_state, 16);
     A((void**)&f->surf, P * 32);
+    A((void**)&f->surf_mat, P * 16);
     A((void**)&f->block_counts, (size_t)chunks * 4);
     A((void**)&f->lit_count, 4);
     A((void**)&f->d_scene, sizeof(luz_scene));
@@ -708,9 +709,11 @@ luz_status luz_frame_write(luz_ctx* ctx, luz_frame* f, int32_t plane, const void
     if (need == 0) return LUZ_OK;
     LUZ_CUDA(ctx, cudaMemcpyAsync(dst, src, need, cudaMemcpyHostToDevice, ctx->stream));
     LUZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    // the lit list comes from the normal and depth planes, and its pass writes the
-    // background pixels of the light plane
-    if (plane == LUZ_PLANE_NORMAL || plane == LUZ_PLANE_DEPTH || plane == LUZ_PLANE_LIGHT) f->surf_valid = false;
+    // the lit list comes from the normal, depth, albedo, material and emission planes,
+    // and its pass writes the background pixels of the light plane
+    if (plane == LUZ_PLANE_NORMAL || plane == LUZ_PLANE_DEPTH || plane == LUZ_PLANE_LIGHT ||
+        plane == LUZ_PLANE_ALBEDO || plane == LUZ_PLANE_MATERIAL || plane == LUZ_PLANE_EMISSION)
+        f->surf_valid = false;
     return LUZ_OK;
 }
 

@@ -111,10 +111,18 @@ struct AlphaTest {
     }
 };
 
+// What gbuffer_pixel wrote: the normal (xyz) and depth (w), and the albedo, material
+// and emission words.
+struct GbufPixel {
+    float4 nd;
+    uint32_t albedo, material, emission;
+};
+
 // opaque.vert:21-31 + opaque.frag:21-58 evaluated at the closest hit of the
-// pixel-centre ray of pixel (x, y), written into the G-buffer planes. Returns the
-// written normal (xyz) and depth (w); a miss returns normal 0 and depth 1.
-__device__ __forceinline__ float4 gbuffer_pixel(const GbufParams& G, uint32_t x, uint32_t y) {
+// pixel-centre ray of pixel (x, y), written into the G-buffer planes and returned; a
+// miss has normal 0, depth 1 and zero words.
+// G: the pass's inputs (read-only; no plane it writes overlaps them).
+__device__ __forceinline__ GbufPixel gbuffer_pixel(const GbufParams& __restrict__ G, uint32_t x, uint32_t y) {
     uint32_t pix = y * G.width + x;
     TlasView T{G.tlas_nodes, G.instances, G.instance_count};
     float u = pixel_uv(x, G.width), v = pixel_uv(y, G.height);
@@ -134,7 +142,7 @@ __device__ __forceinline__ float4 gbuffer_pixel(const GbufParams& G, uint32_t x,
         G.emission[pix] = 0u;
         G.depth[pix] = 1.0f;
         G.primary_hit[pix] = make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
-        return make_float4(0.f, 0.f, 0.f, 1.0f);
+        return GbufPixel{make_float4(0.f, 0.f, 0.f, 1.0f), 0u, 0u, 0u};
     }
     V3 p = cam + dir * h.t;
     float pw[4] = {p.x, p.y, p.z, 1.0f}, clip[4];
@@ -216,13 +224,15 @@ __device__ __forceinline__ float4 gbuffer_pixel(const GbufParams& G, uint32_t x,
         }
     }
     if (err) atomicOr(G.status, err);
-    G.albedo[pix] = pack_unorm8(color[0], color[1], color[2], color[3]);
+    const GbufPixel out{make_float4(N.x, N.y, N.z, depth), pack_unorm8(color[0], color[1], color[2], color[3]),
+                        pack_unorm8(roughness, metallic, occlusion, 1.0f), pack_unorm8(em[0], em[1], em[2], em[3])};
+    G.albedo[pix] = out.albedo;
     G.normal[pix] = make_float4(N.x, N.y, N.z, 1.0f);
-    G.material[pix] = pack_unorm8(roughness, metallic, occlusion, 1.0f);
-    G.emission[pix] = pack_unorm8(em[0], em[1], em[2], em[3]);
+    G.material[pix] = out.material;
+    G.emission[pix] = out.emission;
     G.depth[pix] = depth;
     G.primary_hit[pix] = make_uint2(h.custom, h.prim);
-    return make_float4(N.x, N.y, N.z, depth);
+    return out;
 }
 
 }  // namespace luz

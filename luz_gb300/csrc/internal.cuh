@@ -207,6 +207,7 @@ struct luz_frame {
     uint32_t shadow_slots = 0, ao_samples = 0;
     // compacted lit pixels
     float4* surf = nullptr;         // 2 float4 per lit pixel: (fragPos, pixel), (N, x | y << 16)
+    uint4* surf_mat = nullptr;      // 1 uint4 per lit pixel: (albedo, material, emission, pixel) words
     bool surf_valid = false;        // surf / lit_count match the current planes and scene
     uint32_t* block_counts = nullptr;
     uint32_t* lit_count = nullptr;  // device counter

@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(256) ao_resolve_kernel(const float4* normal, c
 LightParams make_light_params(luz_ctx* ctx, luz_frame* f) {
     LightParams P;
     P.surf = f->surf;
+    P.surf_mat = f->surf_mat;
     P.lit_count = f->lit_count;
     P.albedo = f->albedo;
     P.normal = f->normal;

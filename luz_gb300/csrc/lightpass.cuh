@@ -9,6 +9,7 @@ namespace luz {
 
 struct LightParams {
     const float4* surf;          // compacted lit pixels: (fragPos, pixel), (N, x | y << 16)
+    const uint4* surf_mat;       // beside them: (albedo, material, emission, pixel) words
     const uint32_t* lit_count;
     const uint32_t* albedo;
     const float4* normal;
@@ -82,16 +83,9 @@ __device__ __forceinline__ void light_pass_pixel(const LightParams& P, const luz
     const float4 s0 = kCoherent ? __ldcg(sp) : __ldg(sp), s1 = kCoherent ? __ldcg(sp + 1) : __ldg(sp + 1);
     const uint32_t pix = __float_as_uint(s0.w);
     const V3 N = V3{s1.x, s1.y, s1.z};
-    uint32_t a8, m8, e8;
-    if (kCoherent) {
-        a8 = __ldcg(P.albedo + pix);
-        m8 = __ldcg(P.material + pix);
-        e8 = __ldcg(P.emission + pix);
-    } else {
-        a8 = P.albedo[pix];
-        m8 = P.material[pix];
-        e8 = P.emission[pix];
-    }
+    // the pixel's G-buffer words, one 16-B record in list order
+    const uint4 gw = kCoherent ? __ldcg(P.surf_mat + t) : __ldg(P.surf_mat + t);
+    const uint32_t a8 = gw.x, m8 = gw.y, e8 = gw.z;
     V3 albedo = V3{__ldg(P.srgb_lut + (a8 & 0xFF)), __ldg(P.srgb_lut + ((a8 >> 8) & 0xFF)),
                      __ldg(P.srgb_lut + ((a8 >> 16) & 0xFF))};
     float roughness = unorm8_to_float(m8 & 0xFF);

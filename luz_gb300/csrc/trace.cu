@@ -95,13 +95,17 @@ __global__ void __launch_bounds__(1024) lit_scan_kernel(uint32_t* chunk_counts, 
 
 // Also writes light.frag's background colour (light.frag:178-181: ambient colour x
 // intensity, alpha 1) into the light plane at every unlit pixel, so the light pass
-// touches lit pixels only.
+// touches lit pixels only, and packs each lit pixel's albedo, material and emission
+// words beside it, so that the light pass reads its G-buffer inputs as 16-B records in
+// list order.
 __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, const float* depth,
+                                                        const uint32_t* albedo, const uint32_t* material,
+                                                        const uint32_t* emission,
                                                         uint32_t width, uint32_t height,
                                                         const uint32_t* chunk_offsets,
                                                         const float* inverse_proj,
                                                         const float* inverse_view, const float* ambient,
-                                                        float4* surf, float4* light) {
+                                                        float4* surf, uint4* surf_mat, float4* light) {
     __shared__ uint32_t s_tmp[8];
     __shared__ float s_ip[16], s_iv[16];
     __shared__ float4 s_bg;
@@ -133,6 +137,7 @@ __global__ void __launch_bounds__(256) lit_write_kernel(const float4* normal, co
         float4 nn = normal[pix];
         surf[2 * (size_t)pos] = make_float4(p.x, p.y, p.z, __uint_as_float(pix));
         surf[2 * (size_t)pos + 1] = make_float4(nn.x, nn.y, nn.z, __uint_as_float(x | (y << 16)));
+        surf_mat[pos] = make_uint4(albedo[pix], material[pix], emission[pix], pix);
         ++pos;
     }
 }
@@ -198,12 +203,13 @@ luz_status launch_lit_compaction(luz_ctx* ctx, luz_frame* f) {
     LUZ_LAUNCHED(ctx, "lit_count_kernel");
     lit_scan_kernel<<<1, 1024, 0, ctx->stream>>>(f->block_counts, chunks, f->lit_count);
     LUZ_LAUNCHED(ctx, "lit_scan_kernel");
-    lit_write_kernel<<<chunks, 256, 0, ctx->stream>>>(f->normal, f->depth, f->width, f->height,
+    lit_write_kernel<<<chunks, 256, 0, ctx->stream>>>(f->normal, f->depth, f->albedo, f->material, f->emission,
+                                                      f->width, f->height,
                                                       f->block_counts,
                                                       (const float*)((const char*)f->d_scene + offsetof(luz_scene, inverse_proj)),
                                                       (const float*)((const char*)f->d_scene + offsetof(luz_scene, inverse_view)),
                                                       (const float*)((const char*)f->d_scene + offsetof(luz_scene, ambient_light_color)),
-                                                      f->surf, f->light);
+                                                      f->surf, f->surf_mat, f->light);
     LUZ_LAUNCHED(ctx, "lit_write_kernel");
     f->surf_valid = true;
     return LUZ_OK;
