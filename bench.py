@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-denoise", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=64, help="scenes of the batched workload (64 as configured)")
+    ap.add_argument("--batch-no-tune", action="store_true",
+                    help="keep the default traversal launch shape in the batched workload (profiling captures)")
     ap.add_argument("--no-stress", action="store_true", help="skip the 4K 4096-instance stress scene")
     return ap.parse_args()
 
@@ -462,7 +465,7 @@ def stress_config5(ctx, stream, flush, K, W):
 
 
 # ---------------------------------------------------------------------------- batched workload
-def batched_uneven(ctx, stream, flush, K, W, count=64, seed=4004):
+def batched_uneven(ctx, stream, flush, K, W, count=64, seed=4004, tune=True):
     """count scenes, triangles log-uniform in [1e3, 2e6] from the cube/quad and
     displaced-icosphere generators, resolutions from {256^2, 512^2, 1280x720,
     1920x1080}, 4 AO rays per pixel; one batched BLAS build at creation, then every
@@ -516,7 +519,7 @@ def batched_uneven(ctx, stream, flush, K, W, count=64, seed=4004):
         b.set_fused(False)
         staged = replay_ms()
         b.set_fused(True)
-    tun, tune_ms = b.autotune(3)
+    tun, tune_ms = b.autotune(3) if tune else (ctx.vis_tuning(), None)
     b.render(0)
     st = b.stats(0)
     # light.frag's rays (the unit of grays_per_s, as for the single frame) and the
@@ -713,7 +716,8 @@ def run_ours(args, rank, world, local):
     batched = None
     if not args.no_batch:
         saved = ctx.vis_tuning()
-        batched = batched_uneven(ctx, stream, flush, K, args.warmup)
+        batched = batched_uneven(ctx, stream, flush, K, args.warmup, count=args.batch_scenes,
+                                 tune=not args.batch_no_tune)
         ctx.set_vis_tuning(**saved)
 
     post = post_passes(g, stream, flush, K, args.warmup)

@@ -100,6 +100,12 @@ __device__ __forceinline__ void write_slot(float4* node, int slot, float4 lo, fl
 // Leaf g (global index) of segment sd: writes its box into its parent and climbs
 // while it is the second child to arrive. kBlock: every leaf of the tree is handled
 // by one CTA, so block-scope fences order the node writes.
+__device__ __forceinline__ uint32_t atomic_add_acq_rel_gpu(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 template <bool kBlock>
 __device__ __forceinline__ void refit_leaf(const SegDesc& sd, uint32_t g, const float4* leaf_box,
                                            const uint32_t* node_parent, const uint32_t* leaf_parent,
@@ -113,10 +119,19 @@ __device__ __forceinline__ void refit_leaf(const SegDesc& sd, uint32_t g, const 
         if (p == 0xFFFFFFFFu || local >= node_count) return;
         float4* node = sd.nodes + (size_t)local * kNodeF4;
         write_slot(node, p & 1, lo, hi);
-        if (kBlock) __threadfence_block(); else __threadfence();
-        uint32_t old = atomicAdd(flags + sd.node_off + local, 1u);
-        if (old == 0) return;
-        if (kBlock) __threadfence_block(); else __threadfence();
+        uint32_t old;
+        if (kBlock) {
+            __threadfence_block();
+            old = atomicAdd(flags + sd.node_off + local, 1u);
+            if (old == 0) return;
+            __threadfence_block();
+        } else {
+            // One acquire-release atomic instead of two device-wide fences: its release
+            // half publishes this child's slot, its acquire half (for the second
+            // arrival) makes the first child's slot visible to the L2 loads below.
+            old = atomic_add_acq_rel_gpu(flags + sd.node_off + local, 1u);
+            if (old == 0) return;
+        }
         float4 n0 = __ldcg(node + 0), n1 = __ldcg(node + 1), n2 = __ldcg(node + 2);
         lo = make_float4(fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z), 0.f);
         hi = make_float4(fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w), 0.f);
