@@ -168,7 +168,10 @@ __device__ __noinline__ void frame_gbuffer_item(const FrameScene& F, uint32_t k,
     const uint32_t width = F.gb.width, height = F.gb.height;
     const bool inside = x < width && y < height;
     GbufPixel gp{make_float4(0.f, 0.f, 0.f, 1.f), 0u, 0u, 0u};
-    if (inside) gp = gbuffer_pixel(F.gb, x, y);
+    if (inside) {
+        GbufRay ray;
+        if (gbuffer_trace<const GbufParams&>(F.gb, x, y, ray)) gp = gbuffer_shade<const GbufParams&>(F.gb, x, y, ray);
+    }
     const float4 nd = gp.nd;
     const bool lit = inside && !(length(V3{nd.x, nd.y, nd.z}) == 0.0f);
     const uint32_t rank = block_excl(lit ? 1u : 0u, s_tmp);
@@ -198,7 +201,7 @@ __device__ __noinline__ void frame_gbuffer_item(const FrameScene& F, uint32_t k,
 __device__ __noinline__ void frame_tlas_item(const FrameScene& F, unsigned long long* s_keys, uint32_t* s_bounds,
                                              uint32_t* status) {
     if (threadIdx.x == 0) *F.lit_count = 0u;
-    if (F.tlas.n > 0) tlas_build_block(F.tlas, s_keys, s_bounds, status);
+    if (F.tlas.n > 0) tlas_build_block<const TlasBuildArgs&>(F.tlas, s_keys, s_bounds, status);
 }
 
 // Light-pass item: lit pixels [c * 256, c * 256 + 256) of scene F, lights staged in

@@ -96,44 +96,60 @@ __device__ __forceinline__ void hit_uv(const DevShadeInstance& S, uint32_t prim,
     v = (v0.texcoord[1] * b0 + v1.texcoord[1] * b1) + v2.texcoord[1] * b2;
 }
 
-// opaque.frag:29-34: albedo = color * colorMap; discarded below 0.5.
+// opaque.frag:29-34: albedo = color * colorMap; discarded below 0.5. Holds the few
+// inputs it needs by value: taking the address of the pass's parameter block would move
+// the whole block to local memory and every access of the pass with it.
 struct AlphaTest {
-    const GbufParams* G;
+    const luz_model* models;
+    uint32_t model_count;
+    const DevTexture* textures;
+    uint32_t texture_count;
+    const DevShadeInstance* shade;
     __device__ __forceinline__ bool operator()(uint32_t input, uint32_t custom, uint32_t prim, float b0, float b1,
                                                float b2) const {
-        if (custom >= G->model_count) return true;
-        const luz_model& m = G->models[custom];
-        if (m.color_map < 0 || (uint32_t)m.color_map >= G->texture_count) return !(m.color[3] < 0.5f);
+        if (custom >= model_count) return true;
+        const luz_model& m = models[custom];
+        if (m.color_map < 0 || (uint32_t)m.color_map >= texture_count) return !(m.color[3] < 0.5f);
         float u, v;
-        hit_uv(G->shade[input], prim, b0, b1, b2, u, v);
-        float a = m.color[3] * tex_sample(G->textures[m.color_map], u, v).w;
+        hit_uv(shade[input], prim, b0, b1, b2, u, v);
+        float a = m.color[3] * tex_sample(textures[m.color_map], u, v).w;
         return !(a < 0.5f);
     }
 };
 
-// What gbuffer_pixel wrote: the normal (xyz) and depth (w), and the albedo, material
-// and emission words.
+// What gbuffer_shade wrote: the normal (xyz) and depth (w), and the albedo, material
+// and emission words (a miss: normal 0, depth 1 and zero words).
 struct GbufPixel {
     float4 nd;
     uint32_t albedo, material, emission;
 };
 
-// opaque.vert:21-31 + opaque.frag:21-58 evaluated at the closest hit of the
-// pixel-centre ray of pixel (x, y), written into the G-buffer planes and returned; a
-// miss has normal 0, depth 1 and zero words.
-// G: the pass's inputs (read-only; no plane it writes overlaps them).
-__device__ __forceinline__ GbufPixel gbuffer_pixel(const GbufParams& __restrict__ G, uint32_t x, uint32_t y) {
-    uint32_t pix = y * G.width + x;
+// The primary ray of pixel (x, y) and its closest hit.
+struct GbufRay {
+    V3 cam, dir;
+    ClosestHit h;
+};
+
+// opaque.vert:21-31 + opaque.frag:21-58 at pixel (x, y), in two parts so that a caller
+// can end a thread whose ray missed (an early exit: a miss path that rejoins the hit
+// path at the end of one inlined function made the G-buffer kernel 9 % slower).
+// gbuffer_trace traces the pixel-centre ray; on a miss it writes the miss values of
+// every plane and returns false. gbuffer_shade evaluates the hit and writes the planes.
+// Params: GbufParams (by value) where G is a kernel parameter, const GbufParams& where
+// it sits in device memory.
+template <typename Params>
+__device__ __forceinline__ bool gbuffer_trace(Params G, uint32_t x, uint32_t y, GbufRay& r) {
+    const uint32_t pix = y * G.width + x;
     TlasView T{G.tlas_nodes, G.instances, G.instance_count};
     float u = pixel_uv(x, G.width), v = pixel_uv(y, G.height);
-    V3 cam = V3{G.cam[0], G.cam[1], G.cam[2]};
+    r.cam = V3{G.cam[0], G.cam[1], G.cam[2]};
     V3 target = depth_to_world(G.inverse_proj, G.inverse_view, u, v, 1.0f);
-    V3 dir = normalize(target - cam);
-    ClosestHit h;
+    r.dir = normalize(target - r.cam);
     uint32_t err = 0;
     const float inf = __int_as_float(0x7f800000);
-    bool hit = trace_ray<true, false, AlphaTest>(T, cam, dir, 0.0f, inf, 0xFFu, G.model_skip, G.model_count, &h, err,
-                                                 nullptr, AlphaTest{&G});
+    bool hit = trace_ray<true, false, AlphaTest>(T, r.cam, r.dir, 0.0f, inf, 0xFFu, G.model_skip, G.model_count, &r.h,
+                                                 err, nullptr,
+                                                 AlphaTest{G.models, G.model_count, G.textures, G.texture_count, G.shade});
     if (err) atomicOr(G.status, err);
     if (!hit) {
         G.albedo[pix] = 0u;
@@ -142,8 +158,16 @@ __device__ __forceinline__ GbufPixel gbuffer_pixel(const GbufParams& __restrict_
         G.emission[pix] = 0u;
         G.depth[pix] = 1.0f;
         G.primary_hit[pix] = make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
-        return GbufPixel{make_float4(0.f, 0.f, 0.f, 1.0f), 0u, 0u, 0u};
     }
+    return hit;
+}
+
+template <typename Params>
+__device__ __forceinline__ GbufPixel gbuffer_shade(Params G, uint32_t x, uint32_t y, const GbufRay& r) {
+    const uint32_t pix = y * G.width + x;
+    const ClosestHit& h = r.h;
+    const V3 cam = r.cam, dir = r.dir;
+    uint32_t err = 0;
     V3 p = cam + dir * h.t;
     float pw[4] = {p.x, p.y, p.z, 1.0f}, clip[4];
     mat4_mul_vec4(G.view_proj, pw, clip);

@@ -563,7 +563,7 @@ bfs_relayout_kernel(const float4* src, float4* dst, uint32_t m, uint32_t* queue,
 __global__ void __launch_bounds__(1024) tlas_fused_kernel(TlasBuildArgs A, uint32_t* dev_status) {
     __shared__ unsigned long long s_keys[kFusedTlasMax];
     __shared__ uint32_t s_bounds[6];
-    tlas_build_block(A, s_keys, s_bounds, dev_status);
+    tlas_build_block<TlasBuildArgs>(A, s_keys, s_bounds, dev_status);
 }
 
 // ---------------------------------------------------------------- host drivers

@@ -408,9 +408,12 @@ struct TlasBuildArgs {
 // separated by block barriers. Same results as the multi-kernel path, bit for bit, at
 // any block size (a multiple of 32 up to 1024). s_keys: kFusedTlasMax entries of shared
 // memory, s_bounds: 6 words of shared memory. Every thread of the block calls it.
+// Args: TlasBuildArgs by value where A is a kernel parameter (no local copy of the
+// parameter block), const TlasBuildArgs& where it sits in device memory.
 constexpr uint32_t kFusedTlasMax = 4096;
-__device__ __forceinline__ void tlas_build_block(const TlasBuildArgs& A, unsigned long long* s_keys,
-                                                 uint32_t* s_bounds, uint32_t* dev_status) {
+template <typename Args>
+__device__ __forceinline__ void tlas_build_block(Args A, unsigned long long* s_keys, uint32_t* s_bounds,
+                                                 uint32_t* dev_status) {
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     const uint32_t n = A.n;
     const uint32_t m = max(n, 2u) - 1;
