@@ -345,6 +345,96 @@ __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, 
     refit_leaf<false>(segs[s], g, leaf_box, node_parent, leaf_parent, flags);
 }
 
+// The refit with the nodes of a block's own leaves in shared memory. Block b takes the
+// kRefitLeaves consecutive leaves [b0, b0 + kRefitLeaves) of the sorted order. An
+// internal node whose leaf range (kept by the hierarchy pass) lies inside them has both
+// children inside as well, so its two child boxes, its arrival count, its parent and
+// its range live in shared memory at index (first leaf of its segment + node index -
+// b0): the node index lies in its own leaf range. The climbs through these nodes touch
+// shared memory only, and the block writes their slots to device memory at the end,
+// one node per thread. The first node whose range leaves the block (and so every node above
+// it) goes through refit_leaf's device-memory protocol. Same slots as refit_kernel, bit
+// for bit: every box is a min / max union.
+__global__ void __launch_bounds__(kRefitLeaves)
+refit_local_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg, uint32_t total,
+                   const float4* leaf_box, const uint32_t* node_parent, const uint32_t* leaf_parent,
+                   uint32_t* flags) {
+    __shared__ float s_box[kRefitLeaves][2][6];   // per local node: child slot 0 / 1 (lo xyz, hi xyz)
+    __shared__ uint32_t s_flag[kRefitLeaves];
+    __shared__ uint32_t s_parent[kRefitLeaves];   // parent and leaf range of node (g - prim_off)
+    __shared__ uint2 s_range[kRefitLeaves];
+    const uint32_t b0 = blockIdx.x * kRefitLeaves, g = b0 + threadIdx.x;
+    s_flag[threadIdx.x] = 0u;
+    int s = 0;
+    SegDesc sd{};
+    if (g < total) {
+        s = find_seg(seg_prim_off, nseg, g);
+        sd = segs[s];
+        // the node with the index of this leaf position (every leaf position of a segment
+        // but its last has one): loaded once, coalesced, for the climbs of the block
+        const uint32_t q = g - sd.prim_off;
+        if (q + 1 < sd.prim_count) {
+            s_parent[threadIdx.x] = node_parent[sd.node_off + q];
+            s_range[threadIdx.x] = sd.node_range[q];
+        }
+    }
+    __syncthreads();
+    if (g < total) {
+        float4 lo = leaf_box[2 * g], hi = leaf_box[2 * g + 1];
+        uint32_t p = leaf_parent[g];
+        const uint32_t node_count = sd.prim_count > 1 ? sd.prim_count - 1 : 1;
+        bool global = sd.prim_count <= 1;   // a one-primitive segment's node has one child (one arrival)
+        for (uint32_t guard = 0; guard <= sd.prim_count + 1; ++guard) {
+            const uint32_t local = p >> 1;
+            if (p == 0xFFFFFFFFu || local >= node_count) break;
+            // the node index lies in its own leaf range: a node whose index is outside the
+            // block's positions spans other blocks' leaves (and so does every node above it)
+            const uint32_t k = sd.prim_off + local - b0;
+            if (!global) {
+                if (k >= (uint32_t)kRefitLeaves) {
+                    global = true;
+                } else {
+                    const uint2 range = s_range[k];
+                    global = sd.prim_off + range.x < b0 || sd.prim_off + range.y >= b0 + kRefitLeaves;
+                }
+            }
+            if (global) {
+                float4* node = sd.nodes + (size_t)local * kNodeF4;
+                write_slot(node, p & 1, lo, hi);
+                if (atomic_add_acq_rel_gpu(flags + sd.node_off + local, 1u) == 0) break;
+                const float4 n0 = __ldcg(node + 0), n1 = __ldcg(node + 1), n2 = __ldcg(node + 2);
+                lo = make_float4(fmin_(n0.x, n1.x), fmin_(n0.z, n1.z), fmin_(n2.x, n2.z), 0.f);
+                hi = make_float4(fmax_(n0.y, n1.y), fmax_(n0.w, n1.w), fmax_(n2.y, n2.w), 0.f);
+                p = node_parent[sd.node_off + local];
+                continue;
+            }
+            // local: shared memory only; the block writes these nodes' slots at the end
+            float* slot = s_box[k][p & 1];
+            slot[0] = lo.x; slot[1] = lo.y; slot[2] = lo.z;
+            slot[3] = hi.x; slot[4] = hi.y; slot[5] = hi.z;
+            __threadfence_block();
+            if (atomicAdd(s_flag + k, 1u) == 0) break;
+            __threadfence_block();
+            const float* c0 = s_box[k][0];
+            const float* c1 = s_box[k][1];
+            lo = make_float4(fmin_(c0[0], c1[0]), fmin_(c0[1], c1[1]), fmin_(c0[2], c1[2]), 0.f);
+            hi = make_float4(fmax_(c0[3], c1[3]), fmax_(c0[4], c1[4]), fmax_(c0[5], c1[5]), 0.f);
+            p = s_parent[k];
+        }
+    }
+    __syncthreads();
+    // the slots of every node completed in shared memory (both arrivals), one node per
+    // thread at the node of this thread's leaf position
+    if (g < total && s_flag[threadIdx.x] == 2u) {
+        const float* c0 = s_box[threadIdx.x][0];
+        const float* c1 = s_box[threadIdx.x][1];
+        float4* node = sd.nodes + (size_t)(g - sd.prim_off) * kNodeF4;
+        node[0] = make_float4(c0[0], c0[3], c0[1], c0[4]);
+        node[1] = make_float4(c1[0], c1[3], c1[1], c1[4]);
+        node[2] = make_float4(c0[2], c0[5], c1[2], c1[5]);
+    }
+}
+
 // ---------------------------------------------------------------- bounding sphere
 
 // Bounding sphere of every BLAS about its root box centre: the largest squared
@@ -721,7 +811,7 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
                   align256((size_t)std::max(N, 1u) * 32) + align256((size_t)M * 4) +
                   align256((size_t)std::max(N, 1u) * 4) + align256((size_t)M * 4) +
                   2 * align256((size_t)std::max(N, 1u) * 4) + 2 * align256((size_t)M * 4) +
-                  align256((size_t)(M / 1024 + 1) * 4);
+                  align256((size_t)(M / 1024 + 1) * 4) + align256((size_t)M * 8);
     luz_status stt = ensure_scratch(ctx, need);
     if (stt != LUZ_OK) { cudaFree(arena->base); delete arena; return stt; }
     char* p = (char*)ctx->d_scratch;
@@ -740,6 +830,8 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
     uint32_t* d_even = (uint32_t*)p; p += align256((size_t)M * 4);
     uint32_t* d_idx4 = (uint32_t*)p; p += align256((size_t)M * 4);
     uint32_t* d_sums = (uint32_t*)p; p += align256((size_t)(M / 1024 + 1) * 4);
+    uint2* d_range = (uint2*)p; p += align256((size_t)M * 8);
+    for (uint32_t s = 0; s < count; ++s) segs[s].node_range = d_range + node_off[s];
 
     LUZ_CUDA(ctx, cudaMemcpyAsync(d_segs, segs.data(), count * sizeof(SegDesc), cudaMemcpyHostToDevice, st));
     LUZ_CUDA(ctx, cudaMemcpyAsync(d_prim_off, prim_off.data(), count * 4, cudaMemcpyHostToDevice, st));
@@ -773,9 +865,10 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
         blas_emit_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, sb.keys[res],
                                                        sb.vals[res], d_leaf_box, d_mort, d_ord);
         LUZ_LAUNCHED(ctx, "blas_emit_kernel");
-        refit_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, d_leaf_box,
-                                                   d_node_parent, d_leaf_parent, d_flags);
-        LUZ_LAUNCHED(ctx, "refit_kernel");
+        refit_local_kernel<<<cdiv(N, kRefitLeaves), kRefitLeaves, 0, st>>>(d_segs, d_prim_off, count, N,
+                                                                           d_leaf_box, d_node_parent, d_leaf_parent,
+                                                                           d_flags);
+        LUZ_LAUNCHED(ctx, "refit_local_kernel");
         blas_radius_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N);
         LUZ_LAUNCHED(ctx, "blas_radius_kernel");
     }

@@ -56,6 +56,7 @@ __device__ __forceinline__ void karras_node(const SegDesc& sd, int i, const unsi
         node[3] = make_float4(__int_as_float(c0), __int_as_float(kEmptyChild), 0.f, 0.f);
         if (n == 1) leaf_parent[sd.prim_off] = 0u;
         node_parent[sd.node_off] = 0xFFFFFFFFu;
+        if (sd.node_range) sd.node_range[0] = make_uint2(0u, 0u);
         return;
     }
     const unsigned long long* k = keys + sd.prim_off;
@@ -79,6 +80,7 @@ __device__ __forceinline__ void karras_node(const SegDesc& sd, int i, const unsi
     } while (step > 1);
     int gamma = i + split * d + min(d, 0);
     int lo = min(i, j), hi = max(i, j);
+    if (sd.node_range) sd.node_range[i] = make_uint2((uint32_t)lo, (uint32_t)hi);
     int c0, c1;
     if (lo == gamma) { c0 = ~gamma; leaf_parent[sd.prim_off + gamma] = ((uint32_t)i << 1) | 0u; }
     else { c0 = gamma; node_parent[sd.node_off + gamma] = ((uint32_t)i << 1) | 0u; }

@@ -17,6 +17,7 @@ struct SegDesc {
     float4* nodes;         // output nodes of this segment
     float4* tris;          // output triangles of this segment
     float4* nodes4;        // output 4-wide nodes (NULL: not built)
+    uint2* node_range;     // leaf range [lo, hi] of each internal node (NULL: not kept)
 };
 
 // Onesweep radix sort geometry.
@@ -59,6 +60,12 @@ __global__ void blas_emit_kernel(const SegDesc* segs, const uint32_t* seg_prim_o
 __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                              uint32_t total, const float4* leaf_box, const uint32_t* node_parent,
                              const uint32_t* leaf_parent, uint32_t* flags);
+// Leaves per block of refit_local_kernel (one thread each).
+constexpr int kRefitLeaves = 512;
+__global__ void __launch_bounds__(kRefitLeaves)
+refit_local_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg, uint32_t total,
+                   const float4* leaf_box, const uint32_t* node_parent, const uint32_t* leaf_parent,
+                   uint32_t* flags);
 __global__ void blas_radius_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                                    uint32_t total);
 
