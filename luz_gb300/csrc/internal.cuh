@@ -36,16 +36,18 @@ constexpr int kNode4F4 = 8;
 constexpr uint32_t kRayChunk = 1u << 27;
 
 // One TLAS leaf, in sorted (leaf) order. 96 B, 16-B aligned for vector loads.
+// sphere: the BLAS's bounding sphere in object space, (centre, radius): the root box
+// centre and the square root of the largest squared vertex distance from it (the
+// root node's spare word), +inf when that word is not finite.
 struct __align__(16) DevInstance {
     float w2o[12];          // world -> object, 3x4 row-major
-    const float4* nodes;    // BLAS binary nodes
-    const float4* tris;     // BLAS triangles
+    float4 sphere;
     uint32_t custom_index;  // instanceCustomIndex = modelRID
     uint32_t mask;
     uint32_t input_index;   // position in the caller's instance array
     uint32_t blas_prims;    // BLAS primitive count
     const float4* nodes4;   // BLAS 4-wide nodes
-    const float4* pad;
+    const float4* tris;     // BLAS triangles
 };
 static_assert(sizeof(DevInstance) == 96, "DevInstance layout");
 

@@ -286,9 +286,14 @@ __device__ __forceinline__ void tlas_emit_one(const DevInstanceInput* in, const 
     const DevInstanceInput ii = in[i];
     DevInstance d;
     affine_inverse(ii.o2w, d.w2o);
-    d.nodes = ii.nodes;
+    d.sphere = make_float4(0.f, 0.f, 0.f, __int_as_float(0x7f800000));
+    if (ii.blas_prims > 0) {
+        const float4 n0 = ii.nodes[0], n1 = ii.nodes[1], n2 = ii.nodes[2];
+        const V3 c = root_centre(n0, n1, n2);
+        const uint32_t r2 = __float_as_uint(ii.nodes[3].z);
+        if (r2 < 0x7F800000u) d.sphere = make_float4(c.x, c.y, c.z, sqrtf(__uint_as_float(r2)));
+    }
     d.nodes4 = ii.nodes4;
-    d.pad = nullptr;
     d.tris = ii.tris;
     d.custom_index = ii.custom_index;
     d.mask = ii.mask;

@@ -98,6 +98,28 @@ __device__ __forceinline__ bool slab_ordered(float nx, float fx, float ny, float
     tnear = tn;
     return tn * kSlabShrink <= tf;
 }
+// True when the segment o + t d, t in [tmin, tmax], provably passes outside the
+// sphere s = (centre, radius) of a BLAS, so that no triangle of it can be hit: the
+// instance is then not entered. Conservative: the segment point at the clamped
+// projection parameter t* (rounded: any segment point bounds the distance from
+// above, and the error of t* moves it by at most a few ulps of |c - o|) is compared
+// against the radius grown by 2^-16 x (|c - o|_1 + radius), which covers the
+// rounding of that distance, of the stored radius and of the watertight test's
+// hit point (within a few ulps of |vertex - o| of the triangle). A NaN anywhere
+// keeps the instance, as does a |d|^2 outside [2^-100, 2^100] (where the fast
+// division could be off).
+__device__ __forceinline__ bool sphere_misses(V3 o, V3 d, float tmin, float tmax, float4 s) {
+    const float wx = s.x - o.x, wy = s.y - o.y, wz = s.z - o.z;
+    const float dd = __fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, d.z * d.z));
+    if (!(dd > 0x1p-100f && dd < 0x1p100f)) return false;
+    float t = __fdividef(__fmaf_rn(wx, d.x, __fmaf_rn(wy, d.y, wz * d.z)), dd);
+    t = fminf(fmaxf(t, tmin), tmax);
+    const float qx = __fmaf_rn(t, d.x, -wx), qy = __fmaf_rn(t, d.y, -wy), qz = __fmaf_rn(t, d.z, -wz);
+    const float q2 = __fmaf_rn(qx, qx, __fmaf_rn(qy, qy, qz * qz));
+    const float r = __fmaf_rn(0x1p-16f, fabsf(wx) + fabsf(wy) + fabsf(wz) + s.w, s.w);
+    return q2 > r * r;
+}
+
 __device__ __forceinline__ int dir_signs(V3 idir) {
     return (idir.x < 0.0f ? 1 : 0) | (idir.y < 0.0f ? 2 : 0) | (idir.z < 0.0f ? 4 : 0);
 }
@@ -197,7 +219,7 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
             if (kStats) cnt->instances++;
             const DevInstance* I = T.instances + (~node);
             const float4* wp = reinterpret_cast<const float4*>(I->w2o);
-            float4 r0 = __ldg(wp), r1 = __ldg(wp + 1), r2 = __ldg(wp + 2);
+            float4 r0 = __ldg(wp), r1 = __ldg(wp + 1), r2 = __ldg(wp + 2), sph = __ldg(&I->sphere);
             const float4* pnodes = I->nodes4;
             const float4* ptris = I->tris;
             uint4 meta = __ldg(reinterpret_cast<const uint4*>(&I->custom_index));
@@ -208,10 +230,10 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
                 take = skip[meta.x] != 1;
                 tested = skip[meta.x] == 2;
             }
-            if (take) {
-                float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
-                V3 oo = xform_point(m, wo);
-                V3 od = xform_dir(m, wd);
+            // Skipped too when the segment provably misses the BLAS's bounding sphere.
+            const float m[12] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y, r2.z, r2.w};
+            const V3 oo = xform_point(m, wo), od = xform_dir(m, wd);
+            if (take && !sphere_misses(oo, od, tmin, tmax, sph)) {
                 if (sp >= kStackSize) { err |= LUZ_DEV_STACK_OVERFLOW; return false; }
                 stack[sp++] = kStackMarker;
                 o = oo;

@@ -23,12 +23,14 @@ constexpr uint32_t kRayStepCap = 1u << 22;
 // Ray state that traversal touches only when it enters or leaves a BLAS, tests a
 // triangle or finishes lives in shared memory, one 32-bit field per row of
 // kVisThreads entries (conflict-free): world origin and direction, the output word
-// and bit, the watertight shear and origin of the current BLAS, and the world-space
-// box-test state restored when the ray leaves a BLAS.
+// and bit, the origin and direction in the current BLAS's object space (the
+// watertight shear is derived from them per triangle test: most entered BLASes see
+// no triangle test), and the world-space box-test state restored when the ray leaves
+// a BLAS.
 enum ColdField : int {
     kWoX, kWoY, kWoZ, kWdX, kWdY, kWdZ,
     kOutLo, kOutHi, kOutBits,     // bit | record_hit << 5
-    kWtK, kWtSx, kWtSy, kWtSz,    // kx | ky << 2 | kz << 4; shear
+    kOdX, kOdY, kOdZ,             // direction in the current BLAS's object space
     kBtLo, kBtHi,                 // triangles of the current BLAS
     kOoX, kOoY, kOoZ,             // origin in the current BLAS's object space
     kWiX, kWiY, kWiZ,             // world inverse direction and origin offsets, restored on
@@ -58,6 +60,7 @@ struct Cold {
     __device__ __forceinline__ V3 wo() const { return V3{(*this)[kWoX], (*this)[kWoY], (*this)[kWoZ]}; }
     __device__ __forceinline__ V3 wd() const { return V3{(*this)[kWdX], (*this)[kWdY], (*this)[kWdZ]}; }
     __device__ __forceinline__ V3 oo() const { return V3{(*this)[kOoX], (*this)[kOoY], (*this)[kOoZ]}; }
+    __device__ __forceinline__ V3 od() const { return V3{(*this)[kOdX], (*this)[kOdY], (*this)[kOdZ]}; }
 };
 
 // Near-plane rows of a 4-wide node for a ray with inverse direction id: the lower
@@ -262,29 +265,29 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
                 if (!finished) continue;
             }
         } else if (!r.in_blas) {
+            // Instance leaf: entered unless its mask or BLAS is empty or the ray
+            // segment provably misses the BLAS's bounding sphere.
             if (kStats) cnt.instances++;
             const DevInstance* I = insts + (~r.node);
             const float4* wp = reinterpret_cast<const float4*>(I->w2o);
             uint4 meta = __ldg(reinterpret_cast<const uint4*>(&I->custom_index));
-            if ((meta.y & 0xFFu) != 0 && meta.w > 0) {
-                float4 q0 = __ldg(wp), q1 = __ldg(wp + 1), q2 = __ldg(wp + 2);
-                float m[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
-                V3 od = xform_dir(m, c.wd());
-                WtRay wt = wt_setup(xform_point(m, c.wo()), od);
-                c[kWtK] = __int_as_float(wt.kx | (wt.ky << 2) | (wt.kz << 4));
-                c[kWtSx] = wt.sx;
-                c[kWtSy] = wt.sy;
-                c[kWtSz] = wt.sz;
-                c[kOoX] = wt.o.x;
-                c[kOoY] = wt.o.y;
-                c[kOoZ] = wt.o.z;
+            float4 q0 = __ldg(wp), q1 = __ldg(wp + 1), q2 = __ldg(wp + 2), sph = __ldg(&I->sphere);
+            float m[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+            const V3 od = xform_dir(m, c.wd()), oo = xform_point(m, c.wo());
+            if ((meta.y & 0xFFu) != 0 && meta.w > 0 && !sphere_misses(oo, od, r.tmin, r.tmax, sph)) {
+                c[kOdX] = od.x;
+                c[kOdY] = od.y;
+                c[kOdZ] = od.z;
+                c[kOoX] = oo.x;
+                c[kOoY] = oo.y;
+                c[kOoZ] = oo.z;
                 r.idir = safe_inv(od);
-                set_origin(r, wt.o);
+                set_origin(r, oo);
                 near_planes(r);
-                r.nb = I->nodes4;
-                const unsigned long long bt = reinterpret_cast<unsigned long long>(I->tris);
-                c[kBtLo] = __uint_as_float((uint32_t)bt);
-                c[kBtHi] = __uint_as_float((uint32_t)(bt >> 32));
+                const ulonglong2 pt = __ldg(reinterpret_cast<const ulonglong2*>(&I->nodes4));
+                r.nb = reinterpret_cast<const float4*>(pt.x);
+                c[kBtLo] = __uint_as_float((uint32_t)pt.y);
+                c[kBtHi] = __uint_as_float((uint32_t)(pt.y >> 32));
                 if (r.sp < kSmemStack) s_stack[r.sp * 32] = (uint32_t)kStackMarker;
                 else if (r.sp < kStackSize) lstack[r.sp - kSmemStack] = kStackMarker;
                 else { err |= LUZ_DEV_STACK_OVERFLOW; finished = true; }
@@ -299,15 +302,7 @@ __device__ __forceinline__ void run_steps(LaneRay& r, const Cold& c, bool& activ
                                                                ((unsigned long long)__float_as_uint(c[kBtHi]) << 32));
             const float4* tp = bt + (size_t)(~r.node) * kTriF4;
             float4 a = __ldg(tp), b = __ldg(tp + 1), cc = __ldg(tp + 2);
-            WtRay wt;
-            int k = __float_as_int(c[kWtK]);
-            wt.o = c.oo();
-            wt.kx = k & 3;
-            wt.ky = (k >> 2) & 3;
-            wt.kz = k >> 4;
-            wt.sx = c[kWtSx];
-            wt.sy = c[kWtSy];
-            wt.sz = c[kWtSz];
+            const WtRay wt = wt_setup(c.oo(), c.od());
             float t, U, V, W, det;
             if (wt_test(wt, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, V3{cc.x, cc.y, cc.z}, t, U, V, W, det) &&
                 t >= r.tmin && t <= r.tmax) {
