@@ -162,6 +162,8 @@ extern "C" luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint3
     seg.indices = idx;
     seg.nodes = (float4*)d_nodes;
     seg.tris = (float4*)d_tris;
+    seg.morton = d_morton;
+    seg.order = d_order;
     const uint32_t m = n > 1 ? n - 1 : 1;
     const uint32_t tiles = n > 0 ? cdiv(n, kSortTile) : 1;
 
@@ -198,8 +200,7 @@ extern "C" luz_status luz_blas_build_noalloc(const luz_vertex* d_vertices, uint3
     karras_kernel<<<cdiv(m, 256), 256, 0, st>>>(d_seg, zero, 1, m, keys[0], node_parent, leaf_parent, status);
     NOALLOC_LAUNCHED();
     if (n > 0) {
-        blas_emit_kernel<<<cdiv(n, 256), 256, 0, st>>>(d_seg, zero, 1, n, keys[0], vals[0], leaf_box, d_morton,
-                                                       d_order);
+        blas_emit_kernel<<<cdiv(n, 256), 256, 0, st>>>(d_seg, zero, 1, n, keys[0], vals[0], leaf_box);
         NOALLOC_LAUNCHED();
         refit_kernel<<<cdiv(n, 256), 256, 0, st>>>(d_seg, zero, 1, n, leaf_box, node_parent, leaf_parent, flags);
         NOALLOC_LAUNCHED();

@@ -308,19 +308,19 @@ __global__ void karras_kernel(const SegDesc* segs, const uint32_t* seg_node_off,
 }
 
 // ---------------------------------------------------------------- leaves + refit
-// BLAS: gather triangles into leaf order; padded leaf boxes; sorted morton/order.
+// BLAS: gather triangles into leaf order; padded leaf boxes; sorted morton/order into
+// the segment's own arrays.
 __global__ void blas_emit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                                  uint32_t total, const unsigned long long* keys,
-                                 const uint32_t* vals, float4* leaf_box, uint32_t* morton_out,
-                                 uint32_t* order_out) {
+                                 const uint32_t* vals, float4* leaf_box) {
     uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total) return;
     int s = find_seg(seg_prim_off, nseg, g);
     const SegDesc sd = segs[s];
     uint32_t j = g - sd.prim_off;
     uint32_t prim = vals[g] - sd.prim_off;
-    morton_out[g] = (uint32_t)keys[g] & 0x3FFFFFFFu;
-    order_out[g] = prim;
+    sd.morton[j] = (uint32_t)keys[g] & 0x3FFFFFFFu;
+    sd.order[j] = prim;
     uint32_t i0 = sd.indices[3 * prim], i1 = sd.indices[3 * prim + 1], i2 = sd.indices[3 * prim + 2];
     V3 a = load_pos(sd.vertices, i0), b = load_pos(sd.vertices, i1), c = load_pos(sd.vertices, i2);
     float4* t = sd.tris + (size_t)j * kTriF4;
@@ -801,16 +801,18 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
         sd.nodes = (float4*)(ab + off_nodes[s]);
         sd.tris = (float4*)(ab + off_tris[s]);
         sd.nodes4 = (float4*)(ab + off_nodes4[s]);
+        sd.morton = (uint32_t*)(ab + off_mort[s]);
+        sd.order = (uint32_t*)(ab + off_ord[s]);
     }
     // Scratch: segs | prim_off | node_off | bounds | sort | leaf boxes | parents | flags |
-    // sorted morton/order staging.
+    // 4-wide collapse indices | leaf ranges.
     uint32_t N = (uint32_t)total_prims, M = (uint32_t)total_nodes;
     int passes = passes_for((int)count);
     size_t need = align256(count * sizeof(SegDesc)) + 2 * align256(count * 4) +
                   align256(count * 24) + sort_scratch_bytes(std::max(N, 1u), passes) +
                   align256((size_t)std::max(N, 1u) * 32) + align256((size_t)M * 4) +
                   align256((size_t)std::max(N, 1u) * 4) + align256((size_t)M * 4) +
-                  2 * align256((size_t)std::max(N, 1u) * 4) + 2 * align256((size_t)M * 4) +
+                  2 * align256((size_t)M * 4) +
                   align256((size_t)(M / 1024 + 1) * 4) + align256((size_t)M * 8);
     luz_status stt = ensure_scratch(ctx, need);
     if (stt != LUZ_OK) { cudaFree(arena->base); delete arena; return stt; }
@@ -825,8 +827,6 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
     uint32_t* d_node_parent = (uint32_t*)p; p += align256((size_t)M * 4);
     uint32_t* d_leaf_parent = (uint32_t*)p; p += align256((size_t)std::max(N, 1u) * 4);
     uint32_t* d_flags = (uint32_t*)p; p += align256((size_t)M * 4);
-    uint32_t* d_mort = (uint32_t*)p; p += align256((size_t)std::max(N, 1u) * 4);
-    uint32_t* d_ord = (uint32_t*)p; p += align256((size_t)std::max(N, 1u) * 4);
     uint32_t* d_even = (uint32_t*)p; p += align256((size_t)M * 4);
     uint32_t* d_idx4 = (uint32_t*)p; p += align256((size_t)M * 4);
     uint32_t* d_sums = (uint32_t*)p; p += align256((size_t)(M / 1024 + 1) * 4);
@@ -863,7 +863,7 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
     LUZ_LAUNCHED(ctx, "karras_kernel");
     if (N > 0) {
         blas_emit_kernel<<<cdiv(N, 256), 256, 0, st>>>(d_segs, d_prim_off, count, N, sb.keys[res],
-                                                       sb.vals[res], d_leaf_box, d_mort, d_ord);
+                                                       sb.vals[res], d_leaf_box);
         LUZ_LAUNCHED(ctx, "blas_emit_kernel");
         refit_local_kernel<<<cdiv(N, kRefitLeaves), kRefitLeaves, 0, st>>>(d_segs, d_prim_off, count, N,
                                                                            d_leaf_box, d_node_parent, d_leaf_parent,
@@ -886,15 +886,6 @@ luz_status build_blas_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* d
         LUZ_LAUNCHED(ctx, "chunk_apply_kernel");
         bvh4_emit_kernel<<<cdiv(M, 256), 256, 0, st>>>(d_segs, d_node_off, count, M, d_even, d_idx4);
         LUZ_LAUNCHED(ctx, "bvh4_emit_kernel");
-    }
-    for (uint32_t s = 0; s < count; ++s) {
-        uint32_t n = segs[s].prim_count;
-        if (n)
-            LUZ_CUDA(ctx, cudaMemcpyAsync(ab + off_mort[s], d_mort + prim_off[s], (size_t)n * 4,
-                                          cudaMemcpyDeviceToDevice, st));
-        if (n)
-            LUZ_CUDA(ctx, cudaMemcpyAsync(ab + off_ord[s], d_ord + prim_off[s], (size_t)n * 4,
-                                          cudaMemcpyDeviceToDevice, st));
     }
     LUZ_CUDA(ctx, cudaEventRecord(ctx->build_ev[1], st));
     ctx->build_timed = true;

@@ -18,6 +18,8 @@ struct SegDesc {
     float4* tris;          // output triangles of this segment
     float4* nodes4;        // output 4-wide nodes (NULL: not built)
     uint2* node_range;     // leaf range [lo, hi] of each internal node (NULL: not kept)
+    uint32_t* morton;      // BLAS: output sorted 30-bit Morton codes of this segment
+    uint32_t* order;       // BLAS: output primitive index of each leaf
 };
 
 // Onesweep radix sort geometry.
@@ -55,8 +57,7 @@ __global__ void karras_kernel(const SegDesc* segs, const uint32_t* seg_node_off,
                               uint32_t* node_parent, uint32_t* leaf_parent, uint32_t* dev_status);
 __global__ void blas_emit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                                  uint32_t total, const unsigned long long* keys,
-                                 const uint32_t* vals, float4* leaf_box, uint32_t* morton_out,
-                                 uint32_t* order_out);
+                                 const uint32_t* vals, float4* leaf_box);
 __global__ void refit_kernel(const SegDesc* segs, const uint32_t* seg_prim_off, int nseg,
                              uint32_t total, const float4* leaf_box, const uint32_t* node_parent,
                              const uint32_t* leaf_parent, uint32_t* flags);
