@@ -320,8 +320,9 @@ luz_status luz_blas_download(luz_ctx* ctx, const luz_blas* blas, void* nodes, vo
  * the number of even-depth binary nodes. For parity tests. */
 luz_status luz_blas_download_wide(luz_ctx* ctx, const luz_blas* blas, void* nodes4);
 
-/* Device bytes held by a BLAS / TLAS, by part: binary nodes (closest-hit primary
- * rays), 4-wide nodes (visibility), triangles / instance records, other (sort keys,
+/* Device bytes held by a BLAS / TLAS, by part: binary nodes (the parity-checked tree;
+ * a TLAS build reads each BLAS root's box and bounding sphere from it), 4-wide nodes
+ * (every traversal), triangles / instance records, other (sort keys,
  * order, shading copies of the vertex and index buffers, build scratch of a TLAS).
  * The counterpart of the reference's vkGetAccelerationStructureBuildSizesKHR query
  * (source/Graphics/VulkanWrapper.cpp:692-698, 809-812). */
