@@ -74,12 +74,12 @@ luz_status ensure_scratch(luz_ctx* ctx, size_t bytes) {
 
 static void free_frame_buffers(luz_frame* f) {
     void* ptrs[] = {f->albedo, f->normal, f->material, f->emission, f->depth, f->light,
-                    f->primary_hit, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->signal,
+                    f->primary_hit, f->hit_instance, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->signal,
                     f->unshadowed, f->denoised, f->surf, f->surf_mat,
                     f->features, f->lin_depth, f->taa, f->taa_next, f->compose, f->hist, f->hist_state,
                     f->block_counts, f->lit_count, f->dn_list, f->dn_count, f->d_scene, f->d_lights, f->d_models,
                     f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter, f->d_textures,
-                    f->d_texels, f->d_shadow_lights, f->d_shadow_maps, f->rays_a, f->rays_b};
+                    f->d_texels, f->d_shadow_lights, f->d_shadow_maps, f->rays_a, f->rays_b, f->rays_c};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -377,6 +377,8 @@ void luz_tlas_destroy(luz_tlas* t) {
     if (t->h_input) cudaFreeHost(t->h_input);
     if (t->morton) cudaFree(t->morton);
     if (t->order) cudaFree(t->order);
+    if (t->near) cudaFree(t->near);
+    if (t->leaf_of) cudaFree(t->leaf_of);
     if (t->tmp) cudaFree(t->tmp);
     if (t->input_copied) cudaEventDestroy(t->input_copied);
     delete t;
@@ -436,6 +438,7 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     A((void**)&f->depth, P * 4);
     A((void**)&f->light, P * 16);
     A((void**)&f->primary_hit, P * 8);
+    A((void**)&f->hit_instance, P * 4);
     A((void**)&f->ao, P * 4);
     A((void**)&f->ao_denoised, P * 4);
     A((void**)&f->signal, P * 16);

@@ -81,6 +81,7 @@ struct GbufParams {
     uint32_t* emission;
     float* depth;
     uint2* primary_hit;
+    uint32_t* hit_instance;   // input index of the hit instance (~0 = miss)
     uint32_t* status;
     const DevTexture* textures;
     uint32_t texture_count;
@@ -158,6 +159,7 @@ __device__ __forceinline__ bool gbuffer_trace(Params G, uint32_t x, uint32_t y, 
         G.emission[pix] = 0u;
         G.depth[pix] = 1.0f;
         G.primary_hit[pix] = make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
+        G.hit_instance[pix] = 0xFFFFFFFFu;
     }
     return hit;
 }
@@ -256,6 +258,7 @@ __device__ __forceinline__ GbufPixel gbuffer_shade(Params G, uint32_t x, uint32_
     G.emission[pix] = out.emission;
     G.depth[pix] = depth;
     G.primary_hit[pix] = make_uint2(h.custom, h.prim);
+    G.hit_instance[pix] = h.inst_input;
     return out;
 }
 

@@ -163,6 +163,8 @@ struct luz_tlas {
     luz::DevInstanceInput* h_input = nullptr;     // pinned staging
     uint32_t* morton = nullptr;
     uint32_t* order = nullptr;
+    uint4* near = nullptr;               // per instance (input order): near list of short rays
+    uint32_t* leaf_of = nullptr;         // per instance (input order): its TLAS leaf
     uint32_t node_count = 0;
     cudaEvent_t input_copied = nullptr;           // h_input may be rewritten after this
     // build temporaries
@@ -181,6 +183,7 @@ struct luz_frame {
     float* depth = nullptr;         // F32
     float4* light = nullptr;        // RGBA32F
     uint2* primary_hit = nullptr;
+    uint32_t* hit_instance = nullptr;    // input index of the primary hit's instance (~0 = miss)
     // visibility
     uint32_t* shadow_bits = nullptr;
     uint32_t* ao_bits = nullptr;
@@ -234,6 +237,7 @@ struct luz_frame {
     // (origin, tMax) and (direction, pixel); tMax = -inf marks an item with no ray
     float4* rays_a = nullptr;
     float4* rays_b = nullptr;
+    uint32_t* rays_c = nullptr;          // own instance of a ray that starts at its near list
     uint32_t rays_cap = 0;
 };
 

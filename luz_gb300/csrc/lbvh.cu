@@ -943,6 +943,8 @@ luz_status tlas_alloc(luz_ctx* ctx, luz_tlas* t) {
     LUZ_CUDA(ctx, cudaMallocHost(&t->h_input, (size_t)cap * sizeof(DevInstanceInput)));
     LUZ_CUDA(ctx, cudaMalloc(&t->morton, (size_t)cap * 4));
     LUZ_CUDA(ctx, cudaMalloc(&t->order, (size_t)cap * 4));
+    LUZ_CUDA(ctx, cudaMalloc(&t->near, (size_t)cap * 4 * sizeof(uint4)));
+    LUZ_CUDA(ctx, cudaMalloc(&t->leaf_of, (size_t)cap * 4));
     t->tmp_bytes = tlas_tmp_bytes(cap);
     LUZ_CUDA(ctx, cudaMalloc(&t->tmp, t->tmp_bytes));
     return LUZ_OK;
@@ -1021,6 +1023,7 @@ static TlasScratch carve_tlas(luz_tlas* t) {
 }
 
 TlasBuildArgs tlas_build_args(luz_tlas* t) { return carve_tlas(t).a; }
+const float4* tlas_instance_boxes(const luz_tlas* t) { return carve_tlas(const_cast<luz_tlas*>(t)).a.inst_box; }
 
 // Device part of a TLAS build from the packed staging buffer: one host-to-device copy
 // from pinned memory and the LBVH kernels; no host synchronisation (graph-capturable).

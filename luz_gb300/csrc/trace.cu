@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(kGbTile * kGbTile, kGbMinBlocks) gbuffer_kerne
         G.emission[pix] = 0u;
         G.depth[pix] = 1.0f;
         G.primary_hit[pix] = make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
+        G.hit_instance[pix] = 0xFFFFFFFFu;
         return;
     }
 
@@ -135,6 +136,7 @@ __global__ void __launch_bounds__(kGbTile * kGbTile, kGbMinBlocks) gbuffer_kerne
     G.emission[pix] = pack_unorm8(em[0], em[1], em[2], em[3]);
     G.depth[pix] = depth;
     G.primary_hit[pix] = make_uint2(h.custom, h.prim);
+    G.hit_instance[pix] = h.inst_input;
 }
 
 // ---------------------------------------------------------------- lit-pixel compaction
@@ -283,6 +285,7 @@ luz_status make_gbuf_params(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, GbufP
     G.emission = f->emission;
     G.depth = f->depth;
     G.primary_hit = f->primary_hit;
+    G.hit_instance = f->hit_instance;
     G.status = ctx->d_status;
     G.textures = f->d_textures;
     G.texture_count = f->texture_count;

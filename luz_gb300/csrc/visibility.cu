@@ -18,11 +18,151 @@
 // (world origin and direction, output bit, watertight shear) sits in shared memory,
 // which keeps the kernel at 64 registers and 4 CTAs per SM without spills.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "vis_trace.cuh"
 
 namespace luz {
+
+// ---------------------------------------------------------------- near lists
+// A ray whose whole segment stays within `reach` of its own instance's box can only
+// hit instances whose boxes come within `reach` of that box: for such a ray the
+// traversal starts at its own TLAS leaf with the leaves of those of them whose boxes
+// its segment overlaps on its stack, in place of the TLAS root. Short rays (AO rays of
+// radius aoMax) then skip the TLAS levels above their own instance. Per instance
+// (input order) the record holds (leaf, count, near[0..1]), (near[2..5]), (box lo,
+// near[6]), (box hi, near[7]), near[] as input indices; count = ~0 when there are more
+// than kNearMax such instances or the box is empty or not finite. The result is that
+// of the full traversal: a hit at q on instance j needs box_j within
+// |q - o| + dist(o, box_i) of box_i and the segment to overlap box_j, and entering an
+// instance whose leaf box the full traversal would cull finds no hit either (boxes
+// are conservative).
+constexpr uint32_t kNearMax = 8;
+#ifndef LUZ_NEAR_REACH
+#define LUZ_NEAR_REACH 1.5f
+#endif
+constexpr uint32_t kNearFlag = 0x80000000u;   // rays_b.w: the ray starts at its near list
+constexpr uint32_t kNearLeafBits = 24;        // rays_c: own leaf | overlapped near[] bits << 24
+
+__device__ __forceinline__ bool box_ok(float4 lo, float4 hi) {
+    return lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z;   // false for empty or NaN boxes
+}
+__device__ __forceinline__ float box_mag(float4 lo, float4 hi) {
+    return fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(lo.y)), fmaxf(fabsf(lo.z), fabsf(hi.x))),
+                 fmaxf(fabsf(hi.y), fabsf(hi.z)));
+}
+
+__global__ void near_leaf_kernel(const uint32_t* __restrict__ order, uint32_t n, uint32_t* __restrict__ leaf_of) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) leaf_of[order[j]] = j;
+}
+
+// One block per instance i: the instances (other than i, with valid boxes) whose box
+// distance to box_i is at most reach, grown by 2^-10 relative and 2^-18 of the boxes'
+// coordinate magnitude (the rounding of the distances here and in near_start), in
+// index order.
+__global__ void __launch_bounds__(256) near_list_kernel(const float4* __restrict__ inst_box,
+                                                        const uint32_t* __restrict__ leaf_of, uint32_t n,
+                                                        float reach, uint4* __restrict__ near) {
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_list[kNearMax];
+    const uint32_t i = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float4 lo = inst_box[2 * i], hi = inst_box[2 * i + 1];
+    const bool valid = box_ok(lo, hi);
+    const float mi = box_mag(lo, hi);
+    uint32_t total = 0;
+    for (uint32_t base = 0; valid && base < n; base += blockDim.x) {
+        const uint32_t j = base + tid;
+        bool nb = false;
+        if (j < n && j != i) {
+            const float4 lj = inst_box[2 * j], hj = inst_box[2 * j + 1];
+            if (box_ok(lj, hj)) {
+                const float dx = fmaxf(fmaxf(lj.x - hi.x, lo.x - hj.x), 0.0f);
+                const float dy = fmaxf(fmaxf(lj.y - hi.y, lo.y - hj.y), 0.0f);
+                const float dz = fmaxf(fmaxf(lj.z - hi.z, lo.z - hj.z), 0.0f);
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                const float lim = reach * (1.0f + 0x1p-10f) + 0x1p-18f * (mi + box_mag(lj, hj));
+                nb = d2 <= lim * lim;
+            }
+        }
+        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, nb);
+        if (lane == 0) s_warp[warp] = __popc(bal);
+        __syncthreads();
+        uint32_t off = total, sum = 0;
+        for (uint32_t w = 0; w < blockDim.x / 32; ++w) {
+            if (w < warp) off += s_warp[w];
+            sum += s_warp[w];
+        }
+        const uint32_t pos = off + __popc(bal & ((1u << lane) - 1u));
+        if (nb && pos < kNearMax) s_list[pos] = j;
+        total += sum;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const uint32_t cnt = valid && total <= kNearMax ? total : 0xFFFFFFFFu;
+        uint32_t l[kNearMax];
+#pragma unroll
+        for (uint32_t k = 0; k < kNearMax; ++k) l[k] = k < cnt ? s_list[k] : 0u;
+        near[4 * i] = make_uint4(leaf_of[i], cnt, l[0], l[1]);
+        near[4 * i + 1] = make_uint4(l[2], l[3], l[4], l[5]);
+        near[4 * i + 2] = make_uint4(__float_as_uint(lo.x), __float_as_uint(lo.y), __float_as_uint(lo.z), l[6]);
+        near[4 * i + 3] = make_uint4(__float_as_uint(hi.x), __float_as_uint(hi.y), __float_as_uint(hi.z), l[7]);
+    }
+}
+
+// Whether the segment o + t d, t in [tmin, tmax], may overlap the box: the slab
+// interval with the near / far distances widened by 2^-12 relative (their rounding;
+// the inverse direction is that of safe_inv, finite).
+__device__ __forceinline__ bool segment_overlaps(V3 o, V3 id, float tmin, float tmax, float4 lo, float4 hi) {
+    const float x0 = (lo.x - o.x) * id.x, x1 = (hi.x - o.x) * id.x;
+    const float y0 = (lo.y - o.y) * id.y, y1 = (hi.y - o.y) * id.y;
+    const float z0 = (lo.z - o.z) * id.z, z1 = (hi.z - o.z) * id.z;
+    const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
+    const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tmax));
+    return tn * (1.0f - 0x1p-12f) <= tf + fabsf(tf) * 0x1p-12f;
+}
+
+// The start of a ray of pixel pix at its near list, or ~0: the own instance's TLAS
+// leaf | the bits of the near instances whose boxes the segment may overlap << 24.
+// The segment's length plus the origin's distance to the box of the pixel's
+// primary-hit instance, grown by 2^-10 relative and 2^-18 of the coordinates'
+// magnitude, must stay within S.near_reach.
+__device__ __forceinline__ uint32_t near_start(const SceneVis& S, V3 o, V3 d, float tmin, float tmax, uint32_t pix) {
+    const float len = tmax * sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+    if (!(len <= S.near_reach)) return ~0u;
+    const uint32_t inst = __ldg(S.hit_instance + pix);
+    if (inst >= S.instance_count) return ~0u;
+    const uint4* rec = S.near + 4 * (size_t)inst;
+    const uint4 u0 = __ldg(rec);
+    if (u0.y > kNearMax) return ~0u;
+    const uint4 u2 = __ldg(rec + 2), u3 = __ldg(rec + 3);
+    const float4 lo = make_float4(__uint_as_float(u2.x), __uint_as_float(u2.y), __uint_as_float(u2.z), 0.f),
+                 hi = make_float4(__uint_as_float(u3.x), __uint_as_float(u3.y), __uint_as_float(u3.z), 0.f);
+    if (!box_ok(lo, hi)) return ~0u;
+    const float ex = fmaxf(fmaxf(lo.x - o.x, o.x - hi.x), 0.0f);
+    const float ey = fmaxf(fmaxf(lo.y - o.y, o.y - hi.y), 0.0f);
+    const float ez = fmaxf(fmaxf(lo.z - o.z, o.z - hi.z), 0.0f);
+    const float m = fmaxf(box_mag(lo, hi), fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)));
+    const float r = (sqrtf(ex * ex + ey * ey + ez * ez) + len) * (1.0f + 0x1p-10f) + 0x1p-18f * m;
+    if (!(r <= S.near_reach)) return ~0u;
+    uint32_t bits = 0;
+    if (u0.y > 0) {
+        const uint4 u1 = __ldg(rec + 1);
+        const uint32_t l[kNearMax] = {u0.z, u0.w, u1.x, u1.y, u1.z, u1.w, u2.w, u3.w};
+        const V3 id = safe_inv(d);
+#pragma unroll
+        for (uint32_t k = 0; k < kNearMax; ++k) {
+            if (k >= u0.y) break;
+            const uint4* nr = S.near + 4 * (size_t)l[k];
+            const uint4 a = __ldg(nr + 2), b = __ldg(nr + 3);
+            const float4 nlo = make_float4(__uint_as_float(a.x), __uint_as_float(a.y), __uint_as_float(a.z), 0.f),
+                         nhi = make_float4(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z), 0.f);
+            if (segment_overlaps(o, id, tmin, tmax, nlo, nhi)) bits |= 1u << k;
+        }
+    }
+    return u0.x | (bits << kNearLeafBits);
+}
 
 // Ray generation pass of one chunk: items [k0, k0 + chunk) of the frame's
 // (slot, lit pixel) list, slot-major, one record per item in structure-of-arrays
@@ -32,7 +172,7 @@ namespace luz {
 // lanes of a traversing warp. Also resets the traversal's work counter.
 __global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, unsigned long long k0,
                                                      unsigned long long chunk, float4* __restrict__ rays_a,
-                                                     float4* __restrict__ rays_b) {
+                                                     float4* __restrict__ rays_b, uint32_t* __restrict__ rays_c) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *C.work_counter = 0ull;
     const uint32_t lit = *S.lit_count;
     const unsigned long long total = (unsigned long long)lit * (S.shadow_slots + S.ao_samples);
@@ -52,7 +192,17 @@ __global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, un
         uint32_t pix;
         bool ok = gen_ray(S, C, slot, j, wo, wd, tmin, tmax, out, record_hit, pix);
         rays_a[item - k0] = make_float4(wo.x, wo.y, wo.z, ok ? tmax : ninf);
-        if (ok) rays_b[item - k0] = make_float4(wd.x, wd.y, wd.z, __uint_as_float(pix));   // read only for rays
+        if (ok) {   // read only for rays
+            uint32_t tag = pix;
+            if (S.near_reach > 0.0f) {
+                const uint32_t start = near_start(S, wo, wd, tmin, tmax, pix);
+                if (start != ~0u) {
+                    tag |= kNearFlag;
+                    rays_c[item - k0] = start;
+                }
+            }
+            rays_b[item - k0] = make_float4(wd.x, wd.y, wd.z, __uint_as_float(tag));
+        }
         slot += step_slot;
         j += step_j;
         if (j >= lit) { j -= lit; ++slot; }
@@ -65,7 +215,8 @@ __global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, un
 template <bool kStats, bool kStaged>
 __global__ void __launch_bounds__(kVisThreads, LUZ_VIS_MIN_BLOCKS)
 visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long long chunk,
-                  const float4* __restrict__ rays_a, const float4* __restrict__ rays_b, unsigned long long* stats) {
+                  const float4* __restrict__ rays_a, const float4* __restrict__ rays_b,
+                  const uint32_t* __restrict__ rays_c, unsigned long long* stats) {
     extern __shared__ float4 smem[];
     const uint32_t staged = min(S.tlas_node_count, C.smem_nodes);
     for (uint32_t i = threadIdx.x; i < staged * kNode4F4; i += blockDim.x) smem[i] = __ldg(S.tlas_nodes + i);
@@ -113,10 +264,27 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
                     if (tmin <= a.w) {
                         const float4 b = __ldg(rays_b + local);
                         if (kStats) ++rays;
-                        const uint32_t pix = __float_as_uint(b.w);
+                        const uint32_t tag = __float_as_uint(b.w), pix = tag & ~kNearFlag;
                         uint32_t* out = record_hit ? S.shadow_bits + (size_t)slot * S.words + (pix >> 5)
                                                    : S.ao_bits + (size_t)(slot - S.shadow_slots) * S.words + (pix >> 5);
                         start_ray(r, c, S, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, tmin, a.w, out, record_hit, pix);
+                        if (tag & kNearFlag) {
+                            // Start at the own instance's leaf, the overlapped near
+                            // instances' leaves stacked.
+                            const uint32_t start = __ldg(rays_c + local), leaf = start & ((1u << kNearLeafBits) - 1u);
+                            r.node = ~(int)leaf;
+                            if (start >> kNearLeafBits) {
+                                const uint4* rec = S.near + 4 * (size_t)__ldg(S.order + leaf);
+                                const uint4 u0 = __ldg(rec), u1 = __ldg(rec + 1);
+                                const uint32_t l[kNearMax] = {u0.z, u0.w, u1.x, u1.y, u1.z, u1.w,
+                                                              __ldg(rec + 2).w, __ldg(rec + 3).w};
+                                int sp = 0;
+#pragma unroll
+                                for (uint32_t k = 0; k < kNearMax; ++k)
+                                    if ((start >> (kNearLeafBits + k)) & 1u) s_stack[(sp++) * 32] = ~__ldg(S.leaf_of + l[k]);
+                                r.sp = sp;
+                            }
+                        }
                         active = true;
                     }
                 }
@@ -227,6 +395,11 @@ SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index) 
     S.shadow_bits = f->shadow_bits;
     S.ao_bits = f->ao_bits;
     S.cull = f->shadow_cull ? 1 : 0;
+    S.near = t->near;
+    S.order = t->order;
+    S.leaf_of = t->leaf_of;
+    S.hit_instance = f->hit_instance;
+    S.near_reach = 0.0f;
     return S;
 }
 
@@ -284,13 +457,26 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         LUZ_CUDA(ctx, cudaStreamSynchronize(st));
         cudaFree(f->rays_a);
         cudaFree(f->rays_b);
+        cudaFree(f->rays_c);
         f->rays_a = f->rays_b = nullptr;
+        f->rays_c = nullptr;
         f->rays_cap = 0;
         LUZ_CUDA(ctx, cudaMalloc(&f->rays_a, (size_t)need * sizeof(float4)));
         LUZ_CUDA(ctx, cudaMalloc(&f->rays_b, (size_t)need * sizeof(float4)));
+        LUZ_CUDA(ctx, cudaMalloc(&f->rays_c, (size_t)need * sizeof(uint32_t)));
         f->rays_cap = need;
     }
     const unsigned long long chunk = std::min<unsigned long long>(max_items, f->rays_cap);
+    // Near lists of this TLAS for rays that stay within LUZ_NEAR_REACH AO radii of their
+    // own instance's box (the AO rays, and shadow rays to nearby lights).
+    const float reach = LUZ_NEAR_REACH * f->h_scene.ao_max;
+    if (t->count > 0 && t->count < (1u << kNearLeafBits) && reach > 0.0f && std::isfinite(reach)) {
+        near_leaf_kernel<<<(t->count + 255) / 256, 256, 0, st>>>(t->order, t->count, t->leaf_of);
+        LUZ_LAUNCHED(ctx, "near_leaf_kernel");
+        near_list_kernel<<<t->count, 256, 0, st>>>(tlas_instance_boxes(t), t->leaf_of, t->count, reach, t->near);
+        LUZ_LAUNCHED(ctx, "near_list_kernel");
+        S.near_reach = reach;
+    }
     static int raygen_blocks = 0;   // resident 256-thread blocks per SM: the grid is one wave
     if (raygen_blocks == 0) {
         LUZ_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&raygen_blocks, raygen_kernel, 256, 0));
@@ -299,17 +485,17 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     for (unsigned long long k0 = 0; k0 < max_items; k0 += chunk) {
         prof_begin(ctx, LUZ_KERNEL_RAYGEN);
         raygen_kernel<<<(uint32_t)(ctx->sm_count * raygen_blocks), 256, 0, st>>>(S, C, k0, chunk, f->rays_a,
-                                                                                  f->rays_b);
+                                                                                  f->rays_b, f->rays_c);
         prof_end(ctx);
         LUZ_LAUNCHED(ctx, "raygen_kernel");
         if (d_stats) {
-            if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, d_stats);
-            else visibility_kernel<true, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, d_stats);
+            if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, d_stats);
+            else visibility_kernel<true, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, d_stats);
             LUZ_LAUNCHED(ctx, "visibility_kernel<stats>");
         } else {
             prof_begin(ctx, LUZ_KERNEL_TRAVERSAL);
-            if (staged) visibility_kernel<false, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, nullptr);
-            else visibility_kernel<false, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, nullptr);
+            if (staged) visibility_kernel<false, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, nullptr);
+            else visibility_kernel<false, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, nullptr);
             prof_end(ctx);
             LUZ_LAUNCHED(ctx, "visibility_kernel");
         }

@@ -22,6 +22,12 @@ struct SceneVis {
     uint32_t width, words;
     uint32_t* shadow_bits;
     uint32_t* ao_bits;
+    // Short rays (near lists, visibility_kernel only; near_reach = 0 disables them)
+    const uint4* near;
+    const uint32_t* order;      // TLAS leaf -> instance input index
+    const uint32_t* leaf_of;    // instance input index -> TLAS leaf
+    const uint32_t* hit_instance;
+    float near_reach;
 };
 
 struct VisCommon {
@@ -38,6 +44,8 @@ const VisTuning& vis_tuning(const luz_ctx* ctx);
 // Launch-independent inputs of the visibility kernels (blue noise, status word, shape).
 VisCommon make_vis_common(luz_ctx* ctx, unsigned long long* work_counter);
 SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index);
+// World boxes of the last TLAS build's instances (input order, lo / hi float4 pairs).
+const float4* tlas_instance_boxes(const luz_tlas* t);
 luz_status clear_visibility(luz_ctx* ctx, luz_frame* f);
 luz_status launch_visibility_batch(luz_ctx* ctx, const SceneVis* d_scenes, uint32_t n,
                                    unsigned long long* d_offsets, unsigned long long* work_counter,
