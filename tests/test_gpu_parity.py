@@ -116,6 +116,38 @@ def test_config2_reduced_resolution_parity(ctx):
     assert rel.max() <= RADIANCE_RTOL, rel.max()
 
 
+@pytest.mark.parametrize("ao_max", [0.5, 3.0, 12.0])
+def test_short_rays_near_lists_match_oracle(ctx, ao_max):
+    """AO rays whose segment stays within 1.5 AO radii of their own instance's box start
+    at that instance's TLAS leaf, with the near instances whose boxes the segment
+    overlaps on the stack; a list of more than 8 instances falls back to the TLAS root.
+    On the config-1 cubes a short radius gives few near instances, a medium one masks
+    near instances in and out, a long one overflows most lists: the masks stay the
+    oracle's."""
+    s = _cfg1(160, 160)
+    s.set_sampling(8, ao_max=ao_max)
+    g = gpu_frame(ctx, s)
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    assert bits_mismatch(g.frame.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+    assert bits_mismatch(g.frame.read(L.PLANE_SHADOW_BITS), f.shadow_bits[: f.shadow_slots]) == 0
+
+
+def test_short_rays_skip_the_tlas(ctx):
+    """AO rays of the sparse two-level scene all start at their own instance's leaf: the
+    counting build of the traversal sees almost no TLAS node per ray, and the masks are
+    the oracle's."""
+    s = L.HostScene(2, width=240, height=136, meshes=8, instances=256, subdivisions=4)
+    s.set_sampling(4, light_samples=0)
+    g = gpu_frame(ctx, s)
+    st = g.frame.trace_stats(g.tlas, 0)
+    assert st["rays"] > 0
+    assert st["tlas_nodes"] < 0.5 * st["rays"], st
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    assert bits_mismatch(g.frame.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+
+
 def test_render_frame_single_call_matches_stages(ctx):
     s = _cfg1(128, 128)
     g = gpu_frame(ctx, s)
