@@ -74,7 +74,7 @@ luz_status ensure_scratch(luz_ctx* ctx, size_t bytes) {
 
 static void free_frame_buffers(luz_frame* f) {
     void* ptrs[] = {f->albedo, f->normal, f->material, f->emission, f->depth, f->light,
-                    f->primary_hit, f->hit_instance, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->signal,
+                    f->primary_hit, f->hit_instance, f->gb_coarse, f->gb_fine, f->shadow_bits, f->ao_bits, f->ao, f->ao_denoised, f->signal,
                     f->unshadowed, f->denoised, f->surf, f->surf_mat,
                     f->features, f->lin_depth, f->taa, f->taa_next, f->compose, f->hist, f->hist_state,
                     f->block_counts, f->lit_count, f->dn_list, f->dn_count, f->d_scene, f->d_lights, f->d_models,
@@ -439,6 +439,8 @@ luz_status luz_frame_create(luz_ctx* ctx, uint32_t width, uint32_t height, luz_f
     A((void**)&f->light, P * 16);
     A((void**)&f->primary_hit, P * 8);
     A((void**)&f->hit_instance, P * 4);
+    A((void**)&f->gb_coarse, (size_t)((width + 63) / 64) * ((height + 63) / 64) * 256 * 4);
+    A((void**)&f->gb_fine, (size_t)((width + 7) / 8) * ((height + 7) / 8) * 16 * 4);
     A((void**)&f->ao, P * 4);
     A((void**)&f->ao_denoised, P * 4);
     A((void**)&f->signal, P * 16);

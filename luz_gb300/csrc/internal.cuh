@@ -184,6 +184,8 @@ struct luz_frame {
     float4* light = nullptr;        // RGBA32F
     uint2* primary_hit = nullptr;
     uint32_t* hit_instance = nullptr;    // input index of the primary hit's instance (~0 = miss)
+    uint32_t* gb_coarse = nullptr;       // G-buffer candidate leaves per 64x64 tile (count + 255)
+    uint32_t* gb_fine = nullptr;         // and per 8x8 tile (count + 15)
     // visibility
     uint32_t* shadow_bits = nullptr;
     uint32_t* ao_bits = nullptr;

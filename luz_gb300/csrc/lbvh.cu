@@ -635,10 +635,10 @@ __global__ void tlas_morton_kernel(const float4* inst_box, uint32_t n, const uin
 __global__ void tlas_emit_kernel(const DevInstanceInput* in, const float4* inst_box, uint32_t n,
                                  const unsigned long long* keys, const uint32_t* vals,
                                  DevInstance* inst_out, float4* leaf_box, uint32_t* morton_out,
-                                 uint32_t* order_out) {
+                                 uint32_t* order_out, uint32_t* leaf_of_out) {
     uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    tlas_emit_one(in, inst_box, j, keys[j], vals[j], inst_out, leaf_box, morton_out, order_out);
+    tlas_emit_one(in, inst_box, j, keys[j], vals[j], inst_out, leaf_box, morton_out, order_out, leaf_of_out);
 }
 
 
@@ -1016,6 +1016,7 @@ static TlasScratch carve_tlas(luz_tlas* t) {
     a.inst_out = t->instances;
     a.morton_out = t->morton;
     a.order_out = t->order;
+    a.leaf_of_out = t->leaf_of;
     a.nodes_out = t->nodes;
     a.levels = t->levels;
     a.nodes4 = t->nodes4;
@@ -1024,6 +1025,7 @@ static TlasScratch carve_tlas(luz_tlas* t) {
 
 TlasBuildArgs tlas_build_args(luz_tlas* t) { return carve_tlas(t).a; }
 const float4* tlas_instance_boxes(const luz_tlas* t) { return carve_tlas(const_cast<luz_tlas*>(t)).a.inst_box; }
+const float4* tlas_leaf_boxes(const luz_tlas* t) { return carve_tlas(const_cast<luz_tlas*>(t)).a.leaf_box; }
 
 // Device part of a TLAS build from the packed staging buffer: one host-to-device copy
 // from pinned memory and the LBVH kernels; no host synchronisation (graph-capturable).
@@ -1082,7 +1084,7 @@ luz_status launch_tlas_build(luz_ctx* ctx, luz_tlas* t) {
     LUZ_LAUNCHED(ctx, "karras_kernel");
     tlas_emit_kernel<<<cdiv(n, 128), 128, 0, st>>>(t->d_input, inst_box, n, sb.keys[res],
                                                    sb.vals[res], t->instances, leaf_box,
-                                                   t->morton, t->order);
+                                                   t->morton, t->order, t->leaf_of);
     LUZ_LAUNCHED(ctx, "tlas_emit_kernel");
     refit_kernel<<<cdiv(n, 128), 128, 0, st>>>(d_seg, d_zero, 1, n, leaf_box, node_parent,
                                                leaf_parent, flags);

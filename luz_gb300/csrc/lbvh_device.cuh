@@ -280,9 +280,11 @@ __device__ __forceinline__ bool tlas_instance_one(const DevInstanceInput* in, ui
 // Leaf j of the sorted order: instance record, leaf box, sorted Morton key and order.
 __device__ __forceinline__ void tlas_emit_one(const DevInstanceInput* in, const float4* inst_box, uint32_t j,
                                               unsigned long long key, uint32_t i, DevInstance* inst_out,
-                                              float4* leaf_box, uint32_t* morton_out, uint32_t* order_out) {
+                                              float4* leaf_box, uint32_t* morton_out, uint32_t* order_out,
+                                              uint32_t* leaf_of_out) {
     morton_out[j] = (uint32_t)key & 0x3FFFFFFFu;
     order_out[j] = i;
+    leaf_of_out[i] = j;
     const DevInstanceInput ii = in[i];
     DevInstance d;
     affine_inverse(ii.o2w, d.w2o);
@@ -400,6 +402,7 @@ struct TlasBuildArgs {
     float4* leaf_box;
     uint32_t* morton_out;
     uint32_t* order_out;
+    uint32_t* leaf_of_out;      // instance input index -> its leaf
     float4* nodes_out;
     uint32_t* queue;
     uint32_t* newidx;
@@ -478,7 +481,8 @@ __device__ __forceinline__ void tlas_build_block(Args A, unsigned long long* s_k
     for (uint32_t q = tid; q < m; q += nt) karras_node(sd, (int)q, A.keys, A.node_parent, A.leaf_parent, dev_status);
     __syncthreads();
     for (uint32_t j = tid; j < n; j += nt)
-        tlas_emit_one(A.in, A.inst_box, j, A.keys[j], A.vals[j], A.inst_out, A.leaf_box, A.morton_out, A.order_out);
+        tlas_emit_one(A.in, A.inst_box, j, A.keys[j], A.vals[j], A.inst_out, A.leaf_box, A.morton_out, A.order_out,
+                      A.leaf_of_out);
     __syncthreads();
     for (uint32_t g = tid; g < n; g += nt) refit_leaf<true>(sd, g, A.leaf_box, A.node_parent, A.leaf_parent, A.flags);
     __syncthreads();

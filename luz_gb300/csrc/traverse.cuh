@@ -153,12 +153,16 @@ struct AcceptAll {
 // flag of 2 every candidate hit is offered to `accept(instance input, custom index,
 // primitive, b0, b1, b2)` first, and a rejected hit leaves the ray going (an
 // alpha test).
+// start / nstart: when nstart >= 0 the ray visits only the TLAS leaves start[0..nstart)
+// (in that order), in place of the TLAS from its root: a superset of the instances
+// whose boxes the ray can reach gives the full traversal's result.
 template <bool kClosest, bool kStats = false, typename Accept = AcceptAll>
 __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float tmin, float tmax,
                                           uint32_t ray_mask, const uint8_t* __restrict__ skip,
                                           uint32_t skip_count, ClosestHit* hit, uint32_t& err,
-                                          TraceCounters* cnt = nullptr, const Accept& accept = Accept()) {
-    if (T.count == 0) return false;
+                                          TraceCounters* cnt = nullptr, const Accept& accept = Accept(),
+                                          const uint32_t* start = nullptr, int nstart = -1) {
+    if (T.count == 0 || nstart == 0) return false;
     if (!finite3(wo) || !finite3(wd) || !(tmin <= tmax)) return false;
     if (wd.x == 0.0f && wd.y == 0.0f && wd.z == 0.0f) return false;
     const V3 widir = safe_inv(wd);
@@ -169,6 +173,10 @@ __device__ __forceinline__ bool trace_ray(const TlasView& T, V3 wo, V3 wd, float
     int stack[kStackSize];
     int sp = 0;
     int node = 0;
+    if (nstart > 0) {   // nstart <= kStackSize: the caller's lists are short
+        node = ~(int)start[0];
+        for (int k = nstart - 1; k >= 1; --k) stack[sp++] = ~(int)start[k];
+    }
     bool in_blas = false;
     const float4* __restrict__ nodes = T.nodes;
     const float4* __restrict__ tris = nullptr;

@@ -53,11 +53,6 @@ __device__ __forceinline__ float box_mag(float4 lo, float4 hi) {
                  fmaxf(fabsf(hi.y), fabsf(hi.z)));
 }
 
-__global__ void near_leaf_kernel(const uint32_t* __restrict__ order, uint32_t n, uint32_t* __restrict__ leaf_of) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < n) leaf_of[order[j]] = j;
-}
-
 // One block per instance i: the instances (other than i, with valid boxes) whose box
 // distance to box_i is at most reach, grown by 2^-10 relative and 2^-18 of the boxes'
 // coordinate magnitude (the rounding of the distances here and in near_start), in
@@ -471,8 +466,6 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     // own instance's box (the AO rays, and shadow rays to nearby lights).
     const float reach = LUZ_NEAR_REACH * f->h_scene.ao_max;
     if (t->count > 0 && t->count < (1u << kNearLeafBits) && reach > 0.0f && std::isfinite(reach)) {
-        near_leaf_kernel<<<(t->count + 255) / 256, 256, 0, st>>>(t->order, t->count, t->leaf_of);
-        LUZ_LAUNCHED(ctx, "near_leaf_kernel");
         near_list_kernel<<<t->count, 256, 0, st>>>(tlas_instance_boxes(t), t->leaf_of, t->count, reach, t->near);
         LUZ_LAUNCHED(ctx, "near_list_kernel");
         S.near_reach = reach;
