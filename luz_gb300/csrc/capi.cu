@@ -79,7 +79,8 @@ static void free_frame_buffers(luz_frame* f) {
                     f->features, f->lin_depth, f->taa, f->taa_next, f->compose, f->hist, f->hist_state,
                     f->block_counts, f->lit_count, f->dn_list, f->dn_count, f->d_scene, f->d_lights, f->d_models,
                     f->d_slot_table, f->d_light_slot, f->d_model_skip, f->work_counter, f->d_textures,
-                    f->d_texels, f->d_shadow_lights, f->d_shadow_maps, f->rays_a, f->rays_b, f->rays_c};
+                    f->d_texels, f->d_shadow_lights, f->d_shadow_maps, f->rays_a, f->rays_b, f->rays_c, f->beams,
+                    f->beam_lists};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }

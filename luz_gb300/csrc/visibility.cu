@@ -39,6 +39,15 @@ namespace luz {
 // instance whose leaf box the full traversal would cull finds no hit either (boxes
 // are conservative).
 constexpr uint32_t kNearMax = 8;
+// Shadow-ray beams: groups of kBeamGroup consecutive items (lanes of a warp in ray
+// generation), lists of up to kBeamMax TLAS leaves.
+#ifndef LUZ_BEAM_SHIFT
+#define LUZ_BEAM_SHIFT 5
+#endif
+constexpr uint32_t kBeamShift = LUZ_BEAM_SHIFT;
+constexpr uint32_t kBeamGroup = 1u << kBeamShift;
+constexpr uint32_t kBeamMax = 15;             // list: count + 15 leaves (64 B per group)
+constexpr uint32_t kBeamWords = kBeamMax + 1;
 #ifndef LUZ_NEAR_REACH
 #define LUZ_NEAR_REACH 1.5f
 #endif
@@ -165,28 +174,33 @@ __device__ __forceinline__ uint32_t near_start(const SceneVis& S, V3 o, V3 d, fl
 // gets tMax = -inf (its AO miss is recorded here) and no rays_b entry. Separated from traversal so the
 // long arithmetic of light.frag's sampling runs on full warps, not on the few idle
 // lanes of a traversing warp. Also resets the traversal's work counter.
-__global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, unsigned long long k0,
+__global__ void __launch_bounds__(256, 5) raygen_kernel(SceneVis S, VisCommon C, unsigned long long k0,
                                                      unsigned long long chunk, float4* __restrict__ rays_a,
-                                                     float4* __restrict__ rays_b, uint32_t* __restrict__ rays_c) {
+                                                     float4* __restrict__ rays_b, uint32_t* __restrict__ rays_c,
+                                                     float4* __restrict__ beams) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *C.work_counter = 0ull;
     const uint32_t lit = *S.lit_count;
     const unsigned long long total = (unsigned long long)lit * (S.shadow_slots + S.ao_samples);
     if (k0 >= total) return;
     const unsigned long long end = min(total, k0 + chunk);
-    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t stride = gridDim.x * blockDim.x, lane = threadIdx.x & 31;
+    const unsigned long long shadow_items = (unsigned long long)lit * S.shadow_slots;
     const float ninf = __int_as_float(0xff800000);
-    // (slot, j) of the thread's first item by one division, then stepped by the stride
+    // (slot, j) of the thread's first item by one division, then stepped by the stride.
+    // The loop runs while any lane of the warp has an item (the beam reductions below
+    // take the whole warp): a warp's 32 items are consecutive and 32-aligned.
     unsigned long long item = k0 + blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t slot = (uint32_t)(item / lit), j = (uint32_t)(item - (unsigned long long)slot * lit);
     const uint32_t step_slot = stride / lit, step_j = stride - step_slot * lit;
-    for (; item < end; item += stride) {
-        V3 wo, wd;
-        float tmin, tmax;
+    for (; item - lane < end; item += stride) {
+        const bool live = item < end;
+        V3 wo{0.f, 0.f, 0.f}, wd{0.f, 0.f, 0.f};
+        float tmin = 0.f, tmax = 0.f;
         uint32_t* out;
-        bool record_hit;
+        bool record_hit = false;
         uint32_t pix;
-        bool ok = gen_ray(S, C, slot, j, wo, wd, tmin, tmax, out, record_hit, pix);
-        rays_a[item - k0] = make_float4(wo.x, wo.y, wo.z, ok ? tmax : ninf);
+        const bool ok = live && gen_ray(S, C, slot, j, wo, wd, tmin, tmax, out, record_hit, pix);
+        if (live) rays_a[item - k0] = make_float4(wo.x, wo.y, wo.z, ok ? tmax : ninf);
         if (ok) {   // read only for rays
             uint32_t tag = pix;
             if (S.near_reach > 0.0f) {
@@ -198,10 +212,142 @@ __global__ void __launch_bounds__(256) raygen_kernel(SceneVis S, VisCommon C, un
             }
             rays_b[item - k0] = make_float4(wd.x, wd.y, wd.z, __uint_as_float(tag));
         }
+        if (beams && item - lane < shadow_items) {
+            // Beam of a group of kBeamGroup items (lanes): balls around the origins and
+            // around the end points of its traced shadow rays, centred on the first such ray.
+            const bool sh = ok && record_hit;
+            const uint32_t first = lane & ~(kBeamGroup - 1u);
+            const uint32_t m = (__ballot_sync(0xFFFFFFFFu, sh) >> first) & (0xFFFFFFFFu >> (32 - kBeamGroup));
+            const unsigned long long g = (item - k0) >> kBeamShift;
+            if (m == 0u) {
+                if (lane == first) beams[2 * g] = make_float4(0.f, 0.f, 0.f, -1.0f);   // no traced shadow ray
+            }
+            {
+                const int src = (int)first + (m ? __ffs(m) - 1 : 0);
+                const V3 e = V3{wo.x + wd.x * tmax, wo.y + wd.y * tmax, wo.z + wd.z * tmax};
+                const V3 co = V3{__shfl_sync(0xFFFFFFFFu, wo.x, src), __shfl_sync(0xFFFFFFFFu, wo.y, src),
+                                 __shfl_sync(0xFFFFFFFFu, wo.z, src)};
+                const V3 ce = V3{__shfl_sync(0xFFFFFFFFu, e.x, src), __shfl_sync(0xFFFFFFFFu, e.y, src),
+                                 __shfl_sync(0xFFFFFFFFu, e.z, src)};
+                float ro = sh ? length(wo - co) : 0.0f, re = sh ? length(e - ce) : 0.0f;
+                uint32_t bad = sh && !(finite3(e) && ro <= 3.0e38f && re <= 3.0e38f) ? 1u : 0u;
+#pragma unroll
+                for (int o = kBeamGroup / 2; o >= 1; o >>= 1) {
+                    ro = fmaxf(ro, __shfl_xor_sync(0xFFFFFFFFu, ro, o));
+                    re = fmaxf(re, __shfl_xor_sync(0xFFFFFFFFu, re, o));
+                    bad |= __shfl_xor_sync(0xFFFFFFFFu, bad, o);
+                }
+                if (lane == first && m != 0u) {   // r_o = +inf: an end point not finite
+                    beams[2 * g] = make_float4(co.x, co.y, co.z, bad ? __int_as_float(0x7f800000) : ro);
+                    beams[2 * g + 1] = make_float4(ce.x, ce.y, ce.z, re);
+                }
+            }
+        }
         slot += step_slot;
         j += step_j;
         if (j >= lit) { j -= lit; ++slot; }
     }
+}
+
+// ---------------------------------------------------------------- beam lists
+// The traced shadow rays of a group of kBeamGroup consecutive items (one light sample,
+// neighbouring lit pixels in tile order) start in a ball B_o around their origins and
+// end in a ball B_e around their end points, so each lies in the convex hull of the
+// two balls, itself inside the capsule of radius max(r_o, r_e) around the segment
+// between the centres. A leaf whose box, grown by that radius, the segment misses
+// cannot be hit by any ray of the group: the group's rays traverse only the leaves the
+// capsule reaches (nearest first), or the TLAS from its root when there are more than
+// kBeamMax of them. The radius is grown by 2^-10 relative and 2^-16 of the centres'
+// magnitude, above the rounding of the centres, radii, end points and hit points.
+constexpr uint32_t kBeamAll = 0xFFFFFFFFu;    // count: traverse from the TLAS root
+constexpr int kBeamStack = 48;                 // overflow: the list falls back to the TLAS root
+
+__global__ void __launch_bounds__(256) beam_list_kernel(SceneVis S, unsigned long long k0, unsigned long long chunk,
+                                                        const float4* __restrict__ beams, uint32_t* __restrict__ lists) {
+    const uint32_t lit = *S.lit_count;
+    const unsigned long long shadow_items = (unsigned long long)lit * S.shadow_slots;
+    if (k0 >= shadow_items) return;
+    const unsigned long long n = min(chunk, shadow_items - k0);
+    const unsigned long long g = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (n + kBeamGroup - 1) / kBeamGroup) return;
+    uint32_t* list = lists + kBeamWords * g;
+    const float4 bo = beams[2 * g], be = beams[2 * g + 1];
+    if (bo.w < 0.0f) return;   // no traced shadow ray in the group: the list is never read
+    const V3 o = V3{bo.x, bo.y, bo.z}, d = V3{be.x - bo.x, be.y - bo.y, be.z - bo.z};
+    const float r0 = fmaxf(bo.w, be.w);
+    const float mag = ((fabsf(bo.x) + fabsf(bo.y)) + (fabsf(bo.z) + fabsf(be.x))) + (fabsf(be.y) + fabsf(be.z));
+    const float r = r0 * (1.0f + 0x1p-10f) + 0x1p-16f * (mag + r0);
+    if (!(r <= 3.0e38f) || !finite3(o) || !finite3(d)) {
+        list[0] = kBeamAll;
+        return;
+    }
+    const V3 id = safe_inv(d);
+    uint32_t out[kBeamMax];
+    uint32_t cnt = 0;
+    int stack[kBeamStack];
+    int sp = 0, node = 0;
+    for (uint32_t iter = 0; iter < kTraversalCap; ++iter) {
+        const float4* np = S.tlas_nodes + (size_t)node * kNode4F4;
+        const float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3), lz = __ldg(np + 4),
+                     hz = __ldg(np + 5), cf = __ldg(np + 6);
+        const float L[3][4] = {{lx.x, lx.y, lx.z, lx.w}, {ly.x, ly.y, ly.z, ly.w}, {lz.x, lz.y, lz.z, lz.w}};
+        const float H[3][4] = {{hx.x, hx.y, hx.z, hx.w}, {hy.x, hy.y, hy.z, hy.w}, {hz.x, hz.y, hz.z, hz.w}};
+        const int ch[4] = {__float_as_int(cf.x), __float_as_int(cf.y), __float_as_int(cf.z), __float_as_int(cf.w)};
+        float tk[4];
+        bool hk[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float ax0 = (L[0][k] - r - o.x) * id.x, ax1 = (H[0][k] + r - o.x) * id.x;
+            const float ay0 = (L[1][k] - r - o.y) * id.y, ay1 = (H[1][k] + r - o.y) * id.y;
+            const float az0 = (L[2][k] - r - o.z) * id.z, az1 = (H[2][k] + r - o.z) * id.z;
+            const float tn = fmaxf(fmaxf(fminf(ax0, ax1), fminf(ay0, ay1)), fmaxf(fminf(az0, az1), 0.0f));
+            const float tf = fminf(fminf(fmaxf(ax0, ax1), fmaxf(ay0, ay1)), fminf(fmaxf(az0, az1), 1.0f));
+            hk[k] = ch[k] != kEmptyChild && tn <= tf + fabsf(tf) * 0x1p-12f;
+            tk[k] = tn;
+        }
+        // Hit children by entry distance (misses last): leaves appended nearest first,
+        // internal nodes pushed farthest first (the nearest is visited next).
+        int ck[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            ck[k] = hk[k] ? ch[k] : kEmptyChild;
+            if (!hk[k]) tk[k] = __int_as_float(0x7f800000);
+        }
+#define LUZ_BX(a, b)                                                                          \
+        if (tk[b] < tk[a]) {                                                                  \
+            const float t_ = tk[a]; tk[a] = tk[b]; tk[b] = t_;                               \
+            const int c_ = ck[a]; ck[a] = ck[b]; ck[b] = c_;                                  \
+        }
+        LUZ_BX(0, 1) LUZ_BX(2, 3) LUZ_BX(0, 2) LUZ_BX(1, 3) LUZ_BX(1, 2)
+#undef LUZ_BX
+        bool overflow = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (ck[q] < 0 && ck[q] != kEmptyChild) {
+                if (cnt < kBeamMax) out[cnt] = (uint32_t)~ck[q];
+                ++cnt;
+            }
+        }
+#pragma unroll
+        for (int q = 3; q >= 0; --q) {
+            if (ck[q] >= 0) {
+                if (sp < kBeamStack) stack[sp++] = ck[q];
+                else overflow = true;
+            }
+        }
+        if (overflow || cnt > kBeamMax) {
+            list[0] = kBeamAll;
+            return;
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    if (sp != 0) {   // the step cap ran out
+        list[0] = kBeamAll;
+        return;
+    }
+    list[0] = cnt;
+    for (uint32_t k = 0; k < cnt; ++k) list[1 + k] = out[k];
 }
 
 // Traversal of one chunk of generated rays (one scene; the TLAS top may be staged
@@ -263,6 +409,30 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
                         uint32_t* out = record_hit ? S.shadow_bits + (size_t)slot * S.words + (pix >> 5)
                                                    : S.ao_bits + (size_t)(slot - S.shadow_slots) * S.words + (pix >> 5);
                         start_ray(r, c, S, V3{a.x, a.y, a.z}, V3{b.x, b.y, b.z}, tmin, a.w, out, record_hit, pix);
+                        bool go = true;
+                        if (record_hit && S.beam_lists) {
+                            // A shadow ray starts at its group's beam list unless that ran over.
+                            const uint4* bl = reinterpret_cast<const uint4*>(S.beam_lists + kBeamWords * (local >> kBeamShift));
+                            const uint4 u0 = __ldg(bl);
+                            if (u0.x != kBeamAll) {
+                                go = u0.x > 0;   // no leaf reaches the group's capsule: unoccluded
+                                r.node = ~(int)u0.y;
+                                // list words 2..count stacked, the nearest on top
+                                int sp = 0;
+#pragma unroll
+                                for (int q = (int)kBeamWords / 4 - 1; q >= 0; --q) {
+                                    if (4u * (uint32_t)q > u0.x) continue;
+                                    const uint4 u = q == 0 ? u0 : __ldg(bl + q);
+                                    const uint32_t l[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                                    for (int k = 3; k >= 0; --k) {
+                                        const uint32_t w = 4u * (uint32_t)q + (uint32_t)k;
+                                        if (w >= 2 && w <= u0.x) s_stack[(sp++) * 32] = ~l[k];
+                                    }
+                                }
+                                r.sp = sp;
+                            }
+                        }
                         if (tag & kNearFlag) {
                             // Start at the own instance's leaf, the overlapped near
                             // instances' leaves stacked.
@@ -280,7 +450,7 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
                                 r.sp = sp;
                             }
                         }
-                        active = true;
+                        active = go;
                     }
                 }
             }
@@ -395,6 +565,7 @@ SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index) 
     S.leaf_of = t->leaf_of;
     S.hit_instance = f->hit_instance;
     S.near_reach = 0.0f;
+    S.beam_lists = nullptr;
     return S;
 }
 
@@ -453,12 +624,18 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         cudaFree(f->rays_a);
         cudaFree(f->rays_b);
         cudaFree(f->rays_c);
+        cudaFree(f->beams);
+        cudaFree(f->beam_lists);
         f->rays_a = f->rays_b = nullptr;
-        f->rays_c = nullptr;
+        f->rays_c = f->beam_lists = nullptr;
+        f->beams = nullptr;
         f->rays_cap = 0;
+        const size_t groups = ((size_t)need + kBeamGroup - 1) / kBeamGroup;
         LUZ_CUDA(ctx, cudaMalloc(&f->rays_a, (size_t)need * sizeof(float4)));
         LUZ_CUDA(ctx, cudaMalloc(&f->rays_b, (size_t)need * sizeof(float4)));
         LUZ_CUDA(ctx, cudaMalloc(&f->rays_c, (size_t)need * sizeof(uint32_t)));
+        LUZ_CUDA(ctx, cudaMalloc(&f->beams, groups * 2 * sizeof(float4)));
+        LUZ_CUDA(ctx, cudaMalloc(&f->beam_lists, groups * kBeamWords * sizeof(uint32_t)));
         f->rays_cap = need;
     }
     const unsigned long long chunk = std::min<unsigned long long>(max_items, f->rays_cap);
@@ -470,6 +647,8 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         LUZ_LAUNCHED(ctx, "near_list_kernel");
         S.near_reach = reach;
     }
+    const bool beam = t->count > 0 && f->shadow_slots > 0;
+    if (beam) S.beam_lists = f->beam_lists;
     static int raygen_blocks = 0;   // resident 256-thread blocks per SM: the grid is one wave
     if (raygen_blocks == 0) {
         LUZ_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&raygen_blocks, raygen_kernel, 256, 0));
@@ -478,9 +657,15 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     for (unsigned long long k0 = 0; k0 < max_items; k0 += chunk) {
         prof_begin(ctx, LUZ_KERNEL_RAYGEN);
         raygen_kernel<<<(uint32_t)(ctx->sm_count * raygen_blocks), 256, 0, st>>>(S, C, k0, chunk, f->rays_a,
-                                                                                  f->rays_b, f->rays_c);
-        prof_end(ctx);
+                                                                                  f->rays_b, f->rays_c,
+                                                                                  beam ? f->beams : nullptr);
         LUZ_LAUNCHED(ctx, "raygen_kernel");
+        if (beam) {   // timed with ray generation
+            const unsigned long long groups = (chunk + kBeamGroup - 1) / kBeamGroup;
+            beam_list_kernel<<<(uint32_t)((groups + 255) / 256), 256, 0, st>>>(S, k0, chunk, f->beams, f->beam_lists);
+            LUZ_LAUNCHED(ctx, "beam_list_kernel");
+        }
+        prof_end(ctx);
         if (d_stats) {
             if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, d_stats);
             else visibility_kernel<true, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, d_stats);

@@ -28,6 +28,9 @@ struct SceneVis {
     const uint32_t* leaf_of;    // instance input index -> TLAS leaf
     const uint32_t* hit_instance;
     float near_reach;
+    // Shadow-ray beam lists (visibility_kernel only; null disables them): per group of
+    // 32 items, count + 7 TLAS leaves
+    const uint32_t* beam_lists;
 };
 
 struct VisCommon {
