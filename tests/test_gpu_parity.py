@@ -116,6 +116,34 @@ def test_config2_reduced_resolution_parity(ctx):
     assert rel.max() <= RADIANCE_RTOL, rel.max()
 
 
+@pytest.mark.parametrize("place", ["inside_cube", "inside_field"])
+def test_gbuffer_tile_lists_camera_inside_scene(ctx, place):
+    """The G-buffer traces each 8x8 tile through the TLAS leaves its corner-ray cone
+    keeps. With the camera inside an instance's box (every cone keeps that box) or in
+    the middle of the cube field (instances behind the camera and beside it) the planes
+    are still the oracle's bit for bit."""
+    s = _cfg1(96, 64)
+    tr = s.transforms().reshape(-1, 3, 4)
+    c = s.camera()
+    if place == "inside_cube":
+        c.eye[:] = [float(v) for v in tr[1][:, 3]]
+        c.center[:] = [0.0, 0.0, 0.0]
+    else:
+        c.eye[:] = [0.0, 1.0, 0.0]
+        c.center[:] = [8.0, 1.5, 8.0]
+    s.set_camera(c)
+    g = gpu_frame(ctx, s)
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    fr = g.frame
+    assert np.array_equal(fr.read(L.PLANE_DEPTH).ravel().view(np.uint32), f.depth.view(np.uint32))
+    assert np.array_equal(fr.read(L.PLANE_NORMAL).reshape(-1, 4).view(np.uint32), f.normal.view(np.uint32))
+    assert np.array_equal(fr.read(L.PLANE_PRIMARY_HIT).reshape(-1, 2), f.primary_hit)
+    assert (f.primary_hit[:, 0] != 0xFFFFFFFF).sum() > 0
+    assert bits_mismatch(fr.read(L.PLANE_SHADOW_BITS), f.shadow_bits[: f.shadow_slots]) == 0
+    assert bits_mismatch(fr.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+
+
 @pytest.mark.parametrize("ao_max", [0.5, 3.0, 12.0])
 def test_short_rays_near_lists_match_oracle(ctx, ao_max):
     """AO rays whose segment stays within 1.5 AO radii of their own instance's box start
@@ -145,6 +173,26 @@ def test_short_rays_skip_the_tlas(ctx):
     assert st["tlas_nodes"] < 0.5 * st["rays"], st
     _, tl = oracle_scene(s)
     f = oracle_frame(s, tl)
+    assert bits_mismatch(g.frame.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
+
+
+@pytest.mark.parametrize("light_samples", [1, 3])
+def test_shadow_beams_skip_the_tlas(ctx, light_samples):
+    """Shadow rays start at their group's beam list (the TLAS leaves the capsule around
+    32 neighbouring rays of one light sample reaches): on the sparse two-level scene
+    few TLAS nodes are visited per traversed ray, and the masks are the oracle's, with
+    one and with several samples per light (groups then also span slot ends)."""
+    s = L.HostScene(2, width=960, height=540, meshes=8, instances=256, subdivisions=4)
+    s.set_sampling(2, light_samples=light_samples)
+    g = gpu_frame(ctx, s)
+    st = g.frame.trace_stats(g.tlas, 0)
+    assert st["rays"] > 0
+    # 1.5-1.6 measured at this size (the lists get shorter as the pixels get smaller:
+    # 6.0 per ray at 240x136)
+    assert st["tlas_nodes"] < 2.5 * st["rays"], st
+    _, tl = oracle_scene(s)
+    f = oracle_frame(s, tl)
+    assert bits_mismatch(g.frame.read(L.PLANE_SHADOW_BITS), f.shadow_bits[: f.shadow_slots]) == 0
     assert bits_mismatch(g.frame.read(L.PLANE_AO_BITS), f.ao_bits[: f.ao_samples]) == 0
 
 
