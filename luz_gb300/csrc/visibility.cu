@@ -350,6 +350,16 @@ __global__ void __launch_bounds__(256) beam_list_kernel(SceneVis S, unsigned lon
     for (uint32_t k = 0; k < cnt; ++k) list[1 + k] = out[k];
 }
 
+// The slab test of a TLAS leaf's box for the lane's (world-space) ray, as a 4-wide
+// node applies it to the slot holding that leaf.
+__device__ __forceinline__ bool leaf_overlaps(const LaneRay& r, const float4* __restrict__ leaf_box, uint32_t leaf) {
+    const float4 lo = __ldg(leaf_box + 2 * (size_t)leaf), hi = __ldg(leaf_box + 2 * (size_t)leaf + 1);
+    const bool sx = r.signs & 1, sy = (r.signs >> 1) & 1, sz = (r.signs >> 2) & 1;
+    float tn;
+    return slab_ordered(sx ? hi.x : lo.x, sx ? lo.x : hi.x, sy ? hi.y : lo.y, sy ? lo.y : hi.y, sz ? hi.z : lo.z,
+                        sz ? lo.z : hi.z, r, tn);
+}
+
 // Traversal of one chunk of generated rays (one scene; the TLAS top may be staged
 // in shared memory). Shared memory: staged TLAS nodes, then the stacks, then the
 // cold ray state.
@@ -415,10 +425,11 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
                             const uint4* bl = reinterpret_cast<const uint4*>(S.beam_lists + kBeamWords * (local >> kBeamShift));
                             const uint4 u0 = __ldg(bl);
                             if (u0.x != kBeamAll) {
-                                go = u0.x > 0;   // no leaf reaches the group's capsule: unoccluded
-                                r.node = ~(int)u0.y;
-                                // list words 2..count stacked, the nearest on top
-                                int sp = 0;
+                                // The list's leaves whose boxes this ray's slab test keeps
+                                // (the test the TLAS node holding the leaf would apply),
+                                // the nearest first: it starts at the nearest, the others
+                                // stacked; with none it ends unoccluded.
+                                int sp = 0, cur = 0;
 #pragma unroll
                                 for (int q = (int)kBeamWords / 4 - 1; q >= 0; --q) {
                                     if (4u * (uint32_t)q > u0.x) continue;
@@ -427,9 +438,14 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
 #pragma unroll
                                     for (int k = 3; k >= 0; --k) {
                                         const uint32_t w = 4u * (uint32_t)q + (uint32_t)k;
-                                        if (w >= 2 && w <= u0.x) s_stack[(sp++) * 32] = ~l[k];
+                                        if (w >= 1 && w <= u0.x && leaf_overlaps(r, S.leaf_box, l[k])) {
+                                            if (cur) s_stack[(sp++) * 32] = (uint32_t)cur;
+                                            cur = ~(int)l[k];
+                                        }
                                     }
                                 }
+                                go = cur != 0;
+                                r.node = cur;
                                 r.sp = sp;
                             }
                         }
@@ -566,6 +582,7 @@ SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index) 
     S.hit_instance = f->hit_instance;
     S.near_reach = 0.0f;
     S.beam_lists = nullptr;
+    S.leaf_box = nullptr;
     return S;
 }
 
@@ -648,7 +665,10 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         S.near_reach = reach;
     }
     const bool beam = t->count > 0 && f->shadow_slots > 0;
-    if (beam) S.beam_lists = f->beam_lists;
+    if (beam) {
+        S.beam_lists = f->beam_lists;
+        S.leaf_box = tlas_leaf_boxes(t);
+    }
     static int raygen_blocks = 0;   // resident 256-thread blocks per SM: the grid is one wave
     if (raygen_blocks == 0) {
         LUZ_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&raygen_blocks, raygen_kernel, 256, 0));

@@ -31,6 +31,7 @@ struct SceneVis {
     // Shadow-ray beam lists (visibility_kernel only; null disables them): per group of
     // 32 items, count + 7 TLAS leaves
     const uint32_t* beam_lists;
+    const float4* leaf_box;      // TLAS leaf boxes (lo, hi), leaf order
 };
 
 struct VisCommon {
@@ -47,8 +48,10 @@ const VisTuning& vis_tuning(const luz_ctx* ctx);
 // Launch-independent inputs of the visibility kernels (blue noise, status word, shape).
 VisCommon make_vis_common(luz_ctx* ctx, unsigned long long* work_counter);
 SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index);
-// World boxes of the last TLAS build's instances (input order, lo / hi float4 pairs).
+// World boxes of the last TLAS build's instances (input order, lo / hi float4 pairs)
+// and its leaf boxes (leaf order).
 const float4* tlas_instance_boxes(const luz_tlas* t);
+const float4* tlas_leaf_boxes(const luz_tlas* t);
 luz_status clear_visibility(luz_ctx* ctx, luz_frame* f);
 luz_status launch_visibility_batch(luz_ctx* ctx, const SceneVis* d_scenes, uint32_t n,
                                    unsigned long long* d_offsets, unsigned long long* work_counter,
