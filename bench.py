@@ -646,7 +646,7 @@ def run_ours(args, rank, world, local):
                 "frac": achieved / l2_gbs, "traffic": None, "algorithmic_bytes": trav_bytes,
                 "ms_per_launch": trav_ms,
                 "note": "traffic (DRAM bytes per launch) comes from an ncu capture, not from this run; "
-                        "the kernel is issue-bound (about 71 % of issue slots and 17 of 32 lanes per instruction in an ncu capture)",
+                        "the kernel is issue-bound (about 69 % of issue slots and 13 of 32 lanes per instruction in an ncu capture)",
                 "per_ray": {k: stats[k] / max(stats["rays"], 1) for k in
                             ("tlas_nodes", "blas_nodes", "tris", "instances")}}
     # the light pass against HBM: per lit pixel the 32-B surface record, the 16-B record of

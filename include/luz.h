@@ -400,11 +400,17 @@ luz_status luz_frame_read_shadow_map(luz_ctx* ctx, luz_frame* frame, uint32_t li
  * opaque.frag:21-58; main.cpp:242-258) as closest-hit rays through pixel centres.
  * Texture maps are sampled at the hit's interpolated texcoord; a model with a colour
  * map is alpha-tested per hit (opaque.frag's discard below 0.5), so the ray goes on
- * to the surface behind. */
+ * to the surface behind. Each 8x8 tile traces only the TLAS leaves its corner-ray
+ * cone keeps (lists built per call from the TLAS's last build); the planes are those
+ * of a full traversal bit for bit. Also records each pixel's hit instance for the
+ * visibility pass's short-ray starts. */
 luz_status luz_gbuffer_primary(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas);
 /* Shadow (light.frag:86-109,137-146) and AO (light.frag:111-135) any-hit rays of
  * every lit pixel; writes the visibility bit planes (shadow: 1 = occluded, AO: 1 =
- * miss). By default a shadow sample keeps bit 0 without a ray when the light pass's
+ * miss). Rays start below the TLAS root where that cannot change a bit: an AO ray
+ * that stays near its primary-hit instance at that instance's leaf (per-call near
+ * lists), a shadow ray at the leaves its 32-ray group's capsule reaches (per-call
+ * beam lists). By default a shadow sample keeps bit 0 without a ray when the light pass's
  * term of its light cannot depend on the shadow factor (light.frag:209-226 adds
  * ((kD * albedo / pi + spec) * radiance) * max(dot(N, L), 0) with radiance =
  * ((color * intensity) * attenuation) * (1 - shadow)): (a) max(dot(N, L), 0) is 0 or
@@ -421,7 +427,8 @@ luz_status luz_trace_visibility(luz_ctx* ctx, luz_frame* frame, const luz_tlas* 
 luz_status luz_frame_set_shadow_cull(luz_frame* frame, int32_t enable);
 /* The same trace with per-ray work counters (a separate kernel build, for
  * roofline accounting): out[0] rays traversed, out[1] TLAS node visits, out[2] BLAS
- * node visits, out[3] triangle tests, out[4] instance entries. Rays with nothing to
+ * node visits, out[3] triangle tests, out[4] instance leaves reached (entered or
+ * rejected by the bounding-sphere test). Rays with nothing to
  * trace are not counted: a shadow ray left out by the cull above, a ray with a
  * non-finite origin or direction or tMin > tMax (AO: recorded as a miss). */
 luz_status luz_trace_visibility_stats(luz_ctx* ctx, luz_frame* frame, const luz_tlas* tlas,
