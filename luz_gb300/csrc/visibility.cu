@@ -547,8 +547,10 @@ __global__ void batch_offsets_kernel(const SceneVis* scenes, uint32_t n, unsigne
 // ---------------------------------------------------------------- host side
 // Defaults: the best shape of a sweep on the 1080p two-level scene (smem nodes
 // {0,128} x refill {2,4,8,16,24} x steps {8,16,32} x CTAs/SM {3,4}, kernel compiled
-// for 4 CTAs/SM). Staging the TLAS top in shared memory did not pay: L1 holds it.
-static const VisTuning g_tuning{0, 24, 16, 4, 1};
+// for 4 CTAs/SM; steps 16 until the near and beam lists made the rays shorter, then
+// refill {16,24,32} x steps {8,16,24}: 8 steps, 2.28 vs 2.33 ms). Staging the TLAS top
+// in shared memory did not pay: L1 holds it.
+static const VisTuning g_tuning{0, 24, 8, 4, 1};
 
 const VisTuning& vis_tuning(const luz_ctx* ctx) { return ctx->vis_tuning.set ? ctx->vis_tuning : g_tuning; }
 
