@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(256, 5) raygen_kernel(SceneVis S, VisCommon C,
         if (live) rays_a[item - k0] = make_float4(wo.x, wo.y, wo.z, ok ? tmax : ninf);
         if (ok) {   // read only for rays
             uint32_t tag = pix;
-            if (S.near_reach > 0.0f) {
+            if (S.near_reach > 0.0f && !record_hit) {   // AO rays (shadow rays have their beams)
                 const uint32_t start = near_start(S, wo, wd, tmin, tmax, pix);
                 if (start != ~0u) {
                     tag |= kNearFlag;
@@ -658,8 +658,8 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         f->rays_cap = need;
     }
     const unsigned long long chunk = std::min<unsigned long long>(max_items, f->rays_cap);
-    // Near lists of this TLAS for rays that stay within LUZ_NEAR_REACH AO radii of their
-    // own instance's box (the AO rays, and shadow rays to nearby lights).
+    // Near lists of this TLAS for the AO rays that stay within LUZ_NEAR_REACH AO radii
+    // of their own instance's box.
     const float reach = LUZ_NEAR_REACH * f->h_scene.ao_max;
     if (t->count > 0 && t->count < (1u << kNearLeafBits) && reach > 0.0f && std::isfinite(reach)) {
         near_list_kernel<<<t->count, 256, 0, st>>>(tlas_instance_boxes(t), t->leaf_of, t->count, reach, t->near);
