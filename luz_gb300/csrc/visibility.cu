@@ -286,6 +286,7 @@ __global__ void __launch_bounds__(256) beam_list_kernel(SceneVis S, unsigned lon
     uint32_t cnt = 0;
     int stack[kBeamStack];
     int sp = 0, node = 0;
+    bool done = false;
     for (uint32_t iter = 0; iter < kTraversalCap; ++iter) {
         const float4* np = S.tlas_nodes + (size_t)node * kNode4F4;
         const float4 lx = __ldg(np), hx = __ldg(np + 1), ly = __ldg(np + 2), hy = __ldg(np + 3), lz = __ldg(np + 4),
@@ -339,10 +340,13 @@ __global__ void __launch_bounds__(256) beam_list_kernel(SceneVis S, unsigned lon
             list[0] = kBeamAll;
             return;
         }
-        if (sp == 0) break;
+        if (sp == 0) {
+            done = true;
+            break;
+        }
         node = stack[--sp];
     }
-    if (sp != 0) {   // the step cap ran out
+    if (!done) {   // the step cap ran out
         list[0] = kBeamAll;
         return;
     }
