@@ -46,8 +46,15 @@ constexpr uint32_t kNearMax = 8;
 #endif
 constexpr uint32_t kBeamShift = LUZ_BEAM_SHIFT;
 constexpr uint32_t kBeamGroup = 1u << kBeamShift;
-constexpr uint32_t kBeamMax = 15;             // list: count + 15 leaves (64 B per group)
+constexpr uint32_t kBeamMax = 31;             // list room: count + 31 leaves (128 B per group)
 constexpr uint32_t kBeamWords = kBeamMax + 1;
+// Leaves a list may hold before its group falls back to the TLAS root: 15 up to 2048
+// instances, 31 above. The traversal kernel is built for each cap (its start loop
+// reads that many): on the 1080p two-level frame the longer lists cost 0.5 % of the
+// traversal and 3 % of the list kernel, on the 4096-instance scene they take the TLAS
+// visits per traversed ray from 3.1 to 0.9.
+constexpr uint32_t kBeamCapSmall = 15, kBeamCapLarge = 31;
+inline uint32_t beam_cap(uint32_t instances) { return instances > 2048 ? kBeamCapLarge : kBeamCapSmall; }
 #ifndef LUZ_NEAR_REACH
 #define LUZ_NEAR_REACH 1.5f
 #endif
@@ -257,7 +264,7 @@ __global__ void __launch_bounds__(256, 5) raygen_kernel(SceneVis S, VisCommon C,
 // between the centres. A leaf whose box, grown by that radius, the segment misses
 // cannot be hit by any ray of the group: the group's rays traverse only the leaves the
 // capsule reaches (nearest first), or the TLAS from its root when there are more than
-// kBeamMax of them. The radius is grown by 2^-10 relative and 2^-16 of the centres'
+// S.beam_cap of them. The radius is grown by 2^-10 relative and 2^-16 of the centres'
 // magnitude, above the rounding of the centres, radii, end points and hit points.
 constexpr uint32_t kBeamAll = 0xFFFFFFFFu;    // count: traverse from the TLAS root
 constexpr int kBeamStack = 48;                 // overflow: the list falls back to the TLAS root
@@ -336,7 +343,7 @@ __global__ void __launch_bounds__(256) beam_list_kernel(SceneVis S, unsigned lon
                 else overflow = true;
             }
         }
-        if (overflow || cnt > kBeamMax) {
+        if (overflow || cnt > S.beam_cap) {
             list[0] = kBeamAll;
             return;
         }
@@ -367,7 +374,7 @@ __device__ __forceinline__ bool leaf_overlaps(const LaneRay& r, const float4* __
 // Traversal of one chunk of generated rays (one scene; the TLAS top may be staged
 // in shared memory). Shared memory: staged TLAS nodes, then the stacks, then the
 // cold ray state.
-template <bool kStats, bool kStaged>
+template <bool kStats, bool kStaged, uint32_t kCap>
 __global__ void __launch_bounds__(kVisThreads, LUZ_VIS_MIN_BLOCKS)
 visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long long chunk,
                   const float4* __restrict__ rays_a, const float4* __restrict__ rays_b,
@@ -435,7 +442,7 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
                                 // stacked; with none it ends unoccluded.
                                 int sp = 0, cur = 0;
 #pragma unroll
-                                for (int q = (int)kBeamWords / 4 - 1; q >= 0; --q) {
+                                for (int q = (int)(kCap + 1) / 4 - 1; q >= 0; --q) {
                                     if (4u * (uint32_t)q > u0.x) continue;
                                     const uint4 u = q == 0 ? u0 : __ldg(bl + q);
                                     const uint32_t l[4] = {u.x, u.y, u.z, u.w};
@@ -443,7 +450,11 @@ visibility_kernel(SceneVis S, VisCommon C, unsigned long long k0, unsigned long 
                                     for (int k = 3; k >= 0; --k) {
                                         const uint32_t w = 4u * (uint32_t)q + (uint32_t)k;
                                         if (w >= 1 && w <= u0.x && leaf_overlaps(r, S.leaf_box, l[k])) {
-                                            if (cur) s_stack[(sp++) * 32] = (uint32_t)cur;
+                                            if (cur) {   // past the shared part (kCap 31): local
+                                                if (kCap < kSmemStack || sp < kSmemStack) s_stack[sp * 32] = (uint32_t)cur;
+                                                else lstack[sp - kSmemStack] = cur;
+                                                ++sp;
+                                            }
                                             cur = ~(int)l[k];
                                         }
                                     }
@@ -589,6 +600,7 @@ SceneVis make_scene_vis(const luz_frame* f, const luz_tlas* t, int frame_index) 
     S.near_reach = 0.0f;
     S.beam_lists = nullptr;
     S.leaf_box = nullptr;
+    S.beam_cap = 0;
     return S;
 }
 
@@ -616,6 +628,19 @@ luz_status clear_visibility(luz_ctx* ctx, luz_frame* f) {
 }
 
 
+// The traversal of one chunk, built for the scene's beam-list cap.
+template <bool kStats, uint32_t kCap>
+static void launch_traversal(bool staged, uint32_t grid, size_t smem, cudaStream_t st, const SceneVis& S,
+                             const VisCommon& C, unsigned long long k0, unsigned long long chunk, const luz_frame* f,
+                             unsigned long long* d_stats) {
+    if (staged)
+        visibility_kernel<kStats, true, kCap><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b,
+                                                                       f->rays_c, d_stats);
+    else
+        visibility_kernel<kStats, false, kCap><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b,
+                                                                        f->rays_c, d_stats);
+}
+
 luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int frame_index,
                              unsigned long long* d_stats) {
     luz_status s = clear_visibility(ctx, f);
@@ -630,10 +655,16 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     size_t smem = (size_t)staged * kNode4F4 * 16 + kStackBytes + kColdBytes;
     static size_t attr_bytes = 0;
     if (smem > attr_bytes) {
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(visibility_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const void* fns[8] = {(const void*)visibility_kernel<false, false, kBeamCapSmall>,
+                              (const void*)visibility_kernel<true, false, kBeamCapSmall>,
+                              (const void*)visibility_kernel<false, true, kBeamCapSmall>,
+                              (const void*)visibility_kernel<true, true, kBeamCapSmall>,
+                              (const void*)visibility_kernel<false, false, kBeamCapLarge>,
+                              (const void*)visibility_kernel<true, false, kBeamCapLarge>,
+                              (const void*)visibility_kernel<false, true, kBeamCapLarge>,
+                              (const void*)visibility_kernel<true, true, kBeamCapLarge>};
+        for (const void* fn : fns)
+            LUZ_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_bytes = smem;
     }
     uint32_t grid = (uint32_t)ctx->sm_count * tu.ctas_per_sm;
@@ -675,6 +706,7 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         S.beam_lists = f->beam_lists;
         S.leaf_box = tlas_leaf_boxes(t);
     }
+    S.beam_cap = beam_cap(t->count);
     static int raygen_blocks = 0;   // resident 256-thread blocks per SM: the grid is one wave
     if (raygen_blocks == 0) {
         LUZ_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&raygen_blocks, raygen_kernel, 256, 0));
@@ -693,13 +725,17 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         }
         prof_end(ctx);
         if (d_stats) {
-            if (staged) visibility_kernel<true, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, d_stats);
-            else visibility_kernel<true, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, d_stats);
+            if (S.beam_cap == kBeamCapLarge)
+                launch_traversal<true, kBeamCapLarge>(staged, grid, smem, st, S, C, k0, chunk, f, d_stats);
+            else
+                launch_traversal<true, kBeamCapSmall>(staged, grid, smem, st, S, C, k0, chunk, f, d_stats);
             LUZ_LAUNCHED(ctx, "visibility_kernel<stats>");
         } else {
             prof_begin(ctx, LUZ_KERNEL_TRAVERSAL);
-            if (staged) visibility_kernel<false, true><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, nullptr);
-            else visibility_kernel<false, false><<<grid, 256, smem, st>>>(S, C, k0, chunk, f->rays_a, f->rays_b, f->rays_c, nullptr);
+            if (S.beam_cap == kBeamCapLarge)
+                launch_traversal<false, kBeamCapLarge>(staged, grid, smem, st, S, C, k0, chunk, f, nullptr);
+            else
+                launch_traversal<false, kBeamCapSmall>(staged, grid, smem, st, S, C, k0, chunk, f, nullptr);
             prof_end(ctx);
             LUZ_LAUNCHED(ctx, "visibility_kernel");
         }

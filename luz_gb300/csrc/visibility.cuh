@@ -32,6 +32,7 @@ struct SceneVis {
     // 32 items, count + 7 TLAS leaves
     const uint32_t* beam_lists;
     const float4* leaf_box;      // TLAS leaf boxes (lo, hi), leaf order
+    uint32_t beam_cap;           // leaves a beam list may hold before it falls back
 };
 
 struct VisCommon {
