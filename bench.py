@@ -744,6 +744,8 @@ def run_ours(args, rank, world, local):
                              "image is unchanged; rays_traversed_per_frame are the rays actually traced.",
                 "traversed_grays_per_s": world * (scene.width * scene.height + stats["rays"]) / (ms * 1e-3) / 1e9,
                 "lit_pixels": lit, "stage_ms": stage_ms, "kernel_ms": kernel_ms,
+                "kernel_ms_note": "gbuffer includes its two tile-list kernels, raygen the near-list check of "
+                                  "the AO rays and the beam-list kernel of the shadow rays",
                 "blas_build": {"ms": g.blas_build_ms, "device_ms": g.blas_build_device_ms,
                                "triangles": g.blas_prims, "meshes": len(g.blas),
                                "algorithmic_bytes_per_triangle": 248,
