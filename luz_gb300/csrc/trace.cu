@@ -31,6 +31,9 @@ constexpr uint32_t kGbCoarse = 64;
 constexpr uint32_t kGbCoarseMax = 255;    // coarse list: count + 255 leaves
 constexpr uint32_t kGbFineMax = 15;       // fine list: count + 15 leaves
 constexpr uint32_t kGbListAll = 0xFFFFFFFFu;   // count: trace through the TLAS
+// The coarse lists test every leaf per 64x64 tile: above this many instances every
+// tile traces through the TLAS.
+constexpr uint32_t kGbListMaxInstances = 65536;
 
 // The cone of the primary rays of the pixels [x0, x1] x [y0, y1]: four planes through
 // the camera spanned by adjacent corner rays and the plane normal to the centre ray,
@@ -474,7 +477,9 @@ luz_status launch_gbuffer(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {
     uint32_t tiles = ((f->width + kGbTile - 1) / kGbTile) * ((f->height + kGbTile - 1) / kGbTile);
     const uint32_t coarse = ((f->width + kGbCoarse - 1) / kGbCoarse) * ((f->height + kGbCoarse - 1) / kGbCoarse);
     prof_begin(ctx, LUZ_KERNEL_GBUFFER);
-    if (t->count > 0) {
+    if (t->count > kGbListMaxInstances) {   // every tile through the TLAS (count word kGbListAll)
+        LUZ_CUDA(ctx, cudaMemsetAsync(f->gb_fine, 0xFF, (size_t)tiles * (kGbFineMax + 1) * 4, ctx->stream));
+    } else if (t->count > 0) {
         const float4* leaf_box = tlas_leaf_boxes(t);
         gb_coarse_kernel<<<coarse, 256, 0, ctx->stream>>>(G, leaf_box, t->count, f->gb_coarse);
         LUZ_LAUNCHED(ctx, "gb_coarse_kernel");

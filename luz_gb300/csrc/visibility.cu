@@ -60,6 +60,7 @@ inline uint32_t beam_cap(uint32_t instances) { return instances > 2048 ? kBeamCa
 #endif
 constexpr uint32_t kNearFlag = 0x80000000u;   // rays_b.w: the ray starts at its near list
 constexpr uint32_t kNearLeafBits = 24;        // rays_c: own leaf | overlapped near[] bits << 24
+constexpr uint32_t kNearMaxInstances = 16384; // pairs tested per call: 2.7e8 at most
 
 __device__ __forceinline__ bool box_ok(float4 lo, float4 hi) {
     return lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z;   // false for empty or NaN boxes
@@ -694,9 +695,10 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     }
     const unsigned long long chunk = std::min<unsigned long long>(max_items, f->rays_cap);
     // Near lists of this TLAS for the AO rays that stay within LUZ_NEAR_REACH AO radii
-    // of their own instance's box.
+    // of their own instance's box. The list kernel tests every pair of instances, so
+    // larger TLASes (above kNearMaxInstances) start their AO rays at the root.
     const float reach = LUZ_NEAR_REACH * f->h_scene.ao_max;
-    if (t->count > 0 && t->count < (1u << kNearLeafBits) && reach > 0.0f && std::isfinite(reach)) {
+    if (t->count > 0 && t->count <= kNearMaxInstances && reach > 0.0f && std::isfinite(reach)) {
         near_list_kernel<<<t->count, 256, 0, st>>>(tlas_instance_boxes(t), t->leaf_of, t->count, reach, t->near);
         LUZ_LAUNCHED(ctx, "near_list_kernel");
         S.near_reach = reach;
