@@ -241,7 +241,7 @@ struct luz_frame {
     float4* rays_b = nullptr;
     uint32_t* rays_c = nullptr;          // own instance of a ray that starts at its near list
     float4* beams = nullptr;             // per group of 32 items: origin ball, end-point ball
-    uint32_t* beam_lists = nullptr;      // per group of 32 items: count + 7 TLAS leaves
+    uint32_t* beam_lists = nullptr;      // per group of 32 items: count + up to 31 TLAS leaves
     uint32_t rays_cap = 0;
 };
 
