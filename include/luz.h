@@ -323,7 +323,8 @@ luz_status luz_blas_download_wide(luz_ctx* ctx, const luz_blas* blas, void* node
 /* Device bytes held by a BLAS / TLAS, by part: binary nodes (the parity-checked tree;
  * a TLAS build reads each BLAS root's box and bounding sphere from it), 4-wide nodes
  * (every traversal), triangles / instance records, other (sort keys,
- * order, shading copies of the vertex and index buffers, build scratch of a TLAS).
+ * order, shading copies of the vertex and index buffers; for a TLAS also the shading
+ * and input records, near lists, leaf indices and build scratch).
  * The counterpart of the reference's vkGetAccelerationStructureBuildSizesKHR query
  * (source/Graphics/VulkanWrapper.cpp:692-698, 809-812). */
 typedef struct luz_memory {

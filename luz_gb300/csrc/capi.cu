@@ -411,7 +411,10 @@ luz_status luz_tlas_memory(const luz_tlas* t, luz_memory* out) {
     out->nodes = m * 64;
     out->wide_nodes = m * 128;
     out->leaves = cap * sizeof(DevInstance);
-    out->other = 66 * 4 + cap * (sizeof(DevShadeInstance) + sizeof(DevInstanceInput) + 8) + t->tmp_bytes;
+    // level table; per instance: shading record, input record, Morton code and order,
+    // near list (4 x uint4) and leaf index; build scratch
+    out->other = 66 * 4 + cap * (sizeof(DevShadeInstance) + sizeof(DevInstanceInput) + 8 + 4 * sizeof(uint4) + 4) +
+                 t->tmp_bytes;
     return LUZ_OK;
 }
 
