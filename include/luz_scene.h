@@ -62,6 +62,19 @@ typedef struct luz_gen_params {
 
 typedef struct luz_host_scene luz_host_scene;
 
+/* Default parameters of a generated workload (seed 1000 + config, 1 shadow sample per
+ * light, the parity sampler); nonzero fields of the params override the defaults:
+ *   1  512x512: 64 unit cubes on a 20x20 quad, 1 directional + 4 point lights,
+ *      4 AO rays per pixel (aoMax 1), fixed camera;
+ *   2  1920x1080: 64 displaced icospheres of 81,920 triangles, 1024 instances in a
+ *      200-unit box, 1 directional + 32 point + 8 spot lights, 16 AO rays (aoMax 2),
+ *      camera at the centre of the instance cloud;
+ *   3  as 1 with a random camera (training and held-out scenes of the denoiser);
+ *   5  3840x2160: as 2 with 4096 instances, 1 + 128 + 16 lights and 64 AO rays;
+ *   6  512x512: a triangle budget (params.triangles, default 100,000) filled with
+ *      cubes below 20,000 triangles, else with icospheres of the needed subdivision
+ *      (one scene of the many-scene batch).
+ * Any other config returns LUZ_ERR_INVALID. */
 luz_status luz_scene_default_params(int32_t config, luz_gen_params* out);
 luz_status luz_scene_generate(const luz_gen_params* params, luz_host_scene** out);
 void luz_scene_destroy(luz_host_scene* scene);
