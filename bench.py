@@ -75,6 +75,25 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """The largest x over the ranks of the default process group (x itself when there
+    is none): every rank's step time is bounded by the slowest replica's."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, units_per_rank: float, ms: float) -> float:
+    """Units per second of all ranks together (each rank processes units_per_rank per
+    step; ms is the max-over-ranks step time), in G units/s."""
+    return world * units_per_rank / (ms * 1e-3) / 1e9
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -618,12 +637,8 @@ def run_ours(args, rank, world, local):
     frame_ms = [e[0].elapsed_time(e[4]) for e in evs]
     stage_ms = {name: statistics.mean(e[i].elapsed_time(e[i + 1]) for e in evs)
                 for i, name in enumerate(["tlas_build", "gbuffer", "visibility", "light_pass"])}
-    ms = statistics.mean(frame_ms)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * rays_per_frame / (ms * 1e-3) / 1e9
+    ms = max_over_ranks(statistics.mean(frame_ms), dev)
+    value = whole_job_rate(world, rays_per_frame, ms)
     if ctx.device_status() != 0:
         raise RuntimeError("device status word raised during timing")
 
@@ -695,10 +710,10 @@ def run_ours(args, rank, world, local):
             e2e_step(k)
             torch.cuda.synchronize()
             ts.append(time.perf_counter() - t0)
-        e2e_s = statistics.mean(ts)
+        e2e_s = max_over_ranks(statistics.mean(ts), dev)
         h2d = C.sizeof(g.block) + C.sizeof(_abi.Light) * scene.light_count + \
             C.sizeof(_abi.Model) * scene.instance_count + C.sizeof(_abi.Instance) * g.n_instances
-        e2e = {"value": world * rays_per_frame / e2e_s / 1e9, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
+        e2e = {"value": whole_job_rate(world, rays_per_frame, e2e_s * 1e3), "unit": UNIT, "ms_per_step": e2e_s * 1e3,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nbytes)}
 
     denoised = None
@@ -742,7 +757,7 @@ def run_ours(args, rank, world, local):
                              "the light pass cannot depend on it (weight max(dot(N, L), 0) = 0 or zero "
                              "unshadowed radiance) is resolved at generation without traversal, the "
                              "image is unchanged; rays_traversed_per_frame are the rays actually traced.",
-                "traversed_grays_per_s": world * (scene.width * scene.height + stats["rays"]) / (ms * 1e-3) / 1e9,
+                "traversed_grays_per_s": whole_job_rate(world, scene.width * scene.height + stats["rays"], ms),
                 "lit_pixels": lit, "stage_ms": stage_ms, "kernel_ms": kernel_ms,
                 "kernel_ms_note": "gbuffer includes its two tile-list kernels, raygen the near-list check of "
                                   "the AO rays and the beam-list kernel of the shadow rays",
