@@ -9,7 +9,9 @@
  *
  * Threading: a luz_ctx is thread-compatible (one host thread at a time), like the
  * reference's single global Vulkan context `_ctx` (source/Graphics/VulkanWrapper.cpp).
- * All GPU work of a context is ordered on the context's CUDA stream.
+ * All GPU work of a context is ordered on the context's CUDA stream. Several contexts
+ * may be driven from several threads at once; they all use one device (one process
+ * per GPU, as the reference runs one Vulkan device per process).
  */
 #ifndef LUZ_GB300_H
 #define LUZ_GB300_H
@@ -190,7 +192,12 @@ enum {
     LUZ_PLANE_COUNT = 18
 };
 
-/* ------------------------------------------------------------------ context */
+/* ------------------------------------------------------------------ context
+ * luz_ctx_create makes `device` current on the calling thread. The contexts of a
+ * process share one device: creating one on another device while a context lives
+ * returns LUZ_ERR_INVALID. The one-time setup the kernels need on the device
+ * (shared-memory limits, constant tables) is done again after the process's last
+ * context was destroyed, so a device reset between contexts is picked up. */
 luz_status luz_ctx_create(int device, luz_ctx** out);
 void luz_ctx_destroy(luz_ctx* ctx);
 const char* luz_last_error(const luz_ctx* ctx);

@@ -1,9 +1,11 @@
 // capi.cu — the extern "C" entry points of include/luz.h: context, BLAS/TLAS
 // handles, frames, uploads and read-back.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "internal.cuh"
@@ -19,6 +21,15 @@ luz_status frame_lit_count(luz_ctx* ctx, luz_frame* f, uint32_t* count);
 luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode);
 uint32_t lit_chunks(uint32_t width, uint32_t height);
 luz_status launch_ao_resolve(luz_ctx* ctx, luz_frame* f);
+
+// The process's live contexts: all on one device (per-device setup is cached per
+// process), and a new setup generation when the first of them is created.
+static std::mutex g_ctx_mutex;
+static int g_ctx_live = 0;
+static int g_ctx_device = -1;
+static std::atomic<uint64_t> g_setup_generation{0};
+
+uint64_t setup_generation() { return g_setup_generation.load(std::memory_order_acquire); }
 
 luz_status set_error(luz_ctx* ctx, luz_status st, const std::string& msg) {
     if (ctx) ctx->last_error = msg;
@@ -112,8 +123,18 @@ luz_status luz_ctx_create(int device, luz_ctx** out) {
     cudaError_t e = cudaGetDeviceCount(&n);
     if (e != cudaSuccess || n == 0) return LUZ_ERR_NO_DEVICE;
     if (device < 0 || device >= n) return LUZ_ERR_INVALID;
+    {
+        std::lock_guard<std::mutex> lock(g_ctx_mutex);
+        if (g_ctx_live > 0 && device != g_ctx_device) return LUZ_ERR_INVALID;   // one device per process
+        if (g_ctx_live == 0) {
+            g_ctx_device = device;
+            g_setup_generation.fetch_add(1, std::memory_order_acq_rel);
+        }
+        ++g_ctx_live;
+    }
     luz_ctx* ctx = new luz_ctx();
     ctx->device = device;
+    ctx->registered = true;
     auto fail = [&](luz_status s) { luz_ctx_destroy(ctx); return s; };
     if (cudaSetDevice(device) != cudaSuccess) return fail(LUZ_ERR_CUDA);
     if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -148,6 +169,10 @@ void luz_ctx_destroy(luz_ctx* ctx) {
     for (auto ev : ctx->build_ev)
         if (ev) cudaEventDestroy(ev);
     for (auto ev : ctx->prof_pool) cudaEventDestroy(ev);
+    if (ctx->registered) {
+        std::lock_guard<std::mutex> lock(g_ctx_mutex);
+        --g_ctx_live;
+    }
     delete ctx;
 }
 

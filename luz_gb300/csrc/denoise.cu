@@ -981,13 +981,13 @@ luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode);
 namespace dn {
 
 static luz_status upload_lut(luz_ctx* ctx) {
-    static bool done = false;
-    if (done) return LUZ_OK;
-    float lut[256];
-    for (int i = 0; i < 256; ++i) lut[i] = (float)std::pow((double)((float)i / 255.0f), 2.2);
-    LUZ_CUDA(ctx, cudaMemcpyToSymbol(c_lin_lut, lut, sizeof(lut)));
-    done = true;
-    return LUZ_OK;
+    static DeviceSetup setup;
+    return device_setup(setup, setup_generation(), 1, [&]() -> luz_status {
+        float lut[256];
+        for (int i = 0; i < 256; ++i) lut[i] = (float)std::pow((double)((float)i / 255.0f), 2.2);
+        LUZ_CUDA(ctx, cudaMemcpyToSymbol(c_lin_lut, lut, sizeof(lut)));
+        return LUZ_OK;
+    });
 }
 
 static luz_status repack(luz_ctx* ctx, luz_denoiser* d) {
@@ -1010,12 +1010,13 @@ static luz_status check_batch(luz_ctx* ctx, const luz_denoise_batch* b) {
 static luz_status run_infer(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_batch* b, float4* out,
                             float* out_ao = nullptr, const uint32_t* list = nullptr,
                             const uint32_t* list_count = nullptr) {
-    static bool attr = false;
-    if (!attr) {
+    static DeviceSetup setup;
+    luz_status st = device_setup(setup, setup_generation(), kTcSmem, [&]() -> luz_status {
         LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            kTcSmem));
-        attr = true;
-    }
+        return LUZ_OK;
+    });
+    if (st != LUZ_OK) return st;
     InferParams P;
     P.wpack = d->pack;
     P.bias = d->bias;
@@ -1054,12 +1055,13 @@ static luz_status run_gradient(luz_ctx* ctx, luz_denoiser* d, const luz_denoise_
     P.partial = d->partial;
     P.partial_loss = d->partial_loss;
     LUZ_CUDA(ctx, cudaMemsetAsync(d->partial, 0, (size_t)d->ctas * kParams * 4, ctx->stream));
-    static bool tc_attr = false;
-    if (!tc_attr) {
+    static DeviceSetup setup;
+    luz_status st = device_setup(setup, setup_generation(), kTtSmem, [&]() -> luz_status {
         LUZ_CUDA(ctx, cudaFuncSetAttribute(denoise_train_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            kTtSmem));
-        tc_attr = true;
-    }
+        return LUZ_OK;
+    });
+    if (st != LUZ_OK) return st;
     prof_begin(ctx, LUZ_KERNEL_DENOISE_TRAIN);
     denoise_train_tc_kernel<<<d->ctas, 128, kTtSmem, ctx->stream>>>(P, ctx->d_status);
     prof_end(ctx);

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/luz.h"
+#include "device_setup.hpp"
 #include "pathmath.cuh"
 
 namespace luz {
@@ -122,6 +123,8 @@ struct luz_ctx {
     void* h_pinned = nullptr;
     size_t pinned_bytes = 0;
     int sm_count = 0;
+    int raygen_blocks = 0;                      // resident ray-generation blocks per SM (0: not queried)
+    bool registered = false;                    // counted among the process's live contexts
     luz::VisTuning vis_tuning{0, 0, 0, 0, 0};   // set == 0: library defaults
     uint32_t debug_step_cap = 0;                // traversal steps per ray, 0 = the library's cap
     // device pipeline of the last batched BLAS build (after its host->device copies)
@@ -251,6 +254,9 @@ luz_status set_error(luz_ctx* ctx, luz_status st, const std::string& msg);
 luz_status cuda_error(luz_ctx* ctx, cudaError_t e, const char* what);
 luz_status ensure_scratch(luz_ctx* ctx, size_t bytes);
 luz_status check_launch(luz_ctx* ctx, const char* what);
+// The current generation of per-device setup (device_setup.hpp): a new one starts
+// when a context is created while no other context of the process is alive.
+uint64_t setup_generation();
 // Rebuilds the frame's lit-pixel list when its planes or scene constants changed.
 luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f);
 // Per-kernel timing: prof_begin records an event before a launch of kernel `kernel`

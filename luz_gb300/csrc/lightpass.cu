@@ -79,10 +79,13 @@ luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode) {
     size_t smem = (size_t)f->light_count * sizeof(luz_light);
     void (*kernels[4])(LightParams) = {light_pass_kernel<kPlain>, light_pass_kernel<kDenoisedAo>,
                                        light_pass_kernel<kSplit>, light_pass_kernel<kCompose>};
-    static size_t attr_bytes[4] = {48 * 1024, 48 * 1024, 48 * 1024, 48 * 1024};
-    if (smem > attr_bytes[mode]) {
-        LUZ_CUDA(ctx, cudaFuncSetAttribute(kernels[mode], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_bytes[mode] = smem;
+    static DeviceSetup setup[4];   // per kernel: the shared-memory limit above the default 48 KB
+    if (smem > 48 * 1024) {
+        luz_status st = device_setup(setup[mode], setup_generation(), smem, [&]() -> luz_status {
+            LUZ_CUDA(ctx, cudaFuncSetAttribute(kernels[mode], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            return LUZ_OK;
+        });
+        if (st != LUZ_OK) return st;
     }
     uint32_t blocks = (f->pixels + 255) / 256;
     prof_begin(ctx, LUZ_KERNEL_LIGHT_PASS);

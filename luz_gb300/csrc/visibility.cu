@@ -654,8 +654,8 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
     const VisTuning& tu = vis_tuning(ctx);
     uint32_t staged = std::min<uint32_t>(S.tlas_node_count, tu.smem_nodes);
     size_t smem = (size_t)staged * kNode4F4 * 16 + kStackBytes + kColdBytes;
-    static size_t attr_bytes = 0;
-    if (smem > attr_bytes) {
+    static DeviceSetup setup;   // the traversal kernels' shared-memory limit
+    s = device_setup(setup, setup_generation(), smem, [&]() -> luz_status {
         const void* fns[8] = {(const void*)visibility_kernel<false, false, kBeamCapSmall>,
                               (const void*)visibility_kernel<true, false, kBeamCapSmall>,
                               (const void*)visibility_kernel<false, true, kBeamCapSmall>,
@@ -666,8 +666,9 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
                               (const void*)visibility_kernel<true, true, kBeamCapLarge>};
         for (const void* fn : fns)
             LUZ_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_bytes = smem;
-    }
+        return LUZ_OK;
+    });
+    if (s != LUZ_OK) return s;
     uint32_t grid = (uint32_t)ctx->sm_count * tu.ctas_per_sm;
     if (d_stats) LUZ_CUDA(ctx, cudaMemsetAsync(d_stats, 0, 5 * sizeof(unsigned long long), st));
     // Chunks of at most rays_cap items over the largest possible ray count (every
@@ -709,11 +710,12 @@ luz_status launch_visibility(luz_ctx* ctx, luz_frame* f, const luz_tlas* t, int 
         S.leaf_box = tlas_leaf_boxes(t);
     }
     S.beam_cap = beam_cap(t->count);
-    static int raygen_blocks = 0;   // resident 256-thread blocks per SM: the grid is one wave
-    if (raygen_blocks == 0) {
-        LUZ_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&raygen_blocks, raygen_kernel, 256, 0));
-        raygen_blocks = std::max(raygen_blocks, 1);
+    if (ctx->raygen_blocks == 0) {   // resident 256-thread blocks per SM: the grid is one wave
+        int blocks = 0;
+        LUZ_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, raygen_kernel, 256, 0));
+        ctx->raygen_blocks = std::max(blocks, 1);
     }
+    const int raygen_blocks = ctx->raygen_blocks;
     for (unsigned long long k0 = 0; k0 < max_items; k0 += chunk) {
         prof_begin(ctx, LUZ_KERNEL_RAYGEN);
         raygen_kernel<<<(uint32_t)(ctx->sm_count * raygen_blocks), 256, 0, st>>>(S, C, k0, chunk, f->rays_a,
