@@ -193,7 +193,9 @@ enum {
 };
 
 /* ------------------------------------------------------------------ context
- * luz_ctx_create makes `device` current on the calling thread. The contexts of a
+ * luz_ctx_create makes `device` current on the calling thread; another thread that
+ * drives the context makes the same device current first (cudaSetDevice), as the
+ * entry points launch on the calling thread's current device. The contexts of a
  * process share one device: creating one on another device while a context lives
  * returns LUZ_ERR_INVALID. The one-time setup the kernels need on the device
  * (shared-memory limits, constant tables) is done again after the process's last
