@@ -81,7 +81,7 @@ luz_status launch_light_pass(luz_ctx* ctx, luz_frame* f, int mode) {
                                        light_pass_kernel<kSplit>, light_pass_kernel<kCompose>};
     static DeviceSetup setup[4];   // per kernel: the shared-memory limit above the default 48 KB
     if (smem > 48 * 1024) {
-        luz_status st = device_setup(setup[mode], setup_generation(), smem, [&]() -> luz_status {
+        st = device_setup(setup[mode], setup_generation(), smem, [&]() -> luz_status {
             LUZ_CUDA(ctx, cudaFuncSetAttribute(kernels[mode], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             return LUZ_OK;
         });
