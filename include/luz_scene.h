@@ -35,16 +35,8 @@ typedef struct luz_camera {
     float jitter[2];          /* NDC jitter (CameraNode::NextJitter); 0 = off */
 } luz_camera;
 
-/* Synthetic scene generators. config:
- *   1  ground quad 20x20 + 64 unit cubes, 1 directional + 4 point lights, 512x512
- *   2  64 displaced icospheres (subdivision 6) x 1024 instances in a 200^3 box,
- *      1 directional + 32 point + 8 spot lights, 1920x1080, 16 AO samples
- *   3  config 1's generator with a seeded random camera (denoiser training scenes)
- *   5  config 2's meshes x 4096 instances, 128 point + 1 directional + 16 spot,
- *      3840x2160, 64 AO samples
- *   6  one member of the batched workload: triangle budget `triangles`, built from
- *      config 1/2 primitives
- * Fields left 0 take the config's default. */
+/* Parameters of the synthetic scene generators (the configs are listed at
+ * luz_scene_default_params). Fields left 0 take the config's default. */
 typedef struct luz_gen_params {
     int32_t config;
     uint32_t pad0;
@@ -119,7 +111,8 @@ luz_status luz_scene_set_shadow_type(luz_host_scene* s, int32_t shadow_type);
 luz_status luz_scene_next_frame(luz_host_scene* s, int32_t use_jitter);
 
 /* Node::ComposeTransform (AssetManager.cpp:38-43): parent * T * R(quat(radians(rot))) * S.
- * parent may be NULL (identity). Column-major 4x4 out. */
+ * parent may be NULL (identity); a NULL pos, rot_deg or scale takes a Node's default
+ * (0, 0, 1); nothing is written when out is NULL. Column-major 4x4 out. */
 void luz_compose_transform(const float pos[3], const float rot_deg[3], const float scale[3],
                            const float* parent, float out[16]);
 /* CameraNode::GetView and GetProjJittered (AssetManager.cpp:334-377). */

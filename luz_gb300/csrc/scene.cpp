@@ -825,9 +825,11 @@ luz_status luz_scene_set_sampling(luz_host_scene* s, int32_t ao_samples, float a
 
 void luz_compose_transform(const float pos[3], const float rot_deg[3], const float scale[3],
                            const float* parent, float out[16]) {
+    if (!out) return;
+    static const float zero[3] = {0.0f, 0.0f, 0.0f}, one[3] = {1.0f, 1.0f, 1.0f};   // a Node's defaults
     M4 par = identity();
     if (parent) memcpy(par.data(), parent, 64);
-    M4 r = compose(pos, rot_deg, scale, par);
+    M4 r = compose(pos ? pos : zero, rot_deg ? rot_deg : zero, scale ? scale : one, par);
     memcpy(out, r.data(), 64);
 }
 

@@ -108,3 +108,46 @@ def test_blue_noise_substitute():
     for c in range(2):
         h = np.bincount(t[..., c].ravel(), minlength=256)
         assert h.max() < 4 * h.mean()
+
+
+_NULL_SWEEP = r"""
+import ctypes as C, json, re, sys
+from pathlib import Path
+sys.path.insert(0, sys.argv[1])
+from luz_gb300 import _abi
+root = Path(sys.argv[1])
+status = set()
+for h in (root / "include").glob("*.h"):
+    text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+    status |= set(re.findall(r"^\s*luz_status\s+(luz_[a-z0-9_]+)\s*\(", text, re.M))
+lib = C.CDLL(str(_abi.LIB_PATH))
+out = {}
+for name, restype, argtypes in _abi.SIGNATURES:
+    print(name, file=sys.stderr, flush=True)     # the last name printed is the one that crashed
+    f = getattr(lib, name)
+    f.restype, f.argtypes = restype, argtypes
+    args = [0.0 if t in (C.c_float, C.c_double) else
+            0 if isinstance(t, type) and issubclass(t, C._SimpleCData) and t not in (C.c_void_p, C.c_char_p)
+            else None for t in argtypes]
+    r = f(*args)
+    if name in status:
+        out[name] = r
+print(json.dumps(out))
+"""
+
+
+def test_null_and_zero_arguments_never_crash_and_statuses_are_invalid():
+    """Every entry point called with NULL pointers and zero sizes returns without
+    touching memory; those returning luz_status return LUZ_ERR_INVALID (the check
+    comes before any CUDA call, so no GPU is needed)."""
+    import json
+    import subprocess
+    import sys
+
+    r = subprocess.run([sys.executable, "-c", _NULL_SWEEP, str(ROOT)], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, "crashed in " + (r.stderr.strip().splitlines() or ["?"])[-1]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert len(res) > 40
+    bad = {k: v for k, v in res.items() if v != 1}
+    assert not bad, bad
