@@ -5,6 +5,7 @@
 // depths; 16-bit samples keep their high byte, sub-byte grey samples are scaled to
 // 0..255, tRNS becomes alpha.
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
@@ -74,7 +75,10 @@ struct Huffman {
     }
 };
 
-inline void inflate_block(BitReader& br, std::vector<uint8_t>& out, const Huffman& lit, const Huffman& dist) {
+// Decodes one Huffman block into out; stops early once out holds `limit` bytes (it
+// may then hold up to one match, 258 bytes, more).
+inline void inflate_block(BitReader& br, std::vector<uint8_t>& out, const Huffman& lit, const Huffman& dist,
+                          size_t limit) {
     static const uint16_t lbase[29] = {3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 15, 17, 19, 23, 27, 31,
                                        35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
     static const uint8_t lextra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2,
@@ -84,7 +88,7 @@ inline void inflate_block(BitReader& br, std::vector<uint8_t>& out, const Huffma
                                        6145, 8193, 12289, 16385, 24577};
     static const uint8_t dextra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6,
                                        6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
-    for (;;) {
+    while (out.size() < limit) {
         int sym = lit.decode(br);
         if (sym < 256) { out.push_back((uint8_t)sym); continue; }
         if (sym == 256) return;
@@ -100,8 +104,9 @@ inline void inflate_block(BitReader& br, std::vector<uint8_t>& out, const Huffma
     }
 }
 
-// zlib stream -> bytes.
-inline std::vector<uint8_t> inflate_zlib(const uint8_t* p, size_t n) {
+// zlib stream -> its first `limit` bytes: decoding stops there, so a stream that
+// expands beyond what the image needs costs no more memory than the image.
+inline std::vector<uint8_t> inflate_zlib(const uint8_t* p, size_t n, size_t limit) {
     if (n < 2) fail("short zlib stream");
     if ((p[0] & 0x0F) != 8 || ((p[0] << 8) | p[1]) % 31 != 0 || (p[1] & 0x20)) fail("bad zlib header");
     BitReader br(p + 2, n - 2);
@@ -128,10 +133,10 @@ inline std::vector<uint8_t> inflate_zlib(const uint8_t* p, size_t n) {
             uint32_t len = q[0] | (q[1] << 8), nlen = q[2] | (q[3] << 8);
             if ((len ^ 0xFFFFu) != nlen) fail("stored block length check");
             if (pos + 4 + len > br.size()) fail("truncated stored block");
-            out.insert(out.end(), q + 4, q + 4 + len);
+            out.insert(out.end(), q + 4, q + 4 + std::min<size_t>(len, limit - out.size()));
             br.skip(4 + len);
         } else if (type == 1) {
-            inflate_block(br, out, fl, fd);
+            inflate_block(br, out, fl, fd, limit);
         } else if (type == 2) {
             int hlit = (int)br.bits(5) + 257, hdist = (int)br.bits(5) + 1, hclen = (int)br.bits(4) + 4;
             static const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
@@ -161,12 +166,13 @@ inline std::vector<uint8_t> inflate_zlib(const uint8_t* p, size_t n) {
             Huffman dl, dd;
             dl.build(lens, hlit);
             dd.build(lens + hlit, hdist);
-            inflate_block(br, out, dl, dd);
+            inflate_block(br, out, dl, dd, limit);
         } else {
             fail("bad block type");
         }
-        if (last) break;
+        if (last || out.size() >= limit) break;
     }
+    if (out.size() > limit) out.resize(limit);
     return out;
 }
 
@@ -260,9 +266,28 @@ inline Image decode(const uint8_t* p, size_t n) {
     bool ok_depth = depth == 8 || depth == 16 || ((ctype == 0 || ctype == 3) && (depth == 1 || depth == 2 || depth == 4));
     if (!ok_depth || (ctype == 3 && depth == 16)) fail("bad bit depth");
     if (ctype == 3 && plte.empty()) fail("palette image without PLTE");
-    std::vector<uint8_t> raw = inflate_zlib(idat.data(), idat.size());
     const size_t bits_pp = (size_t)channels * depth;
     const size_t bpp = bits_pp < 8 ? 1 : bits_pp / 8;
+    static const int x0[7] = {0, 4, 0, 2, 0, 1, 0}, y0[7] = {0, 0, 4, 0, 2, 0, 1};
+    static const int dx[7] = {8, 8, 4, 4, 2, 2, 1}, dy[7] = {8, 8, 8, 4, 4, 2, 2};
+    auto pass_size = [&](int pass, uint32_t& pw, uint32_t& ph) {   // Adam7 pass extent
+        pw = w > (uint32_t)x0[pass] ? (w - x0[pass] + dx[pass] - 1) / dx[pass] : 0;
+        ph = h > (uint32_t)y0[pass] ? (h - y0[pass] + dy[pass] - 1) / dy[pass] : 0;
+    };
+    // The filtered scanlines the header implies: the image data is decoded up to that
+    // size, and nothing of the image's own size is allocated before it is there.
+    size_t expected = 0;
+    if (!interlace) {
+        expected = (((size_t)w * bits_pp + 7) / 8 + 1) * h;
+    } else {
+        for (int pass = 0; pass < 7; ++pass) {
+            uint32_t pw, ph;
+            pass_size(pass, pw, ph);
+            if (pw && ph) expected += (((size_t)pw * bits_pp + 7) / 8 + 1) * ph;
+        }
+    }
+    std::vector<uint8_t> raw = inflate_zlib(idat.data(), idat.size(), expected);
+    if (raw.size() < expected) fail("short image data");
 
     Image img;
     img.width = w;
@@ -329,13 +354,10 @@ inline Image decode(const uint8_t* p, size_t n) {
         for (uint32_t y = 0; y < h; ++y)
             for (uint32_t x = 0; x < w; ++x) put(x, y, rows.data() + y * stride, x);
     } else {
-        static const int x0[7] = {0, 4, 0, 2, 0, 1, 0}, y0[7] = {0, 0, 4, 0, 2, 0, 1};
-        static const int dx[7] = {8, 8, 4, 4, 2, 2, 1}, dy[7] = {8, 8, 8, 4, 4, 2, 2};
         size_t off = 0;
         for (int pass = 0; pass < 7; ++pass) {
-            uint32_t pw = (w - x0[pass] + dx[pass] - 1) / dx[pass], ph = (h - y0[pass] + dy[pass] - 1) / dy[pass];
-            if (w <= (uint32_t)x0[pass]) pw = 0;
-            if (h <= (uint32_t)y0[pass]) ph = 0;
+            uint32_t pw, ph;
+            pass_size(pass, pw, ph);
             if (!pw || !ph) continue;
             size_t stride = ((size_t)pw * bits_pp + 7) / 8;
             if (raw.size() < off + (stride + 1) * ph) fail("short interlaced data");

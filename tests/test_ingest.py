@@ -351,6 +351,32 @@ def test_png_adam7_and_stored_blocks(tmp_path):
     assert np.array_equal(_import_png(tmp_path, png), img)
 
 
+def test_png_header_larger_than_its_data_is_rejected_before_allocating(tmp_path):
+    """A 65536 x 65536 RGBA header over 64 bytes of image data: every scanline the
+    header implies must be decoded before the 16 GiB image is allocated, so the file
+    is rejected at once."""
+    png = (b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", 65536, 65536, 8, 6, 0, 0, 0)) +
+           _chunk(b"IDAT", zlib.compress(bytes(64))) + _chunk(b"IEND", b""))
+    with pytest.raises(L.LuzError, match="short image data"):
+        _import_png(tmp_path, png)
+
+
+@pytest.mark.parametrize("interlace", [0, 1])
+def test_png_data_beyond_the_image_is_not_decoded(tmp_path, interlace):
+    """The image's scanlines followed by 64 MB of zeros in one zlib stream (64 KB
+    compressed): decoding stops at the size the header implies and the image comes
+    from its own scanlines."""
+    img = np.arange(2 * 3 * 4, dtype=np.uint8).reshape(2, 3, 4)
+    if interlace:   # 3x2 under Adam7: passes 1, 2 (none), 3 (none), 4 (x = 2), 5 (none), 6 (x = 1), 7 (row 1)
+        raw = (b"\x00" + img[0, 0].tobytes() + b"\x00" + img[0, 2].tobytes() + b"\x00" + img[0, 1].tobytes() +
+               b"\x00" + img[1].tobytes())
+    else:
+        raw = b"".join(b"\x00" + img[y].tobytes() for y in range(2))
+    png = (b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", 3, 2, 8, 6, 0, 0, interlace)) +
+           _chunk(b"IDAT", zlib.compress(raw + bytes(64 << 20), 9)) + _chunk(b"IEND", b""))
+    assert np.array_equal(_import_png(tmp_path, png), img)
+
+
 def test_errors_are_reported(tmp_path):
     bad = tmp_path / "bad.gltf"
     bad.write_text("{ not json")
