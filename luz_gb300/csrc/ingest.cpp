@@ -33,6 +33,10 @@ namespace ingest {
 
 using json::Value;
 
+// Deepest node tree a scene may have (project files and glTF alike): the readers
+// and the packing walk recurse once per level.
+constexpr int kMaxNodeDepth = 512;
+
 // ---------------------------------------------------------------- object model
 enum ObjType : int {   // ObjectType (AssetManager.hpp:14-25)
     kTexture = 1, kMesh = 2, kMaterial = 3, kScene = 4, kNode = 5, kMeshNode = 6, kLightNode = 7, kCameraNode = 8
@@ -202,7 +206,7 @@ void get_blob(const Value& j, const char* k, const std::vector<uint8_t>& bin, st
 }
 
 Node read_node(const Value& j, int depth) {
-    if (depth > 512) fail("node tree too deep");
+    if (depth > kMaxNodeDepth) fail("node tree too deep");
     Node n;
     n.type = (int)j.at("type").i64();
     get_s(j, "name", n.name);
@@ -884,11 +888,12 @@ SceneAsset import_gltf(const std::string& path, Project& p, UuidGen& ids) {
                     kids[i].push_back(k);
                 }
     std::vector<int> state(gnodes.size(), 0);
-    std::function<Node(size_t)> build = [&](size_t i) -> Node {
+    std::function<Node(size_t, int)> build = [&](size_t i, int depth) -> Node {
+        if (depth > kMaxNodeDepth) fail("node tree too deep");
         if (state[i] == 1) fail("cycle in the glTF node hierarchy");
         state[i] = 1;
         Node n = gnodes[i];
-        for (size_t k : kids[i]) n.children.push_back(build(k));
+        for (size_t k : kids[i]) n.children.push_back(build(k, depth + 1));
         state[i] = 2;
         return n;
     };
@@ -903,7 +908,7 @@ SceneAsset import_gltf(const std::string& path, Project& p, UuidGen& ids) {
                 for (const auto& n : ns->items) {
                     size_t k = (size_t)n.u64();
                     if (k >= gnodes.size()) fail("bad scene node index");
-                    scene.nodes.push_back(build(k));
+                    scene.nodes.push_back(build(k, 0));
                 }
         }
     }
@@ -1241,7 +1246,7 @@ struct Walker {
         return (int32_t)k;
     }
     void walk(const Node& n, const float parent[16], int depth) {
-        if (depth > 512) fail("node tree too deep");
+        if (depth > kMaxNodeDepth) fail("node tree too deep");
         float world[16];
         if (n.has_matrix) {
             float id[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};

@@ -377,6 +377,32 @@ def test_png_data_beyond_the_image_is_not_decoded(tmp_path, interlace):
     assert np.array_equal(_import_png(tmp_path, png), img)
 
 
+@pytest.mark.parametrize("chain", [512, 513, 100000])
+def test_gltf_node_chain_depth(tmp_path, chain):
+    """glTF nodes link by index, so a hierarchy can be deeper than its JSON. A chain of
+    nodes ending in the mesh's node, whose primitive becomes a MeshNode one level
+    further down, loads while that MeshNode is at most 512 levels below the root
+    node, and longer chains are rejected without exhausting the stack."""
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    blob = pos.tobytes() + np.array([0, 1, 2], np.uint32).tobytes()
+    g = {"asset": {"version": "2.0"}, "scene": 0, "scenes": [{"nodes": [0]}],
+         "nodes": [{"children": [i + 1]} for i in range(chain - 1)] + [{"mesh": 0}],
+         "meshes": [{"primitives": [{"attributes": {"POSITION": 0}, "indices": 1}]}],
+         "buffers": [{"byteLength": len(blob), "uri": "data:application/octet-stream;base64," +
+                      __import__("base64").b64encode(blob).decode()}],
+         "bufferViews": [{"buffer": 0, "byteOffset": 0, "byteLength": 36},
+                         {"buffer": 0, "byteOffset": 36, "byteLength": 12}],
+         "accessors": [{"bufferView": 0, "componentType": 5126, "count": 3, "type": "VEC3"},
+                       {"bufferView": 1, "componentType": 5125, "count": 3, "type": "SCALAR"}]}
+    p = tmp_path / "chain.gltf"
+    p.write_text(json.dumps(g))
+    if chain <= 512:
+        assert L.HostScene.import_file(p, 8, 8).instance_count == 1
+    else:
+        with pytest.raises(L.LuzError, match="too deep"):
+            L.HostScene.import_file(p, 8, 8)
+
+
 def test_errors_are_reported(tmp_path):
     bad = tmp_path / "bad.gltf"
     bad.write_text("{ not json")
