@@ -651,7 +651,7 @@ SceneAsset import_gltf(const std::string& path, Project& p, UuidGen& ids) {
         if (bi >= buffers.size()) fail("bad buffer index");
         size_t off = v.has("byteOffset") ? (size_t)v.at("byteOffset").u64() : 0;
         len = (size_t)v.at("byteLength").u64();
-        if (off + len > buffers[bi].size()) fail("bufferView outside its buffer");
+        if (off > buffers[bi].size() || len > buffers[bi].size() - off) fail("bufferView outside its buffer");
         return buffers[bi].data() + off;
     };
     auto accessor = [&](size_t ai) {
@@ -670,7 +670,11 @@ SceneAsset import_gltf(const std::string& path, Project& p, UuidGen& ids) {
         const Value& v = (*views)[(size_t)a.at("bufferView").u64()];
         r.stride = v.has("byteStride") ? (size_t)v.at("byteStride").u64() : csize * r.comps;
         size_t off = a.has("byteOffset") ? (size_t)a.at("byteOffset").u64() : 0;
-        if (r.count && off + (r.count - 1) * r.stride + csize * r.comps > vlen) fail("accessor outside its bufferView");
+        const size_t elem = csize * r.comps;
+        if (r.stride < elem) fail("bufferView byteStride smaller than the accessor's element");
+        // off + (count - 1) * stride + elem <= vlen, without overflow
+        if (r.count && (off > vlen || elem > vlen - off || r.count - 1 > (vlen - off - elem) / r.stride))
+            fail("accessor outside its bufferView");
         r.base = vb + off;
         return r;
     };

@@ -72,11 +72,17 @@ struct Value {
         }
     }
     float f32() const { return (float)num(); }
+    // Integers: a value the target type cannot hold (negative for u64, beyond the
+    // range, NaN) is an error, not a wrapped or undefined conversion.
     int64_t i64() const {
         switch (kind) {
             case Int: return i;
-            case UInt: return (int64_t)u;
-            case Real: return (int64_t)d;
+            case UInt:
+                if (u > (uint64_t)INT64_MAX) throw std::runtime_error("integer out of range");
+                return (int64_t)u;
+            case Real:
+                if (!(d >= -0x1p63 && d < 0x1p63)) throw std::runtime_error("integer out of range");
+                return (int64_t)d;
             case Bool: return b ? 1 : 0;
             default: throw std::runtime_error("integer expected");
         }
@@ -84,8 +90,12 @@ struct Value {
     uint64_t u64() const {
         switch (kind) {
             case UInt: return u;
-            case Int: return (uint64_t)i;
-            case Real: return (uint64_t)d;
+            case Int:
+                if (i < 0) throw std::runtime_error("non-negative integer expected");
+                return (uint64_t)i;
+            case Real:
+                if (!(d >= 0.0 && d < 0x1p64)) throw std::runtime_error("non-negative integer expected");
+                return (uint64_t)d;
             default: throw std::runtime_error("integer expected");
         }
     }

@@ -377,6 +377,39 @@ def test_png_data_beyond_the_image_is_not_decoded(tmp_path, interlace):
     assert np.array_equal(_import_png(tmp_path, png), img)
 
 
+def _triangle_gltf(tmp_path, view0=None, acc0=None):
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    blob = pos.tobytes() + np.array([0, 1, 2], np.uint32).tobytes()
+    g = {"asset": {"version": "2.0"}, "scene": 0, "scenes": [{"nodes": [0]}], "nodes": [{"mesh": 0}],
+         "meshes": [{"primitives": [{"attributes": {"POSITION": 0}, "indices": 1}]}],
+         "buffers": [{"byteLength": len(blob), "uri": "data:application/octet-stream;base64," +
+                      __import__("base64").b64encode(blob).decode()}],
+         "bufferViews": [dict({"buffer": 0, "byteOffset": 0, "byteLength": 36}, **(view0 or {})),
+                         {"buffer": 0, "byteOffset": 36, "byteLength": 12}],
+         "accessors": [dict({"bufferView": 0, "componentType": 5126, "count": 3, "type": "VEC3"}, **(acc0 or {})),
+                       {"bufferView": 1, "componentType": 5125, "count": 3, "type": "SCALAR"}]}
+    p = tmp_path / "tri.gltf"
+    p.write_text(json.dumps(g))
+    return p
+
+
+@pytest.mark.parametrize("view0,acc0,match", [
+    ({"byteOffset": 2 ** 64 - 1, "byteLength": 2}, None, "bufferView outside"),     # offset + length wraps
+    (None, {"count": 2 ** 62 + 1}, "accessor outside"),                             # (count - 1) * 12 wraps
+    (None, {"byteOffset": 2 ** 64 - 8}, "accessor outside"),
+    ({"byteStride": 4}, None, "byteStride smaller"),
+    (None, {"byteOffset": -4}, "non-negative"),
+    (None, {"count": 1e300}, "non-negative"),
+])
+def test_gltf_ranges_that_overflow_are_rejected(tmp_path, view0, acc0, match):
+    """Offsets, lengths and counts near 2^64 (whose sums or products wrap), negative or
+    out-of-range numbers and strides shorter than an element: each is an error, and
+    nothing outside the file's buffers is read."""
+    assert L.HostScene.import_file(_triangle_gltf(tmp_path), 8, 8).instance_count == 1
+    with pytest.raises(L.LuzError, match=match):
+        L.HostScene.import_file(_triangle_gltf(tmp_path, view0, acc0), 8, 8)
+
+
 @pytest.mark.parametrize("chain", [512, 513, 100000])
 def test_gltf_node_chain_depth(tmp_path, chain):
     """glTF nodes link by index, so a hierarchy can be deeper than its JSON. A chain of
