@@ -11,6 +11,7 @@
 // instance with a ModelBlock, every LightNode a LightBlock.
 #include <algorithm>
 #include <array>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1034,9 +1035,11 @@ SceneAsset import_obj(const std::string& path, Project& p, UuidGen& ids) {
     std::vector<Shape> shapes(1);
     int cur_mat = -1;
     std::string line;
+    // 1-based, or negative from the end of what was read so far; 0 is "none" (-1).
+    // An index outside that range maps to INT_MAX, which the checks below reject.
     auto resolve = [&](long i, size_t n) -> int {
-        if (i > 0) return (int)(i - 1);
-        if (i < 0) return (int)((long)n + i);
+        if (i > 0) return (unsigned long)i <= n ? (int)(i - 1) : INT_MAX;
+        if (i < 0) return (unsigned long)(-(i + 1)) < n ? (int)((long)n + i) : INT_MAX;
         return -1;
     };
     while (std::getline(f, line)) {

@@ -410,6 +410,25 @@ def test_gltf_ranges_that_overflow_are_rejected(tmp_path, view0, acc0, match):
         L.HostScene.import_file(_triangle_gltf(tmp_path, view0, acc0), 8, 8)
 
 
+@pytest.mark.parametrize("face,match", [
+    ("f 1 2 4294967297", "missing vertex"),          # would wrap to index 0 in 32 bits
+    ("f 1 2 -4", "missing vertex"),
+    ("f 1 2 99999999999999999999999", "missing vertex"),
+    ("f 1/1 2/1 3/4294967298", "missing texcoord"),
+    ("f 1/1 2/1 3/-2", "missing texcoord"),
+    ("f 1//1 2//1 3//-3", "missing normal"),
+])
+def test_obj_indices_outside_what_was_read_are_rejected(tmp_path, face, match):
+    """OBJ indices are 1-based or count back from the last element read; any index
+    outside that range is an error (none wraps around to a valid element)."""
+    good = "v 0 0 0\nv 1 0 0\nv 0 1 0\nvt 0 0\nvn 0 0 1\n"
+    (tmp_path / "ok.obj").write_text(good + "f 1/1/1 2/1/1 -1/-1/-1\n")
+    assert L.HostScene.import_file(tmp_path / "ok.obj", 8, 8).instance_count == 1
+    (tmp_path / "bad.obj").write_text(good + face + "\n")
+    with pytest.raises(L.LuzError, match=match):
+        L.HostScene.import_file(tmp_path / "bad.obj", 8, 8)
+
+
 @pytest.mark.parametrize("chain", [512, 513, 100000])
 def test_gltf_node_chain_depth(tmp_path, chain):
     """glTF nodes link by index, so a hierarchy can be deeper than its JSON. A chain of
