@@ -29,7 +29,7 @@ enum {
     LUZ_OK = 0,
     LUZ_ERR_INVALID = 1,        /* bad argument / handle / size                 */
     LUZ_ERR_CUDA = 2,           /* a CUDA runtime call failed                   */
-    LUZ_ERR_OOM = 3,            /* device allocation failed                     */
+    LUZ_ERR_OOM = 3,            /* device or host allocation failed             */
     LUZ_ERR_DEVICE = 4,         /* a kernel raised its status word (see below)  */
     LUZ_ERR_LIMIT = 5,          /* a documented size limit was exceeded         */
     LUZ_ERR_NO_DEVICE = 6       /* no CUDA device / driver                      */

@@ -68,6 +68,8 @@ typedef struct luz_host_scene luz_host_scene;
  *      (one scene of the many-scene batch).
  * Any other config returns LUZ_ERR_INVALID. */
 luz_status luz_scene_default_params(int32_t config, luz_gen_params* out);
+/* Generates the scene the params describe. subdivisions above 10 return
+ * LUZ_ERR_LIMIT; a scene that does not fit in host memory returns LUZ_ERR_OOM. */
 luz_status luz_scene_generate(const luz_gen_params* params, luz_host_scene** out);
 void luz_scene_destroy(luz_host_scene* scene);
 

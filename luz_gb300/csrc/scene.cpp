@@ -7,6 +7,7 @@
 #include <map>
 #include <memory>
 #include <new>
+#include <stdexcept>
 #include <utility>
 #include <vector>
 
@@ -603,12 +604,16 @@ luz_status luz_scene_default_params(int32_t config, luz_gen_params* out) {
     return LUZ_OK;
 }
 
-luz_status luz_scene_generate(const luz_gen_params* p, luz_host_scene** out) {
-    if (!p || !out) return LUZ_ERR_INVALID;
-    *out = nullptr;
-    if (p->width == 0 || p->height == 0) return LUZ_ERR_INVALID;
-    luz_host_scene* s = new (std::nothrow) luz_host_scene();
-    if (!s) return LUZ_ERR_OOM;
+}  // extern "C"
+
+namespace {
+constexpr uint32_t kMaxSubdivisions = 10;   // luz_gen_params::subdivisions
+
+// The generator behind luz_scene_generate; throws std::bad_alloc when the scene the
+// parameters ask for does not fit in host memory.
+luz_status generate_scene(const luz_gen_params* p, luz_host_scene** out) {
+    std::unique_ptr<luz_host_scene> owner(new luz_host_scene());
+    luz_host_scene* s = owner.get();
     s->width = p->width;
     s->height = p->height;
     Rng rng(p->seed);
@@ -620,7 +625,7 @@ luz_status luz_scene_generate(const luz_gen_params* p, luz_host_scene** out) {
         case 2: gen_spheres(s, *p, rng, 1024, 32, 8); ao_default = 16; ao_max_default = 2.0f; break;
         case 5: gen_spheres(s, *p, rng, 4096, 128, 16); ao_default = 64; ao_max_default = 2.0f; break;
         case 6: gen_budget(s, *p, rng); break;
-        default: delete s; return LUZ_ERR_INVALID;
+        default: return LUZ_ERR_INVALID;
     }
     luz_scene& b = s->block;
     memset(&b, 0, sizeof(b));
@@ -639,8 +644,27 @@ luz_status luz_scene_generate(const luz_gen_params* p, luz_host_scene** out) {
     for (auto& l : s->lights) l.num_shadow_samples = s->light_samples;
     update_block(s);
     update_block(s);   // prevViewProj = viewProj for a static camera
-    *out = s;
+    *out = owner.release();
     return LUZ_OK;
+}
+}  // namespace
+
+extern "C" {
+
+luz_status luz_scene_generate(const luz_gen_params* p, luz_host_scene** out) {
+    if (!p || !out) return LUZ_ERR_INVALID;
+    *out = nullptr;
+    if (p->width == 0 || p->height == 0) return LUZ_ERR_INVALID;
+    // 20 x 4^10 triangles per icosphere at most (its vertex count stays far inside
+    // the 32-bit index range)
+    if (p->subdivisions > kMaxSubdivisions) return LUZ_ERR_LIMIT;
+    try {
+        return generate_scene(p, out);
+    } catch (const std::bad_alloc&) {
+        return LUZ_ERR_OOM;
+    } catch (const std::exception&) {
+        return LUZ_ERR_INVALID;
+    }
 }
 
 

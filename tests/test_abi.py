@@ -4,6 +4,7 @@ import re
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 import luz_gb300 as L
 from luz_gb300 import _abi
@@ -151,3 +152,21 @@ def test_null_and_zero_arguments_never_crash_and_statuses_are_invalid():
     assert len(res) > 40
     bad = {k: v for k, v in res.items() if v != 1}
     assert not bad, bad
+
+
+def test_scene_generator_limits_and_host_memory_errors():
+    """Parameters past the documented limit return LUZ_ERR_LIMIT, and a scene larger
+    than host memory returns LUZ_ERR_OOM through the C ABI (no exception escapes it):
+    64 icospheres of 21 M triangles in a process held to 1 GB of address space."""
+    import subprocess
+    import sys
+
+    with pytest.raises(L.LuzError, match="LUZ_ERR_LIMIT"):
+        L.HostScene(2, width=16, height=16, subdivisions=11)
+    code = ("import resource, sys; sys.path.insert(0, sys.argv[1]); import luz_gb300 as L\n"
+            "resource.setrlimit(resource.RLIMIT_AS, (1 << 30, 1 << 30))\n"
+            "try:\n    L.HostScene(2, width=16, height=16, meshes=64, subdivisions=10)\n"
+            "except L.LuzError as e:\n    print(e.status)\n")
+    r = subprocess.run([sys.executable, "-c", code, str(ROOT)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.strip() == "3"   # LUZ_ERR_OOM
