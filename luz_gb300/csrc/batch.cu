@@ -507,7 +507,7 @@ using namespace luz;
 
 extern "C" {
 
-luz_status luz_batch_create(luz_ctx* ctx, uint32_t count, const luz_batch_scene* scenes, luz_batch** out) {
+static luz_status batch_create_body(luz_ctx* ctx, uint32_t count, const luz_batch_scene* scenes, luz_batch** out) {
     if (!ctx || !scenes || !out || count == 0) return LUZ_ERR_INVALID;
     luz_batch* b = new luz_batch();
     b->ctx = ctx;
@@ -543,6 +543,10 @@ luz_status luz_batch_create(luz_ctx* ctx, uint32_t count, const luz_batch_scene*
     if (fs != LUZ_OK) return fail(fs);
     *out = b;
     return LUZ_OK;
+}
+
+luz_status luz_batch_create(luz_ctx* ctx, uint32_t count, const luz_batch_scene* scenes, luz_batch** out) {
+    return guarded(ctx, [&] { return batch_create_body(ctx, count, scenes, out); });
 }
 
 void luz_batch_destroy(luz_batch* b) {

@@ -317,13 +317,13 @@ luz_status luz_ctx_set_blue_noise(luz_ctx* ctx, const uint8_t* rgba8, uint32_t s
 // ------------------------------------------------------------------ BLAS
 luz_status luz_blas_build(luz_ctx* ctx, const luz_blas_desc* desc, luz_blas** out) {
     if (!ctx || !desc || !out) return LUZ_ERR_INVALID;
-    return build_blas_batch(ctx, 1, desc, out);
+    return guarded(ctx, [&] { return build_blas_batch(ctx, 1, desc, out); });
 }
 
 luz_status luz_blas_build_batch(luz_ctx* ctx, uint32_t count, const luz_blas_desc* descs, luz_blas** out) {
     if (!ctx || !descs || !out || count == 0) return LUZ_ERR_INVALID;
     if (count > (1u << 18)) return set_error(ctx, LUZ_ERR_LIMIT, "more than 2^18 BLAS in one batch");
-    return build_blas_batch(ctx, count, descs, out);
+    return guarded(ctx, [&] { return build_blas_batch(ctx, count, descs, out); });
 }
 
 void luz_blas_destroy(luz_blas* b) {
@@ -513,8 +513,8 @@ void luz_frame_destroy(luz_frame* f) {
     delete f;
 }
 
-luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, const luz_light* lights,
-                            uint32_t light_count, const luz_model* models, uint32_t model_count) {
+static luz_status frame_upload_body(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, const luz_light* lights,
+                                    uint32_t light_count, const luz_model* models, uint32_t model_count) {
     if (!ctx || !f || !scene || (light_count && !lights) || (model_count && !models))
         return LUZ_ERR_INVALID;
     if (scene->ao_num_samples < 0 || scene->ao_num_samples > LUZ_MAX_AO_SAMPLES)
@@ -591,7 +591,12 @@ luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, 
     return LUZ_OK;
 }
 
-luz_status luz_frame_set_textures(luz_ctx* ctx, luz_frame* f, const luz_texture_desc* tex, uint32_t count) {
+luz_status luz_frame_upload(luz_ctx* ctx, luz_frame* f, const luz_scene* scene, const luz_light* lights,
+                            uint32_t light_count, const luz_model* models, uint32_t model_count) {
+    return guarded(ctx, [&] { return frame_upload_body(ctx, f, scene, lights, light_count, models, model_count); });
+}
+
+static luz_status frame_set_textures_body(luz_ctx* ctx, luz_frame* f, const luz_texture_desc* tex, uint32_t count) {
     if (!ctx || !f || (count && !tex)) return LUZ_ERR_INVALID;
     size_t total = 0;
     std::vector<size_t> off(count);
@@ -619,6 +624,10 @@ luz_status luz_frame_set_textures(luz_ctx* ctx, luz_frame* f, const luz_texture_
     LUZ_CUDA(ctx, cudaMemcpy(f->d_textures, table.data(), (size_t)count * sizeof(DevTexture), cudaMemcpyHostToDevice));
     f->texture_count = count;
     return LUZ_OK;
+}
+
+luz_status luz_frame_set_textures(luz_ctx* ctx, luz_frame* f, const luz_texture_desc* tex, uint32_t count) {
+    return guarded(ctx, [&] { return frame_set_textures_body(ctx, f, tex, count); });
 }
 
 luz_status luz_gbuffer_primary(luz_ctx* ctx, luz_frame* f, const luz_tlas* t) {

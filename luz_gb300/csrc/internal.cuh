@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <new>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -264,6 +266,29 @@ luz_status ensure_lit_list(luz_ctx* ctx, luz_frame* f);
 // profiling is off or the stream is being captured.
 void prof_begin(luz_ctx* ctx, int32_t kernel);
 void prof_end(luz_ctx* ctx);
+
+// Runs the body of a C entry point that sizes host memory from its inputs: a failed
+// host allocation (std::bad_alloc) or another C++ exception becomes a status, as no
+// exception may cross the C ABI.
+template <class F>
+luz_status guarded(luz_ctx* ctx, F&& body) noexcept {
+    auto note = [ctx](luz_status st, const char* what) noexcept {
+        try {
+            if (ctx) ctx->last_error = what;
+        } catch (...) {
+        }
+        return st;
+    };
+    try {
+        return body();
+    } catch (const std::bad_alloc&) {
+        return note(LUZ_ERR_OOM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return note(LUZ_ERR_INVALID, e.what());
+    } catch (...) {
+        return note(LUZ_ERR_INVALID, "unexpected exception");
+    }
+}
 }  // namespace luz
 
 #define LUZ_CUDA(ctx, call)                                          \

@@ -227,9 +227,9 @@ __global__ void fill_kernel(uint32_t* p, size_t n, uint32_t v) {
 
 using namespace luz;
 
-extern "C" luz_status luz_frame_render_shadow_maps(luz_ctx* ctx, luz_frame* f, const luz_tlas* t,
-                                                   const luz_shadow_light* lights, uint32_t count,
-                                                   uint32_t res) {
+static luz_status frame_render_shadow_maps_body(luz_ctx* ctx, luz_frame* f, const luz_tlas* t,
+                                                const luz_shadow_light* lights, uint32_t count,
+                                                uint32_t res) {
     if (!ctx || !f || !t || (count && !lights) || res == 0 || res > 8192) return LUZ_ERR_INVALID;
     cudaStream_t st = ctx->stream;
     LUZ_CUDA(ctx, cudaStreamSynchronize(st));
@@ -326,6 +326,12 @@ extern "C" luz_status luz_frame_render_shadow_maps(luz_ctx* ctx, luz_frame* f, c
     if (result != LUZ_OK) return result;
     if (e != cudaSuccess) return cuda_error(ctx, e, "shadow-map rasterisation");
     return LUZ_OK;
+}
+
+extern "C" luz_status luz_frame_render_shadow_maps(luz_ctx* ctx, luz_frame* f, const luz_tlas* t,
+                                                   const luz_shadow_light* lights, uint32_t count,
+                                                   uint32_t res) {
+    return guarded(ctx, [&] { return frame_render_shadow_maps_body(ctx, f, t, lights, count, res); });
 }
 
 extern "C" luz_status luz_frame_read_shadow_map(luz_ctx* ctx, luz_frame* f, uint32_t light, float* dst, size_t bytes) {
