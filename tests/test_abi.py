@@ -170,3 +170,31 @@ def test_scene_generator_limits_and_host_memory_errors():
     r = subprocess.run([sys.executable, "-c", code, str(ROOT)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip() == "3"   # LUZ_ERR_OOM
+
+
+def test_headers_are_c_and_link_from_c(tmp_path):
+    """include/*.h compile as strict C99, and a C program that takes the address of
+    every declared function links against the library and runs (its one call returns
+    LUZ_ERR_INVALID for a NULL output, with no GPU)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    names = sorted(declared_functions())
+    src = tmp_path / "abi.c"
+    src.write_text('#include "luz.h"\n#include "luz_scene.h"\n#include <stdio.h>\n'
+                   "static void (*const table[])(void) = {\n" +
+                   "".join(f"    (void (*)(void)){n},\n" for n in names) +
+                   "};\nint main(void) {\n"
+                   "    printf(\"%d %d\\n\", (int)(sizeof table / sizeof table[0]), (int)luz_ctx_create(0, 0));\n"
+                   "    return 0;\n}\n")
+    exe = tmp_path / "abi"
+    lib = Path(_abi.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", str(ROOT / "include"),
+                    str(src), "-o", str(exe), "-L", str(lib.parent), "-l:" + lib.name,
+                    "-Wl,-rpath," + str(lib.parent)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == [str(len(names)), "1"]
